@@ -1,0 +1,226 @@
+/*
+ * nosh_gb300.h -- C ABI of the GB300-native Newton-Krylov core for nosh's
+ * finite-volume Ginzburg-Landau / nonlinear Schroedinger problem
+ *
+ *     0 = F(psi) = (K + V + g|psi|^2) psi .
+ *
+ * Each entry point names the reference (nschloe/nosh) interface it replaces,
+ * as file:line within the nosh source tree.  The reference binds these
+ * through Tpetra / Thyra objects; here every argument is a plain pointer plus
+ * sizes so that any FFI (C++, ctypes, cgo, JNI) can bind it.
+ *
+ * Conventions
+ *  - Return value: NOSH_OK (0) or one of the NOSH_ERR_* codes; a message is
+ *    kept per thread in nosh_last_error().  No exception crosses the ABI.
+ *  - Complex vectors are interleaved [Re0, Im0, Re1, Im1, ...] of length
+ *    2*N doubles (the reference's complex map, src/mesh.cpp:597-607).
+ *  - Vector arguments may live in host memory (pageable or pinned) or in
+ *    device memory of the current CUDA device; the library detects which.
+ *  - The parameter vector p follows the reference's sorted parameter names
+ *    (src/model_evaluator_nls.cpp:102-130): p[0] = "g", p[1] = "mu".
+ *  - Handles are not thread-safe (the reference's operators are mutated by
+ *    rebuild()/refill_ too); use one handle per host thread.  Each nls
+ *    handle owns one CUDA stream; calls return after their work on it is
+ *    complete unless the name ends in _async.
+ *  - There is no CPU fallback: on a machine without a usable GPU every
+ *    compute entry point fails with NOSH_ERR_CUDA.
+ */
+#ifndef NOSH_GB300_H
+#define NOSH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NOSH_OK 0
+#define NOSH_ERR_INVALID 1       /* bad argument / size mismatch           */
+#define NOSH_ERR_CUDA 2          /* CUDA runtime error, or no GPU          */
+#define NOSH_ERR_NOT_CONVERGED 3 /* iteration limit reached                */
+#define NOSH_ERR_NAN 4           /* NaN/Inf met in a reduction             */
+#define NOSH_ERR_BREAKDOWN 5     /* Krylov breakdown (indefinite precond.) */
+#define NOSH_ERR_UNSUPPORTED 6   /* e.g. apply() with mode/alpha/beta the
+                                    reference rejects too                  */
+#define NOSH_ERR_MESH 7          /* degenerate cell                        */
+#define NOSH_ERR_NO_MEMORY 8
+
+/* operator / Krylov precision */
+#define NOSH_PREC_FP64 0  /* everything in FP64                             */
+#define NOSH_PREC_MIXED 1 /* FP32 KEO/SpMV/MINRES/AMG, FP64 residual+scalars */
+
+/* apply() mode, as Teuchos::ETransp */
+#define NOSH_NO_TRANS 0
+#define NOSH_TRANS 1
+
+typedef struct nosh_mesh_s *nosh_mesh;
+typedef struct nosh_nls_s *nosh_nls;
+
+/* Last error message of the calling thread ("" when none). */
+const char *nosh_last_error(void);
+/* Library version (major*10000 + minor*100 + patch). */
+int nosh_version(void);
+/* Number of CUDA devices visible; 0 (and NOSH_ERR_CUDA) without a GPU. */
+int nosh_device_count(int *count);
+
+/* ------------------------------------------------------------------ mesh */
+/* Builds the mesh and all its derived data.  Replaces nosh::read +
+ * mesh_tri / mesh_tetra construction (src/mesh_reader.cpp:20-162,
+ * src/mesh_tri.cpp:14-39, src/mesh_tetra.cpp:14-35): edges
+ * (build_entity_relations_, src/mesh.cpp:631-691), edge data
+ * (compute_edge_data_, src/mesh_tri.cpp:46-103 / src/mesh_tetra.cpp:43-103)
+ * and control volumes (compute_control_volumes_t_, src/mesh_tri.cpp:187-210 /
+ * src/mesh_tetra.cpp:196-271).  coords: 3*N doubles; cells: T*verts_per_cell
+ * vertex ids, verts_per_cell = 3 (triangles) or 4 (tetrahedra).  Geometry is
+ * computed on the GPU in FP64; integer work on the host. */
+int nosh_mesh_create(const double *coords, int64_t num_vertices,
+                     const int32_t *cells, int64_t num_cells,
+                     int verts_per_cell, nosh_mesh *out);
+int nosh_mesh_destroy(nosh_mesh mesh);
+/* nnz_blocks = N + 2E, the number of 2x2 blocks of the KEO graph. */
+int nosh_mesh_sizes(nosh_mesh mesh, int64_t *num_vertices, int64_t *num_edges,
+                    int64_t *num_cells, int64_t *nnz_blocks);
+/* Edge list (E x 2 vertex ids, v0 < v1, lexicographic): mesh::my_edges /
+ * edge_lids (src/mesh.hpp:103-107, src/mesh.cpp:450-471). */
+int nosh_mesh_edges(nosh_mesh mesh, int32_t *edges);
+/* Complex global indices per edge (E x 4: 2g, 2g+1, 2h, 2h+1 with 1-based
+ * vertex GIDs g, h): mesh::build_edge_gids_complex_ (src/mesh.cpp:514-537). */
+int nosh_mesh_edge_gids_complex(nosh_mesh mesh, int32_t *idx);
+/* Edge lengths and covolumes: mesh::get_edge_data (src/mesh.hpp:256-259). */
+int nosh_mesh_edge_data(nosh_mesh mesh, double *length, double *covolume);
+/* Control volumes (N): mesh::control_volumes (src/mesh.hpp:250-252). */
+int nosh_mesh_control_volumes(nosh_mesh mesh, double *cv);
+/* KEO graph in complex (2x2-block) form: row_ptr[N+1], cols[N+2E], sorted
+ * columns, diagonal included.  Expanding each block into 2x2 real entries
+ * gives mesh::build_complex_graph (src/mesh.cpp:789-882). */
+int nosh_mesh_complex_graph(nosh_mesh mesh, int32_t *row_ptr, int32_t *cols);
+
+/* ------------------------------------------------------ model evaluator */
+/* nosh::model_evaluator::nls constructor (src/model_evaluator_nls.cpp:57-138)
+ * together with its fields:
+ *   mvp              3*N doubles: vector potential sampled per vertex, as
+ *                    vector_field::explicit_values(mesh, "A", mu)
+ *                    (src/vector_field_explicit_values.cpp:14-50);
+ *   scalar_potential N doubles, V (scalar_field::explicit_values /
+ *                    constant, src/scalar_field_constant.cpp:45-58);
+ *   thickness        N doubles (likewise);
+ *   g, mu            initial parameter values;
+ *   deriv_parameter  "mu" or "g": the parameter DkeoDP differentiates by
+ *                    (src/parameter_matrix_dkeo_dp.cpp:29-45).
+ * The mesh must outlive the nls handle. */
+int nosh_nls_create(nosh_mesh mesh, const double *mvp, double mu,
+                    const double *scalar_potential, double g,
+                    const double *thickness, const char *deriv_parameter,
+                    nosh_nls *out);
+int nosh_nls_destroy(nosh_nls nls);
+/* Number of parameters and their sorted names (get_p_names,
+ * src/model_evaluator_nls.cpp:196-205); name buffer gets a NUL-terminated
+ * string. */
+int nosh_nls_num_params(nosh_nls nls, int *num);
+int nosh_nls_param_name(nosh_nls nls, int index, char *buf, size_t len);
+/* Precision of J/K_reg applies and of the Krylov solver: NOSH_PREC_*. */
+int nosh_nls_set_precision(nosh_nls nls, int precision);
+/* The CUDA stream the handle's work runs on (a cudaStream_t). */
+int nosh_nls_stream(nosh_nls nls, void **stream);
+
+/* F(x) at parameters p: nls::evalModelImpl with out_args.f set
+ * (src/model_evaluator_nls.cpp:445-461) -> compute_f_ (:529-628).  FP64. */
+int nosh_nls_compute_f(nosh_nls nls, const double *x, const double *p,
+                       double *f);
+/* Same, plus ||F||_2 (FP64 reduction) written to *norm (may be NULL). */
+int nosh_nls_compute_f_norm(nosh_nls nls, const double *x, const double *p,
+                            double *f, double *norm);
+/* dF/dp for every parameter (num_params columns of 2N, column-major):
+ * out_args.DfDp by column (src/model_evaluator_nls.cpp:463-489) ->
+ * computeDFDP_ (:632-695). */
+int nosh_nls_compute_dfdp(nosh_nls nls, const double *x, const double *p,
+                          double *dfdp);
+/* -sum cv |psi|^4 / sum cv: the value nls::gibbs_energy computes before its
+ * "return 0.0" (src/model_evaluator_nls.cpp:742-770). */
+int nosh_nls_gibbs_energy(nosh_nls nls, const double *psi, double *out);
+/* sum cv (Re phi Re psi + Im phi Im psi) / sum cv (nls::inner_product,
+ * src/model_evaluator_nls.cpp:699-738, normalised as its comment states). */
+int nosh_nls_inner_product(nosh_nls nls, const double *phi, const double *psi,
+                           double *out);
+
+/* ---------------------------------------------------- parameter matrices */
+/* keo::set_parameters -> refill_ (src/parameter_object.cpp:7-47,
+ * src/parameter_matrix_keo.cpp:76-184): edge-parallel KEO assembly into the
+ * device CSR at p ("mu" used).  Fills FP64 and FP32 copies. */
+int nosh_keo_set_parameters(nosh_nls nls, const double *p);
+/* Current KEO values in nosh_mesh_complex_graph order, complex interleaved
+ * (2*(N+2E) doubles): one value z per 2x2 block [[Re z, -Im z], [Im z, Re z]]
+ * (the blocks of src/parameter_matrix_keo.cpp:155-160). */
+int nosh_keo_values(nosh_nls nls, double *vals);
+/* Y = K X (Tpetra::CrsMatrix::apply as used at
+ * src/model_evaluator_nls.cpp:537), FP64. */
+int nosh_keo_apply(nosh_nls nls, const double *x, double *y);
+/* DkeoDP::set_parameters -> refill_ (src/parameter_matrix_dkeo_dp.cpp:
+ * 62-155), values and apply, as for the KEO. */
+int nosh_dkeo_set_parameters(nosh_nls nls, const double *p);
+int nosh_dkeo_values(nosh_nls nls, double *vals);
+int nosh_dkeo_apply(nosh_nls nls, const double *x, double *y);
+
+/* ---------------------------------------------------- jacobian operator */
+/* jacobian_operator::rebuild (src/jacobian_operator.cpp:112-141): KEO refill
+ * at p and the diagonal blocks from x (rebuild_diags_, :145-200). */
+int nosh_jacobian_rebuild(nosh_nls nls, const double *p, const double *x);
+/* jacobian_operator::apply (src/jacobian_operator.cpp:40-108) on
+ * num_vectors columns of 2N (column-major).  Like the reference, only
+ * mode = NOSH_NO_TRANS, alpha = 1, beta = 0 are accepted
+ * (NOSH_ERR_UNSUPPORTED otherwise).  Runs in the handle's precision. */
+int nosh_jacobian_apply(nosh_nls nls, const double *X, double *Y,
+                        int num_vectors, int mode, double alpha, double beta);
+
+/* -------------------------------------------------------- preconditioner */
+/* keo_regularized::rebuild (src/keo_regularized.cpp:183-264): regularised
+ * KEO K + g cv t [[2|x|^2+gamma, beta], [beta, 2|x|^2-gamma]] and its
+ * aggregation-AMG hierarchy (the reference builds a MueLu SA-AMG,
+ * :292-336). */
+int nosh_keo_regularized_rebuild(nosh_nls nls, const double *p,
+                                 const double *x);
+/* keo_regularized::apply (src/keo_regularized.cpp:90-165): one V-cycle
+ * (num_cycles == 1).  mode/alpha/beta as for nosh_jacobian_apply. */
+int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y,
+                               int num_vectors, int mode, double alpha,
+                               double beta);
+/* Y = K_reg X (the regularised operator itself, for checking). */
+int nosh_keo_regularized_operator_apply(nosh_nls nls, const double *x,
+                                        double *y);
+
+/* ------------------------------------------------------------- solvers */
+typedef struct {
+  double tol;             /* ||F||_2 target (NOX NormF, examples/conf.xml:
+                             178-189); default 1e-10                      */
+  int max_newton;         /* NOX MaxIters (conf.xml:186-189); default 20  */
+  double forcing;         /* relative MINRES tolerance per Newton step;
+                             <= 0 selects Eisenstat-Walker "Type 1"
+                             (sampleScripts/conf-parallel.xml:78)         */
+  int max_krylov;         /* per linear solve; default 1000 (conf.xml:127)*/
+  int precision;          /* NOSH_PREC_*                                  */
+  int verbose;            /* 0 = silent                                   */
+} nosh_newton_options;
+
+typedef struct {
+  int newton_iters;
+  int krylov_iters;       /* total over the Newton steps                  */
+  double f_norm;          /* final ||F||_2                                */
+  double f_norm0;         /* initial ||F||_2                              */
+  int status;             /* NOSH_OK / NOSH_ERR_NOT_CONVERGED / ...       */
+} nosh_newton_stats;
+
+/* Fills the defaults above. */
+void nosh_newton_default_options(nosh_newton_options *opt);
+/* Full-step inexact Newton with KEO-regularised-AMG-preconditioned MINRES
+ * (NOX "Line Search Based" + "Full Step", examples/conf.xml:77-191; Belos
+ * MINRES, test/linear-solve-test/linop-tester.cpp:288).  x is the initial
+ * guess on entry and the solution on return. */
+int nosh_newton_solve(nosh_nls nls, double *x, const double *p,
+                      const nosh_newton_options *opt,
+                      nosh_newton_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NOSH_GB300_H */

@@ -1,0 +1,382 @@
+"""nosh_gb300 -- GB300-native Newton-Krylov core for nosh's GL / NLS problem.
+
+Python host mirror of the reference's C++ classes over the C ABI of
+``libnosh_gb300.so`` (``include/nosh_gb300.h``).  Class and method names
+follow nschloe/nosh:
+
+=========================================  ====================================
+reference (src/...)                        here
+=========================================  ====================================
+``nosh::mesh`` (mesh.hpp)                  :class:`mesh`
+``vector_field::explicit_values``          ``mvp`` array given to :class:`nls`
+``parameter_matrix::keo`` / ``DkeoDP``     :attr:`nls.keo` / :attr:`nls.dkeo_dp`
+``jacobian_operator``                      :meth:`nls.create_W_op`
+``keo_regularized``                        :meth:`nls.create_W_prec`
+``model_evaluator::nls``                   :class:`nls`
+=========================================  ====================================
+
+Vectors are numpy float64 arrays (host) or anything exposing a CUDA device
+pointer via ``data_ptr()`` (e.g. a torch tensor); complex states are
+interleaved ``[Re0, Im0, Re1, Im1, ...]``.  There is no CPU fallback: the
+package refuses to import without its compiled library, and every compute
+call fails with :class:`NoshError` when no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libnosh_gb300.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"nosh_gb300: compiled library {LIB_PATH} is missing; build it with "
+        "`python -m nosh_gb300.build` (nvcc, sm_103a)"
+    )
+
+_lib = C.CDLL(LIB_PATH)
+
+OK = 0
+ERR_INVALID, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN = 1, 2, 3, 4, 5
+ERR_UNSUPPORTED, ERR_MESH, ERR_NO_MEMORY = 6, 7, 8
+PREC_FP64, PREC_MIXED = 0, 1
+NO_TRANS, TRANS = 0, 1
+
+
+class NoshError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class NewtonOptions(C.Structure):
+    _fields_ = [
+        ("tol", C.c_double),
+        ("max_newton", C.c_int),
+        ("forcing", C.c_double),
+        ("max_krylov", C.c_int),
+        ("precision", C.c_int),
+        ("verbose", C.c_int),
+    ]
+
+
+class NewtonStats(C.Structure):
+    _fields_ = [
+        ("newton_iters", C.c_int),
+        ("krylov_iters", C.c_int),
+        ("f_norm", C.c_double),
+        ("f_norm0", C.c_double),
+        ("status", C.c_int),
+    ]
+
+
+_P, _I64, _D, _I = C.c_void_p, C.c_int64, C.c_double, C.c_int
+_SIGS = {
+    "nosh_last_error": (C.c_char_p, []),
+    "nosh_version": (_I, []),
+    "nosh_device_count": (_I, [C.POINTER(_I)]),
+    "nosh_mesh_create": (_I, [_P, _I64, _P, _I64, _I, C.POINTER(_P)]),
+    "nosh_mesh_destroy": (_I, [_P]),
+    "nosh_mesh_sizes": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)]),
+    "nosh_mesh_edges": (_I, [_P, _P]),
+    "nosh_mesh_edge_gids_complex": (_I, [_P, _P]),
+    "nosh_mesh_edge_data": (_I, [_P, _P, _P]),
+    "nosh_mesh_control_volumes": (_I, [_P, _P]),
+    "nosh_mesh_complex_graph": (_I, [_P, _P, _P]),
+    "nosh_nls_create": (_I, [_P, _P, _D, _P, _D, _P, C.c_char_p, C.POINTER(_P)]),
+    "nosh_nls_destroy": (_I, [_P]),
+    "nosh_nls_num_params": (_I, [_P, C.POINTER(_I)]),
+    "nosh_nls_param_name": (_I, [_P, _I, C.c_char_p, C.c_size_t]),
+    "nosh_nls_set_precision": (_I, [_P, _I]),
+    "nosh_nls_stream": (_I, [_P, C.POINTER(_P)]),
+    "nosh_nls_compute_f": (_I, [_P, _P, _P, _P]),
+    "nosh_nls_compute_f_norm": (_I, [_P, _P, _P, _P, C.POINTER(_D)]),
+    "nosh_nls_compute_dfdp": (_I, [_P, _P, _P, _P]),
+    "nosh_nls_gibbs_energy": (_I, [_P, _P, C.POINTER(_D)]),
+    "nosh_nls_inner_product": (_I, [_P, _P, _P, C.POINTER(_D)]),
+    "nosh_keo_set_parameters": (_I, [_P, _P]),
+    "nosh_keo_values": (_I, [_P, _P]),
+    "nosh_keo_apply": (_I, [_P, _P, _P]),
+    "nosh_dkeo_set_parameters": (_I, [_P, _P]),
+    "nosh_dkeo_values": (_I, [_P, _P]),
+    "nosh_dkeo_apply": (_I, [_P, _P, _P]),
+    "nosh_jacobian_rebuild": (_I, [_P, _P, _P]),
+    "nosh_jacobian_apply": (_I, [_P, _P, _P, _I, _I, _D, _D]),
+    "nosh_keo_regularized_rebuild": (_I, [_P, _P, _P]),
+    "nosh_keo_regularized_apply": (_I, [_P, _P, _P, _I, _I, _D, _D]),
+    "nosh_keo_regularized_operator_apply": (_I, [_P, _P, _P]),
+    "nosh_newton_default_options": (None, [C.POINTER(NewtonOptions)]),
+    "nosh_newton_solve": (_I, [_P, _P, _P, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
+}
+for _name, (_res, _args) in _SIGS.items():
+    _fn = getattr(_lib, _name)
+    _fn.restype = _res
+    _fn.argtypes = _args
+
+
+def lib():
+    """The loaded ctypes library (for low-level use and tests)."""
+    return _lib
+
+
+def _check(rc, allow=()):
+    if rc != OK and rc not in allow:
+        raise NoshError(rc, _lib.nosh_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array (host) or a device tensor (data_ptr)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return C.c_void_p(a.ctypes.data)
+    raise TypeError(f"unsupported vector type {type(a)}")
+
+
+def _f64(a):
+    if hasattr(a, "data_ptr"):
+        return a
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    rc = _lib.nosh_device_count(C.byref(n))
+    return n.value if rc == OK else 0
+
+
+# ---------------------------------------------------------------------------
+class mesh:
+    """``nosh::mesh`` (src/mesh.hpp): simplicial mesh with edges, edge data
+    (length, covolume), control volumes and the KEO graph.  Built from
+    vertex coordinates ``(N, 3)`` and cells ``(T, 3|4)``."""
+
+    def __init__(self, coords, cells):
+        x = np.ascontiguousarray(coords, dtype=np.float64)
+        c = np.ascontiguousarray(cells, dtype=np.int32)
+        if x.ndim != 2 or x.shape[1] != 3 or c.ndim != 2 or c.shape[1] not in (3, 4):
+            raise ValueError("coords must be (N,3) and cells (T,3) or (T,4)")
+        h = C.c_void_p()
+        _check(_lib.nosh_mesh_create(_ptr(x), x.shape[0], _ptr(c), c.shape[0], c.shape[1], C.byref(h)))
+        self._h = h
+        n, e, t, z = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        _check(_lib.nosh_mesh_sizes(h, C.byref(n), C.byref(e), C.byref(t), C.byref(z)))
+        self.num_vertices, self.num_edges, self.num_cells, self.nnz_blocks = n.value, e.value, t.value, z.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.nosh_mesh_destroy(h)
+            self._h = None
+
+    def my_edges(self) -> np.ndarray:
+        out = np.empty((self.num_edges, 2), np.int32)
+        _check(_lib.nosh_mesh_edges(self._h, _ptr(out)))
+        return out
+
+    @property
+    def edge_gids_complex(self) -> np.ndarray:
+        out = np.empty((self.num_edges, 4), np.int32)
+        _check(_lib.nosh_mesh_edge_gids_complex(self._h, _ptr(out)))
+        return out
+
+    def get_edge_data(self):
+        ln = np.empty(self.num_edges)
+        cov = np.empty(self.num_edges)
+        _check(_lib.nosh_mesh_edge_data(self._h, _ptr(ln), _ptr(cov)))
+        return ln, cov
+
+    def control_volumes(self) -> np.ndarray:
+        out = np.empty(self.num_vertices)
+        _check(_lib.nosh_mesh_control_volumes(self._h, _ptr(out)))
+        return out
+
+    def build_complex_graph(self):
+        rp = np.empty(self.num_vertices + 1, np.int32)
+        ci = np.empty(self.nnz_blocks, np.int32)
+        _check(_lib.nosh_mesh_complex_graph(self._h, _ptr(rp), _ptr(ci)))
+        return rp, ci
+
+
+# ---------------------------------------------------------------------------
+class _Matrix:
+    """``parameter_matrix::keo`` / ``DkeoDP`` view of an nls handle."""
+
+    def __init__(self, owner, kind):
+        self._o, self._k = owner, kind
+
+    def set_parameters(self, params: dict):
+        p = self._o._pvec(params)
+        fn = _lib.nosh_keo_set_parameters if self._k == "keo" else _lib.nosh_dkeo_set_parameters
+        _check(fn(self._o._h, _ptr(p)))
+
+    def values(self) -> np.ndarray:
+        """Complex values in ``mesh.build_complex_graph()`` order."""
+        out = np.empty(2 * self._o.mesh.nnz_blocks)
+        fn = _lib.nosh_keo_values if self._k == "keo" else _lib.nosh_dkeo_values
+        _check(fn(self._o._h, _ptr(out)))
+        return out.view(np.complex128)
+
+    def apply(self, x, y=None):
+        x = _f64(x)
+        y = np.empty(2 * self._o.n) if y is None else y
+        fn = _lib.nosh_keo_apply if self._k == "keo" else _lib.nosh_dkeo_apply
+        _check(fn(self._o._h, _ptr(x), _ptr(y)))
+        return y
+
+
+class jacobian_operator:
+    """``nosh::jacobian_operator`` (src/jacobian_operator.hpp)."""
+
+    def __init__(self, owner):
+        self._o = owner
+
+    def rebuild(self, params: dict, x):
+        _check(_lib.nosh_jacobian_rebuild(self._o._h, _ptr(self._o._pvec(params)), _ptr(_f64(x))))
+
+    def apply(self, X, Y=None, mode=NO_TRANS, alpha=1.0, beta=0.0):
+        X = _f64(X)
+        nvec = 1 if getattr(X, "ndim", 1) == 1 else X.shape[0]
+        Y = np.empty_like(X) if Y is None else Y
+        _check(_lib.nosh_jacobian_apply(self._o._h, _ptr(X), _ptr(Y), nvec, mode, alpha, beta))
+        return Y
+
+
+class keo_regularized:
+    """``nosh::keo_regularized`` (src/keo_regularized.hpp): regularised KEO
+    and its AMG V-cycle (``apply`` = one cycle, as ``num_cycles_ == 1``)."""
+
+    def __init__(self, owner):
+        self._o = owner
+
+    def rebuild(self, params: dict, x):
+        _check(_lib.nosh_keo_regularized_rebuild(self._o._h, _ptr(self._o._pvec(params)), _ptr(_f64(x))))
+
+    def apply(self, X, Y=None, mode=NO_TRANS, alpha=1.0, beta=0.0):
+        X = _f64(X)
+        nvec = 1 if getattr(X, "ndim", 1) == 1 else X.shape[0]
+        Y = np.empty_like(X) if Y is None else Y
+        _check(_lib.nosh_keo_regularized_apply(self._o._h, _ptr(X), _ptr(Y), nvec, mode, alpha, beta))
+        return Y
+
+    def operator_apply(self, x, y=None):
+        x = _f64(x)
+        y = np.empty(2 * self._o.n) if y is None else y
+        _check(_lib.nosh_keo_regularized_operator_apply(self._o._h, _ptr(x), _ptr(y)))
+        return y
+
+
+class nls:
+    """``nosh::model_evaluator::nls`` (src/model_evaluator_nls.cpp:57-138).
+
+    ``mvp``: (N,3) vector potential sampled per vertex (explicit values);
+    ``scalar_potential``, ``thickness``: scalars or (N,) arrays.
+    """
+
+    def __init__(self, mesh_: mesh, mvp, scalar_potential=-1.0, g=1.0, thickness=1.0, mu=0.0,
+                 deriv_parameter="mu", precision=PREC_MIXED):
+        self.mesh = mesh_
+        self.n = mesh_.num_vertices
+        N = self.n
+        A = np.ascontiguousarray(mvp, dtype=np.float64).reshape(N, 3)
+        V = np.full(N, float(scalar_potential)) if np.isscalar(scalar_potential) else np.ascontiguousarray(
+            scalar_potential, np.float64)
+        t = np.full(N, float(thickness)) if np.isscalar(thickness) else np.ascontiguousarray(thickness, np.float64)
+        h = C.c_void_p()
+        _check(_lib.nosh_nls_create(mesh_._h, _ptr(A), mu, _ptr(V), g, _ptr(t), deriv_parameter.encode(),
+                                    C.byref(h)))
+        self._h = h
+        self.keo = _Matrix(self, "keo")
+        self.dkeo_dp = _Matrix(self, "dkeo")
+        self.set_precision(precision)
+        self.nominal = {"g": g, "mu": mu}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.nosh_nls_destroy(h)
+            self._h = None
+
+    def set_precision(self, precision):
+        _check(_lib.nosh_nls_set_precision(self._h, precision))
+        self.precision = precision
+
+    def get_p_names(self):
+        n = C.c_int()
+        _check(_lib.nosh_nls_num_params(self._h, C.byref(n)))
+        buf = C.create_string_buffer(32)
+        names = []
+        for k in range(n.value):
+            _check(_lib.nosh_nls_param_name(self._h, k, buf, 32))
+            names.append(buf.value.decode())
+        return names
+
+    def _pvec(self, params):
+        if isinstance(params, dict):
+            p = {**self.nominal, **params}
+            return np.array([p["g"], p["mu"]], np.float64)
+        return np.ascontiguousarray(params, np.float64)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(_lib.nosh_nls_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    # -- evalModel pieces
+    def compute_f(self, x, params, f=None, with_norm=False):
+        x = _f64(x)
+        f = np.empty(2 * self.n) if f is None else f
+        nrm = C.c_double()
+        _check(_lib.nosh_nls_compute_f_norm(self._h, _ptr(x), _ptr(self._pvec(params)), _ptr(f),
+                                            C.byref(nrm) if with_norm else None))
+        return (f, nrm.value) if with_norm else f
+
+    def compute_dfdp(self, x, params):
+        out = np.empty((2, 2 * self.n))
+        _check(_lib.nosh_nls_compute_dfdp(self._h, _ptr(_f64(x)), _ptr(self._pvec(params)), _ptr(out)))
+        return out
+
+    def create_W_op(self):
+        return jacobian_operator(self)
+
+    def create_W_prec(self):
+        return keo_regularized(self)
+
+    def gibbs_energy(self, psi):
+        out = C.c_double()
+        _check(_lib.nosh_nls_gibbs_energy(self._h, _ptr(_f64(psi)), C.byref(out)))
+        return out.value
+
+    def inner_product(self, phi, psi):
+        out = C.c_double()
+        _check(_lib.nosh_nls_inner_product(self._h, _ptr(_f64(phi)), _ptr(_f64(psi)), C.byref(out)))
+        return out.value
+
+    # -- solvers
+    def newton(self, x, params, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000, precision=None,
+               verbose=0):
+        """Full-step inexact Newton with AMG-preconditioned MINRES; ``x`` is
+        updated in place (numpy array or device tensor).  Returns stats."""
+        o = NewtonOptions()
+        _lib.nosh_newton_default_options(C.byref(o))
+        o.tol, o.max_newton, o.forcing, o.max_krylov = tol, max_newton, forcing, max_krylov
+        o.precision = self.precision if precision is None else precision
+        o.verbose = verbose
+        st = NewtonStats()
+        rc = _lib.nosh_newton_solve(self._h, _ptr(x), _ptr(self._pvec(params)), C.byref(o), C.byref(st))
+        _check(rc, allow=(ERR_NOT_CONVERGED,))
+        return {
+            "newton_iters": st.newton_iters,
+            "krylov_iters": st.krylov_iters,
+            "f_norm": st.f_norm,
+            "f_norm0": st.f_norm0,
+            "status": st.status,
+        }

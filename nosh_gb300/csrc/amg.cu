@@ -1,0 +1,701 @@
+// Aggregation AMG preconditioner for the regularised KEO
+// (keo_regularized, src/keo_regularized.cpp).  The reference applies one
+// MueLu SA-AMG V-cycle with 2 equations per node (:292-336); this is a
+// GB300-native aggregation AMG with the same role:
+//
+//  * structure (aggregates, coarse graphs, Galerkin plans) is built on the
+//    host at the first rebuild and reused afterwards (MueLu "reuse: full"
+//    keeps the hierarchy too); every rebuild refreshes all numeric values on
+//    the GPU from the current K_reg;
+//  * plain (unsmoothed) aggregation with 2x2-block identity prolongation:
+//    every level keeps the fine level's compact format -- one complex value
+//    per off-diagonal block plus a symmetric 2x2 diagonal block -- and the
+//    Galerkin product P^T A P is a deterministic segmented sum;
+//  * block-Jacobi Chebyshev smoothing (same polynomial before and after the
+//    coarse correction, so the V-cycle is a fixed SPD operator as MINRES
+//    requires); Gershgorin bound for lambda_max(D^-1 A);
+//  * coarsest level: dense inverse (Gauss-Jordan, FP64) applied as a matvec.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <numeric>
+#include <type_traits>
+
+#include "amg.cuh"
+#include "spmv.cuh"
+
+namespace nosh {
+
+using namespace dev;
+
+namespace {
+
+constexpr double kTheta = 0.05;  // strength-of-connection threshold
+constexpr double kChebRatio = 30.0;  // smoothing interval [lmax/ratio, 1.1 lmax]
+
+struct HostLevel {
+  int64_t n = 0;
+  std::vector<int32_t> rp, ci;  // off-diagonal CSR
+  std::vector<std::complex<double>> off;  // values (strength / next level)
+  std::vector<double> dia;                // 3 per node
+  // transfer to the next level
+  std::vector<int32_t> agg;               // n
+  std::vector<int32_t> mem_ptr, mem_idx;  // coarse node -> fine nodes
+  std::vector<int32_t> seg_ptr, seg_idx;  // coarse nonzero -> fine nonzeros
+  std::vector<int32_t> intra_ptr, intra_idx;  // coarse node -> fine intra nnz
+};
+
+// Greedy aggregation on the strong graph (deterministic, vertex order):
+// 1) a vertex whose strong neighbours are all free roots an aggregate with
+//    them; 2) every remaining vertex joins the aggregate it is most strongly
+//    connected to; 3) isolated leftovers become singletons.
+int64_t aggregate(const HostLevel &L, std::vector<int32_t> &agg) {
+  const int64_t n = L.n;
+  std::vector<double> scale(n);
+  for (int64_t i = 0; i < n; i++) scale[i] = std::max(0.5 * (L.dia[3 * i] + L.dia[3 * i + 1]), 1e-300);
+  auto strong = [&](int64_t i, int64_t k) {
+    const int64_t j = L.ci[k];
+    return std::abs(L.off[k]) >= kTheta * std::sqrt(scale[i] * scale[j]);
+  };
+  agg.assign(n, -1);
+  int64_t na = 0;
+  for (int64_t i = 0; i < n; i++) {
+    if (agg[i] >= 0) continue;
+    bool free = true;
+    for (int64_t k = L.rp[i]; k < L.rp[i + 1] && free; k++)
+      if (strong(i, k) && agg[L.ci[k]] >= 0) free = false;
+    if (!free) continue;
+    agg[i] = (int32_t)na;
+    for (int64_t k = L.rp[i]; k < L.rp[i + 1]; k++)
+      if (strong(i, k)) agg[L.ci[k]] = (int32_t)na;
+    na++;
+  }
+  std::vector<int32_t> agg1 = agg;  // phase 2 reads phase-1 state only
+  for (int64_t i = 0; i < n; i++) {
+    if (agg1[i] >= 0) continue;
+    double best = -1.0;
+    int32_t to = -1;
+    for (int64_t k = L.rp[i]; k < L.rp[i + 1]; k++) {
+      const int32_t a = agg1[L.ci[k]];
+      if (a >= 0 && std::abs(L.off[k]) > best) {
+        best = std::abs(L.off[k]);
+        to = a;
+      }
+    }
+    agg[i] = to;
+  }
+  for (int64_t i = 0; i < n; i++)
+    if (agg[i] < 0) agg[i] = (int32_t)na++;
+  return na;
+}
+
+// Coarse graph + Galerkin plans for plain aggregation, and the coarse values
+// (host copy, used for the next level's strength test).
+void coarsen(HostLevel &F, HostLevel &C) {
+  const int64_t n = F.n;
+  const int64_t na = aggregate(F, F.agg);
+  C.n = na;
+  // members
+  F.mem_ptr.assign(na + 1, 0);
+  for (int64_t i = 0; i < n; i++) F.mem_ptr[F.agg[i] + 1]++;
+  for (int64_t a = 0; a < na; a++) F.mem_ptr[a + 1] += F.mem_ptr[a];
+  F.mem_idx.resize(n);
+  {
+    std::vector<int32_t> fill(F.mem_ptr.begin(), F.mem_ptr.end() - 1);
+    for (int64_t i = 0; i < n; i++) F.mem_idx[fill[F.agg[i]]++] = (int32_t)i;
+  }
+  // coarse rows: unique neighbour aggregates
+  C.rp.assign(na + 1, 0);
+  std::vector<std::vector<int32_t>> rows(na);
+  for (int64_t a = 0; a < na; a++) {
+    auto &r = rows[a];
+    for (int32_t q = F.mem_ptr[a]; q < F.mem_ptr[a + 1]; q++) {
+      const int32_t i = F.mem_idx[q];
+      for (int32_t k = F.rp[i]; k < F.rp[i + 1]; k++) {
+        const int32_t b = F.agg[F.ci[k]];
+        if (b != a) r.push_back(b);
+      }
+    }
+    std::sort(r.begin(), r.end());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+    C.rp[a + 1] = C.rp[a] + (int32_t)r.size();
+  }
+  C.ci.resize(C.rp[na]);
+  for (int64_t a = 0; a < na; a++) std::copy(rows[a].begin(), rows[a].end(), C.ci.begin() + C.rp[a]);
+  // plans: each fine nonzero goes either to one coarse nonzero or to the
+  // coarse diagonal of its aggregate
+  const int64_t nzc = C.rp[na];
+  std::vector<int32_t> target(F.rp[n]);
+  std::vector<int32_t> cnt(nzc + 1, 0), icnt(na + 1, 0);
+  for (int64_t i = 0; i < n; i++) {
+    const int32_t a = F.agg[i];
+    for (int32_t k = F.rp[i]; k < F.rp[i + 1]; k++) {
+      const int32_t b = F.agg[F.ci[k]];
+      if (b == a) {
+        target[k] = -1;
+        icnt[a + 1]++;
+      } else {
+        const int32_t *rb = C.ci.data() + C.rp[a], *re = C.ci.data() + C.rp[a + 1];
+        const int32_t t = (int32_t)(std::lower_bound(rb, re, b) - C.ci.data());
+        target[k] = t;
+        cnt[t + 1]++;
+      }
+    }
+  }
+  for (int64_t t = 0; t < nzc; t++) cnt[t + 1] += cnt[t];
+  for (int64_t a = 0; a < na; a++) icnt[a + 1] += icnt[a];
+  F.seg_ptr = cnt;
+  F.intra_ptr = icnt;
+  F.seg_idx.resize(cnt[nzc]);
+  F.intra_idx.resize(icnt[na]);
+  {
+    std::vector<int32_t> fs(cnt.begin(), cnt.end() - 1), fi(icnt.begin(), icnt.end() - 1);
+    for (int64_t i = 0; i < n; i++)
+      for (int32_t k = F.rp[i]; k < F.rp[i + 1]; k++) {
+        if (target[k] >= 0) F.seg_idx[fs[target[k]]++] = k;
+        else F.intra_idx[fi[F.agg[i]]++] = k;
+      }
+  }
+  // coarse values (host, same arithmetic as the GPU refresh)
+  C.off.assign(nzc, 0.0);
+  for (int64_t t = 0; t < nzc; t++)
+    for (int32_t q = F.seg_ptr[t]; q < F.seg_ptr[t + 1]; q++) C.off[t] += F.off[F.seg_idx[q]];
+  C.dia.assign(3 * na, 0.0);
+  for (int64_t a = 0; a < na; a++) {
+    for (int32_t q = F.mem_ptr[a]; q < F.mem_ptr[a + 1]; q++) {
+      const int32_t i = F.mem_idx[q];
+      for (int c = 0; c < 3; c++) C.dia[3 * a + c] += F.dia[3 * i + c];
+    }
+    for (int32_t q = F.intra_ptr[a]; q < F.intra_ptr[a + 1]; q++) {
+      const double re = F.off[F.intra_idx[q]].real();
+      C.dia[3 * a] += re;
+      C.dia[3 * a + 1] += re;
+    }
+  }
+}
+
+// ------------------------------------------------------------- kernels
+// coarse off-diagonal values: sum of the fine nonzeros of each segment
+template <typename T>
+__global__ void rap_offdiag(int64_t nzc, const int32_t *__restrict__ ptr,
+                            const int32_t *__restrict__ idx, const C2<T> *__restrict__ fine,
+                            C2<T> *__restrict__ coarse) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nzc) return;
+  T sr = 0, si = 0;
+  for (int32_t q = ptr[t]; q < ptr[t + 1]; q++) {
+    const C2<T> v = fine[idx[q]];
+    sr += v.x;
+    si += v.y;
+  }
+  coarse[t] = C2<T>{sr, si};
+}
+
+// coarse diagonal blocks: member diagonal blocks + real parts of the
+// intra-aggregate couplings (their imaginary parts cancel pairwise)
+template <typename T>
+__global__ void rap_diag(int64_t na, const int32_t *__restrict__ mptr,
+                         const int32_t *__restrict__ midx, const int32_t *__restrict__ iptr,
+                         const int32_t *__restrict__ iidx, const T *__restrict__ fdia,
+                         const C2<T> *__restrict__ foff, T *__restrict__ cdia) {
+  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= na) return;
+  T d0 = 0, d1 = 0, d2 = 0;
+  for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
+    const int32_t i = midx[q];
+    d0 += fdia[3 * i];
+    d1 += fdia[3 * i + 1];
+    d2 += fdia[3 * i + 2];
+  }
+  for (int32_t q = iptr[a]; q < iptr[a + 1]; q++) {
+    const T re = foff[iidx[q]].x;
+    d0 += re;
+    d1 += re;
+  }
+  cdia[3 * a] = d0;
+  cdia[3 * a + 1] = d1;
+  cdia[3 * a + 2] = d2;
+}
+
+// inverse diagonal blocks and the Gershgorin bound of lambda_max(D^-1 A):
+// 1 + ||D_i^-1||_2 sum_j |a_ij|, reduced by max over rows
+template <typename T>
+__global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
+                                const C2<T> *__restrict__ off, const T *__restrict__ dia,
+                                T *__restrict__ dinv, unsigned long long *lmax_bits) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double bound = 0.0;
+  if (i < n) {
+    const double a = dia[3 * i], d = dia[3 * i + 1], b = dia[3 * i + 2];
+    const double det = a * d - b * b;
+    dinv[3 * i] = (T)(d / det);
+    dinv[3 * i + 1] = (T)(a / det);
+    dinv[3 * i + 2] = (T)(-b / det);
+    const double lmin = 0.5 * (a + d) - sqrt(0.25 * (a - d) * (a - d) + b * b);
+    double s = 0.0;
+    for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
+      const C2<T> v = off[k];
+      s += sqrt((double)v.x * v.x + (double)v.y * v.y);
+    }
+    bound = (lmin > 0.0 && det > 0.0) ? 1.0 + s / lmin : 1e300;
+  }
+  // max over the block then one atomic per block (non-negative doubles order
+  // like their bit patterns)
+  __shared__ double sm[32];
+  double v = bound;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// Chebyshev coefficients from lambda_max: c[0] = 1/theta, then per step
+// k >= 1 the pair (rho_k rho_{k-1}, 2 rho_k / delta).
+template <typename T>
+__global__ void cheb_coeffs(const unsigned long long *lmax_bits, int deg, T *coef, double *lmax_out) {
+  const double lmax = 1.1 * __longlong_as_double((long long)*lmax_bits);
+  const double lmin = lmax / (1.1 * kChebRatio);
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+  const double sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  coef[0] = (T)(1.0 / theta);
+  for (int k = 1; k < deg; k++) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    coef[2 * k] = (T)(rn * rho);
+    coef[2 * k + 1] = (T)(2.0 * rn / delta);
+    rho = rn;
+  }
+  *lmax_out = lmax;
+}
+
+// first Chebyshev step from x = 0: d = D^-1 b / theta, x = d
+template <typename T>
+__global__ void cheb_first(int64_t n, const T *__restrict__ dinv, const T *__restrict__ coef,
+                           const C2<T> *__restrict__ b, C2<T> *__restrict__ d,
+                           C2<T> *__restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T c0 = coef[0];
+  const C2<T> bi = b[i];
+  const T a = dinv[3 * i], e = dinv[3 * i + 1], f = dinv[3 * i + 2];
+  const C2<T> di{c0 * (a * bi.x + f * bi.y), c0 * (f * bi.x + e * bi.y)};
+  d[i] = di;
+  x[i] = di;
+}
+
+// Chebyshev step with SpMV: r = D^-1 (b - A x_in), d = c1 d + c2 r,
+// x_out = x_in + d.  (k == 0 with x_in != 0: d = r / theta.)
+template <typename T>
+struct ChebOp {
+  static constexpr bool kReduce = false;
+  const T *dia, *dinv, *coef;
+  int step;
+  const C2<T> *b, *xin;
+  C2<T> *d, *xout;
+  __device__ double finish(int i, T sr, T si) const {
+    const C2<T> xi = xin[i], bi = b[i];
+    const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
+    const T rr = bi.x - (sr + d0r * xi.x + d1b * xi.y);
+    const T ri = bi.y - (si + d1b * xi.x + d0i * xi.y);
+    const T a = dinv[3 * i], e = dinv[3 * i + 1], f = dinv[3 * i + 2];
+    const T zr = a * rr + f * ri, zi = f * rr + e * ri;
+    C2<T> dn;
+    if (step == 0) {
+      dn = C2<T>{coef[0] * zr, coef[0] * zi};
+    } else {
+      const C2<T> dold = d[i];
+      const T c1 = coef[2 * step], c2 = coef[2 * step + 1];
+      dn = C2<T>{c1 * dold.x + c2 * zr, c1 * dold.y + c2 * zi};
+    }
+    d[i] = dn;
+    xout[i] = C2<T>{xi.x + dn.x, xi.y + dn.y};
+    return 0.0;
+  }
+};
+
+// res = b - A x
+template <typename T>
+struct ResidOp {
+  static constexpr bool kReduce = false;
+  const T *dia;
+  const C2<T> *b, *x;
+  C2<T> *res;
+  __device__ double finish(int i, T sr, T si) const {
+    const C2<T> xi = x[i], bi = b[i];
+    const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
+    res[i] = C2<T>{bi.x - (sr + d0r * xi.x + d1b * xi.y), bi.y - (si + d1b * xi.x + d0i * xi.y)};
+    return 0.0;
+  }
+};
+
+template <typename T>
+__global__ void restrict_kernel(int64_t na, const int32_t *__restrict__ mptr,
+                                const int32_t *__restrict__ midx, const C2<T> *__restrict__ r,
+                                C2<T> *__restrict__ rc) {
+  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= na) return;
+  T sr = 0, si = 0;
+  for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
+    const C2<T> v = r[midx[q]];
+    sr += v.x;
+    si += v.y;
+  }
+  rc[a] = C2<T>{sr, si};
+}
+
+template <typename T>
+__global__ void prolong_kernel(int64_t n, const int32_t *__restrict__ agg,
+                               const C2<T> *__restrict__ xc, C2<T> *__restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const C2<T> c = xc[agg[i]];
+  C2<T> v = x[i];
+  v.x += c.x;
+  v.y += c.y;
+  x[i] = v;
+}
+
+// Dense real matrix (m = 2n) of the coarsest level from its compact form.
+template <typename T>
+__global__ void coarse_dense(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                             const C2<T> *__restrict__ off, const T *__restrict__ dia, double *A) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t m = 2 * n;
+  double *r0 = A + (2 * i) * m, *r1 = A + (2 * i + 1) * m;
+  for (int64_t j = 0; j < m; j++) {
+    r0[j] = 0.0;
+    r1[j] = 0.0;
+  }
+  r0[2 * i] = dia[3 * i];
+  r0[2 * i + 1] = dia[3 * i + 2];
+  r1[2 * i] = dia[3 * i + 2];
+  r1[2 * i + 1] = dia[3 * i + 1];
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
+    const int32_t j = ci[k];
+    const C2<T> v = off[k];  // block [[re, -im], [im, re]]
+    r0[2 * j] = v.x;
+    r0[2 * j + 1] = -v.y;
+    r1[2 * j] = v.y;
+    r1[2 * j + 1] = v.x;
+  }
+}
+
+// In-place Gauss-Jordan inversion of an SPD matrix (no pivoting needed),
+// one CTA; writes FP64 and FP32 copies.  Records a non-positive pivot.
+__global__ void gauss_jordan_spd(int m, double *A, float *Af, int *err) {
+  for (int k = 0; k < m; k++) {
+    __syncthreads();
+    const double piv = A[(int64_t)k * m + k];
+    __syncthreads();
+    if (threadIdx.x == 0 && !(piv > 0.0)) atomicOr(err, 16);
+    const double ip = 1.0 / piv;
+    for (int j = threadIdx.x; j < m; j += blockDim.x)
+      A[(int64_t)k * m + j] = (j == k) ? ip : A[(int64_t)k * m + j] * ip;
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += blockDim.x) {
+      const int i = (int)(q / m), j = (int)(q % m);
+      if (i == k) continue;
+      const double f = A[(int64_t)i * m + k];
+      if (j == k) continue;
+      A[q] -= f * A[(int64_t)k * m + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      if (i != k) A[(int64_t)i * m + k] = -A[(int64_t)i * m + k] * ip;
+  }
+  __syncthreads();
+  for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += blockDim.x) Af[q] = (float)A[q];
+}
+
+template <typename T>
+__global__ void dense_matvec(int m, const T *__restrict__ Ainv, const T *__restrict__ b, T *__restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    T s = 0;
+    for (int j = 0; j < m; j++) s += Ainv[(int64_t)i * m + j] * b[j];
+    x[i] = s;
+  }
+}
+
+template <typename T>
+int staging_cap_of(const std::vector<int32_t> &rp, int64_t n) {
+  int64_t mx = 0;
+  for (int64_t r0 = 0; r0 < n; r0 += kRows) {
+    const int64_t r1 = std::min<int64_t>(n, r0 + kRows);
+    mx = std::max<int64_t>(mx, rp[r1] - (rp[r0] & ~(int64_t)3));
+  }
+  mx = (mx + 3) & ~(int64_t)3;
+  const int64_t limit = (96 * 1024) / (sizeof(int32_t) + sizeof(C2<T>));
+  return (int)std::min<int64_t>(mx, limit & ~(int64_t)3);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ structures
+struct AmgLevel {
+  int64_t n = 0, nnz = 0;
+  const int32_t *rp = nullptr, *ci = nullptr;  // level 0: the mesh graph
+  DevBuf<int32_t> rp_own, ci_own;
+  int cap32 = 0, cap64 = 0;
+  // transfer to the next level
+  DevBuf<int32_t> agg, mem_ptr, mem_idx, seg_ptr, seg_idx, intra_ptr, intra_idx;
+};
+
+template <typename T>
+struct AmgVals {
+  bool ready = false;
+  std::vector<DevBuf<C2<T>>> off;  // level >= 1
+  std::vector<DevBuf<T>> dia;      // level >= 1
+  std::vector<DevBuf<T>> dinv, coef;
+  std::vector<DevBuf<C2<T>>> b, x, x2, d, res;
+};
+
+struct Amg::Impl {
+  NlsImpl &nls;
+  AmgOptions opt;
+  std::vector<AmgLevel> lev;
+  AmgVals<float> vf;
+  AmgVals<double> vd;
+  DevBuf<unsigned long long> lmax_bits;  // one per level
+  DevBuf<double> lmax;
+  DevBuf<double> dense;   // coarsest (2n)^2 FP64
+  DevBuf<float> densef;
+  DevBuf<int> err;
+  Impl(NlsImpl &s, const AmgOptions &o) : nls(s), opt(o) {}
+  template <typename T> AmgVals<T> &vals();
+  template <typename T> void ensure_vals();
+  template <typename T> void vcycle(int l, const C2<T> *b, C2<T> *x);
+  template <typename T> const C2<T> *off(int l);
+  template <typename T> const T *dia(int l);
+};
+
+template <> AmgVals<float> &Amg::Impl::vals<float>() { return vf; }
+template <> AmgVals<double> &Amg::Impl::vals<double>() { return vd; }
+template <> const C2<float> *Amg::Impl::off<float>(int l) {
+  return l == 0 ? nls.d_keo32.p : vf.off[l].p;
+}
+template <> const C2<double> *Amg::Impl::off<double>(int l) {
+  return l == 0 ? nls.d_keo64.p : vd.off[l].p;
+}
+template <> const float *Amg::Impl::dia<float>(int l) { return l == 0 ? nls.d_rd32.p : vf.dia[l].p; }
+template <> const double *Amg::Impl::dia<double>(int l) { return l == 0 ? nls.d_rd64.p : vd.dia[l].p; }
+
+Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
+  Impl &I = *impl;
+  cudaStream_t st = s.stream;
+  MeshImpl &m = *s.mesh;
+  // host copy of the current fine operator (strength tests)
+  std::vector<HostLevel> H(1);
+  H[0].n = m.N;
+  H[0].rp.assign(m.rp.begin(), m.rp.end());
+  H[0].ci = m.ci;
+  {
+    std::vector<C2<double>> off(2 * m.E);
+    s.d_keo64.download(off.data(), 2 * m.E, st);
+    H[0].dia.resize(3 * m.N);
+    s.d_rd64.download(H[0].dia.data(), 3 * m.N, st);
+    s.sync();
+    H[0].off.resize(2 * m.E);
+    for (int64_t k = 0; k < 2 * m.E; k++) H[0].off[k] = {off[k].x, off[k].y};
+  }
+  while ((int)H.size() < o.max_levels && H.back().n > o.coarse_size) {
+    HostLevel C;
+    coarsen(H.back(), C);
+    if (C.n >= H.back().n) {  // no coarsening progress: stop here
+      H.back().agg.clear();
+      break;
+    }
+    H.push_back(std::move(C));
+  }
+  NOSH_CHECK(H.back().n <= 512, NOSH_ERR_INVALID,
+             "AMG coarsening stalled at " + std::to_string(H.back().n) + " nodes");
+  const int L = (int)H.size();
+  I.lev.resize(L);
+  for (int l = 0; l < L; l++) {
+    AmgLevel &A = I.lev[l];
+    HostLevel &h = H[l];
+    A.n = h.n;
+    A.nnz = h.rp[h.n];
+    if (l == 0) {
+      A.rp = m.d_rp.p;
+      A.ci = m.d_ci.p;
+    } else {
+      A.rp_own.upload(h.rp, st);
+      A.ci_own.alloc(h.ci.size() + kPad);
+      A.ci_own.zero(st);
+      if (!h.ci.empty())
+        NOSH_CUDA(cudaMemcpyAsync(A.ci_own.p, h.ci.data(), h.ci.size() * 4, cudaMemcpyHostToDevice, st));
+      A.rp = A.rp_own.p;
+      A.ci = A.ci_own.p;
+    }
+    A.cap32 = staging_cap_of<float>(h.rp, h.n);
+    A.cap64 = staging_cap_of<double>(h.rp, h.n);
+    if (l + 1 < L) {
+      A.agg.upload(h.agg, st);
+      A.mem_ptr.upload(h.mem_ptr, st);
+      A.mem_idx.upload(h.mem_idx, st);
+      A.seg_ptr.upload(h.seg_ptr, st);
+      A.seg_idx.upload(h.seg_idx, st);
+      A.intra_ptr.upload(h.intra_ptr, st);
+      A.intra_idx.upload(h.intra_idx, st);
+    }
+  }
+  I.lmax_bits.alloc(L);
+  I.lmax.alloc(L);
+  const int64_t m2 = 2 * I.lev.back().n;
+  I.dense.alloc(m2 * m2);
+  I.densef.alloc(m2 * m2);
+  I.err.alloc(1);
+  I.err.zero(st);
+  s.sync();
+}
+
+Amg::~Amg() = default;
+
+int Amg::num_levels() const { return (int)impl->lev.size(); }
+int64_t Amg::level_size(int l) const { return impl->lev[l].n; }
+
+template <typename T>
+void Amg::Impl::ensure_vals() {
+  AmgVals<T> &V = vals<T>();
+  if (V.ready) return;
+  const int L = (int)lev.size();
+  V.off.resize(L);
+  V.dia.resize(L);
+  V.dinv.resize(L);
+  V.coef.resize(L);
+  V.b.resize(L);
+  V.x.resize(L);
+  V.x2.resize(L);
+  V.d.resize(L);
+  V.res.resize(L);
+  for (int l = 0; l < L; l++) {
+    const int64_t n = lev[l].n;
+    if (l > 0) {
+      V.off[l].alloc(lev[l].nnz + kPad);
+      V.off[l].zero(nls.stream);
+      V.dia[l].alloc(3 * n);
+    }
+    V.dinv[l].alloc(3 * n);
+    V.coef[l].alloc(2 * std::max(opt.smooth_degree, 1) + 2);
+    V.b[l].alloc(n);
+    V.x[l].alloc(n);
+    V.x2[l].alloc(n);
+    V.d[l].alloc(n);
+    V.res[l].alloc(n);
+  }
+  V.ready = true;
+}
+
+template <typename T>
+void Amg::refresh() {
+  Impl &I = *impl;
+  I.ensure_vals<T>();
+  AmgVals<T> &V = I.vals<T>();
+  cudaStream_t st = I.nls.stream;
+  const int L = (int)I.lev.size();
+  NOSH_CUDA(cudaMemsetAsync(I.lmax_bits.p, 0, L * sizeof(unsigned long long), st));
+  for (int l = 0; l < L; l++) {
+    AmgLevel &A = I.lev[l];
+    if (l > 0) {
+      AmgLevel &F = I.lev[l - 1];
+      rap_offdiag<T><<<div_up(std::max<int64_t>(A.nnz, 1), 256), 256, 0, st>>>(
+          A.nnz, F.seg_ptr.p, F.seg_idx.p, I.off<T>(l - 1), V.off[l].p);
+      rap_diag<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, F.mem_ptr.p, F.mem_idx.p, F.intra_ptr.p,
+                                                     F.intra_idx.p, I.dia<T>(l - 1), I.off<T>(l - 1),
+                                                     V.dia[l].p);
+    }
+    dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
+                                                          V.dinv[l].p, I.lmax_bits.p + l);
+    cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1),
+                                    V.coef[l].p, I.lmax.p + l);
+  }
+  const AmgLevel &C = I.lev.back();
+  const int m2 = (int)(2 * C.n);
+  coarse_dense<T><<<div_up(C.n, 128), 128, 0, st>>>(C.n, C.rp, C.ci, I.off<T>(L - 1), I.dia<T>(L - 1),
+                                                     I.dense.p);
+  gauss_jordan_spd<<<1, 256, 0, st>>>(m2, I.dense.p, I.densef.p, I.err.p);
+  NOSH_CUDA(cudaGetLastError());
+  int herr = 0;
+  I.err.download(&herr, 1, st);
+  NOSH_CUDA(cudaStreamSynchronize(st));
+  NOSH_CHECK(herr == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
+}
+
+template <typename T, class Op>
+static void launch_level_rows(const AmgLevel &A, const C2<T> *off, const C2<T> *x, const Op &op,
+                              cudaStream_t st, int cap) {
+  static bool attr = false;
+  if (!attr) {
+    NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   100 * 1024));
+    attr = true;
+  }
+  const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
+  row_block_apply<T, Op><<<div_up(A.n, kRows), kRows, smem, st>>>((int)A.n, A.rp, A.ci, off, x, cap, op,
+                                                                 nullptr, nullptr, nullptr);
+}
+
+template <typename T>
+void Amg::Impl::vcycle(int l, const C2<T> *b, C2<T> *x) {
+  AmgVals<T> &V = vals<T>();
+  AmgLevel &A = lev[l];
+  cudaStream_t st = nls.stream;
+  const int L = (int)lev.size();
+  const int cap = sizeof(T) == 4 ? A.cap32 : A.cap64;
+  const int B = 256;
+  if (l == L - 1) {
+    const int m2 = (int)(2 * A.n);
+    const T *Ainv = sizeof(T) == 4 ? (const T *)densef.p : (const T *)dense.p;
+    dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, Ainv, (const T *)b, (T *)x);
+    return;
+  }
+  const int deg = std::max(opt.smooth_degree, 1);
+  const T *dv = dia<T>(l);
+  const C2<T> *ov = off<T>(l);
+  // pre-smoothing from zero; ping-pong between x and x2, ending in x
+  C2<T> *cur = (deg % 2 == 1) ? x : V.x2[l].p;
+  C2<T> *oth = (deg % 2 == 1) ? V.x2[l].p : x;
+  cheb_first<T><<<div_up(A.n, B), B, 0, st>>>(A.n, V.dinv[l].p, V.coef[l].p, b, V.d[l].p, cur);
+  for (int k = 1; k < deg; k++) {
+    ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
+    launch_level_rows<T>(A, ov, cur, op, st, cap);
+    std::swap(cur, oth);
+  }
+  // cur == x here
+  ResidOp<T> rop{dv, b, x, V.res[l].p};
+  launch_level_rows<T>(A, ov, x, rop, st, cap);
+  const AmgLevel &Cl = lev[l + 1];
+  restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p, V.b[l + 1].p);
+  vcycle<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p);
+  prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x);
+  // post-smoothing: same polynomial, now from the corrected x
+  cur = x;
+  oth = V.x2[l].p;
+  for (int k = 0; k < deg; k++) {
+    ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
+    launch_level_rows<T>(A, ov, cur, op, st, cap);
+    std::swap(cur, oth);
+  }
+  if (cur != x)
+    NOSH_CUDA(cudaMemcpyAsync(x, cur, A.n * sizeof(C2<T>), cudaMemcpyDeviceToDevice, st));
+}
+
+template <typename T>
+void Amg::apply(const T *r, T *z) {
+  impl->vcycle<T>(0, (const C2<T> *)r, (C2<T> *)z);
+  NOSH_CUDA(cudaGetLastError());
+}
+
+template void Amg::refresh<float>();
+template void Amg::refresh<double>();
+template void Amg::apply<float>(const float *, float *);
+template void Amg::apply<double>(const double *, double *);
+
+}  // namespace nosh

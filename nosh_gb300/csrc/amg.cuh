@@ -1,0 +1,35 @@
+// Aggregation AMG for the regularised KEO (the keo_regularized
+// preconditioner).  Declared here, defined in amg.cu.
+#pragma once
+
+#include "nls.cuh"
+
+namespace nosh {
+
+struct AmgLevel;
+
+struct AmgOptions {
+  int max_levels = 10;
+  int coarse_size = 64;  // stop coarsening at or below this many nodes
+  int smooth_degree = 2; // Chebyshev degree of pre- and post-smoothing
+  bool smoothed = true;  // smoothed (true) or plain (false) aggregation
+  double omega_scale = 4.0 / 3.0;  // prolongator damping / lambda_max
+};
+
+struct Amg {
+  explicit Amg(NlsImpl &nls, const AmgOptions &opt = AmgOptions());
+  ~Amg();
+  // numeric refresh from the current regularised KEO (nls.d_rd*, d_keo*)
+  template <typename T>
+  void refresh();
+  // z = V-cycle(r); r, z device vectors of 2N (interleaved complex)
+  template <typename T>
+  void apply(const T *r, T *z);
+  int num_levels() const;
+  int64_t level_size(int l) const;
+
+  struct Impl;
+  std::unique_ptr<Impl> impl;
+};
+
+}  // namespace nosh

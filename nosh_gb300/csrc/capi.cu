@@ -1,0 +1,522 @@
+// extern "C" entry points (include/nosh_gb300.h).  Argument checking,
+// host/device pointer staging and error translation; the work itself is in
+// mesh.cu, ops.cu, amg.cu and solver.cu.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "amg.cuh"
+#include "nls.cuh"
+#include "solver.cuh"
+
+struct nosh_mesh_s {
+  nosh::MeshImpl *impl;
+};
+struct nosh_nls_s {
+  nosh::NlsImpl *impl;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    g_last_error.clear();
+    f();
+    return NOSH_OK;
+  } catch (const nosh::Error &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "out of host memory";
+    return NOSH_ERR_NO_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return NOSH_ERR_INVALID;
+  }
+}
+
+void require(bool c, const char *msg) {
+  if (!c) throw nosh::Error(NOSH_ERR_INVALID, msg);
+}
+
+void require_gpu() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    throw nosh::Error(NOSH_ERR_CUDA, "no usable CUDA device");
+  }
+}
+
+nosh::NlsImpl &N(nosh_nls h) {
+  require(h && h->impl, "null nls handle");
+  return *h->impl;
+}
+nosh::MeshImpl &M(nosh_mesh h) {
+  require(h && h->impl, "null mesh handle");
+  return *h->impl;
+}
+
+// Parameter vector [g, mu] from host or device memory.
+void read_params(const double *p, double &g, double &mu) {
+  require(p != nullptr, "null parameter vector");
+  double h[2];
+  if (nosh::is_device_pointer(p)) {
+    NOSH_CUDA(cudaMemcpy(h, p, sizeof(h), cudaMemcpyDeviceToHost));
+  } else {
+    h[0] = p[0];
+    h[1] = p[1];
+  }
+  require(!std::isnan(h[0]) && !std::isnan(h[1]), "parameter is NaN");
+  g = h[0];
+  mu = h[1];
+}
+
+bool usable_in_place(const void *p) {
+  return nosh::is_device_pointer(p) && (reinterpret_cast<uintptr_t>(p) % 16) == 0;
+}
+
+// Device view of a caller's input vector of n doubles.
+const double *stage_in(nosh::NlsImpl &s, const double *user, nosh::DevBuf<double> &buf, size_t n) {
+  require(user != nullptr, "null vector argument");
+  if (usable_in_place(user)) return user;
+  if (buf.n < n) buf.alloc(n);
+  NOSH_CUDA(cudaMemcpyAsync(buf.p, user, n * sizeof(double), cudaMemcpyDefault, s.stream));
+  return buf.p;
+}
+
+// Device destination for a caller's output vector; finish() copies back.
+struct OutVec {
+  double *user, *dev;
+  size_t n;
+  OutVec(nosh::NlsImpl &s, double *u, nosh::DevBuf<double> &buf, size_t count)
+      : user(u), dev(nullptr), n(count) {
+    require(u != nullptr, "null output vector");
+    if (usable_in_place(u)) {
+      dev = u;
+    } else {
+      if (buf.n < n) buf.alloc(n);
+      dev = buf.p;
+    }
+  }
+  void finish(nosh::NlsImpl &s) {
+    if (dev != user)
+      NOSH_CUDA(cudaMemcpyAsync(user, dev, n * sizeof(double), cudaMemcpyDefault, s.stream));
+    s.sync();
+  }
+};
+
+void check_apply_args(int mode, double alpha, double beta, int nvec) {
+  // jacobian_operator::apply accepts only NO_TRANS, alpha == 1, beta == 0
+  // (src/jacobian_operator.cpp:48-59)
+  if (mode != NOSH_NO_TRANS)
+    throw nosh::Error(NOSH_ERR_UNSUPPORTED, "Only untransposed applies supported.");
+  if (alpha != 1.0) throw nosh::Error(NOSH_ERR_UNSUPPORTED, "Only alpha==1.0 supported.");
+  if (beta != 0.0) throw nosh::Error(NOSH_ERR_UNSUPPORTED, "Only beta==0.0 supported.");
+  require(nvec >= 1, "num_vectors must be >= 1");
+}
+
+}  // namespace
+
+namespace nosh {
+bool is_device_pointer(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+}  // namespace nosh
+
+extern "C" {
+
+const char *nosh_last_error(void) { return g_last_error.c_str(); }
+
+int nosh_version(void) { return 100; }
+
+int nosh_device_count(int *count) {
+  return guarded([&] {
+    require(count != nullptr, "null count");
+    *count = 0;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw nosh::Error(NOSH_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *count = n;
+  });
+}
+
+// ---------------------------------------------------------------- mesh
+int nosh_mesh_create(const double *coords, int64_t num_vertices, const int32_t *cells,
+                     int64_t num_cells, int verts_per_cell, nosh_mesh *out) {
+  return guarded([&] {
+    require(out != nullptr && coords != nullptr && cells != nullptr, "null argument");
+    *out = nullptr;
+    require_gpu();
+    auto *h = new nosh_mesh_s{nullptr};
+    try {
+      h->impl = new nosh::MeshImpl(coords, num_vertices, cells, num_cells, verts_per_cell);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int nosh_mesh_destroy(nosh_mesh mesh) {
+  return guarded([&] {
+    if (!mesh) return;
+    delete mesh->impl;
+    delete mesh;
+  });
+}
+
+int nosh_mesh_sizes(nosh_mesh mesh, int64_t *nv, int64_t *ne, int64_t *nc, int64_t *nnz) {
+  return guarded([&] {
+    auto &m = M(mesh);
+    if (nv) *nv = m.N;
+    if (ne) *ne = m.E;
+    if (nc) *nc = m.T;
+    if (nnz) *nnz = m.N + 2 * m.E;
+  });
+}
+
+int nosh_mesh_edges(nosh_mesh mesh, int32_t *edges) {
+  return guarded([&] {
+    auto &m = M(mesh);
+    require(edges != nullptr, "null output");
+    std::memcpy(edges, m.edges.data(), m.edges.size() * sizeof(int32_t));
+  });
+}
+
+int nosh_mesh_edge_gids_complex(nosh_mesh mesh, int32_t *idx) {
+  return guarded([&] {
+    auto &m = M(mesh);
+    require(idx != nullptr, "null output");
+    for (int64_t e = 0; e < m.E; e++) {
+      const int32_t g0 = m.edges[2 * e] + 1, g1 = m.edges[2 * e + 1] + 1;  // 1-based GIDs
+      idx[4 * e + 0] = 2 * g0;
+      idx[4 * e + 1] = 2 * g0 + 1;
+      idx[4 * e + 2] = 2 * g1;
+      idx[4 * e + 3] = 2 * g1 + 1;
+    }
+  });
+}
+
+int nosh_mesh_edge_data(nosh_mesh mesh, double *length, double *covolume) {
+  return guarded([&] {
+    auto &m = M(mesh);
+    if (length) std::memcpy(length, m.h_len.data(), m.E * sizeof(double));
+    if (covolume) std::memcpy(covolume, m.h_covol.data(), m.E * sizeof(double));
+  });
+}
+
+int nosh_mesh_control_volumes(nosh_mesh mesh, double *cv) {
+  return guarded([&] {
+    auto &m = M(mesh);
+    require(cv != nullptr, "null output");
+    std::memcpy(cv, m.h_cv.data(), m.N * sizeof(double));
+  });
+}
+
+int nosh_mesh_complex_graph(nosh_mesh mesh, int32_t *row_ptr, int32_t *cols) {
+  return guarded([&] {
+    auto &m = M(mesh);
+    require(row_ptr != nullptr && cols != nullptr, "null output");
+    m.complex_graph(row_ptr, cols);
+  });
+}
+
+// ------------------------------------------------------------------ nls
+int nosh_nls_create(nosh_mesh mesh, const double *mvp, double mu, const double *V, double g,
+                    const double *t, const char *deriv, nosh_nls *out) {
+  return guarded([&] {
+    require(out != nullptr && mvp != nullptr && V != nullptr && t != nullptr, "null argument");
+    *out = nullptr;
+    auto &m = M(mesh);
+    auto *h = new nosh_nls_s{nullptr};
+    try {
+      h->impl = new nosh::NlsImpl(&m, mvp, mu, V, g, t, deriv);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int nosh_nls_destroy(nosh_nls nls) {
+  return guarded([&] {
+    if (!nls) return;
+    delete nls->impl;
+    delete nls;
+  });
+}
+
+int nosh_nls_num_params(nosh_nls nls, int *num) {
+  return guarded([&] {
+    N(nls);
+    require(num != nullptr, "null output");
+    *num = 2;
+  });
+}
+
+int nosh_nls_param_name(nosh_nls nls, int index, char *buf, size_t len) {
+  return guarded([&] {
+    N(nls);
+    require(buf != nullptr && len >= 3, "buffer too small");
+    require(index == 0 || index == 1, "parameter index out of range");
+    std::strcpy(buf, index == 0 ? "g" : "mu");
+  });
+}
+
+int nosh_nls_set_precision(nosh_nls nls, int precision) {
+  return guarded([&] {
+    require(precision == NOSH_PREC_FP64 || precision == NOSH_PREC_MIXED, "unknown precision");
+    N(nls).precision = precision;
+  });
+}
+
+int nosh_nls_stream(nosh_nls nls, void **stream) {
+  return guarded([&] {
+    require(stream != nullptr, "null output");
+    *stream = (void *)N(nls).stream;
+  });
+}
+
+int nosh_nls_compute_f_norm(nosh_nls nls, const double *x, const double *p, double *f,
+                            double *norm) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
+    OutVec of(s, f, s.d_out, 2 * s.N);
+    s.compute_f64(dx, g, mu, of.dev, norm ? 0 : -1);
+    double n2 = 0.0;
+    if (norm) s.red.out.download(&n2, 1, s.stream);
+    of.finish(s);
+    if (norm) *norm = std::sqrt(n2);
+  });
+}
+
+int nosh_nls_compute_f(nosh_nls nls, const double *x, const double *p, double *f) {
+  return nosh_nls_compute_f_norm(nls, x, p, f, nullptr);
+}
+
+int nosh_nls_compute_dfdp(nosh_nls nls, const double *x, const double *p, double *dfdp) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
+    require(dfdp != nullptr, "null output");
+    for (int k = 0; k < 2; k++) {
+      OutVec o(s, dfdp + k * 2 * s.N, s.d_out, 2 * s.N);
+      s.dfdp64(dx, g, mu, k, o.dev);
+      o.finish(s);
+    }
+  });
+}
+
+int nosh_nls_gibbs_energy(nosh_nls nls, const double *psi, double *out) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(out != nullptr, "null output");
+    *out = s.energy(stage_in(s, psi, s.d_in, 2 * s.N));
+  });
+}
+
+int nosh_nls_inner_product(nosh_nls nls, const double *phi, const double *psi, double *out) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(out != nullptr, "null output");
+    const double *a = stage_in(s, phi, s.d_in, 2 * s.N);
+    const double *b = stage_in(s, psi, s.d_tmp, 2 * s.N);
+    *out = s.inner_product(a, b);
+  });
+}
+
+// --------------------------------------------------- parameter matrices
+int nosh_keo_set_parameters(nosh_nls nls, const double *p) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    s.keo_refill(mu);
+    s.sync();
+  });
+}
+
+int nosh_keo_values(nosh_nls nls, double *vals) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(!std::isnan(s.keo_mu), "KEO not filled: call nosh_keo_set_parameters first");
+    const size_t n = 2 * (s.N + 2 * s.E);
+    nosh::DevBuf<double> tmp(n);
+    s.export_values(s.d_keo64.p, s.d_kdiag.p, tmp.p);
+    tmp.download(vals, n, s.stream);
+    s.sync();
+  });
+}
+
+int nosh_keo_apply(nosh_nls nls, const double *x, double *y) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(!std::isnan(s.keo_mu), "KEO not filled: call nosh_keo_set_parameters first");
+    const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
+    OutVec o(s, y, s.d_out, 2 * s.N);
+    s.keo_apply64(dx, o.dev);
+    o.finish(s);
+  });
+}
+
+int nosh_dkeo_set_parameters(nosh_nls nls, const double *p) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    s.dkeo_refill(mu);
+    s.sync();
+  });
+}
+
+int nosh_dkeo_values(nosh_nls nls, double *vals) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(!std::isnan(s.dkeo_mu), "DkeoDP not filled: call nosh_dkeo_set_parameters first");
+    const size_t n = 2 * (s.N + 2 * s.E);
+    nosh::DevBuf<double> tmp(n);
+    s.export_values(s.d_dkeo64.p, nullptr, tmp.p);
+    tmp.download(vals, n, s.stream);
+    s.sync();
+  });
+}
+
+int nosh_dkeo_apply(nosh_nls nls, const double *x, double *y) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(!std::isnan(s.dkeo_mu), "DkeoDP not filled: call nosh_dkeo_set_parameters first");
+    const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
+    OutVec o(s, y, s.d_out, 2 * s.N);
+    s.dkeo_apply64(dx, o.dev);
+    o.finish(s);
+  });
+}
+
+// --------------------------------------------------- jacobian operator
+int nosh_jacobian_rebuild(nosh_nls nls, const double *p, const double *x) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    s.jac_rebuild(stage_in(s, x, s.d_in, 2 * s.N), g, mu);
+    s.sync();
+  });
+}
+
+int nosh_jacobian_apply(nosh_nls nls, const double *X, double *Y, int nvec, int mode,
+                        double alpha, double beta) {
+  return guarded([&] {
+    auto &s = N(nls);
+    check_apply_args(mode, alpha, beta, nvec);
+    require(s.jac_ready, "Jacobian not built: call nosh_jacobian_rebuild first");
+    for (int k = 0; k < nvec; k++) {
+      const double *dx = stage_in(s, X + (size_t)k * 2 * s.N, s.d_in, 2 * s.N);
+      OutVec o(s, Y + (size_t)k * 2 * s.N, s.d_out, 2 * s.N);
+      if (s.precision == NOSH_PREC_FP64) {
+        s.jac_apply<double>(dx, o.dev);
+      } else {
+        nosh::launch_f64_to_f32(dx, s.d_inf.p, 2 * s.N, s.stream);
+        s.jac_apply<float>(s.d_inf.p, s.d_outf.p);
+        nosh::launch_f32_to_f64(s.d_outf.p, o.dev, 2 * s.N, s.stream);
+      }
+      o.finish(s);
+    }
+  });
+}
+
+// -------------------------------------------------------- preconditioner
+int nosh_keo_regularized_rebuild(nosh_nls nls, const double *p, const double *x) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    s.reg_rebuild(stage_in(s, x, s.d_in, 2 * s.N), g, mu);
+    if (!s.amg) s.amg.reset(new nosh::Amg(s));
+    if (s.precision == NOSH_PREC_FP64) s.amg->refresh<double>();
+    else s.amg->refresh<float>();
+    s.sync();
+  });
+}
+
+int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y, int nvec, int mode,
+                               double alpha, double beta) {
+  return guarded([&] {
+    auto &s = N(nls);
+    check_apply_args(mode, alpha, beta, nvec);
+    require(s.reg_ready && s.amg, "preconditioner not built: call nosh_keo_regularized_rebuild");
+    for (int k = 0; k < nvec; k++) {
+      const double *dx = stage_in(s, X + (size_t)k * 2 * s.N, s.d_in, 2 * s.N);
+      OutVec o(s, Y + (size_t)k * 2 * s.N, s.d_out, 2 * s.N);
+      if (s.precision == NOSH_PREC_FP64) {
+        s.amg->apply<double>(dx, o.dev);
+      } else {
+        nosh::launch_f64_to_f32(dx, s.d_inf.p, 2 * s.N, s.stream);
+        s.amg->apply<float>(s.d_inf.p, s.d_outf.p);
+        nosh::launch_f32_to_f64(s.d_outf.p, o.dev, 2 * s.N, s.stream);
+      }
+      o.finish(s);
+    }
+  });
+}
+
+int nosh_keo_regularized_operator_apply(nosh_nls nls, const double *x, double *y) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(s.reg_ready, "preconditioner not built: call nosh_keo_regularized_rebuild");
+    const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
+    OutVec o(s, y, s.d_out, 2 * s.N);
+    s.reg_apply<double>(dx, o.dev);
+    o.finish(s);
+  });
+}
+
+// --------------------------------------------------------------- solvers
+void nosh_newton_default_options(nosh_newton_options *opt) {
+  if (!opt) return;
+  opt->tol = 1e-10;
+  opt->max_newton = 20;
+  opt->forcing = 0.0;
+  opt->max_krylov = 1000;
+  opt->precision = NOSH_PREC_MIXED;
+  opt->verbose = 0;
+}
+
+int nosh_newton_solve(nosh_nls nls, double *x, const double *p, const nosh_newton_options *opt,
+                      nosh_newton_stats *stats) {
+  nosh_newton_stats st{};
+  int rc = guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    nosh_newton_options o;
+    nosh_newton_default_options(&o);
+    if (opt) o = *opt;
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0, "bad solver options");
+    require(x != nullptr, "null state");
+    nosh::newton_solve(s, x, g, mu, o, st);
+  });
+  if (rc == NOSH_OK) rc = st.status;
+  if (stats) *stats = st;
+  return rc;
+}
+
+}  // extern "C"

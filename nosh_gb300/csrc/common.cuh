@@ -1,0 +1,162 @@
+// Shared helpers of the nosh_gb300 CUDA library (sm_103a only).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "nosh_gb300.h"
+
+namespace nosh {
+
+// ---------------------------------------------------------------- errors
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define NOSH_CUDA(call)                                                      \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      throw ::nosh::Error(NOSH_ERR_CUDA, std::string(#call) + ": " +         \
+                                             cudaGetErrorString(e_));        \
+  } while (0)
+
+#define NOSH_CHECK(cond, code, msg)                                          \
+  do {                                                                       \
+    if (!(cond)) throw ::nosh::Error((code), (msg));                         \
+  } while (0)
+
+// ---------------------------------------------------------- device memory
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error(e == cudaErrorMemoryAllocation ? NOSH_ERR_NO_MEMORY
+                                                 : NOSH_ERR_CUDA,
+                  std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void upload(const T *h, size_t count, cudaStream_t s) {
+    if (count > n) alloc(count);
+    if (count)
+      NOSH_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T> &h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+  void download(T *h, size_t count, cudaStream_t s) const {
+    if (count)
+      NOSH_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+  void zero(cudaStream_t s) {
+    if (n) NOSH_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+};
+
+// True when p points to device (or managed) memory of the CUDA context.
+bool is_device_pointer(const void *p);
+
+// ------------------------------------------------------- host parallelism
+// Static-partition parallel loop over [0, n) on the host cores (integer mesh
+// work during set-up).
+template <class F>
+void parallel_for(int64_t n, F &&f, int64_t grain = 1 << 14) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int64_t nt = hw ? hw : 1;
+  if (nt > 64) nt = 64;
+  if (n < grain * 2 || nt == 1) {
+    for (int64_t i = 0; i < n; i++) f(i);
+    return;
+  }
+  if (nt > n / grain) nt = n / grain;
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int64_t t = 0; t < nt; t++) {
+    int64_t b = n * t / nt, e = n * (t + 1) / nt;
+    th.emplace_back([b, e, &f] {
+      for (int64_t i = b; i < e; i++) f(i);
+    });
+  }
+  for (auto &x : th) x.join();
+}
+
+// ------------------------------------------------------------ launch math
+constexpr int kPad = 8;        // tail padding of nonzero arrays (elements)
+constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time)
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace nosh
+
+// ----------------------------------------------------- device-side helpers
+namespace nosh {
+namespace dev {
+
+template <typename T> struct C2;  // complex pair (interleaved storage)
+template <> struct alignas(8) C2<float> { float x, y; };
+template <> struct alignas(16) C2<double> { double x, y; };
+
+// read-only-path loads of complex pairs
+__device__ __forceinline__ C2<float> ldg(const C2<float> *p) {
+  const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  return C2<float>{v.x, v.y};
+}
+__device__ __forceinline__ C2<double> ldg(const C2<double> *p) {
+  const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+  return C2<double>{v.x, v.y};
+}
+
+template <typename T>
+__device__ __forceinline__ C2<T> cmul(C2<T> a, C2<T> b) {
+  return C2<T>{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+
+// Warp-level sum of a double.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-level sum (blockDim.x multiple of 32, <= 1024); valid in thread 0.
+__device__ __forceinline__ double block_sum(double v, double *smem32) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smem32[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? smem32[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+
+}  // namespace dev
+}  // namespace nosh

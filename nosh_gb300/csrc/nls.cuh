@@ -1,0 +1,98 @@
+// Model-evaluator handle: fields, KEO / DkeoDP values, Jacobian and
+// preconditioner state, all resident in HBM.
+#pragma once
+
+#include <memory>
+#include <string>
+
+#include "mesh.cuh"
+
+namespace nosh {
+
+using dev::C2;
+
+// Scratch for deterministic grid reductions ("last block finishes"):
+// per-block partial sums, an arrival counter and the finished scalars.
+struct Reducer {
+  DevBuf<double> partials;   // >= number of blocks of any reducing launch
+  DevBuf<unsigned> counter;  // zero between launches
+  DevBuf<double> out;        // result slots
+  void init(int max_blocks, int nslots, cudaStream_t s) {
+    partials.alloc(max_blocks * 4 + 64);
+    counter.alloc(8);
+    counter.zero(s);
+    out.alloc(nslots);
+    out.zero(s);
+  }
+};
+
+struct Amg;  // aggregation AMG hierarchy (amg.cu)
+
+struct NlsImpl {
+  MeshImpl *mesh;
+  int64_t N, E;
+  cudaStream_t stream = nullptr;
+  int precision = NOSH_PREC_MIXED;
+  std::string deriv_param;
+  double g0, mu0;
+
+  // fields (FP64) and derived per-edge / per-vertex data
+  DevBuf<double> d_A, d_V, d_t, d_cvt;  // 3N, N, N, N (cv * thickness)
+  std::vector<double> h_V, h_t;
+  DevBuf<double> d_p, d_alpha, d_kdiag;  // E, E, N
+  DevBuf<float> d_pf, d_alphaf, d_kdiagf;
+  double cv_sum = 0.0;
+
+  // off-diagonal KEO values in adjacency-CSR order (2E + kPad)
+  DevBuf<C2<double>> d_keo64, d_dkeo64;
+  DevBuf<C2<float>> d_keo32;
+  double keo_mu = std::nan(""), dkeo_mu = std::nan("");
+
+  // diagonal 2x2 blocks (Re-Re, Im-Im, Re-Im), K_ii included:
+  // Jacobian (rebuild_diags_) and regularised KEO
+  DevBuf<double> d_jd64, d_rd64;  // 3N each
+  DevBuf<float> d_jd32, d_rd32;
+  bool jac_ready = false, reg_ready = false;
+  double reg_g = 0.0;
+
+  // staging for host / misaligned vectors
+  DevBuf<double> d_in, d_out, d_tmp;  // 2N each
+  DevBuf<float> d_inf, d_outf;
+
+  Reducer red;
+  int cap32 = 0, cap64 = 0;  // staged nonzeros per row block (FP32 / FP64)
+
+  std::unique_ptr<Amg> amg;
+  std::shared_ptr<void> solver_state;  // Newton / MINRES work space (solver.cu)
+
+  NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, double g,
+          const double *t, const char *deriv);
+  ~NlsImpl();
+
+  // operators (device pointers to interleaved complex vectors)
+  void keo_refill(double mu);
+  void dkeo_refill(double mu);
+  void keo_apply64(const double *x, double *y);
+  void dkeo_apply64(const double *x, double *y);
+  // y = F(x); optional ||F||^2 into red.out[slot]
+  void compute_f64(const double *x, double g, double mu, double *f, int norm_slot);
+  void dfdp64(const double *x, double g, double mu, int param, double *out);
+  void jac_rebuild(const double *x, double g, double mu);
+  void reg_rebuild(const double *x, double g, double mu);
+  template <typename T>
+  void jac_apply(const T *x, T *y, double *dot_out = nullptr);
+  template <typename T>
+  void reg_apply(const T *x, T *y);
+  double energy(const double *psi);
+  double inner_product(const double *phi, const double *psi);
+  // full-graph values (with diagonal) in complex_graph order, complex
+  void export_values(const C2<double> *offdiag, const double *diag, double *out);
+
+  void sync() { NOSH_CUDA(cudaStreamSynchronize(stream)); }
+};
+
+// launch helpers shared with the solver
+void launch_f64_to_f32(const double *a, float *b, int64_t n, cudaStream_t s);
+void launch_f32_to_f64(const float *a, double *b, int64_t n, cudaStream_t s);
+
+}  // namespace nosh

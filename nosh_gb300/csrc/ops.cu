@@ -1,0 +1,447 @@
+// Model-evaluator operators on the GPU: KEO / DkeoDP assembly, F(psi),
+// dF/dp, Jacobian and regularised-KEO diagonals, fused applies, energy.
+#include <cmath>
+#include <cstring>
+
+#include "amg.cuh"
+#include "nls.cuh"
+#include "spmv.cuh"
+
+namespace nosh {
+
+using namespace dev;
+
+namespace {
+
+// ---------------------------------------------------------------- fields
+// p_e = 1/2 (A(x0) + A(x1)) . (x0 - x1)
+// (vector_field::explicit_values, src/vector_field_explicit_values.cpp:31-48)
+// alpha_e = covolume/length * mean thickness
+// (keo::build_alpha_cache_, src/parameter_matrix_keo.cpp:221-228)
+__global__ void edge_fields_kernel(int64_t E, const int32_t *__restrict__ edges,
+                                   const double *__restrict__ x, const double *__restrict__ A,
+                                   const double *__restrict__ len, const double *__restrict__ covol,
+                                   const double *__restrict__ t, double *p, double *alpha,
+                                   float *pf, float *alphaf) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const int64_t a = edges[2 * e], b = edges[2 * e + 1];
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) s += 0.5 * (A[3 * a + k] + A[3 * b + k]) * (x[3 * a + k] - x[3 * b + k]);
+  const double al = covol[e] / len[e] * 0.5 * (t[a] + t[b]);
+  p[e] = s;
+  alpha[e] = al;
+  pf[e] = (float)s;
+  alphaf[e] = (float)al;
+}
+
+// K_ii = sum of alpha over the edges of row i (mu-independent), in column
+// order; cvt = cv * thickness.
+__global__ void vertex_fields_kernel(int64_t N, const int32_t *__restrict__ rp,
+                                     const int32_t *__restrict__ nz_edge,
+                                     const double *__restrict__ alpha, const double *__restrict__ cv,
+                                     const double *__restrict__ t, double *kdiag, float *kdiagf,
+                                     double *cvt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s = 0.0;
+  for (int k = rp[i]; k < rp[i + 1]; k++) {
+    const int32_t e = nz_edge[k];
+    s += alpha[e >= 0 ? e : ~e];
+  }
+  kdiag[i] = s;
+  kdiagf[i] = (float)s;
+  cvt[i] = cv[i] * t[i];
+}
+
+// --------------------------------------------------------- KEO assembly
+// keo::refill_ (src/parameter_matrix_keo.cpp:106-180): per edge v0->v1,
+// a = mu p_e, complex coefficient -alpha e^{-ia} at (v0,v1) and its
+// conjugate at (v1,v0), written through the edge -> nonzero scatter map.
+// The diagonal (sum alpha) is mu-independent and kept separately.
+__global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha,
+                               const double *__restrict__ p, double mu,
+                               const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
+                               C2<double> *__restrict__ val) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double s, c;
+  sincos(mu * p[e], &s, &c);
+  const double al = alpha[e];
+  val[pf[e]] = C2<double>{-al * c, al * s};
+  val[pb[e]] = C2<double>{-al * c, -al * s};
+}
+
+__global__ void keo_assemble32(int64_t E, const float *__restrict__ alpha,
+                               const float *__restrict__ p, float mu,
+                               const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
+                               C2<float> *__restrict__ val) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  float s, c;
+  sincosf(mu * p[e], &s, &c);
+  const float al = alpha[e];
+  val[pf[e]] = C2<float>{-al * c, al * s};
+  val[pb[e]] = C2<float>{-al * c, -al * s};
+}
+
+// DkeoDP::refill_ (src/parameter_matrix_dkeo_dp.cpp:96-151): block entries
+// v0 = alpha dp sin a, v1 = -alpha dp cos a, no diagonal.  dp = p_e for the
+// derivative parameter "mu", else 0 (get_d_edge_projection_dp,
+// src/vector_field_explicit_values.cpp:80-90).
+__global__ void dkeo_assemble64(int64_t E, const double *__restrict__ alpha,
+                                const double *__restrict__ p, double mu, double dscale,
+                                const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
+                                C2<double> *__restrict__ val) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double s, c;
+  sincos(mu * p[e], &s, &c);
+  const double w = alpha[e] * p[e] * dscale;
+  // complex v0 - i v1 at (v0,v1): w sin a + i w cos a; conjugate at (v1,v0)
+  val[pf[e]] = C2<double>{w * s, w * c};
+  val[pb[e]] = C2<double>{w * s, -w * c};
+}
+
+// ------------------------------------------------------------ diagonals
+// jacobian_operator::rebuild_diags_ (src/jacobian_operator.cpp:184-197),
+// with K_ii folded in: [[d0r, d1b], [d1b, d0i]].
+__global__ void jac_diag_kernel(int64_t N, const double *__restrict__ kdiag,
+                                const double *__restrict__ cvt, const double *__restrict__ V,
+                                double g, const C2<double> *__restrict__ x, double *d64,
+                                float *d32) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const C2<double> p = x[k];
+  const double w = cvt[k];
+  const double al = w * (V[k] + g * 2.0 * (p.x * p.x + p.y * p.y));
+  const double rx2 = g * w * (p.x * p.x - p.y * p.y);
+  const double a = kdiag[k] + al + rx2, b = kdiag[k] + al - rx2, c = g * w * (2.0 * p.x * p.y);
+  d64[3 * k] = a;
+  d64[3 * k + 1] = b;
+  d64[3 * k + 2] = c;
+  d32[3 * k] = (float)a;
+  d32[3 * k + 1] = (float)b;
+  d32[3 * k + 2] = (float)c;
+}
+
+// keo_regularized::rebuild (src/keo_regularized.cpp:233-258): + g cv t
+// [[2|x|^2 + gamma, beta], [beta, 2|x|^2 - gamma]] when g > 0.
+__global__ void reg_diag_kernel(int64_t N, const double *__restrict__ kdiag,
+                                const double *__restrict__ cvt, double g,
+                                const C2<double> *__restrict__ x, double *d64, float *d32) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  double a = kdiag[k], b = kdiag[k], c = 0.0;
+  if (g > 0.0) {
+    const C2<double> p = x[k];
+    const double w = g * cvt[k];
+    const double al = w * 2.0 * (p.x * p.x + p.y * p.y);
+    const double be = w * (2.0 * p.x * p.y);
+    const double ga = w * (p.x * p.x - p.y * p.y);
+    a += al + ga;
+    b += al - ga;
+    c = be;
+  }
+  d64[3 * k] = a;
+  d64[3 * k + 1] = b;
+  d64[3 * k + 2] = c;
+  d32[3 * k] = (float)a;
+  d32[3 * k + 1] = (float)b;
+  d32[3 * k + 2] = (float)c;
+}
+
+// dF/dp diagonal terms (src/model_evaluator_nls.cpp:665-691): out +=
+// cv t |x|^2 x for "g", cv t dV/dp x otherwise (dV/dp = 0 for the explicit
+// potential used here).
+__global__ void dfdp_diag_kernel(int64_t N, const double *__restrict__ cvt, int is_g,
+                                 const C2<double> *__restrict__ x, C2<double> *out) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  if (!is_g) return;
+  const C2<double> p = x[k];
+  const double a = cvt[k] * (p.x * p.x + p.y * p.y);
+  out[k].x += a * p.x;
+  out[k].y += a * p.y;
+}
+
+// -sum cv |psi|^4 (gibbs_energy) and sum cv <phi, psi> (inner_product)
+__global__ void energy_kernel(int64_t N, const double *__restrict__ cv,
+                              const C2<double> *__restrict__ psi, double *partials,
+                              unsigned *counter, double *out) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (k < N) {
+    const C2<double> p = psi[k];
+    const double a = p.x * p.x + p.y * p.y;
+    v = -cv[k] * a * a;
+  }
+  grid_reduce(v, partials, counter, out);
+}
+
+__global__ void inner_kernel(int64_t N, const double *__restrict__ cv,
+                             const C2<double> *__restrict__ a, const C2<double> *__restrict__ b,
+                             double *partials, unsigned *counter, double *out) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (k < N) v = cv[k] * (a[k].x * b[k].x + a[k].y * b[k].y);
+  grid_reduce(v, partials, counter, out);
+}
+
+
+__global__ void d2f_kernel(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+__global__ void f2d_kernel(const float *__restrict__ a, double *__restrict__ b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+
+// full-graph values: off-diagonal + diagonal, in complex_graph order
+__global__ void export_kernel(int64_t N, const int32_t *__restrict__ rp,
+                              const int32_t *__restrict__ ci, const C2<double> *__restrict__ od,
+                              const double *__restrict__ diag, C2<double> *out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int64_t o = rp[i] + i;
+  bool placed = false;
+  for (int k = rp[i]; k < rp[i + 1]; k++) {
+    if (!placed && ci[k] > i) {
+      out[o++] = C2<double>{diag ? diag[i] : 0.0, 0.0};
+      placed = true;
+    }
+    out[o++] = od[k];
+  }
+  if (!placed) out[o] = C2<double>{diag ? diag[i] : 0.0, 0.0};
+}
+
+template <typename T>
+int staging_cap(const MeshImpl &m) {
+  // largest staged range of any row block, capped by the shared memory
+  int64_t mx = 0;
+  for (int64_t r0 = 0; r0 < m.N; r0 += kRows) {
+    const int64_t r1 = std::min<int64_t>(m.N, r0 + kRows);
+    mx = std::max<int64_t>(mx, m.rp[r1] - (m.rp[r0] & ~(int64_t)3));
+  }
+  mx = (mx + 3) & ~(int64_t)3;
+  const int64_t limit = (96 * 1024) / (sizeof(int32_t) + sizeof(C2<T>));
+  return (int)std::min<int64_t>(mx, limit & ~(int64_t)3);
+}
+
+template <typename T, class Op>
+void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &op, int cap,
+                 double *red_out) {
+  const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
+  static bool attr_set = false;  // per instantiation
+  if (!attr_set) {
+    NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    attr_set = true;
+  }
+  const int grid = div_up(s.N, kRows);
+  row_block_apply<T, Op><<<grid, kRows, smem, s.stream>>>(
+      (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, x, cap, op, s.red.partials.p,
+      s.red.counter.p, red_out);
+  NOSH_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+void launch_f64_to_f32(const double *a, float *b, int64_t n, cudaStream_t s) {
+  if (n) d2f_kernel<<<div_up(n, 256), 256, 0, s>>>(a, b, n);
+}
+void launch_f32_to_f64(const float *a, double *b, int64_t n, cudaStream_t s) {
+  if (n) f2d_kernel<<<div_up(n, 256), 256, 0, s>>>(a, b, n);
+}
+
+// ------------------------------------------------------------------------
+NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, double g,
+                 const double *t, const char *deriv)
+    : mesh(m), N(m->N), E(m->E), deriv_param(deriv ? deriv : "mu"), g0(g), mu0(mu) {
+  NOSH_CHECK(deriv_param == "mu" || deriv_param == "g", NOSH_ERR_INVALID,
+             "deriv_parameter must be \"mu\" or \"g\"");
+  NOSH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  cudaStream_t s = stream;
+  h_V.assign(V, V + N);
+  h_t.assign(t, t + N);
+  d_A.upload(mvp, 3 * N, s);
+  d_V.upload(h_V, s);
+  d_t.upload(h_t, s);
+  d_p.alloc(E);
+  d_alpha.alloc(E);
+  d_pf.alloc(E);
+  d_alphaf.alloc(E);
+  d_kdiag.alloc(N);
+  d_kdiagf.alloc(N);
+  d_cvt.alloc(N);
+  edge_fields_kernel<<<div_up(E, 256), 256, 0, s>>>(E, m->d_edges.p, m->d_x.p, d_A.p, m->d_len.p,
+                                                     m->d_covol.p, d_t.p, d_p.p, d_alpha.p, d_pf.p,
+                                                     d_alphaf.p);
+  vertex_fields_kernel<<<div_up(N, 256), 256, 0, s>>>(N, m->d_rp.p, m->d_nz_edge.p, d_alpha.p,
+                                                       m->d_cv.p, d_t.p, d_kdiag.p, d_kdiagf.p,
+                                                       d_cvt.p);
+  NOSH_CUDA(cudaGetLastError());
+  const size_t nz = 2 * E + kPad;
+  d_keo64.alloc(nz);
+  d_keo32.alloc(nz);
+  d_dkeo64.alloc(nz);
+  d_keo64.zero(s);
+  d_keo32.zero(s);
+  d_dkeo64.zero(s);
+  d_jd64.alloc(3 * N);
+  d_rd64.alloc(3 * N);
+  d_jd32.alloc(3 * N);
+  d_rd32.alloc(3 * N);
+  d_in.alloc(2 * N);
+  d_out.alloc(2 * N);
+  d_tmp.alloc(2 * N);
+  d_inf.alloc(2 * N);
+  d_outf.alloc(2 * N);
+  red.init(div_up(N, kRows) + div_up(N, 256) + 1024, 64, s);
+  cap32 = staging_cap<float>(*m);
+  cap64 = staging_cap<double>(*m);
+  for (double c : m->h_cv) cv_sum += c;
+  sync();
+}
+
+NlsImpl::~NlsImpl() {
+  solver_state.reset();
+  amg.reset();
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void NlsImpl::keo_refill(double mu) {
+  keo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, mesh->d_pos_fwd.p,
+                                                      mesh->d_pos_bwd.p, d_keo64.p);
+  keo_assemble32<<<div_up(E, 256), 256, 0, stream>>>(E, d_alphaf.p, d_pf.p, (float)mu,
+                                                      mesh->d_pos_fwd.p, mesh->d_pos_bwd.p,
+                                                      d_keo32.p);
+  NOSH_CUDA(cudaGetLastError());
+  keo_mu = mu;
+}
+
+void NlsImpl::dkeo_refill(double mu) {
+  dkeo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(
+      E, d_alpha.p, d_p.p, mu, deriv_param == "mu" ? 1.0 : 0.0, mesh->d_pos_fwd.p,
+      mesh->d_pos_bwd.p, d_dkeo64.p);
+  NOSH_CUDA(cudaGetLastError());
+  dkeo_mu = mu;
+}
+
+void NlsImpl::keo_apply64(const double *x, double *y) {
+  KeoOp<double> op{d_kdiag.p, (const C2<double> *)x, (C2<double> *)y};
+  launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap64, nullptr);
+}
+
+void NlsImpl::dkeo_apply64(const double *x, double *y) {
+  PlainOp<double> op{(C2<double> *)y};
+  launch_rows<double>(*this, d_dkeo64.p, (const C2<double> *)x, op, cap64,
+                      nullptr);
+}
+
+void NlsImpl::compute_f64(const double *x, double g, double mu, double *f, int norm_slot) {
+  if (!(keo_mu == mu)) keo_refill(mu);
+  const int cap = cap64;
+  if (norm_slot >= 0) {
+    ResidualOp<true> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f};
+    launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, red.out.p + norm_slot);
+  } else {
+    ResidualOp<false> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f};
+    launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, nullptr);
+  }
+}
+
+void NlsImpl::dfdp64(const double *x, double g, double mu, int param, double *out) {
+  (void)g;
+  if (!(dkeo_mu == mu)) dkeo_refill(mu);
+  dkeo_apply64(x, out);
+  dfdp_diag_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_cvt.p, param == 0 ? 1 : 0,
+                                                        (const C2<double> *)x, (C2<double> *)out);
+  NOSH_CUDA(cudaGetLastError());
+}
+
+void NlsImpl::jac_rebuild(const double *x, double g, double mu) {
+  if (!(keo_mu == mu)) keo_refill(mu);
+  jac_diag_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_kdiag.p, d_cvt.p, d_V.p, g,
+                                                       (const C2<double> *)x, d_jd64.p, d_jd32.p);
+  NOSH_CUDA(cudaGetLastError());
+  jac_ready = true;
+}
+
+void NlsImpl::reg_rebuild(const double *x, double g, double mu) {
+  if (!(keo_mu == mu)) keo_refill(mu);
+  reg_diag_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_kdiag.p, d_cvt.p, g,
+                                                       (const C2<double> *)x, d_rd64.p, d_rd32.p);
+  NOSH_CUDA(cudaGetLastError());
+  reg_g = g;
+  reg_ready = true;
+}
+
+template <>
+void NlsImpl::jac_apply<double>(const double *x, double *y, double *dot_out) {
+  const int cap = cap64;
+  if (dot_out) {
+    BlockDiagOp<double, true> op{d_jd64.p, (const C2<double> *)x, (C2<double> *)y};
+    launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, dot_out);
+  } else {
+    BlockDiagOp<double, false> op{d_jd64.p, (const C2<double> *)x, (C2<double> *)y};
+    launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, nullptr);
+  }
+}
+
+template <>
+void NlsImpl::jac_apply<float>(const float *x, float *y, double *dot_out) {
+  const int cap = cap32;
+  if (dot_out) {
+    BlockDiagOp<float, true> op{d_jd32.p, (const C2<float> *)x, (C2<float> *)y};
+    launch_rows<float>(*this, d_keo32.p, (const C2<float> *)x, op, cap, dot_out);
+  } else {
+    BlockDiagOp<float, false> op{d_jd32.p, (const C2<float> *)x, (C2<float> *)y};
+    launch_rows<float>(*this, d_keo32.p, (const C2<float> *)x, op, cap, nullptr);
+  }
+}
+
+template <>
+void NlsImpl::reg_apply<double>(const double *x, double *y) {
+  BlockDiagOp<double, false> op{d_rd64.p, (const C2<double> *)x, (C2<double> *)y};
+  launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap64,
+                      nullptr);
+}
+
+template <>
+void NlsImpl::reg_apply<float>(const float *x, float *y) {
+  BlockDiagOp<float, false> op{d_rd32.p, (const C2<float> *)x, (C2<float> *)y};
+  launch_rows<float>(*this, d_keo32.p, (const C2<float> *)x, op, cap32,
+                     nullptr);
+}
+
+double NlsImpl::energy(const double *psi) {
+  energy_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_cv.p, (const C2<double> *)psi,
+                                                     red.partials.p, red.counter.p, red.out.p);
+  NOSH_CUDA(cudaGetLastError());
+  double e = 0.0;
+  red.out.download(&e, 1, stream);
+  sync();
+  return e / cv_sum;
+}
+
+double NlsImpl::inner_product(const double *phi, const double *psi) {
+  inner_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_cv.p, (const C2<double> *)phi,
+                                                    (const C2<double> *)psi, red.partials.p,
+                                                    red.counter.p, red.out.p);
+  NOSH_CUDA(cudaGetLastError());
+  double e = 0.0;
+  red.out.download(&e, 1, stream);
+  sync();
+  return e / cv_sum;
+}
+
+void NlsImpl::export_values(const C2<double> *offdiag, const double *diag, double *out) {
+  export_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_rp.p, mesh->d_ci.p, offdiag, diag,
+                                                     (C2<double> *)out);
+  NOSH_CUDA(cudaGetLastError());
+}
+
+}  // namespace nosh

@@ -347,3 +347,38 @@ def real_graph_from_complex(row_ptr, cols):
         out[rp[2 * i] : rp[2 * i + 1]] = pair
         out[rp[2 * i + 1] : rp[2 * i + 2]] = pair
     return rp, out
+
+
+# --------------------------------------------------------------------------
+# Newton with exact linear algebra (small cases): the converged-state oracle.
+def newton_exact(P: Problem, psi0, g, mu, tol=1e-12, max_it=30):
+    """Full-step Newton on F(psi) = 0 with MINRES preconditioned by an exact
+    LU of the regularised KEO (scipy), FP64.  The Jacobian is singular along
+    the gauge direction i*psi; MINRES handles the consistent singular system.
+    Returns (psi, [||F|| per step])."""
+    import scipy.sparse.linalg as spla
+
+    psi = np.array(psi0, dtype=np.float64, copy=True)
+    hist = [np.linalg.norm(P.compute_f(psi, g, mu))]
+    for _ in range(max_it):
+        if hist[-1] <= tol:
+            break
+        F = P.compute_f(psi, g, mu)
+        J = P.jac_csr_real(psi, g, mu)
+        lu = spla.splu(P.kreg_csr_real(psi, g, mu).tocsc())
+        M = spla.LinearOperator(J.shape, matvec=lu.solve)
+        dx, _ = spla.minres(J, -F, M=M, rtol=1e-13, maxiter=2000)
+        psi = psi + dx
+        hist.append(np.linalg.norm(P.compute_f(psi, g, mu)))
+    return psi, hist
+
+
+def align_phase(psi, ref):
+    """Rotate psi by the global phase that best matches ref (U(1) gauge)."""
+    z = psi[0::2] + 1j * psi[1::2]
+    zr = ref[0::2] + 1j * ref[1::2]
+    c = np.vdot(z, zr)
+    z = z * (c / abs(c))
+    out = np.empty_like(psi)
+    out[0::2], out[1::2] = z.real, z.imag
+    return out
