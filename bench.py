@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark: mu-continuation steps/s on the 64^3 Kuhn-tetrahedral GL mesh.
+
+Workload (one "step" = one natural continuation step): unit cube, 64^3 cubes
+x 6 Kuhn tetrahedra (274,625 vertices, 1,572,864 tets), interior vertices
+jittered +-0.1h (seed 2), A = 1/2 (-y, x, 0) sampled per vertex (B = (0,0,mu)),
+V = -1, g = 1, thickness 1; mu advances by 0.005 per step from mu = 0.5;
+each step predicts the state (phase-aligned secant predictor) and
+Newton-corrects it to ||F||_2 <= 1e-10 with AMG-preconditioned MINRES, in the
+mixed FP32 (operators, Krylov, AMG) / FP64 (residual, scalars) path.
+The synthetic mesh stands in for the reference's .h5m inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
+
+One JSON line is printed by rank 0.  ``--impl reference`` times the CPU FP64
+restatement of the same path (the reference's Trilinos path cannot be built)
+on the host cores.  With N > 1 GPUs each rank runs an independent replica
+(the single-mesh path does not shard; "replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "continuation steps/s, 64³ tet GL mesh, learned vs plain predictor at ‖F‖≤1e-10"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--m", type=int, default=64, help="cubes per side")
+    ap.add_argument("--mu0", type=float, default=0.5)
+    ap.add_argument("--dmu", type=float, default=0.005)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--predictor", default="secant", choices=["secant", "tangent", "none"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    return {
+        "workload": f"mu-continuation, {args.m}^3 Kuhn-tet unit cube (jittered 0.1h, seed 2), "
+        f"A=1/2(-y,x,0), V=-1, g=1, mu={args.mu0}+k*{args.dmu}, Newton to ||F||_2<=1e-10",
+        "mesh_cubes": args.m,
+        "dmu": args.dmu,
+        "mu0": args.mu0,
+        "precision": args.precision,
+        "predictor": args.predictor,
+    }
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- helpers
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic():
+    """dram read+write bytes per launch of the timed kernel from the committed
+    ncu summary (profiles/traffic.txt: `<kernel> <bytes per launch>` lines)."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    out = {}
+    try:
+        with open(p) as f:
+            for ln in f:
+                ln = ln.split("#")[0].split()
+                if len(ln) == 2:
+                    out[ln[0]] = float(ln[1])
+    except OSError:
+        pass
+    return out
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------- CPU arm
+def cpu_run(args, steps, time_budget=None, x=None, cells=None, psi0=None):
+    """The CPU FP64 restatement (oracle/nosh_solver.c, OpenMP over the host
+    cores): a Newton solve at mu0 (untimed), then continuation steps."""
+    from oracle import oracle as O
+
+    if x is None:
+        from nosh_gb300 import meshgen
+
+        x, cells, psi0 = meshgen.cube(args.m, 2)
+    m = O.finish_mesh(x, cells)
+    P = O.Problem(m, O.mvp_constant_curl(m.x))
+    S = O.CpuSolver(P)
+    cur = psi0.copy()
+    st = S.newton(cur, args.mu0)
+    assert st["status"] == 0, st
+    prev = cur.copy()
+    st = S.continuation_step(cur, None, args.mu0 + args.dmu, args.mu0, float("nan"))
+    mus = [args.mu0, args.mu0 + args.dmu]
+    times, its = [], []
+    t_start = time.perf_counter()
+    for k in range(steps):
+        mu_new = mus[-1] + args.dmu
+        t0 = time.perf_counter()
+        st = S.continuation_step(cur, prev, mu_new, mus[-1], mus[-2])
+        times.append(time.perf_counter() - t0)
+        its.append((st["newton_iters"], st["krylov_iters"]))
+        assert st["status"] == 0 and st["f_norm"] <= 1e-10, st
+        mus.append(mu_new)
+        if time_budget and time.perf_counter() - t_start > time_budget and k >= 0:
+            break
+    return times, its, S.threads()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    times, its, threads = cpu_run(args, args.warmup + args.steps, time_budget=240.0)
+    timed = times[min(args.warmup, len(times) - 1):] if len(times) > args.warmup else times
+    ms = 1000.0 * float(np.mean(timed))
+    val = 1000.0 / ms
+    sample = f"{len(timed)} continuation steps after {len(times) - len(timed)} warm-up, FP64, {threads} threads"
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": val,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": len(timed),
+        "warmup": len(times) - len(timed),
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": workload(args) | {"precision": "fp64", "solver": "CPU restatement (oracle/nosh_solver.c)"},
+        "cpu_baseline": {"value": val, "unit": "steps/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    import nosh_gb300 as ng
+    from nosh_gb300 import meshgen
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x, cells, psi0 = meshgen.cube(args.m, 2)
+    A = meshgen.mvp_constant_curl(x)
+    gm = ng.mesh(x, cells)
+    prec = ng.PREC_MIXED if args.precision == "mixed" else ng.PREC_FP64
+    model = ng.nls(gm, A, -1.0, 1.0, 1.0, mu=args.mu0, precision=prec)
+    pred = {"secant": ng.PREDICT_SECANT, "tangent": ng.PREDICT_TANGENT, "none": ng.PREDICT_NONE}[args.predictor]
+    stream = torch.cuda.ExternalStream(model.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+
+    def flush_l2():
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # -- device-resident state
+    cur = torch.tensor(psi0, dtype=torch.float64, device=dev)
+    prev = torch.empty_like(cur)
+    st = model.newton(cur, {"mu": args.mu0})
+    assert st["status"] == 0, st
+    mus = [args.mu0]
+    st = model.continuation_step(cur, prev, args.mu0 + args.dmu, args.mu0, predictor=ng.PREDICT_NONE)
+    mus.append(args.mu0 + args.dmu)
+
+    def step(xc, xp):
+        mu_new = mus[-1] + args.dmu
+        s = model.continuation_step(xc, xp, mu_new, mus[-1], mus[-2], predictor=pred)
+        assert s["status"] == 0 and s["f_norm"] <= 1e-10, s
+        mus.append(mu_new)
+        return s
+
+    for _ in range(args.warmup):
+        step(cur, prev)
+    # -- timed region: device-resident inputs, L2 flushed before every step
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    model.profile(True)
+    model.profile_read(ng.KERNEL_JACOBIAN)
+    model.profile_read(ng.KERNEL_SMOOTHER)
+    model.profile_read(ng.KERNEL_ALL)
+    its = []
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    for k in range(args.steps):
+        flush_l2()
+        ev[k][0].record(stream)
+        s = step(cur, prev)
+        ev[k][1].record(stream)
+        its.append((s["newton_iters"], s["krylov_iters"]))
+    barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    launches = model.profile_read(ng.KERNEL_ALL)[0]
+    jac = model.profile_read(ng.KERNEL_JACOBIAN)
+    smo = model.profile_read(ng.KERNEL_SMOOTHER)
+    model.profile(False)
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+
+    # -- e2e: the same steps through the C ABI with pinned HOST buffers
+    e2e = None
+    if not args.no_e2e:
+        hc = torch.empty(cur.numel(), dtype=torch.float64, pin_memory=True)
+        hp = torch.empty_like(hc, pin_memory=True)
+        hc.copy_(cur.cpu())
+        hp.copy_(prev.cpu())
+        hcn, hpn = hc.numpy(), hp.numpy()
+        tt = []
+        barrier()
+        for k in range(args.steps):
+            flush_l2()
+            t0 = time.perf_counter()
+            step(hcn, hpn)  # copies x, x_prev in and both out inside the call
+            tt.append(time.perf_counter() - t0)
+        e2e_ms = 1000.0 * float(np.mean(tt))
+        if world > 1:
+            t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        nbytes = cur.numel() * 8
+        e2e = {"value": world * 1000.0 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": 2 * nbytes,
+               "d2h_bytes_per_step": 2 * nbytes, "ms_per_step": e2e_ms}
+
+    # -- roofline of the dominant timed kernel class
+    peak, peak_kind = measured_peak()
+    traffic = profiled_traffic()
+    cands = {"smoother_spmv": smo, "jacobian_spmv": jac}
+    dom = max(cands, key=lambda k: cands[k][1])
+    n_l, ms_l, bytes_l = cands[dom]
+    roof = None
+    if n_l > 0 and ms_l > 0:
+        ach = (bytes_l / n_l) / (ms_l / n_l * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_kind": peak_kind, "kernel": dom, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
+                "algorithmic_bytes_per_launch": bytes_l / n_l, "traffic": traffic.get(dom)}
+    other = [k for k in cands if k != dom][0]
+    n_o, ms_o, b_o = cands[other]
+    secondary = None
+    if n_o > 0 and ms_o > 0:
+        a2 = (b_o / n_o) / (ms_o / n_o * 1e-3) / 1e9
+        secondary = {"kernel": other, "achieved": a2, "frac": a2 / peak, "launches": n_o,
+                     "avg_launch_us": 1000.0 * ms_o / n_o, "algorithmic_bytes_per_launch": b_o / n_o,
+                     "traffic": traffic.get(other)}
+
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic",
+        "config": workload(args) | {"l2": "flushed (256 MB write) before every timed step",
+                                    "parallelism": f"replicas x{world}"},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "roofline_secondary": secondary,
+        "clocks": clk,
+        "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
+    }
+    # -- CPU baseline: bounded sample of the same workload on the host cores
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        times, cits, threads = cpu_run(args, 1000, time_budget=args.cpu_seconds, x=x, cells=cells, psi0=psi0)
+        cv = 1.0 / float(np.mean(times))
+        out["cpu_baseline"] = {"value": cv, "unit": "steps/s", "cores": threads, "kind": "port",
+                               "sample": f"{len(times)} continuation steps of the same workload "
+                                         f"(FP64 CPU restatement, {threads} OpenMP threads)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -220,6 +220,41 @@ int nosh_newton_solve(nosh_nls nls, double *x, const double *p,
                       const nosh_newton_options *opt,
                       nosh_newton_stats *stats);
 
+/* ---------------------------------------------------------- continuation */
+#define NOSH_PREDICT_NONE 0    /* x(mu_new) = x(mu_cur)                      */
+#define NOSH_PREDICT_SECANT 1  /* LOCA "Secant" (examples/conf.xml:39-41)    */
+#define NOSH_PREDICT_TANGENT 2 /* LOCA "Tangent": x + dmu * (-J^-1 dF/dmu)   */
+
+/* One natural-parameter continuation step (LOCA stepper semantics,
+ * examples/conf.xml:35-75; driven by executables/nosh-cont/nosh-cont.cpp:
+ * 226-345): predict the state at p_new[1] = mu_new from the states at
+ * mu_cur and mu_prev, then Newton-correct it to opt->tol.
+ *   x       in: x(mu_cur)             out: x(mu_new)
+ *   x_prev  in: x(mu_prev)            out: x(mu_cur)     (secant only; may be
+ *           NULL for the other predictors)
+ * Predicted states are aligned in global phase first (the solutions are
+ * defined up to the U(1) gauge psi -> e^{i phi} psi).  stats->f_norm0 is the
+ * residual of the prediction. */
+int nosh_continuation_step(nosh_nls nls, double *x, double *x_prev,
+                           const double *p_new, double mu_cur, double mu_prev,
+                           int predictor, const nosh_newton_options *opt,
+                           nosh_newton_stats *stats);
+
+/* ------------------------------------------------------ kernel timing */
+#define NOSH_KERNEL_JACOBIAN 0 /* fine-level Jacobian apply (MINRES)       */
+#define NOSH_KERNEL_SMOOTHER 1 /* fine-level AMG smoothing/residual SpMVs  */
+#define NOSH_KERNEL_ALL 2      /* every kernel the handle launched (count
+                                  only; always on)                         */
+/* While enabled, every launch of the selected fine-level SpMV kernels is
+ * bracketed by CUDA events on the handle's stream. */
+int nosh_nls_profile_enable(nosh_nls nls, int enable);
+/* Launch count, summed device time and summed algorithmic bytes (the bytes
+ * the kernel must move at minimum: matrix, indices and vectors once each)
+ * of one kernel class since the last read; resets the counters.  For
+ * NOSH_KERNEL_ALL only the launch count is returned. */
+int nosh_nls_profile_read(nosh_nls nls, int kernel, int64_t *launches,
+                          double *total_ms, double *bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,7 +34,7 @@ LIB_PATH = os.path.join(_HERE, "libnosh_gb300.so")
 if not os.path.exists(LIB_PATH):
     raise ImportError(
         f"nosh_gb300: compiled library {LIB_PATH} is missing; build it with "
-        "`python -m nosh_gb300.build` (nvcc, sm_103a)"
+        "`python nosh_gb300/build.py` (nvcc, sm_103a)"
     )
 
 _lib = C.CDLL(LIB_PATH)
@@ -44,6 +44,8 @@ ERR_INVALID, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN = 1, 2, 3, 4, 5
 ERR_UNSUPPORTED, ERR_MESH, ERR_NO_MEMORY = 6, 7, 8
 PREC_FP64, PREC_MIXED = 0, 1
 NO_TRANS, TRANS = 0, 1
+PREDICT_NONE, PREDICT_SECANT, PREDICT_TANGENT = 0, 1, 2
+KERNEL_JACOBIAN, KERNEL_SMOOTHER, KERNEL_ALL = 0, 1, 2
 
 
 class NoshError(RuntimeError):
@@ -110,6 +112,10 @@ _SIGS = {
     "nosh_keo_regularized_operator_apply": (_I, [_P, _P, _P]),
     "nosh_newton_default_options": (None, [C.POINTER(NewtonOptions)]),
     "nosh_newton_solve": (_I, [_P, _P, _P, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
+    "nosh_continuation_step": (_I, [_P, _P, _P, _P, _D, _D, _I, C.POINTER(NewtonOptions),
+                                    C.POINTER(NewtonStats)]),
+    "nosh_nls_profile_enable": (_I, [_P, _I]),
+    "nosh_nls_profile_read": (_I, [_P, _I, C.POINTER(_I64), C.POINTER(_D), C.POINTER(_D)]),
 }
 for _name, (_res, _args) in _SIGS.items():
     _fn = getattr(_lib, _name)
@@ -360,19 +366,28 @@ class nls:
         _check(_lib.nosh_nls_inner_product(self._h, _ptr(_f64(phi)), _ptr(_f64(psi)), C.byref(out)))
         return out.value
 
+    # -- kernel timing (roofline figures)
+    def profile(self, enable: bool):
+        _check(_lib.nosh_nls_profile_enable(self._h, 1 if enable else 0))
+
+    def profile_read(self, kernel):
+        """(launches, total device ms, total algorithmic bytes) since the
+        last read of this kernel class; resets it."""
+        n, ms, b = C.c_int64(), C.c_double(), C.c_double()
+        _check(_lib.nosh_nls_profile_read(self._h, kernel, C.byref(n), C.byref(ms), C.byref(b)))
+        return n.value, ms.value, b.value
+
     # -- solvers
-    def newton(self, x, params, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000, precision=None,
-               verbose=0):
-        """Full-step inexact Newton with AMG-preconditioned MINRES; ``x`` is
-        updated in place (numpy array or device tensor).  Returns stats."""
+    def _options(self, tol, max_newton, forcing, max_krylov, precision, verbose):
         o = NewtonOptions()
         _lib.nosh_newton_default_options(C.byref(o))
         o.tol, o.max_newton, o.forcing, o.max_krylov = tol, max_newton, forcing, max_krylov
         o.precision = self.precision if precision is None else precision
         o.verbose = verbose
-        st = NewtonStats()
-        rc = _lib.nosh_newton_solve(self._h, _ptr(x), _ptr(self._pvec(params)), C.byref(o), C.byref(st))
-        _check(rc, allow=(ERR_NOT_CONVERGED,))
+        return o
+
+    @staticmethod
+    def _stats(st):
         return {
             "newton_iters": st.newton_iters,
             "krylov_iters": st.krylov_iters,
@@ -380,3 +395,27 @@ class nls:
             "f_norm0": st.f_norm0,
             "status": st.status,
         }
+
+    def continuation_step(self, x, x_prev, mu_new, mu_cur, mu_prev=float("nan"), predictor=PREDICT_SECANT,
+                          params=None, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000, precision=None,
+                          verbose=0):
+        """One natural continuation step to ``mu_new`` (LOCA stepper);
+        ``x`` (state at ``mu_cur``) becomes the state at ``mu_new`` and
+        ``x_prev`` (state at ``mu_prev``) becomes the state at ``mu_cur``."""
+        p = self._pvec({**(params or {}), "mu": mu_new})
+        o = self._options(tol, max_newton, forcing, max_krylov, precision, verbose)
+        st = NewtonStats()
+        rc = _lib.nosh_continuation_step(self._h, _ptr(x), _ptr(x_prev), _ptr(p), mu_cur, mu_prev, predictor,
+                                         C.byref(o), C.byref(st))
+        _check(rc, allow=(ERR_NOT_CONVERGED,))
+        return self._stats(st)
+
+    def newton(self, x, params, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000, precision=None,
+               verbose=0):
+        """Full-step inexact Newton with AMG-preconditioned MINRES; ``x`` is
+        updated in place (numpy array or device tensor).  Returns stats."""
+        o = self._options(tol, max_newton, forcing, max_krylov, precision, verbose)
+        st = NewtonStats()
+        rc = _lib.nosh_newton_solve(self._h, _ptr(x), _ptr(self._pvec(params)), C.byref(o), C.byref(st))
+        _check(rc, allow=(ERR_NOT_CONVERGED,))
+        return self._stats(st)

@@ -607,20 +607,26 @@ void Amg::refresh() {
       AmgLevel &F = I.lev[l - 1];
       rap_offdiag<T><<<div_up(std::max<int64_t>(A.nnz, 1), 256), 256, 0, st>>>(
           A.nnz, F.seg_ptr.p, F.seg_idx.p, I.off<T>(l - 1), V.off[l].p);
+      ++I.nls.launch_count;
       rap_diag<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, F.mem_ptr.p, F.mem_idx.p, F.intra_ptr.p,
                                                      F.intra_idx.p, I.dia<T>(l - 1), I.off<T>(l - 1),
                                                      V.dia[l].p);
+      ++I.nls.launch_count;
     }
     dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
                                                           V.dinv[l].p, I.lmax_bits.p + l);
+    ++I.nls.launch_count;
     cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1),
                                     V.coef[l].p, I.lmax.p + l);
+    ++I.nls.launch_count;
   }
   const AmgLevel &C = I.lev.back();
   const int m2 = (int)(2 * C.n);
   coarse_dense<T><<<div_up(C.n, 128), 128, 0, st>>>(C.n, C.rp, C.ci, I.off<T>(L - 1), I.dia<T>(L - 1),
                                                      I.dense.p);
+  ++I.nls.launch_count;
   gauss_jordan_spd<<<1, 256, 0, st>>>(m2, I.dense.p, I.densef.p, I.err.p);
+  ++I.nls.launch_count;
   NOSH_CUDA(cudaGetLastError());
   int herr = 0;
   I.err.download(&herr, 1, st);
@@ -630,7 +636,7 @@ void Amg::refresh() {
 
 template <typename T, class Op>
 static void launch_level_rows(const AmgLevel &A, const C2<T> *off, const C2<T> *x, const Op &op,
-                              cudaStream_t st, int cap) {
+                              cudaStream_t st, int cap, int64_t &launches) {
   static bool attr = false;
   if (!attr) {
     NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -640,6 +646,7 @@ static void launch_level_rows(const AmgLevel &A, const C2<T> *off, const C2<T> *
   const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
   row_block_apply<T, Op><<<div_up(A.n, kRows), kRows, smem, st>>>((int)A.n, A.rp, A.ci, off, x, cap, op,
                                                                  nullptr, nullptr, nullptr);
+  ++launches;
 }
 
 template <typename T>
@@ -654,6 +661,7 @@ void Amg::Impl::vcycle(int l, const C2<T> *b, C2<T> *x) {
     const int m2 = (int)(2 * A.n);
     const T *Ainv = sizeof(T) == 4 ? (const T *)densef.p : (const T *)dense.p;
     dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, Ainv, (const T *)b, (T *)x);
+    ++nls.launch_count;
     return;
   }
   const int deg = std::max(opt.smooth_degree, 1);
@@ -663,24 +671,40 @@ void Amg::Impl::vcycle(int l, const C2<T> *b, C2<T> *x) {
   C2<T> *cur = (deg % 2 == 1) ? x : V.x2[l].p;
   C2<T> *oth = (deg % 2 == 1) ? V.x2[l].p : x;
   cheb_first<T><<<div_up(A.n, B), B, 0, st>>>(A.n, V.dinv[l].p, V.coef[l].p, b, V.d[l].p, cur);
+  ++nls.launch_count;
+  // fine-level SpMV launches are timed when profiling is on; algorithmic
+  // bytes per vertex: Chebyshev x_in, diag, b, D^-1, d (r+w), x_out;
+  // residual x, diag, b, res
+  const int vb = (int)sizeof(T);
+  KernelTimer *tm = l == 0 ? &nls.timers[NOSH_KERNEL_SMOOTHER] : nullptr;
+  const double cheb_bytes = nls.spmv_bytes(2 * vb, 16 * vb);
+  const double res_bytes = nls.spmv_bytes(2 * vb, 9 * vb);
   for (int k = 1; k < deg; k++) {
     ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
-    launch_level_rows<T>(A, ov, cur, op, st, cap);
+    if (tm) tm->begin(st);
+    launch_level_rows<T>(A, ov, cur, op, st, cap, nls.launch_count);
+    if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
   // cur == x here
   ResidOp<T> rop{dv, b, x, V.res[l].p};
-  launch_level_rows<T>(A, ov, x, rop, st, cap);
+  if (tm) tm->begin(st);
+  launch_level_rows<T>(A, ov, x, rop, st, cap, nls.launch_count);
+  if (tm) tm->end(st, res_bytes);
   const AmgLevel &Cl = lev[l + 1];
   restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p, V.b[l + 1].p);
+  ++nls.launch_count;
   vcycle<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p);
   prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x);
+  ++nls.launch_count;
   // post-smoothing: same polynomial, now from the corrected x
   cur = x;
   oth = V.x2[l].p;
   for (int k = 0; k < deg; k++) {
     ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
-    launch_level_rows<T>(A, ov, cur, op, st, cap);
+    if (tm) tm->begin(st);
+    launch_level_rows<T>(A, ov, cur, op, st, cap, nls.launch_count);
+    if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
   if (cur != x)

@@ -519,4 +519,52 @@ int nosh_newton_solve(nosh_nls nls, double *x, const double *p, const nosh_newto
   return rc;
 }
 
+int nosh_continuation_step(nosh_nls nls, double *x, double *x_prev, const double *p_new,
+                           double mu_cur, double mu_prev, int predictor,
+                           const nosh_newton_options *opt, nosh_newton_stats *stats) {
+  nosh_newton_stats st{};
+  int rc = guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p_new, g, mu);
+    require(predictor >= NOSH_PREDICT_NONE && predictor <= NOSH_PREDICT_TANGENT, "unknown predictor");
+    require(x != nullptr, "null state");
+    require(predictor != NOSH_PREDICT_SECANT || x_prev != nullptr, "secant predictor needs x_prev");
+    nosh_newton_options o;
+    nosh_newton_default_options(&o);
+    if (opt) o = *opt;
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0, "bad solver options");
+    nosh::continuation_step(s, x, x_prev, g, mu, mu_cur, mu_prev, predictor, o, st);
+  });
+  if (rc == NOSH_OK) rc = st.status;
+  if (stats) *stats = st;
+  return rc;
+}
+
+int nosh_nls_profile_enable(nosh_nls nls, int enable) {
+  return guarded([&] {
+    auto &s = N(nls);
+    for (auto &t : s.timers) t.on = enable != 0;
+  });
+}
+
+int nosh_nls_profile_read(nosh_nls nls, int kernel, int64_t *launches, double *total_ms,
+                          double *bytes) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(kernel >= NOSH_KERNEL_JACOBIAN && kernel <= NOSH_KERNEL_ALL, "unknown kernel class");
+    int64_t n = 0;
+    double ms = 0.0, b = 0.0;
+    if (kernel == NOSH_KERNEL_ALL) {
+      n = s.launch_count;
+      s.launch_count = 0;
+    } else {
+      s.timers[kernel].read(n, ms, b);
+    }
+    if (launches) *launches = n;
+    if (total_ms) *total_ms = ms;
+    if (bytes) *bytes = b;
+  });
+}
+
 }  // extern "C"

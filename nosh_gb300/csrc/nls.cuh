@@ -28,6 +28,50 @@ struct Reducer {
 
 struct Amg;  // aggregation AMG hierarchy (amg.cu)
 
+// Event pairs around the launches of one kernel class (roofline timing).
+struct KernelTimer {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;  // start, stop, start, stop, ...
+  size_t used = 0;
+  int64_t launches = 0;
+  double bytes = 0.0;
+  void begin(cudaStream_t s) {
+    if (!on) return;
+    if (used + 2 > ev.size()) {
+      for (int k = 0; k < 2; k++) {
+        cudaEvent_t e;
+        NOSH_CUDA(cudaEventCreate(&e));
+        ev.push_back(e);
+      }
+    }
+    NOSH_CUDA(cudaEventRecord(ev[used], s));
+  }
+  void end(cudaStream_t s, double b) {
+    if (!on) return;
+    NOSH_CUDA(cudaEventRecord(ev[used + 1], s));
+    used += 2;
+    launches++;
+    bytes += b;
+  }
+  void read(int64_t &n, double &ms, double &b) {
+    ms = 0.0;
+    for (size_t k = 0; k < used; k += 2) {
+      NOSH_CUDA(cudaEventSynchronize(ev[k + 1]));
+      float t = 0.f;
+      NOSH_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      ms += t;
+    }
+    n = launches;
+    b = bytes;
+    used = 0;
+    launches = 0;
+    bytes = 0.0;
+  }
+  ~KernelTimer() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+};
+
 struct NlsImpl {
   MeshImpl *mesh;
   int64_t N, E;
@@ -63,6 +107,13 @@ struct NlsImpl {
   int cap32 = 0, cap64 = 0;  // staged nonzeros per row block (FP32 / FP64)
 
   std::unique_ptr<Amg> amg;
+  KernelTimer timers[2];  // NOSH_KERNEL_JACOBIAN, NOSH_KERNEL_SMOOTHER
+  mutable int64_t launch_count = 0;  // kernels launched by this handle
+  // algorithmic bytes of one fine-level SpMV launch: matrix + indices once,
+  // plus `vec_bytes_per_vertex` of vector traffic per vertex
+  double spmv_bytes(int value_bytes, int vec_bytes_per_vertex) const {
+    return 4.0 * (N + 1) + (4.0 + value_bytes) * 2.0 * E + (double)vec_bytes_per_vertex * N;
+  }
   std::shared_ptr<void> solver_state;  // Newton / MINRES work space (solver.cu)
 
   NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, double g,

@@ -244,6 +244,7 @@ void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &o
   row_block_apply<T, Op><<<grid, kRows, smem, s.stream>>>(
       (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, x, cap, op, s.red.partials.p,
       s.red.counter.p, red_out);
+  ++s.launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
 
@@ -279,9 +280,11 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
   edge_fields_kernel<<<div_up(E, 256), 256, 0, s>>>(E, m->d_edges.p, m->d_x.p, d_A.p, m->d_len.p,
                                                      m->d_covol.p, d_t.p, d_p.p, d_alpha.p, d_pf.p,
                                                      d_alphaf.p);
+  ++launch_count;
   vertex_fields_kernel<<<div_up(N, 256), 256, 0, s>>>(N, m->d_rp.p, m->d_nz_edge.p, d_alpha.p,
                                                        m->d_cv.p, d_t.p, d_kdiag.p, d_kdiagf.p,
                                                        d_cvt.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   const size_t nz = 2 * E + kPad;
   d_keo64.alloc(nz);
@@ -315,9 +318,11 @@ NlsImpl::~NlsImpl() {
 void NlsImpl::keo_refill(double mu) {
   keo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, mesh->d_pos_fwd.p,
                                                       mesh->d_pos_bwd.p, d_keo64.p);
+  ++launch_count;
   keo_assemble32<<<div_up(E, 256), 256, 0, stream>>>(E, d_alphaf.p, d_pf.p, (float)mu,
                                                       mesh->d_pos_fwd.p, mesh->d_pos_bwd.p,
                                                       d_keo32.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   keo_mu = mu;
 }
@@ -326,6 +331,7 @@ void NlsImpl::dkeo_refill(double mu) {
   dkeo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(
       E, d_alpha.p, d_p.p, mu, deriv_param == "mu" ? 1.0 : 0.0, mesh->d_pos_fwd.p,
       mesh->d_pos_bwd.p, d_dkeo64.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   dkeo_mu = mu;
 }
@@ -359,6 +365,7 @@ void NlsImpl::dfdp64(const double *x, double g, double mu, int param, double *ou
   dkeo_apply64(x, out);
   dfdp_diag_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_cvt.p, param == 0 ? 1 : 0,
                                                         (const C2<double> *)x, (C2<double> *)out);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
 
@@ -366,6 +373,7 @@ void NlsImpl::jac_rebuild(const double *x, double g, double mu) {
   if (!(keo_mu == mu)) keo_refill(mu);
   jac_diag_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_kdiag.p, d_cvt.p, d_V.p, g,
                                                        (const C2<double> *)x, d_jd64.p, d_jd32.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   jac_ready = true;
 }
@@ -374,6 +382,7 @@ void NlsImpl::reg_rebuild(const double *x, double g, double mu) {
   if (!(keo_mu == mu)) keo_refill(mu);
   reg_diag_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_kdiag.p, d_cvt.p, g,
                                                        (const C2<double> *)x, d_rd64.p, d_rd32.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   reg_g = g;
   reg_ready = true;
@@ -420,6 +429,7 @@ void NlsImpl::reg_apply<float>(const float *x, float *y) {
 double NlsImpl::energy(const double *psi) {
   energy_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_cv.p, (const C2<double> *)psi,
                                                      red.partials.p, red.counter.p, red.out.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   double e = 0.0;
   red.out.download(&e, 1, stream);
@@ -431,6 +441,7 @@ double NlsImpl::inner_product(const double *phi, const double *psi) {
   inner_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_cv.p, (const C2<double> *)phi,
                                                     (const C2<double> *)psi, red.partials.p,
                                                     red.counter.p, red.out.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   double e = 0.0;
   red.out.download(&e, 1, stream);
@@ -441,6 +452,7 @@ double NlsImpl::inner_product(const double *phi, const double *psi) {
 void NlsImpl::export_values(const C2<double> *offdiag, const double *diag, double *out) {
   export_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_rp.p, mesh->d_ci.p, offdiag, diag,
                                                      (C2<double> *)out);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
 

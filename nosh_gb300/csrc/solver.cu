@@ -176,20 +176,28 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
   T *wa = w0.p, *wb = w1.p, *wc = w2.p;  // (w1, w2, w) of the recurrence
   s.amg->apply<T>(pr2, zc);
   dot_kernel<T><<<G, 256, 0, st>>>(n2, pr2, zc, s.red.partials.p, s.red.counter.p, &d->rz);
+  ++s.launch_count;
   minres_init<<<1, 1, 0, st>>>(d, rtol, maxit);
+  ++s.launch_count;
   NOSH_CUDA(cudaGetLastError());
   const int check_every = 4;
   int it = 0;
   for (;;) {
     for (int k = 0; k < check_every; k++, it++) {
-      // u = J z, <z, u>
+      // u = J z, <z, u>   (bytes per vertex: x, diag block, y)
+      s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
       s.jac_apply<T>(zc, u.p, &d->zu);
+      s.timers[NOSH_KERNEL_JACOBIAN].end(st, s.spmv_bytes(2 * sizeof(T), 7 * sizeof(T)));
       lanczos_update<T><<<G, 256, 0, st>>>(n2, d, u.p, pr1, pr2);
+      ++s.launch_count;
       std::swap(pr1, pr2);  // r2 = r_new, r1 = previous r2
       s.amg->apply<T>(pr2, zn);
       dot_kernel<T><<<G, 256, 0, st>>>(n2, pr2, zn, s.red.partials.p, s.red.counter.p, &d->rz);
+      ++s.launch_count;
       minres_scalars<<<1, 1, 0, st>>>(d);
+      ++s.launch_count;
       minres_wx<T><<<G, 256, 0, st>>>(n2, d, zc, wa, wb, wc, x.p);
+      ++s.launch_count;
       // (w1, w2, w) <- (w2, w, w_new)
       T *t = wa;
       wa = wb;
@@ -213,19 +221,59 @@ template struct Minres<double>;
 // ------------------------------------------------------------------ Newton
 namespace {
 struct NewtonState {
-  DevBuf<double> psi, f;
+  DevBuf<double> psi, f, xc, xp, tmp;  // working state, residual, staged inputs
   DevBuf<float> b32;
   DevBuf<double> b64;
+  DevBuf<double> red2;  // complex reduction (phase alignment)
   std::unique_ptr<Minres<float>> m32;
   std::unique_ptr<Minres<double>> m64;
 };
+
+// c = sum conj(a_i) b_i (complex), deterministic two-slot reduction
+__global__ void cdot_kernel(int64_t n, const C2<double> *__restrict__ a,
+                            const C2<double> *__restrict__ b, double *partials,
+                            unsigned *counter, double *out) {
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> x = a[i], y = b[i];
+    re += x.x * y.x + x.y * y.y;
+    im += x.x * y.y - x.y * y.x;
+  }
+  grid_reduce(re, partials, counter, out);
+  grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
+}
+
+// secant prediction x_new = x + r (x - e^{i phi} x_prev), phi aligning
+// x_prev to x; x_prev <- x
+__global__ void secant_kernel(int64_t n, const double *__restrict__ c, double r,
+                              C2<double> *__restrict__ xn, C2<double> *__restrict__ x,
+                              C2<double> *__restrict__ xp) {
+  const double m = sqrt(c[0] * c[0] + c[1] * c[1]);
+  const double er = m > 0 ? c[0] / m : 1.0, ei = m > 0 ? c[1] / m : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> a = x[i], p = xp[i];
+    const double pr = er * p.x - ei * p.y, pi = er * p.y + ei * p.x;
+    xn[i] = C2<double>{a.x + r * (a.x - pr), a.y + r * (a.y - pi)};
+    xp[i] = a;
+  }
+}
+
+template <typename T>
+__global__ void axpy_to(int64_t n, double a, const T *__restrict__ t, const double *__restrict__ x,
+                        double *__restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = x[i] + a * (double)t[i];
+}
 }  // namespace
 
 static NewtonState &state_of(NlsImpl &s) {
   if (!s.solver_state) {
     auto *ns = new NewtonState();
-    ns->psi.alloc(2 * s.N);
-    ns->f.alloc(2 * s.N);
+    for (DevBuf<double> *b : {&ns->psi, &ns->f, &ns->xc, &ns->xp, &ns->tmp}) b->alloc(2 * s.N);
+    ns->red2.alloc(2);
     s.solver_state = std::shared_ptr<void>(ns, [](void *p) { delete (NewtonState *)p; });
   }
   return *(NewtonState *)s.solver_state.get();
@@ -239,23 +287,48 @@ static double residual_norm(NlsImpl &s, const double *psi, double g, double mu, 
   return std::sqrt(n2);
 }
 
+// Refresh the Jacobian and the preconditioner at (psi, g, mu) in precision T.
+template <typename T>
+static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu) {
+  s.jac_rebuild(psi, g, mu);
+  s.reg_rebuild(psi, g, mu);
+  if (!s.amg) s.amg.reset(new Amg(s));
+  s.amg->refresh<T>();
+}
+
+template <typename T>
+static Minres<T> &minres_of(NlsImpl &s, NewtonState &ns);
+template <>
+Minres<float> &minres_of<float>(NlsImpl &s, NewtonState &ns) {
+  if (!ns.m32) ns.m32.reset(new Minres<float>(s));
+  if (ns.b32.n < (size_t)(2 * s.N)) ns.b32.alloc(2 * s.N);
+  return *ns.m32;
+}
+template <>
+Minres<double> &minres_of<double>(NlsImpl &s, NewtonState &ns) {
+  if (!ns.m64) ns.m64.reset(new Minres<double>(s));
+  if (ns.b64.n < (size_t)(2 * s.N)) ns.b64.alloc(2 * s.N);
+  return *ns.m64;
+}
+template <typename T> static DevBuf<T> &rhs_of(NewtonState &ns);
+template <> DevBuf<float> &rhs_of<float>(NewtonState &ns) { return ns.b32; }
+template <> DevBuf<double> &rhs_of<double>(NewtonState &ns) { return ns.b64; }
+
+// Newton on ns.psi (device), residual already in ns.f with norm st.f_norm0.
 template <typename T>
 static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
-                        const nosh_newton_options &opt, nosh_newton_stats &st,
-                        std::unique_ptr<Minres<T>> &mr, DevBuf<T> &b) {
-  if (!mr) mr.reset(new Minres<T>(s));
-  if (b.n < (size_t)(2 * s.N)) b.alloc(2 * s.N);
+                        const nosh_newton_options &opt, nosh_newton_stats &st) {
+  Minres<T> &mr = minres_of<T>(s, ns);
+  DevBuf<T> &b = rhs_of<T>(ns);
   const int64_t n2 = 2 * s.N;
   const int G = vec_grid(n2);
   // FP32 Krylov cannot resolve relative residuals much below ~1e-6
   const double eta_min = sizeof(T) == 4 ? 1e-6 : 1e-12;
   double fn = st.f_norm0, fn_prev = fn;
   for (int it = 0; it < opt.max_newton && fn > opt.tol; it++) {
-    s.jac_rebuild(ns.psi.p, g, mu);
-    s.reg_rebuild(ns.psi.p, g, mu);
-    if (!s.amg) s.amg.reset(new Amg(s));
-    s.amg->refresh<T>();
+    rebuild_operators<T>(s, ns.psi.p, g, mu);
     neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.f.p, b.p);
+    ++s.launch_count;
     double eta;
     if (opt.forcing > 0) {
       eta = opt.forcing;
@@ -268,13 +341,14 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     eta = std::max(eta, eta_min);
     int status = 0;
     double rel = 0.0;
-    const int its = mr->solve(b.p, eta, opt.max_krylov, status, rel);
+    const int its = mr.solve(b.p, eta, opt.max_krylov, status, rel);
     st.krylov_iters += its;
     if (status == NOSH_ERR_NAN || status == NOSH_ERR_BREAKDOWN) {
       st.status = status;
       return;
     }
-    axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr->x.p, ns.psi.p);
+    axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, ns.psi.p);
+    ++s.launch_count;
     fn_prev = fn;
     fn = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
     st.newton_iters = it + 1;
@@ -289,20 +363,81 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
   }
 }
 
+static void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
+                        nosh_newton_stats &st) {
+  st = nosh_newton_stats{};
+  st.f_norm0 = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+  st.f_norm = st.f_norm0;
+  NOSH_CHECK(!std::isnan(st.f_norm0), NOSH_ERR_NAN, "initial residual is NaN");
+  if (opt.precision == NOSH_PREC_FP64) newton_loop<double>(s, ns, g, mu, opt, st);
+  else newton_loop<float>(s, ns, g, mu, opt, st);
+  if (st.status == NOSH_OK && !(st.f_norm <= opt.tol)) st.status = NOSH_ERR_NOT_CONVERGED;
+}
+
 void newton_solve(NlsImpl &s, double *x_user, double g, double mu, const nosh_newton_options &opt,
                   nosh_newton_stats &st) {
   NewtonState &ns = state_of(s);
   const size_t bytes = 2 * s.N * sizeof(double);
   NOSH_CUDA(cudaMemcpyAsync(ns.psi.p, x_user, bytes, cudaMemcpyDefault, s.stream));
-  st = nosh_newton_stats{};
-  st.f_norm0 = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
-  st.f_norm = st.f_norm0;
-  NOSH_CHECK(!std::isnan(st.f_norm0), NOSH_ERR_NAN, "initial residual is NaN");
-  if (opt.precision == NOSH_PREC_FP64) newton_loop<double>(s, ns, g, mu, opt, st, ns.m64, ns.b64);
-  else newton_loop<float>(s, ns, g, mu, opt, st, ns.m32, ns.b32);
+  newton_core(s, ns, g, mu, opt, st);
   NOSH_CUDA(cudaMemcpyAsync(x_user, ns.psi.p, bytes, cudaMemcpyDefault, s.stream));
   s.sync();
-  if (st.status == NOSH_OK && !(st.f_norm <= opt.tol)) st.status = NOSH_ERR_NOT_CONVERGED;
+}
+
+template <typename T>
+static void tangent_predict(NlsImpl &s, NewtonState &ns, double g, double mu_cur, double dmu,
+                            const nosh_newton_options &opt, nosh_newton_stats &st) {
+  // dx/dmu = -J^-1 dF/dmu at (x, mu_cur) (LOCA tangent predictor; dF/dmu is
+  // DkeoDP x, src/model_evaluator_nls.cpp:632-695)
+  Minres<T> &mr = minres_of<T>(s, ns);
+  DevBuf<T> &b = rhs_of<T>(ns);
+  const int64_t n2 = 2 * s.N;
+  const int G = vec_grid(n2);
+  rebuild_operators<T>(s, ns.xc.p, g, mu_cur);
+  s.dfdp64(ns.xc.p, g, mu_cur, 1, ns.tmp.p);
+  neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.tmp.p, b.p);
+  ++s.launch_count;
+  int status = 0;
+  double rel = 0.0;
+  st.krylov_iters += mr.solve(b.p, sizeof(T) == 4 ? 1e-5 : 1e-8, opt.max_krylov, status, rel);
+  NOSH_CHECK(status != NOSH_ERR_NAN && status != NOSH_ERR_BREAKDOWN, status, "tangent solve failed");
+  axpy_to<T><<<G, 256, 0, s.stream>>>(n2, dmu, mr.x.p, ns.xc.p, ns.psi.p);
+  ++s.launch_count;
+}
+
+void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double mu_new, double mu_cur,
+                       double mu_prev, int predictor, const nosh_newton_options &opt,
+                       nosh_newton_stats &st) {
+  NewtonState &ns = state_of(s);
+  const size_t bytes = 2 * s.N * sizeof(double);
+  const int64_t n2 = 2 * s.N;
+  const int G = vec_grid(n2);
+  cudaStream_t st_ = s.stream;
+  NOSH_CUDA(cudaMemcpyAsync(ns.xc.p, x, bytes, cudaMemcpyDefault, st_));
+  nosh_newton_stats pst{};
+  if (predictor == NOSH_PREDICT_SECANT && x_prev && mu_cur != mu_prev && !std::isnan(mu_prev)) {
+    NOSH_CUDA(cudaMemcpyAsync(ns.xp.p, x_prev, bytes, cudaMemcpyDefault, st_));
+    cdot_kernel<<<G, 256, 0, st_>>>(s.N, (const C2<double> *)ns.xp.p, (const C2<double> *)ns.xc.p,
+                                    s.red.partials.p, s.red.counter.p, ns.red2.p);
+    ++s.launch_count;
+    secant_kernel<<<G, 256, 0, st_>>>(s.N, ns.red2.p, (mu_new - mu_cur) / (mu_cur - mu_prev),
+                                      (C2<double> *)ns.psi.p, (C2<double> *)ns.xc.p,
+                                      (C2<double> *)ns.xp.p);
+    ++s.launch_count;
+    NOSH_CUDA(cudaGetLastError());
+    NOSH_CUDA(cudaMemcpyAsync(x_prev, ns.xp.p, bytes, cudaMemcpyDefault, st_));
+  } else if (predictor == NOSH_PREDICT_TANGENT) {
+    if (opt.precision == NOSH_PREC_FP64) tangent_predict<double>(s, ns, g, mu_cur, mu_new - mu_cur, opt, pst);
+    else tangent_predict<float>(s, ns, g, mu_cur, mu_new - mu_cur, opt, pst);
+    if (x_prev) NOSH_CUDA(cudaMemcpyAsync(x_prev, ns.xc.p, bytes, cudaMemcpyDefault, st_));
+  } else {
+    NOSH_CUDA(cudaMemcpyAsync(ns.psi.p, ns.xc.p, bytes, cudaMemcpyDeviceToDevice, st_));
+    if (x_prev) NOSH_CUDA(cudaMemcpyAsync(x_prev, ns.xc.p, bytes, cudaMemcpyDefault, st_));
+  }
+  newton_core(s, ns, g, mu_new, opt, st);
+  st.krylov_iters += pst.krylov_iters;
+  NOSH_CUDA(cudaMemcpyAsync(x, ns.psi.p, bytes, cudaMemcpyDefault, st_));
+  s.sync();
 }
 
 }  // namespace nosh

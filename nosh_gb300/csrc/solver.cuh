@@ -31,5 +31,8 @@ struct Minres {
 
 void newton_solve(NlsImpl &s, double *x_user, double g, double mu,
                   const nosh_newton_options &opt, nosh_newton_stats &st);
+void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double mu_new,
+                       double mu_cur, double mu_prev, int predictor,
+                       const nosh_newton_options &opt, nosh_newton_stats &st);
 
 }  // namespace nosh

@@ -103,6 +103,25 @@ double nor_energy(int64_t N, const double *cv, const double *psi);
 double nor_inner_product(int64_t N, const double *cv, const double *phi,
                          const double *psi);
 
+/* ---- CPU solver (nosh_solver.c): Newton / MINRES / AMG / continuation -- */
+#define NOSH_ERR_NOT_CONVERGED_ORACLE 3
+#define NOSH_ERR_BREAKDOWN_ORACLE 5
+typedef struct nor_solver nor_solver;
+nor_solver *nor_solver_create(int64_t N, int64_t E, const int32_t *edges,
+                              const double *alpha, const double *p,
+                              const double *cv, const double *t,
+                              const double *V, double g);
+void nor_solver_destroy(nor_solver *s);
+int nor_num_threads(void);
+int nor_newton(nor_solver *s, double *psi, double mu, double tol,
+               int max_newton, int *newton_its, int *krylov_its,
+               double *fnorm0, double *fnorm);
+int nor_continuation_step(nor_solver *s, double *x, double *x_prev,
+                          double mu_new, double mu_cur, double mu_prev,
+                          double tol, int *newton_its, int *krylov_its,
+                          double *fnorm0, double *fnorm);
+int nor_amg_levels(const nor_solver *s, int64_t *sizes);
+
 #ifdef __cplusplus
 }
 #endif

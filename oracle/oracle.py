@@ -65,6 +65,14 @@ def lib():
             "nor_kreg_apply": (None, [I64, I64, i32p, f64p, f64p, F64, F64, f64p, f64p, f64p, f64p, f64p]),
             "nor_energy": (F64, [I64, f64p, f64p]),
             "nor_inner_product": (F64, [I64, f64p, f64p, f64p]),
+            "nor_solver_create": (C.c_void_p, [I64, I64, i32p, f64p, f64p, f64p, f64p, f64p, F64]),
+            "nor_solver_destroy": (None, [C.c_void_p]),
+            "nor_num_threads": (I, []),
+            "nor_newton": (I, [C.c_void_p, f64p, F64, F64, I, C.POINTER(I), C.POINTER(I),
+                               C.POINTER(F64), C.POINTER(F64)]),
+            "nor_continuation_step": (I, [C.c_void_p, f64p, C.c_void_p, F64, F64, F64, F64, C.POINTER(I),
+                                          C.POINTER(I), C.POINTER(F64), C.POINTER(F64)]),
+            "nor_amg_levels": (I, [C.c_void_p, np.ctypeslib.ndpointer(dtype=np.int64)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -382,3 +390,45 @@ def align_phase(psi, ref):
     out = np.empty_like(psi)
     out[0::2], out[1::2] = z.real, z.imag
     return out
+
+
+# --------------------------------------------------------------------------
+class CpuSolver:
+    """The C FP64 Newton / AMG-MINRES / continuation solver (nosh_solver.c):
+    the CPU baseline, OpenMP over OMP_NUM_THREADS host cores."""
+
+    def __init__(self, P: Problem, g=1.0):
+        L = lib()
+        m = P.m
+        self.P = P
+        self._h = L.nor_solver_create(m.N, m.E, m.edges.ravel(), P.alpha, P.p, m.cv, P.t, P.V, g)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nor_solver_destroy(self._h)
+            self._h = None
+
+    @staticmethod
+    def threads():
+        return lib().nor_num_threads()
+
+    def newton(self, psi, mu, tol=1e-10, max_newton=20):
+        ni, ki = C.c_int(), C.c_int()
+        f0, f1 = C.c_double(), C.c_double()
+        rc = lib().nor_newton(self._h, psi, mu, tol, max_newton, C.byref(ni), C.byref(ki), C.byref(f0), C.byref(f1))
+        return {"status": rc, "newton_iters": ni.value, "krylov_iters": ki.value, "f_norm0": f0.value,
+                "f_norm": f1.value}
+
+    def continuation_step(self, x, x_prev, mu_new, mu_cur, mu_prev, tol=1e-10):
+        ni, ki = C.c_int(), C.c_int()
+        f0, f1 = C.c_double(), C.c_double()
+        xp = None if x_prev is None else C.c_void_p(x_prev.ctypes.data)
+        rc = lib().nor_continuation_step(self._h, x, xp, mu_new, mu_cur, mu_prev, tol, C.byref(ni), C.byref(ki),
+                                         C.byref(f0), C.byref(f1))
+        return {"status": rc, "newton_iters": ni.value, "krylov_iters": ki.value, "f_norm0": f0.value,
+                "f_norm": f1.value}
+
+    def amg_levels(self):
+        s = np.zeros(16, np.int64)
+        n = lib().nor_amg_levels(self._h, s)
+        return list(s[:n])
