@@ -255,6 +255,43 @@ int nosh_nls_profile_enable(nosh_nls nls, int enable);
 int nosh_nls_profile_read(nosh_nls nls, int kernel, int64_t *launches,
                           double *total_ms, double *bytes);
 
+/* ------------------------------------------------ allocation-free residual */
+/* F(psi) and ||F||_2 for callers that cannot allocate device memory: code
+ * that runs inside a host framework owning the whole device memory pool,
+ * plugins held to a fixed memory budget, or loops that must not pay the
+ * implicit device synchronisation of cudaMalloc / cudaFree.  It has no
+ * counterpart in the reference (whose F is compute_f_, reached through an
+ * nls handle that owns its buffers).
+ *
+ * Every array is caller-owned device memory of the current device:
+ *   row_ptr[N+1], cols[2E]  off-diagonal KEO graph (the complex graph of
+ *                           nosh_mesh_complex_graph without the diagonal)
+ *   keo_offdiag[2*2E]       its complex values (16-byte aligned)
+ *   keo_diag[N]             real KEO diagonal, sum of the incident edge
+ *                           coefficients
+ *   cv_thickness[N], scalar_potential[N], g
+ *   psi[2N] (in), f[2N] (out)  interleaved complex, 16-byte aligned
+ *   norm[1] (out)           ||F||_2
+ * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream)
+ * and the call returns without waiting for it.
+ *
+ * Limit: N <= 8,388,608 vertices (65,536 CTAs of 128 rows).  The reduction's
+ * scratch is one fixed 512 KiB __device__ array inside the library, which
+ * every GPU that loads the library holds until the process exits; larger
+ * meshes are rejected with NOSH_ERR_INVALID (use nosh_nls_compute_f_norm).
+ * The first call on a device looks up that array's device address, so make
+ * the first call on each device before any stream capture.  All calls share
+ * the one array: calls that overlap on the GPU (other streams, other host
+ * threads) race and give wrong norms; serialise them.  No device memory is
+ * allocated or freed by this call. */
+int nosh_residual_norm_noalloc(int64_t num_vertices, const int32_t *row_ptr,
+                               const int32_t *cols, const double *keo_offdiag,
+                               const double *keo_diag,
+                               const double *cv_thickness,
+                               const double *scalar_potential, double g,
+                               const double *psi, double *f, double *norm,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif

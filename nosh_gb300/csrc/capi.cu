@@ -122,6 +122,9 @@ void check_apply_args(int mode, double alpha, double beta, int nvec) {
 }  // namespace
 
 namespace nosh {
+// lets other translation units report through nosh_last_error()
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
 bool is_device_pointer(const void *p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
