@@ -46,7 +46,10 @@ def parse():
     ap.add_argument("--mu0", type=float, default=0.5)
     ap.add_argument("--dmu", type=float, default=0.005)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--predictor", default="secant", choices=["secant", "tangent", "none"])
+    ap.add_argument("--predictor", default="learned", choices=["learned", "secant", "quadratic", "none"])
+    ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
+    ap.add_argument("--train-iters", type=int, default=40, help="optimiser iterations per training step")
+    ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -238,7 +241,6 @@ def run_gb300(args):
     gm = ng.mesh(x, cells)
     prec = ng.PREC_MIXED if args.precision == "mixed" else ng.PREC_FP64
     model = ng.nls(gm, A, -1.0, 1.0, 1.0, mu=args.mu0, precision=prec)
-    pred = {"secant": ng.PREDICT_SECANT, "tangent": ng.PREDICT_TANGENT, "none": ng.PREDICT_NONE}[args.predictor]
     stream = torch.cuda.ExternalStream(model.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
 
@@ -251,98 +253,113 @@ def run_gb300(args):
         if world > 1:
             torch.distributed.barrier()
 
-    # -- device-resident state
-    cur = torch.tensor(psi0, dtype=torch.float64, device=dev)
-    prev = torch.empty_like(cur)
-    st = model.newton(cur, {"mu": args.mu0})
+    # converged state at mu0 (untimed set-up)
+    x0 = torch.tensor(psi0, dtype=torch.float64, device=dev)
+    st = model.newton(x0, {"mu": args.mu0})
     assert st["status"] == 0, st
-    mus = [args.mu0]
-    st = model.continuation_step(cur, prev, args.mu0 + args.dmu, args.mu0, predictor=ng.PREDICT_NONE)
-    mus.append(args.mu0 + args.dmu)
 
-    def step(xc, xp):
-        mu_new = mus[-1] + args.dmu
-        s = model.continuation_step(xc, xp, mu_new, mus[-1], mus[-2], predictor=pred)
-        assert s["status"] == 0 and s["f_norm"] <= 1e-10, s
-        mus.append(mu_new)
-        return s
+    preds = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC, "learned": ng.PREDICT_LEARNED,
+             "none": ng.PREDICT_NONE}
 
-    for _ in range(args.warmup):
-        step(cur, prev)
-    # -- timed region: device-resident inputs, L2 flushed before every step
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    model.profile(True)
-    model.profile_read(ng.KERNEL_JACOBIAN)
-    model.profile_read(ng.KERNEL_SMOOTHER)
-    model.profile_read(ng.KERNEL_ALL)
-    its = []
-    clocks = ClockSampler(local)
-    barrier()
-    clocks.start()
-    for k in range(args.steps):
-        flush_l2()
-        ev[k][0].record(stream)
-        s = step(cur, prev)
-        ev[k][1].record(stream)
-        its.append((s["newton_iters"], s["krylov_iters"]))
-    barrier()
-    clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    launches = model.profile_read(ng.KERNEL_ALL)[0]
-    jac = model.profile_read(ng.KERNEL_JACOBIAN)
-    smo = model.profile_read(ng.KERNEL_SMOOTHER)
-    model.profile(False)
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+    def run(pred_name, steps, warmup, profile=False, e2e=False):
+        """A continuation handle from x0; `warmup` untimed steps (for the
+        learned predictor: its online-training window first), then `steps`
+        steps timed with CUDA events on the library stream, L2 flushed before
+        each.  With e2e, each step also reads the state back to pinned host
+        memory inside the timed region."""
+        cont = ng.continuation(model, x0, args.mu0)
+        pred = preds[pred_name]
+        mu = args.mu0
+        if pred == ng.PREDICT_LEARNED:
+            cont.learning(args.train_steps, args.train_iters, args.lr)
+            warmup = warmup + args.train_steps + 3
+        for _ in range(warmup):
+            mu += args.dmu
+            s = cont.advance(mu, predictor=pred)
+            assert s["status"] == 0, s
+        if profile:
+            model.profile(True)
+            model.profile_read(ng.KERNEL_JACOBIAN)
+            model.profile_read(ng.KERNEL_SMOOTHER)
+        model.profile_read(ng.KERNEL_ALL)
+        host = torch.empty(x0.numel(), dtype=torch.float64, pin_memory=True).numpy() if e2e else None
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        its, used, wall = [], [], []
+        barrier()
+        for k in range(steps):
+            flush_l2()
+            mu += args.dmu
+            t0 = time.perf_counter()
+            ev[k][0].record(stream)
+            s = cont.advance(mu, predictor=pred)
+            if e2e:
+                cont.state(host)
+            ev[k][1].record(stream)
+            wall.append(time.perf_counter() - t0)
+            assert s["status"] == 0 and s["f_norm"] <= 1e-10, s
+            its.append((s["newton_iters"], s["krylov_iters"]))
+            used.append(cont.last_prediction()["used"])
+        barrier()
+        out = {"ms": float(np.mean([a.elapsed_time(b) for a, b in ev])), "wall_ms": 1000.0 * float(np.mean(wall)),
+               "launches": model.profile_read(ng.KERNEL_ALL)[0],
+               "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
+               "learned_used": int(sum(1 for u in used if u == ng.PREDICT_LEARNED)),
+               "train_loss": cont.last_prediction()["train_loss"]}
+        if profile:
+            out["jac"] = model.profile_read(ng.KERNEL_JACOBIAN)
+            out["smo"] = model.profile_read(ng.KERNEL_SMOOTHER)
+            model.profile(False)
+        return out
+
+    def maxrank(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1000.0 / ms
+        return float(t.item())
 
-    # -- e2e: the same steps through the C ABI with pinned HOST buffers
+    clocks = ClockSampler(local)
+    clocks.start()
+    plain = run("secant", args.steps, args.warmup)
+    head = run(args.predictor, args.steps, args.warmup) if args.predictor != "secant" else plain
+    clk = clocks.stop()
+    ms = maxrank(head["ms"])
+    value = world * 1000.0 / ms
+    plain_ms = maxrank(plain["ms"])
+
+    # e2e: the headline steps through the C ABI, state read back to host
     e2e = None
     if not args.no_e2e:
-        hc = torch.empty(cur.numel(), dtype=torch.float64, pin_memory=True)
-        hp = torch.empty_like(hc, pin_memory=True)
-        hc.copy_(cur.cpu())
-        hp.copy_(prev.cpu())
-        hcn, hpn = hc.numpy(), hp.numpy()
-        tt = []
-        barrier()
-        for k in range(args.steps):
-            flush_l2()
-            t0 = time.perf_counter()
-            step(hcn, hpn)  # copies x, x_prev in and both out inside the call
-            tt.append(time.perf_counter() - t0)
-        e2e_ms = 1000.0 * float(np.mean(tt))
-        if world > 1:
-            t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        nbytes = cur.numel() * 8
-        e2e = {"value": world * 1000.0 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": 2 * nbytes,
-               "d2h_bytes_per_step": 2 * nbytes, "ms_per_step": e2e_ms}
+        r = run(args.predictor, args.steps, args.warmup, e2e=True)
+        e2e_ms = maxrank(r["wall_ms"])
+        e2e = {"value": world * 1000.0 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": 16,
+               "d2h_bytes_per_step": x0.numel() * 8, "ms_per_step": e2e_ms,
+               "note": "device-resident continuation handle: per step the host sends the parameters "
+                       "and reads the new state back"}
 
-    # -- roofline of the dominant timed kernel class
+    # roofline: extra steps of the same workload with CUDA events around every
+    # fine-level SpMV launch (events disable graph replay, so these steps are
+    # kept out of the timed regions above)
+    prof = run("secant", max(3, args.steps // 2), 2, profile=True)
     peak, peak_kind = measured_peak()
     traffic = profiled_traffic()
-    cands = {"smoother_spmv": smo, "jacobian_spmv": jac}
+    cands = {"smoother_spmv": prof["smo"], "jacobian_spmv": prof["jac"]}
     dom = max(cands, key=lambda k: cands[k][1])
-    n_l, ms_l, bytes_l = cands[dom]
-    roof = None
-    if n_l > 0 and ms_l > 0:
+    roof, secondary = None, None
+    for name in (dom, [k for k in cands if k != dom][0]):
+        n_l, ms_l, bytes_l = cands[name]
+        if n_l <= 0 or ms_l <= 0:
+            continue
         ach = (bytes_l / n_l) / (ms_l / n_l * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "peak_kind": peak_kind, "kernel": dom, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
-                "algorithmic_bytes_per_launch": bytes_l / n_l, "traffic": traffic.get(dom)}
-    other = [k for k in cands if k != dom][0]
-    n_o, ms_o, b_o = cands[other]
-    secondary = None
-    if n_o > 0 and ms_o > 0:
-        a2 = (b_o / n_o) / (ms_o / n_o * 1e-3) / 1e9
-        secondary = {"kernel": other, "achieved": a2, "frac": a2 / peak, "launches": n_o,
-                     "avg_launch_us": 1000.0 * ms_o / n_o, "algorithmic_bytes_per_launch": b_o / n_o,
-                     "traffic": traffic.get(other)}
+        d = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+             "peak_kind": peak_kind, "kernel": name, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
+             "algorithmic_bytes_per_launch": bytes_l / n_l, "traffic": traffic.get(name),
+             "timing": "CUDA events around each launch on the library stream, during extra continuation "
+                       "steps of the same workload run after the timed ones"}
+        if name == dom:
+            roof = d
+        else:
+            secondary = d
 
     out = {
         "metric": METRIC,
@@ -359,19 +376,24 @@ def run_gb300(args):
         "data": "synthetic",
         "config": workload(args) | {"l2": "flushed (256 MB write) before every timed step",
                                     "parallelism": f"replicas x{world}"},
+        "plain_predictor": {"predictor": "secant", "value": world * 1000.0 / plain_ms, "ms_per_step": plain_ms,
+                            "newton_krylov_per_step": plain["newton_krylov_per_step"]},
+        "learned_vs_plain": plain_ms / ms,
+        "newton_krylov_per_step": head["newton_krylov_per_step"],
+        "learned_used_steps": head["learned_used"],
+        "train_loss": head["train_loss"],
         "e2e": e2e,
-        "gpu_launches": int(launches),
+        "gpu_launches": int(head["launches"]),
         "roofline": roof,
         "roofline_secondary": secondary,
         "clocks": clk,
-        "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
     }
     # -- CPU baseline: bounded sample of the same workload on the host cores
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         times, cits, threads = cpu_run(args, 1000, time_budget=args.cpu_seconds, x=x, cells=cells, psi0=psi0)
         cv = 1.0 / float(np.mean(times))
         out["cpu_baseline"] = {"value": cv, "unit": "steps/s", "cores": threads, "kind": "port",
-                               "sample": f"{len(times)} continuation steps of the same workload "
+                               "sample": f"{len(times)} secant continuation steps of the same workload "
                                          f"(FP64 CPU restatement, {threads} OpenMP threads)"}
     if rank == 0:
         print(json.dumps(out), flush=True)

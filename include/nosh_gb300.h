@@ -224,6 +224,10 @@ int nosh_newton_solve(nosh_nls nls, double *x, const double *p,
 #define NOSH_PREDICT_NONE 0    /* x(mu_new) = x(mu_cur)                      */
 #define NOSH_PREDICT_SECANT 1  /* LOCA "Secant" (examples/conf.xml:39-41)    */
 #define NOSH_PREDICT_TANGENT 2 /* LOCA "Tangent": x + dmu * (-J^-1 dF/dmu)   */
+#define NOSH_PREDICT_QUADRATIC 3 /* 3-point polynomial extrapolation       */
+#define NOSH_PREDICT_LEARNED 4   /* edge message-passing network on top of the
+                                    secant, trained online; falls back to the
+                                    secant when its residual is larger       */
 
 /* One natural-parameter continuation step (LOCA stepper semantics,
  * examples/conf.xml:35-75; driven by executables/nosh-cont/nosh-cont.cpp:
@@ -239,6 +243,53 @@ int nosh_continuation_step(nosh_nls nls, double *x, double *x_prev,
                            const double *p_new, double mu_cur, double mu_prev,
                            int predictor, const nosh_newton_options *opt,
                            nosh_newton_stats *stats);
+
+/* A device-resident continuation run: the handle keeps the last converged
+ * states (and the learned predictor) in HBM, so a step moves no state
+ * through the host.  Same stepper semantics as nosh_continuation_step.
+ * x0 is the converged state at mu0 (host or device). */
+typedef struct nosh_continuation_s *nosh_continuation;
+int nosh_continuation_create(nosh_nls nls, const double *x0, double mu0,
+                             nosh_continuation *out);
+int nosh_continuation_destroy(nosh_continuation c);
+/* One step to mu_new with the given predictor (NOSH_PREDICT_*); the
+ * polynomial predictors fall back to lower order while the history is
+ * short.  stats->f_norm0 is the residual of the prediction actually used. */
+int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
+                              const nosh_newton_options *opt,
+                              nosh_newton_stats *stats);
+/* The current state (2N doubles, host or device) and its mu. */
+int nosh_continuation_state(nosh_continuation c, double *x, double *mu);
+/* Learned predictor: train on the transitions of the next `train_steps`
+ * steps (online, `iters_per_step` optimiser iterations each), then predict.
+ * Returns the last training loss (relative) in *loss when not NULL. */
+int nosh_continuation_learning(nosh_continuation c, int train_steps,
+                               int iters_per_step, double learning_rate);
+/* Predictor telemetry: which predictor the last advance used
+ * (NOSH_PREDICT_*), the learned prediction's residual and the secant one's
+ * (NaN when not evaluated), and the last training loss. */
+int nosh_continuation_last_prediction(nosh_continuation c, int *used,
+                                      double *f_learned, double *f_secant,
+                                      double *train_loss);
+
+/* The learned predictor's network, for inspection and gradient checks (the
+ * continuation handle owns its own instance).  Parameters are one flat FP32
+ * vector: encoder W [8x64] (row-major), b [64]; per layer l = 0..2:
+ * W_a [64x64], W_b [64x64], W_c [4x64], b_m [64], W_u [128x64], b_u [64];
+ * decoder W [64x2], b [2].  Node features are N x 8, outputs N x 2, edge
+ * features 2E x 4 in the order of the off-diagonal KEO graph (the complex
+ * graph of nosh_mesh_complex_graph without its diagonal). */
+typedef struct nosh_mpnn_s *nosh_mpnn;
+int nosh_mpnn_create(nosh_nls nls, nosh_mpnn *out);
+int nosh_mpnn_destroy(nosh_mpnn net);
+int nosh_mpnn_num_params(nosh_mpnn net, int64_t *n);
+/* copies the parameters out (get != NULL) and/or in (set != NULL) */
+int nosh_mpnn_params(nosh_mpnn net, float *get, const float *set);
+int nosh_mpnn_edge_features(nosh_mpnn net, float *ef);
+int nosh_mpnn_forward(nosh_mpnn net, const float *X, float *Y);
+/* mean-squared loss against targets T (N x 2) and its parameter gradient */
+int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const float *T,
+                        double *loss, float *grad);
 
 /* ------------------------------------------------------ kernel timing */
 #define NOSH_KERNEL_JACOBIAN 0 /* fine-level Jacobian apply (MINRES)       */

@@ -44,7 +44,7 @@ ERR_INVALID, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN = 1, 2, 3, 4, 5
 ERR_UNSUPPORTED, ERR_MESH, ERR_NO_MEMORY = 6, 7, 8
 PREC_FP64, PREC_MIXED = 0, 1
 NO_TRANS, TRANS = 0, 1
-PREDICT_NONE, PREDICT_SECANT, PREDICT_TANGENT = 0, 1, 2
+PREDICT_NONE, PREDICT_SECANT, PREDICT_TANGENT, PREDICT_QUADRATIC, PREDICT_LEARNED = 0, 1, 2, 3, 4
 KERNEL_JACOBIAN, KERNEL_SMOOTHER, KERNEL_ALL = 0, 1, 2
 
 
@@ -114,6 +114,19 @@ _SIGS = {
     "nosh_newton_solve": (_I, [_P, _P, _P, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "nosh_continuation_step": (_I, [_P, _P, _P, _P, _D, _D, _I, C.POINTER(NewtonOptions),
                                     C.POINTER(NewtonStats)]),
+    "nosh_continuation_create": (_I, [_P, _P, _D, C.POINTER(_P)]),
+    "nosh_continuation_destroy": (_I, [_P]),
+    "nosh_continuation_advance": (_I, [_P, _D, _I, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
+    "nosh_continuation_state": (_I, [_P, _P, C.POINTER(_D)]),
+    "nosh_continuation_learning": (_I, [_P, _I, _I, _D]),
+    "nosh_continuation_last_prediction": (_I, [_P, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), C.POINTER(_D)]),
+    "nosh_mpnn_create": (_I, [_P, C.POINTER(_P)]),
+    "nosh_mpnn_destroy": (_I, [_P]),
+    "nosh_mpnn_num_params": (_I, [_P, C.POINTER(_I64)]),
+    "nosh_mpnn_params": (_I, [_P, _P, _P]),
+    "nosh_mpnn_edge_features": (_I, [_P, _P]),
+    "nosh_mpnn_forward": (_I, [_P, _P, _P]),
+    "nosh_mpnn_loss_grad": (_I, [_P, _P, _P, C.POINTER(_D), _P]),
     "nosh_nls_profile_enable": (_I, [_P, _I]),
     "nosh_nls_profile_read": (_I, [_P, _I, C.POINTER(_I64), C.POINTER(_D), C.POINTER(_D)]),
 }
@@ -419,3 +432,90 @@ class nls:
         rc = _lib.nosh_newton_solve(self._h, _ptr(x), _ptr(self._pvec(params)), C.byref(o), C.byref(st))
         _check(rc, allow=(ERR_NOT_CONVERGED,))
         return self._stats(st)
+
+
+# ---------------------------------------------------------------------------
+class continuation:
+    """Device-resident natural continuation run (LOCA stepper semantics): the
+    last converged states stay on the GPU between steps."""
+
+    def __init__(self, model: nls, x0, mu0: float):
+        self.model = model
+        h = C.c_void_p()
+        _check(_lib.nosh_continuation_create(model._h, _ptr(_f64(x0)), mu0, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.nosh_continuation_destroy(h)
+            self._h = None
+
+    def advance(self, mu_new, predictor=PREDICT_SECANT, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000,
+                precision=None, verbose=0):
+        o = self.model._options(tol, max_newton, forcing, max_krylov, precision, verbose)
+        st = NewtonStats()
+        rc = _lib.nosh_continuation_advance(self._h, mu_new, predictor, C.byref(o), C.byref(st))
+        _check(rc, allow=(ERR_NOT_CONVERGED,))
+        return nls._stats(st)
+
+    def state(self, x=None):
+        mu = C.c_double()
+        x = np.empty(2 * self.model.n) if x is None else x
+        _check(_lib.nosh_continuation_state(self._h, _ptr(x), C.byref(mu)))
+        return x, mu.value
+
+    def learning(self, train_steps, iters_per_step=20, learning_rate=1e-3):
+        _check(_lib.nosh_continuation_learning(self._h, train_steps, iters_per_step, learning_rate))
+
+    def last_prediction(self):
+        u, fl, fs, tl = C.c_int(), C.c_double(), C.c_double(), C.c_double()
+        _check(_lib.nosh_continuation_last_prediction(self._h, C.byref(u), C.byref(fl), C.byref(fs), C.byref(tl)))
+        return {"used": u.value, "f_learned": fl.value, "f_secant": fs.value, "train_loss": tl.value}
+
+
+class mpnn:
+    """The learned predictor's message-passing network (inspection and
+    gradient checks); flat FP32 parameter layout as in nosh_gb300.h."""
+
+    def __init__(self, model: nls):
+        self.model = model
+        h = C.c_void_p()
+        _check(_lib.nosh_mpnn_create(model._h, C.byref(h)))
+        self._h = h
+        n = C.c_int64()
+        _check(_lib.nosh_mpnn_num_params(h, C.byref(n)))
+        self.num_params = n.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.nosh_mpnn_destroy(h)
+            self._h = None
+
+    def params(self, new=None):
+        out = np.empty(self.num_params, np.float32)
+        _check(_lib.nosh_mpnn_params(self._h, _ptr(out), None))
+        if new is not None:
+            new = np.ascontiguousarray(new, np.float32)
+            _check(_lib.nosh_mpnn_params(self._h, None, _ptr(new)))
+        return out
+
+    def edge_features(self):
+        out = np.empty((2 * self.model.mesh.num_edges, 4), np.float32)
+        _check(_lib.nosh_mpnn_edge_features(self._h, _ptr(out)))
+        return out
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.empty((X.shape[0], 2), np.float32)
+        _check(_lib.nosh_mpnn_forward(self._h, _ptr(X), _ptr(Y)))
+        return Y
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        g = np.empty(self.num_params, np.float32)
+        loss = C.c_double()
+        _check(_lib.nosh_mpnn_loss_grad(self._h, _ptr(X), _ptr(T), C.byref(loss), _ptr(g)))
+        return loss.value, g

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnosh_gb300.so")
-SOURCES = ["mesh.cu", "ops.cu", "amg.cu", "solver.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["mesh.cu", "ops.cu", "amg.cu", "solver.cu", "continuation.cu", "mpnn.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -75,5 +75,27 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
+CPP_TESTS = {"test_reference_api": os.path.join(ROOT, "tests", "cpp", "test_reference_api.cpp")}
+
+
+def build_cpp_tests(force: bool = False) -> dict:
+    """Compile the C++ programs that exercise include/nosh_gb300.hpp against
+    the library (g++, linked with an rpath to the in-tree library)."""
+    out = {}
+    cxx = shutil.which("g++") or "g++"
+    for name, src in CPP_TESTS.items():
+        exe = os.path.join(BUILD, name)
+        deps = [src, LIB, os.path.join(ROOT, "include", "nosh_gb300.h"), os.path.join(ROOT, "include", "nosh_gb300.hpp")]
+        if force or _needs(exe, deps):
+            cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), src, "-L", PKG,
+                   "-lnosh_gb300", "-Wl,-rpath," + PKG, "-o", exe]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"g++ failed on {name}:\n{r.stderr}")
+        out[name] = exe
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose=True, force="--force" in sys.argv))
+    print(build_cpp_tests(force="--force" in sys.argv))

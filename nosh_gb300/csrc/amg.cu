@@ -32,6 +32,7 @@ namespace {
 
 constexpr double kTheta = 0.05;  // strength-of-connection threshold
 constexpr double kChebRatio = 30.0;  // smoothing interval [lmax/ratio, 1.1 lmax]
+constexpr int64_t kTailMax = 1024;   // levels this small run in one CTA
 
 struct HostLevel {
   int64_t n = 0;
@@ -218,7 +219,7 @@ __global__ void rap_diag(int64_t na, const int32_t *__restrict__ mptr,
 }
 
 // inverse diagonal blocks and the Gershgorin bound of lambda_max(D^-1 A):
-// 1 + ||D_i^-1||_2 sum_j |a_ij|, reduced by max over rows
+// 1 + ||D_i^-1||_2 sum_j |a_ij|, reduced by max over rows (arithmetic in T)
 template <typename T>
 __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
                                 const C2<T> *__restrict__ off, const T *__restrict__ dia,
@@ -226,21 +227,21 @@ __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double bound = 0.0;
   if (i < n) {
-    const double a = dia[3 * i], d = dia[3 * i + 1], b = dia[3 * i + 2];
-    const double det = a * d - b * b;
-    dinv[3 * i] = (T)(d / det);
-    dinv[3 * i + 1] = (T)(a / det);
-    dinv[3 * i + 2] = (T)(-b / det);
-    const double lmin = 0.5 * (a + d) - sqrt(0.25 * (a - d) * (a - d) + b * b);
-    double s = 0.0;
+    const T a = dia[3 * i], d = dia[3 * i + 1], b = dia[3 * i + 2];
+    const T det = a * d - b * b;
+    dinv[3 * i] = d / det;
+    dinv[3 * i + 1] = a / det;
+    dinv[3 * i + 2] = -b / det;
+    const T lmin = (T)0.5 * (a + d) - sqrt((T)0.25 * (a - d) * (a - d) + b * b);
+    T s = 0;
     for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
       const C2<T> v = off[k];
-      s += sqrt((double)v.x * v.x + (double)v.y * v.y);
+      s += sqrt(v.x * v.x + v.y * v.y);
     }
-    bound = (lmin > 0.0 && det > 0.0) ? 1.0 + s / lmin : 1e300;
+    bound = (lmin > 0 && det > 0) ? 1.0 + (double)(s / lmin) : 1e300;
   }
-  // max over the block then one atomic per block (non-negative doubles order
-  // like their bit patterns)
+  // max over the block, then one atomic per block (non-negative doubles
+  // order like their bit patterns)
   __shared__ double sm[32];
   double v = bound;
 #pragma unroll
@@ -274,23 +275,71 @@ __global__ void cheb_coeffs(const unsigned long long *lmax_bits, int deg, T *coe
   *lmax_out = lmax;
 }
 
-// first Chebyshev step from x = 0: d = D^-1 b / theta, x = d
+// ---- smoother building blocks (shared by the grid kernels and the tail)
+// d = c0 D^-1 b, x = d  (first Chebyshev step from x = 0)
 template <typename T>
-__global__ void cheb_first(int64_t n, const T *__restrict__ dinv, const T *__restrict__ coef,
-                           const C2<T> *__restrict__ b, C2<T> *__restrict__ d,
-                           C2<T> *__restrict__ x) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const T c0 = coef[0];
-  const C2<T> bi = b[i];
+__device__ __forceinline__ void cheb_first_elem(int64_t i, const T *dinv, T c0, C2<T> bi, C2<T> *d,
+                                                C2<T> *x) {
   const T a = dinv[3 * i], e = dinv[3 * i + 1], f = dinv[3 * i + 2];
   const C2<T> di{c0 * (a * bi.x + f * bi.y), c0 * (f * bi.x + e * bi.y)};
   d[i] = di;
   x[i] = di;
 }
 
-// Chebyshev step with SpMV: r = D^-1 (b - A x_in), d = c1 d + c2 r,
-// x_out = x_in + d.  (k == 0 with x_in != 0: d = r / theta.)
+// Chebyshev step k given (sr, si) = (offdiag A x_in)_i:
+// r = D^-1 (b - A x_in), d = c1 d + c2 r (d = c0 r for k == 0), x_out = x_in + d
+template <typename T>
+__device__ __forceinline__ C2<T> cheb_elem(int64_t i, int k, T sr, T si, const T *dia, const T *dinv,
+                                           const T *coef, const C2<T> *b, const C2<T> *xin, C2<T> *d,
+                                           C2<T> *xout) {
+  const C2<T> xi = xin[i], bi = b[i];
+  const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
+  const T rr = bi.x - (sr + d0r * xi.x + d1b * xi.y);
+  const T ri = bi.y - (si + d1b * xi.x + d0i * xi.y);
+  const T a = dinv[3 * i], e = dinv[3 * i + 1], f = dinv[3 * i + 2];
+  const T zr = a * rr + f * ri, zi = f * rr + e * ri;
+  C2<T> dn;
+  if (k == 0) {
+    dn = C2<T>{coef[0] * zr, coef[0] * zi};
+  } else {
+    const C2<T> dold = d[i];
+    const T c1 = coef[2 * k], c2 = coef[2 * k + 1];
+    dn = C2<T>{c1 * dold.x + c2 * zr, c1 * dold.y + c2 * zi};
+  }
+  d[i] = dn;
+  const C2<T> xo{xi.x + dn.x, xi.y + dn.y};
+  xout[i] = xo;
+  return xo;
+}
+
+template <typename T>
+__global__ void cheb_first(int64_t n, const T *__restrict__ dinv, const T *__restrict__ coef,
+                           const C2<T> *__restrict__ b, C2<T> *__restrict__ d,
+                           C2<T> *__restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cheb_first_elem<T>(i, dinv, coef[0], b[i], d, x);
+}
+
+// MINRES head fused with the first Chebyshev step of the fine level:
+// r_new = J z / beta - (beta/oldb) r_old - (alfa/beta) r_cur over r_old, then
+// d = c0 D^-1 r_new, x = d
+template <typename T>
+__global__ void lanczos_first(int64_t n, const MinresScalars *__restrict__ s,
+                              const C2<T> *__restrict__ u, C2<T> *__restrict__ r_old,
+                              const C2<T> *__restrict__ r_cur, const T *__restrict__ dinv,
+                              const T *__restrict__ coef, C2<T> *__restrict__ d, C2<T> *__restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T *la = lanczos_coef<T>(s);
+  const T a = la[0], bb = la[1], c = la[2];
+  const C2<T> ui = u[i], ro = r_old[i], rc = r_cur[i];
+  const C2<T> bi{a * ui.x - bb * ro.x - c * rc.x, a * ui.y - bb * ro.y - c * rc.y};
+  r_old[i] = bi;
+  cheb_first_elem<T>(i, dinv, coef[0], bi, d, x);
+}
+
+// Chebyshev step with SpMV (grid kernel epilogue)
 template <typename T>
 struct ChebOp {
   static constexpr bool kReduce = false;
@@ -299,24 +348,28 @@ struct ChebOp {
   const C2<T> *b, *xin;
   C2<T> *d, *xout;
   __device__ double finish(int i, T sr, T si) const {
-    const C2<T> xi = xin[i], bi = b[i];
-    const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
-    const T rr = bi.x - (sr + d0r * xi.x + d1b * xi.y);
-    const T ri = bi.y - (si + d1b * xi.x + d0i * xi.y);
-    const T a = dinv[3 * i], e = dinv[3 * i + 1], f = dinv[3 * i + 2];
-    const T zr = a * rr + f * ri, zi = f * rr + e * ri;
-    C2<T> dn;
-    if (step == 0) {
-      dn = C2<T>{coef[0] * zr, coef[0] * zi};
-    } else {
-      const C2<T> dold = d[i];
-      const T c1 = coef[2 * step], c2 = coef[2 * step + 1];
-      dn = C2<T>{c1 * dold.x + c2 * zr, c1 * dold.y + c2 * zi};
-    }
-    d[i] = dn;
-    xout[i] = C2<T>{xi.x + dn.x, xi.y + dn.y};
+    cheb_elem<T>(i, step, sr, si, dia, dinv, coef, b, xin, d, xout);
     return 0.0;
   }
+};
+
+// Last post-smoothing step of the fine level inside MINRES: also reduces
+// <r_new, z_new> and, in the finishing thread, advances the Givens recurrence.
+template <typename T>
+struct ChebMinresOp {
+  static constexpr bool kReduce = true;
+  static constexpr bool kHook = true;
+  const T *dia, *dinv, *coef;
+  int step;
+  const C2<T> *b, *xin;
+  C2<T> *d, *xout;
+  MinresScalars *s;
+  __device__ double finish(int i, T sr, T si) const {
+    const C2<T> z = cheb_elem<T>(i, step, sr, si, dia, dinv, coef, b, xin, d, xout);
+    const C2<T> bi = b[i];
+    return (double)bi.x * (double)z.x + (double)bi.y * (double)z.y;
+  }
+  __device__ void hook(double total) const { minres_advance(s, total); }
 };
 
 // res = b - A x
@@ -347,6 +400,26 @@ __global__ void restrict_kernel(int64_t na, const int32_t *__restrict__ mptr,
     si += v.y;
   }
   rc[a] = C2<T>{sr, si};
+}
+
+// restriction fused with the coarse level's first Chebyshev step
+template <typename T>
+__global__ void restrict_first(int64_t na, const int32_t *__restrict__ mptr,
+                               const int32_t *__restrict__ midx, const C2<T> *__restrict__ r,
+                               C2<T> *__restrict__ rc, const T *__restrict__ dinv,
+                               const T *__restrict__ coef, C2<T> *__restrict__ d,
+                               C2<T> *__restrict__ x) {
+  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= na) return;
+  T sr = 0, si = 0;
+  for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
+    const C2<T> v = r[midx[q]];
+    sr += v.x;
+    si += v.y;
+  }
+  const C2<T> b{sr, si};
+  rc[a] = b;
+  cheb_first_elem<T>(a, dinv, coef[0], b, d, x);
 }
 
 template <typename T>
@@ -387,8 +460,45 @@ __global__ void coarse_dense(int64_t n, const int32_t *__restrict__ rp, const in
   }
 }
 
-// In-place Gauss-Jordan inversion of an SPD matrix (no pivoting needed),
-// one CTA; writes FP64 and FP32 copies.  Records a non-positive pivot.
+// In-place Gauss-Jordan inversion of an SPD matrix (no pivoting needed) in
+// shared memory, one CTA, m <= kDenseSmem, in the arithmetic type C (FP32 for
+// the mixed path: FP64 arithmetic is slow on GB300 and the coarsest operator
+// is well conditioned); writes the FP64 and FP32 copies.
+constexpr int kDenseSmem = 128;
+template <typename C>
+__global__ void gauss_jordan_spd_smem(int m, double *A, float *Af, int *err) {
+  extern __shared__ __align__(16) unsigned char gj_raw[];
+  C *S = reinterpret_cast<C *>(gj_raw);
+  __shared__ C ip_s;
+  for (int q = threadIdx.x; q < m * m; q += blockDim.x) S[q] = (C)A[q];
+  __syncthreads();
+  for (int k = 0; k < m; k++) {
+    if (threadIdx.x == 0) {
+      const C piv = S[k * m + k];
+      if (!(piv > (C)0)) atomicOr(err, 16);
+      ip_s = (C)1 / piv;
+    }
+    __syncthreads();
+    const C ip = ip_s;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) S[k * m + j] = (j == k) ? ip : S[k * m + j] * ip;
+    __syncthreads();
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+      const int i = q / m, j = q % m;
+      if (i == k || j == k) continue;
+      S[q] -= S[i * m + k] * S[k * m + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      if (i != k) S[i * m + k] = -S[i * m + k] * ip;
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+    A[q] = (double)S[q];
+    Af[q] = (float)S[q];
+  }
+}
+
+// The same in global memory for larger coarsest levels.
 __global__ void gauss_jordan_spd(int m, double *A, float *Af, int *err) {
   for (int k = 0; k < m; k++) {
     __syncthreads();
@@ -401,10 +511,8 @@ __global__ void gauss_jordan_spd(int m, double *A, float *Af, int *err) {
     __syncthreads();
     for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += blockDim.x) {
       const int i = (int)(q / m), j = (int)(q % m);
-      if (i == k) continue;
-      const double f = A[(int64_t)i * m + k];
-      if (j == k) continue;
-      A[q] -= f * A[(int64_t)k * m + j];
+      if (i == k || j == k) continue;
+      A[q] -= A[(int64_t)i * m + k] * A[(int64_t)k * m + j];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < m; i += blockDim.x)
@@ -421,6 +529,133 @@ __global__ void dense_matvec(int m, const T *__restrict__ Ainv, const T *__restr
     for (int j = 0; j < m; j++) s += Ainv[(int64_t)i * m + j] * b[j];
     x[i] = s;
   }
+}
+
+// ---- single-CTA tail: every level from `lt` down, in one launch
+template <typename T>
+struct LevelDesc {
+  int64_t n;
+  const int32_t *rp, *ci;
+  const C2<T> *off;
+  const T *dia, *dinv, *coef;
+  C2<T> *b, *x, *x2, *d, *res;
+  const int32_t *agg, *mem_ptr, *mem_idx;  // transfer to the next level
+};
+
+template <typename T>
+__device__ __forceinline__ void tail_row_sum(const LevelDesc<T> &A, int64_t i, const C2<T> *x, T &sr,
+                                             T &si) {
+  sr = 0;
+  si = 0;
+  for (int32_t k = A.rp[i]; k < A.rp[i + 1]; k++) {
+    const C2<T> v = A.off[k], xv = x[A.ci[k]];
+    sr += v.x * xv.x - v.y * xv.y;
+    si += v.x * xv.y + v.y * xv.x;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restrict__ lv, int lt, int L,
+                                                    int deg, const T *__restrict__ Ainv) {
+  const int tid = threadIdx.x, bs = blockDim.x;
+  for (int l = lt; l < L - 1; l++) {
+    const LevelDesc<T> A = lv[l];
+    C2<T> *cur = (deg % 2) ? A.x : A.x2, *oth = (deg % 2) ? A.x2 : A.x;
+    for (int64_t i = tid; i < A.n; i += bs) cheb_first_elem<T>(i, A.dinv, A.coef[0], A.b[i], A.d, cur);
+    __syncthreads();
+    for (int k = 1; k < deg; k++) {
+      for (int64_t i = tid; i < A.n; i += bs) {
+        T sr, si;
+        tail_row_sum(A, i, cur, sr, si);
+        cheb_elem<T>(i, k, sr, si, A.dia, A.dinv, A.coef, A.b, cur, A.d, oth);
+      }
+      __syncthreads();
+      C2<T> *t = cur;
+      cur = oth;
+      oth = t;
+    }
+    for (int64_t i = tid; i < A.n; i += bs) {
+      T sr, si;
+      tail_row_sum(A, i, A.x, sr, si);
+      const C2<T> xi = A.x[i], bi = A.b[i];
+      const T d0r = A.dia[3 * i], d0i = A.dia[3 * i + 1], d1b = A.dia[3 * i + 2];
+      A.res[i] = C2<T>{bi.x - (sr + d0r * xi.x + d1b * xi.y), bi.y - (si + d1b * xi.x + d0i * xi.y)};
+    }
+    __syncthreads();
+    const LevelDesc<T> Cl = lv[l + 1];
+    for (int64_t a = tid; a < Cl.n; a += bs) {
+      T sr = 0, si = 0;
+      for (int32_t q = A.mem_ptr[a]; q < A.mem_ptr[a + 1]; q++) {
+        const C2<T> v = A.res[A.mem_idx[q]];
+        sr += v.x;
+        si += v.y;
+      }
+      Cl.b[a] = C2<T>{sr, si};
+    }
+    __syncthreads();
+  }
+  {
+    const LevelDesc<T> C = lv[L - 1];
+    const int m = (int)(2 * C.n);
+    const T *b = reinterpret_cast<const T *>(C.b);
+    T *x = reinterpret_cast<T *>(C.x);
+    for (int i = tid; i < m; i += bs) {
+      T s = 0;
+      for (int j = 0; j < m; j++) s += Ainv[(int64_t)i * m + j] * b[j];
+      x[i] = s;
+    }
+    __syncthreads();
+  }
+  for (int l = L - 2; l >= lt; l--) {
+    const LevelDesc<T> A = lv[l];
+    const C2<T> *xc = lv[l + 1].x;
+    for (int64_t i = tid; i < A.n; i += bs) {
+      const C2<T> c = xc[A.agg[i]];
+      C2<T> v = A.x[i];
+      v.x += c.x;
+      v.y += c.y;
+      A.x[i] = v;
+    }
+    __syncthreads();
+    C2<T> *cur = A.x, *oth = A.x2;
+    for (int k = 0; k < deg; k++) {
+      for (int64_t i = tid; i < A.n; i += bs) {
+        T sr, si;
+        tail_row_sum(A, i, cur, sr, si);
+        cheb_elem<T>(i, k, sr, si, A.dia, A.dinv, A.coef, A.b, cur, A.d, oth);
+      }
+      __syncthreads();
+      C2<T> *t = cur;
+      cur = oth;
+      oth = t;
+    }
+    if (cur != A.x) {
+      for (int64_t i = tid; i < A.n; i += bs) A.x[i] = cur[i];
+      __syncthreads();
+    }
+  }
+}
+
+// plain MINRES pieces for the single-level case
+template <typename T>
+__global__ void lanczos_only(int64_t n, const MinresScalars *__restrict__ s, const C2<T> *__restrict__ u,
+                             C2<T> *__restrict__ r_old, const C2<T> *__restrict__ r_cur) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T *la = lanczos_coef<T>(s);
+  const T a = la[0], bb = la[1], c = la[2];
+  const C2<T> ui = u[i], ro = r_old[i], rc = r_cur[i];
+  r_old[i] = C2<T>{a * ui.x - bb * ro.x - c * rc.x, a * ui.y - bb * ro.y - c * rc.y};
+}
+
+template <typename T>
+__global__ void dot_advance(int64_t n, const C2<T> *__restrict__ a, const C2<T> *__restrict__ b,
+                            double *partials, unsigned *counter, MinresScalars *s) {
+  double v = 0.0;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) v = (double)a[i].x * b[i].x + (double)a[i].y * b[i].y;
+  double total = 0.0;
+  if (grid_reduce(v, partials, counter, &s->rz, &total)) minres_advance(s, total);
 }
 
 template <typename T>
@@ -454,25 +689,30 @@ struct AmgVals {
   std::vector<DevBuf<T>> dia;      // level >= 1
   std::vector<DevBuf<T>> dinv, coef;
   std::vector<DevBuf<C2<T>>> b, x, x2, d, res;
+  DevBuf<LevelDesc<T>> desc;       // for the single-CTA tail
 };
 
 struct Amg::Impl {
   NlsImpl &nls;
   AmgOptions opt;
   std::vector<AmgLevel> lev;
+  int lt = 1;  // first level handled by the single-CTA tail
   AmgVals<float> vf;
   AmgVals<double> vd;
   DevBuf<unsigned long long> lmax_bits;  // one per level
   DevBuf<double> lmax;
-  DevBuf<double> dense;   // coarsest (2n)^2 FP64
+  DevBuf<double> dense;  // coarsest (2n)^2 FP64
   DevBuf<float> densef;
   DevBuf<int> err;
   Impl(NlsImpl &s, const AmgOptions &o) : nls(s), opt(o) {}
   template <typename T> AmgVals<T> &vals();
   template <typename T> void ensure_vals();
-  template <typename T> void vcycle(int l, const C2<T> *b, C2<T> *x);
   template <typename T> const C2<T> *off(int l);
   template <typename T> const T *dia(int l);
+  template <typename T> const T *dense_inv();
+  template <typename T, class Op> void rows(int l, const C2<T> *x, const Op &op);
+  template <typename T> void descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *ms);
+  template <typename T> void prime();
 };
 
 template <> AmgVals<float> &Amg::Impl::vals<float>() { return vf; }
@@ -485,6 +725,8 @@ template <> const C2<double> *Amg::Impl::off<double>(int l) {
 }
 template <> const float *Amg::Impl::dia<float>(int l) { return l == 0 ? nls.d_rd32.p : vf.dia[l].p; }
 template <> const double *Amg::Impl::dia<double>(int l) { return l == 0 ? nls.d_rd64.p : vd.dia[l].p; }
+template <> const float *Amg::Impl::dense_inv<float>() { return densef.p; }
+template <> const double *Amg::Impl::dense_inv<double>() { return dense.p; }
 
 Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
   Impl &I = *impl;
@@ -546,6 +788,15 @@ Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
       A.intra_idx.upload(h.intra_idx, st);
     }
   }
+  // the fine level always runs on the whole grid; the first level at or
+  // below kTailMax nodes and everything under it run in one CTA
+  I.lt = L - 1;
+  for (int l = 1; l < L; l++)
+    if (I.lev[l].n <= kTailMax) {
+      I.lt = l;
+      break;
+    }
+  if (I.lt < 1) I.lt = L - 1;
   I.lmax_bits.alloc(L);
   I.lmax.alloc(L);
   const int64_t m2 = 2 * I.lev.back().n;
@@ -553,6 +804,10 @@ Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
   I.densef.alloc(m2 * m2);
   I.err.alloc(1);
   I.err.zero(st);
+  NOSH_CUDA(cudaFuncSetAttribute(gauss_jordan_spd_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kDenseSmem * kDenseSmem * (int)sizeof(double)));
+  NOSH_CUDA(cudaFuncSetAttribute(gauss_jordan_spd_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kDenseSmem * kDenseSmem * (int)sizeof(float)));
   s.sync();
 }
 
@@ -560,6 +815,16 @@ Amg::~Amg() = default;
 
 int Amg::num_levels() const { return (int)impl->lev.size(); }
 int64_t Amg::level_size(int l) const { return impl->lev[l].n; }
+int Amg::tail_level() const { return impl->lt; }
+
+const int *Amg::error_flag_ptr() const { return impl->err.p; }
+
+int Amg::error_flag() {
+  int herr = 0;
+  impl->err.download(&herr, 1, impl->nls.stream);
+  impl->nls.sync();
+  return herr;
+}
 
 template <typename T>
 void Amg::Impl::ensure_vals() {
@@ -590,9 +855,33 @@ void Amg::Impl::ensure_vals() {
     V.d[l].alloc(n);
     V.res[l].alloc(n);
   }
+  std::vector<LevelDesc<T>> desc(L);
+  for (int l = 0; l < L; l++) {
+    LevelDesc<T> &D = desc[l];
+    D.n = lev[l].n;
+    D.rp = lev[l].rp;
+    D.ci = lev[l].ci;
+    D.off = off<T>(l);
+    D.dia = dia<T>(l);
+    D.dinv = V.dinv[l].p;
+    D.coef = V.coef[l].p;
+    D.b = V.b[l].p;
+    D.x = V.x[l].p;
+    D.x2 = V.x2[l].p;
+    D.d = V.d[l].p;
+    D.res = V.res[l].p;
+    D.agg = lev[l].agg.p;
+    D.mem_ptr = lev[l].mem_ptr.p;
+    D.mem_idx = lev[l].mem_idx.p;
+  }
+  V.desc.upload(desc, nls.stream);
+  nls.sync();
+  prime<T>();
   V.ready = true;
 }
 
+// Numeric refresh from the current regularised KEO; stream-ordered, no host
+// synchronisation (the pivot check is read later through error_flag()).
 template <typename T>
 void Amg::refresh() {
   Impl &I = *impl;
@@ -613,107 +902,171 @@ void Amg::refresh() {
                                                      V.dia[l].p);
       ++I.nls.launch_count;
     }
-    dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
-                                                          V.dinv[l].p, I.lmax_bits.p + l);
-    ++I.nls.launch_count;
-    cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1),
-                                    V.coef[l].p, I.lmax.p + l);
-    ++I.nls.launch_count;
+    if (l < L - 1) {  // the coarsest level is solved directly
+      dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
+                                                            V.dinv[l].p, I.lmax_bits.p + l);
+      ++I.nls.launch_count;
+      cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1),
+                                      V.coef[l].p, I.lmax.p + l);
+      ++I.nls.launch_count;
+    }
   }
   const AmgLevel &C = I.lev.back();
   const int m2 = (int)(2 * C.n);
   coarse_dense<T><<<div_up(C.n, 128), 128, 0, st>>>(C.n, C.rp, C.ci, I.off<T>(L - 1), I.dia<T>(L - 1),
                                                      I.dense.p);
   ++I.nls.launch_count;
-  gauss_jordan_spd<<<1, 256, 0, st>>>(m2, I.dense.p, I.densef.p, I.err.p);
+  if (m2 <= kDenseSmem)
+    gauss_jordan_spd_smem<T><<<1, 1024, m2 * m2 * sizeof(T), st>>>(m2, I.dense.p, I.densef.p, I.err.p);
+  else
+    gauss_jordan_spd<<<1, 1024, 0, st>>>(m2, I.dense.p, I.densef.p, I.err.p);
   ++I.nls.launch_count;
   NOSH_CUDA(cudaGetLastError());
-  int herr = 0;
-  I.err.download(&herr, 1, st);
-  NOSH_CUDA(cudaStreamSynchronize(st));
-  NOSH_CHECK(herr == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
-}
-
-template <typename T, class Op>
-static void launch_level_rows(const AmgLevel &A, const C2<T> *off, const C2<T> *x, const Op &op,
-                              cudaStream_t st, int cap, int64_t &launches) {
-  static bool attr = false;
-  if (!attr) {
-    NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   100 * 1024));
-    attr = true;
-  }
-  const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
-  row_block_apply<T, Op><<<div_up(A.n, kRows), kRows, smem, st>>>((int)A.n, A.rp, A.ci, off, x, cap, op,
-                                                                 nullptr, nullptr, nullptr);
-  ++launches;
 }
 
 template <typename T>
-void Amg::Impl::vcycle(int l, const C2<T> *b, C2<T> *x) {
+void Amg::Impl::prime() {
+  // shared-memory opt-in of every row kernel instantiation, set before any
+  // stream capture
+  NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, ChebOp<T>>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, ChebMinresOp<T>>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, ResidOp<T>>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+}
+
+template <typename T, class Op>
+void Amg::Impl::rows(int l, const C2<T> *x, const Op &op) {
+  const AmgLevel &A = lev[l];
+  const int cap = sizeof(T) == 4 ? A.cap32 : A.cap64;
+  const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
+  row_block_apply<T, Op><<<row_grid((const void *)row_block_apply<T, Op>, smem, A.n), kRows, smem,
+                            nls.stream>>>(
+      (int)A.n, A.rp, A.ci, off<T>(l), x, cap, op, nls.red.partials.p, nls.red.counter.p,
+      Op::kReduce ? &nls.red.out.p[32] : nullptr);
+  ++nls.launch_count;
+}
+
+// Level l of the V-cycle after its first Chebyshev step: finish the
+// pre-smoothing (its result ends in x), coarse correction, post-smoothing.
+// With ms != nullptr the fine level's last step also advances MINRES.
+template <typename T>
+void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *ms) {
   AmgVals<T> &V = vals<T>();
   AmgLevel &A = lev[l];
   cudaStream_t st = nls.stream;
   const int L = (int)lev.size();
-  const int cap = sizeof(T) == 4 ? A.cap32 : A.cap64;
-  const int B = 256;
-  if (l == L - 1) {
-    const int m2 = (int)(2 * A.n);
-    const T *Ainv = sizeof(T) == 4 ? (const T *)densef.p : (const T *)dense.p;
-    dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, Ainv, (const T *)b, (T *)x);
-    ++nls.launch_count;
-    return;
-  }
   const int deg = std::max(opt.smooth_degree, 1);
+  const int B = 256;
   const T *dv = dia<T>(l);
-  const C2<T> *ov = off<T>(l);
-  // pre-smoothing from zero; ping-pong between x and x2, ending in x
   C2<T> *cur = (deg % 2 == 1) ? x : V.x2[l].p;
   C2<T> *oth = (deg % 2 == 1) ? V.x2[l].p : x;
-  cheb_first<T><<<div_up(A.n, B), B, 0, st>>>(A.n, V.dinv[l].p, V.coef[l].p, b, V.d[l].p, cur);
-  ++nls.launch_count;
-  // fine-level SpMV launches are timed when profiling is on; algorithmic
-  // bytes per vertex: Chebyshev x_in, diag, b, D^-1, d (r+w), x_out;
-  // residual x, diag, b, res
-  const int vb = (int)sizeof(T);
   KernelTimer *tm = l == 0 ? &nls.timers[NOSH_KERNEL_SMOOTHER] : nullptr;
+  const int vb = (int)sizeof(T);
   const double cheb_bytes = nls.spmv_bytes(2 * vb, 16 * vb);
   const double res_bytes = nls.spmv_bytes(2 * vb, 9 * vb);
   for (int k = 1; k < deg; k++) {
     ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
     if (tm) tm->begin(st);
-    launch_level_rows<T>(A, ov, cur, op, st, cap, nls.launch_count);
+    rows<T>(l, cur, op);
     if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
-  // cur == x here
   ResidOp<T> rop{dv, b, x, V.res[l].p};
   if (tm) tm->begin(st);
-  launch_level_rows<T>(A, ov, x, rop, st, cap, nls.launch_count);
+  rows<T>(l, x, rop);
   if (tm) tm->end(st, res_bytes);
   const AmgLevel &Cl = lev[l + 1];
-  restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p, V.b[l + 1].p);
-  ++nls.launch_count;
-  vcycle<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p);
+  if (l + 1 < lt) {
+    // restriction + first step of level l+1, whose pre-smoothing must end in
+    // its x buffer
+    C2<T> *first = (deg % 2 == 1) ? V.x[l + 1].p : V.x2[l + 1].p;
+    restrict_first<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
+                                                      V.b[l + 1].p, V.dinv[l + 1].p, V.coef[l + 1].p,
+                                                      V.d[l + 1].p, first);
+    ++nls.launch_count;
+    descend_ascend<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p, nullptr);
+  } else {
+    restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
+                                                       V.b[l + 1].p);
+    ++nls.launch_count;
+    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>());
+    ++nls.launch_count;
+  }
   prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x);
   ++nls.launch_count;
-  // post-smoothing: same polynomial, now from the corrected x
   cur = x;
   oth = V.x2[l].p;
   for (int k = 0; k < deg; k++) {
-    ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
     if (tm) tm->begin(st);
-    launch_level_rows<T>(A, ov, cur, op, st, cap, nls.launch_count);
+    if (ms && k == deg - 1) {
+      ChebMinresOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, ms};
+      rows<T>(l, cur, op);
+    } else {
+      ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
+      rows<T>(l, cur, op);
+    }
     if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
-  if (cur != x)
+  if (cur != x) {
     NOSH_CUDA(cudaMemcpyAsync(x, cur, A.n * sizeof(C2<T>), cudaMemcpyDeviceToDevice, st));
+  }
 }
 
+// z = V-cycle(r)
 template <typename T>
 void Amg::apply(const T *r, T *z) {
-  impl->vcycle<T>(0, (const C2<T> *)r, (C2<T> *)z);
+  Impl &I = *impl;
+  AmgVals<T> &V = I.vals<T>();
+  cudaStream_t st = I.nls.stream;
+  const int L = (int)I.lev.size();
+  const AmgLevel &A = I.lev[0];
+  if (L == 1) {
+    const int m2 = (int)(2 * A.n);
+    dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, I.dense_inv<T>(), r, z);
+    ++I.nls.launch_count;
+    NOSH_CUDA(cudaGetLastError());
+    return;
+  }
+  const int deg = std::max(I.opt.smooth_degree, 1);
+  C2<T> *first = (deg % 2 == 1) ? (C2<T> *)z : V.x2[0].p;
+  cheb_first<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, V.dinv[0].p, V.coef[0].p, (const C2<T> *)r,
+                                                  V.d[0].p, first);
+  ++I.nls.launch_count;
+  I.descend_ascend<T>(0, (const C2<T> *)r, (C2<T> *)z, nullptr);
+  NOSH_CUDA(cudaGetLastError());
+}
+
+// One MINRES Lanczos step around the V-cycle:
+//   r_old <- J z / beta - (beta/oldb) r_old - (alfa/beta) r_cur  (= r_new)
+//   z_out <- V-cycle(r_new),  <r_new, z_out> and the Givens recurrence.
+template <typename T>
+void Amg::apply_minres(MinresScalars *ms, const T *u, T *r_old, const T *r_cur, T *z_out) {
+  Impl &I = *impl;
+  AmgVals<T> &V = I.vals<T>();
+  cudaStream_t st = I.nls.stream;
+  const int L = (int)I.lev.size();
+  const AmgLevel &A = I.lev[0];
+  if (L == 1) {
+    lanczos_only<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, ms, (const C2<T> *)u, (C2<T> *)r_old,
+                                                      (const C2<T> *)r_cur);
+    apply<T>(r_old, z_out);
+    dot_advance<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, (const C2<T> *)r_old, (const C2<T> *)z_out,
+                                                     I.nls.red.partials.p, I.nls.red.counter.p, ms);
+    I.nls.launch_count += 2;
+    NOSH_CUDA(cudaGetLastError());
+    return;
+  }
+  const int deg = std::max(I.opt.smooth_degree, 1);
+  // the fine level's right-hand side is r_new itself: point b[0] at r_old
+  C2<T> *first = (deg % 2 == 1) ? (C2<T> *)z_out : V.x2[0].p;
+  lanczos_first<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, ms, (const C2<T> *)u, (C2<T> *)r_old,
+                                                     (const C2<T> *)r_cur, V.dinv[0].p, V.coef[0].p,
+                                                     V.d[0].p, first);
+  ++I.nls.launch_count;
+  I.descend_ascend<T>(0, (const C2<T> *)r_old, (C2<T> *)z_out, ms);
   NOSH_CUDA(cudaGetLastError());
 }
 
@@ -721,5 +1074,7 @@ template void Amg::refresh<float>();
 template void Amg::refresh<double>();
 template void Amg::apply<float>(const float *, float *);
 template void Amg::apply<double>(const double *, double *);
+template void Amg::apply_minres<float>(MinresScalars *, const float *, float *, const float *, float *);
+template void Amg::apply_minres<double>(MinresScalars *, const double *, double *, const double *, double *);
 
 }  // namespace nosh

@@ -2,6 +2,7 @@
 // preconditioner).  Declared here, defined in amg.cu.
 #pragma once
 
+#include "minres_state.cuh"
 #include "nls.cuh"
 
 namespace nosh {
@@ -25,8 +26,15 @@ struct Amg {
   // z = V-cycle(r); r, z device vectors of 2N (interleaved complex)
   template <typename T>
   void apply(const T *r, T *z);
+  // One MINRES Lanczos step fused around the V-cycle (see amg.cu)
+  template <typename T>
+  void apply_minres(MinresScalars *ms, const T *u, T *r_old, const T *r_cur, T *z_out);
   int num_levels() const;
   int64_t level_size(int l) const;
+  int tail_level() const;
+  // pivot-failure flags of the coarsest factorisation (synchronises)
+  int error_flag();
+  const int *error_flag_ptr() const;  // device address of the same flags
 
   struct Impl;
   std::unique_ptr<Impl> impl;

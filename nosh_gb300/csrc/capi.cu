@@ -7,6 +7,8 @@
 
 #include "amg.cuh"
 #include "nls.cuh"
+#include "continuation.cuh"
+#include "mpnn.cuh"
 #include "solver.cuh"
 
 struct nosh_mesh_s {
@@ -14,6 +16,12 @@ struct nosh_mesh_s {
 };
 struct nosh_nls_s {
   nosh::NlsImpl *impl;
+};
+struct nosh_continuation_s {
+  nosh::ContinuationImpl *impl;
+};
+struct nosh_mpnn_s {
+  nosh::Mpnn *impl;
 };
 
 namespace {
@@ -542,6 +550,139 @@ int nosh_continuation_step(nosh_nls nls, double *x, double *x_prev, const double
   if (rc == NOSH_OK) rc = st.status;
   if (stats) *stats = st;
   return rc;
+}
+
+int nosh_continuation_create(nosh_nls nls, const double *x0, double mu0, nosh_continuation *out) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(out != nullptr && x0 != nullptr, "null argument");
+    *out = nullptr;
+    auto *h = new nosh_continuation_s{nullptr};
+    try {
+      h->impl = new nosh::ContinuationImpl(s, x0, mu0);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int nosh_continuation_destroy(nosh_continuation c) {
+  return guarded([&] {
+    if (!c) return;
+    delete c->impl;
+    delete c;
+  });
+}
+
+int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
+                              const nosh_newton_options *opt, nosh_newton_stats *stats) {
+  nosh_newton_stats st{};
+  int rc = guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    nosh_newton_options o;
+    nosh_newton_default_options(&o);
+    if (opt) o = *opt;
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0, "bad solver options");
+    c->impl->advance(mu_new, predictor, o, st);
+  });
+  if (rc == NOSH_OK) rc = st.status;
+  if (stats) *stats = st;
+  return rc;
+}
+
+int nosh_continuation_state(nosh_continuation c, double *x, double *mu) {
+  return guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    auto &C = *c->impl;
+    if (x) {
+      NOSH_CUDA(cudaMemcpyAsync(x, C.slot(0), 2 * C.s.N * sizeof(double), cudaMemcpyDefault, C.s.stream));
+      C.s.sync();
+    }
+    if (mu) *mu = C.mu_of(0);
+  });
+}
+
+int nosh_continuation_learning(nosh_continuation c, int train_steps, int iters_per_step, double learning_rate) {
+  return guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    require(train_steps >= 0 && iters_per_step >= 0 && learning_rate >= 0, "bad learning settings");
+    c->impl->enable_learning(train_steps, iters_per_step, learning_rate);
+  });
+}
+
+int nosh_continuation_last_prediction(nosh_continuation c, int *used, double *f_learned, double *f_secant,
+                                      double *train_loss) {
+  return guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    auto &C = *c->impl;
+    if (used) *used = C.last_used;
+    if (f_learned) *f_learned = C.f_learned;
+    if (f_secant) *f_secant = C.f_secant;
+    if (train_loss) *train_loss = C.train_loss;
+  });
+}
+
+int nosh_mpnn_create(nosh_nls nls, nosh_mpnn *out) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(out != nullptr, "null argument");
+    *out = nullptr;
+    auto *h = new nosh_mpnn_s{nullptr};
+    try {
+      h->impl = new nosh::Mpnn(s);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int nosh_mpnn_destroy(nosh_mpnn net) {
+  return guarded([&] {
+    if (!net) return;
+    delete net->impl;
+    delete net;
+  });
+}
+
+int nosh_mpnn_num_params(nosh_mpnn net, int64_t *n) {
+  return guarded([&] {
+    require(net && net->impl && n, "null argument");
+    *n = net->impl->num_params();
+  });
+}
+
+int nosh_mpnn_params(nosh_mpnn net, float *get, const float *set) {
+  return guarded([&] {
+    require(net && net->impl, "null mpnn handle");
+    if (get) net->impl->get_params(get);
+    if (set) net->impl->set_params(set);
+  });
+}
+
+int nosh_mpnn_edge_features(nosh_mpnn net, float *ef) {
+  return guarded([&] {
+    require(net && net->impl && ef, "null argument");
+    net->impl->get_edge_features(ef);
+  });
+}
+
+int nosh_mpnn_forward(nosh_mpnn net, const float *X, float *Y) {
+  return guarded([&] {
+    require(net && net->impl && X && Y, "null argument");
+    net->impl->forward_features(X, Y);
+  });
+}
+
+int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const float *T, double *loss, float *grad) {
+  return guarded([&] {
+    require(net && net->impl && X && T && grad, "null argument");
+    const double l = net->impl->loss_and_grad(X, T, grad);
+    if (loss) *loss = l;
+  });
 }
 
 int nosh_nls_profile_enable(nosh_nls nls, int enable) {

@@ -1,0 +1,165 @@
+// Device-resident natural continuation (LOCA stepper semantics,
+// examples/conf.xml:35-75; the driver loop of
+// executables/nosh-cont/nosh-cont.cpp:226-345): the last converged states stay
+// in HBM, predictions are formed on the GPU and corrected by Newton.
+#include <cmath>
+
+#include "continuation.cuh"
+#include "mpnn.cuh"
+#include "spmv.cuh"
+
+namespace nosh {
+
+using namespace dev;
+
+namespace {
+
+// c = sum conj(a_i) b_i, two deterministic reductions into out[0..1]
+__global__ void cdot2_kernel(int64_t n, const C2<double> *__restrict__ a, const C2<double> *__restrict__ b,
+                             double *partials, unsigned *counter, double *out) {
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> x = a[i], y = b[i];
+    re += x.x * y.x + x.y * y.y;
+    im += x.x * y.y - x.y * y.x;
+  }
+  grid_reduce(re, partials, counter, out);
+  grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
+}
+
+__device__ __forceinline__ void unit_phase(const double *c, double &er, double &ei) {
+  const double m = sqrt(c[0] * c[0] + c[1] * c[1]);
+  er = m > 0 ? c[0] / m : 1.0;
+  ei = m > 0 ? c[1] / m : 0.0;
+}
+
+// out = L0 x0 + L1 e^{i phi1} x1 + L2 e^{i phi2} x2, the phases aligning x1
+// and x2 with x0 (solutions are defined up to a global U(1) phase)
+__global__ void extrapolate_kernel(int64_t n, int order, const double *__restrict__ c, double L0, double L1,
+                                   double L2, const C2<double> *__restrict__ x0,
+                                   const C2<double> *__restrict__ x1, const C2<double> *__restrict__ x2,
+                                   C2<double> *__restrict__ out) {
+  double e1r = 1.0, e1i = 0.0, e2r = 1.0, e2i = 0.0;
+  if (order >= 1) unit_phase(c, e1r, e1i);
+  if (order >= 2) unit_phase(c + 2, e2r, e2i);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> a = x0[i];
+    double r = L0 * a.x, im = L0 * a.y;
+    if (order >= 1) {
+      const C2<double> p = x1[i];
+      r += L1 * (e1r * p.x - e1i * p.y);
+      im += L1 * (e1r * p.y + e1i * p.x);
+    }
+    if (order >= 2) {
+      const C2<double> p = x2[i];
+      r += L2 * (e2r * p.x - e2i * p.y);
+      im += L2 * (e2r * p.y + e2i * p.x);
+    }
+    out[i] = C2<double>{r, im};
+  }
+}
+
+inline int vgrid(int64_t n) { return (int)std::min<int64_t>(div_up(n, 256), kNumSMs * 8); }
+
+}  // namespace
+
+ContinuationImpl::ContinuationImpl(NlsImpl &nls, const double *x0, double mu0) : s(nls) {
+  for (auto &h : hist) h.alloc(2 * s.N);
+  dots.alloc(8);
+  NOSH_CUDA(cudaMemcpyAsync(hist[0].p, x0, 2 * s.N * sizeof(double), cudaMemcpyDefault, s.stream));
+  mu[0] = mu0;
+  head = 0;
+  count = 1;
+  s.sync();
+}
+
+ContinuationImpl::~ContinuationImpl() = default;
+
+// phase-aligned Lagrange extrapolation of the newest (order+1) states to mu_new
+void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
+  cudaStream_t st = s.stream;
+  const double *x0 = slot(0), *x1 = order >= 1 ? slot(1) : slot(0), *x2 = order >= 2 ? slot(2) : slot(0);
+  const double t = mu_new, t0 = mu_of(0), t1 = order >= 1 ? mu_of(1) : 0.0, t2 = order >= 2 ? mu_of(2) : 0.0;
+  double L0 = 1.0, L1 = 0.0, L2 = 0.0;
+  if (order == 1) {
+    L0 = (t - t1) / (t0 - t1);
+    L1 = (t - t0) / (t1 - t0);
+  } else if (order == 2) {
+    L0 = (t - t1) * (t - t2) / ((t0 - t1) * (t0 - t2));
+    L1 = (t - t0) * (t - t2) / ((t1 - t0) * (t1 - t2));
+    L2 = (t - t0) * (t - t1) / ((t2 - t0) * (t2 - t1));
+  }
+  const int G = vgrid(s.N);
+  if (order >= 1) {
+    cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)x1, (const C2<double> *)x0, s.red.partials.p,
+                                    s.red.counter.p, dots.p);
+    ++s.launch_count;
+  }
+  if (order >= 2) {
+    cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)x2, (const C2<double> *)x0, s.red.partials.p,
+                                    s.red.counter.p, dots.p + 2);
+    ++s.launch_count;
+  }
+  extrapolate_kernel<<<G, 256, 0, st>>>(s.N, order, dots.p, L0, L1, L2, (const C2<double> *)x0,
+                                        (const C2<double> *)x1, (const C2<double> *)x2, (C2<double> *)out);
+  ++s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+}
+
+void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_options &opt,
+                               nosh_newton_stats &st) {
+  NOSH_CHECK(predictor == NOSH_PREDICT_NONE || predictor == NOSH_PREDICT_SECANT ||
+                 predictor == NOSH_PREDICT_QUADRATIC || predictor == NOSH_PREDICT_LEARNED,
+             NOSH_ERR_INVALID, "continuation handles predict NONE, SECANT, QUADRATIC or LEARNED");
+  NOSH_CHECK(mu_new != mu_of(0), NOSH_ERR_INVALID, "mu_new equals the current mu");
+  NewtonState &ns = state_of(s);
+  const double g = s.g0;
+  int order = 0;
+  if (predictor == NOSH_PREDICT_SECANT || predictor == NOSH_PREDICT_LEARNED) order = 1;
+  if (predictor == NOSH_PREDICT_QUADRATIC) order = 2;
+  order = std::min(order, count - 1);
+  last_used = order == 0 ? NOSH_PREDICT_NONE : (order == 1 ? NOSH_PREDICT_SECANT : NOSH_PREDICT_QUADRATIC);
+  f_learned = std::nan("");
+  f_secant = std::nan("");
+  extrapolate(order, mu_new, ns.psi.p);
+  if (predictor == NOSH_PREDICT_LEARNED && net && net->trained() && count >= 3) {
+    // learned correction of the secant prediction; keep whichever starts
+    // Newton from the smaller residual (the secant is the fallback)
+    f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.f.p);
+    NOSH_CUDA(cudaMemcpyAsync(ns.tmp.p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
+    net->predict(slot(0), slot(1), slot(2), mu_of(0), mu_of(1), mu_of(2), mu_new, ns.tmp.p);
+    f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
+    if (f_learned < f_secant) {
+      std::swap(ns.psi, ns.tmp);
+      last_used = NOSH_PREDICT_LEARNED;
+    }
+  }
+  newton_core(s, ns, g, mu_new, opt, st);
+  if (st.status != NOSH_OK) return;
+  // push the converged state
+  head = (head + 1) % kHist;
+  NOSH_CUDA(cudaMemcpyAsync(hist[head].p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice,
+                            s.stream));
+  mu[head] = mu_new;
+  count = std::min(count + 1, kHist);
+  // online training on the transition (x_{k-2}, x_{k-1}, x_k) -> x_{k+1}
+  if (net && train_left > 0 && count >= 4) {
+    train_loss = net->train(slot(1), slot(2), slot(3), mu_of(1), mu_of(2), mu_of(3), slot(0), mu_of(0),
+                            iters_per_step, learning_rate);
+    train_left--;
+    if (train_left == 0) net->set_trained(true);
+  }
+  s.sync();
+}
+
+void ContinuationImpl::enable_learning(int train_steps, int iters, double lr) {
+  if (!net) net.reset(new Mpnn(s));
+  train_left = train_steps;
+  iters_per_step = iters;
+  learning_rate = lr;
+  net->set_trained(train_steps == 0);
+}
+
+}  // namespace nosh

@@ -1,0 +1,861 @@
+// Learned continuation predictor: an edge message-passing network that
+// corrects the secant prediction of the next continuation state, trained
+// online on the states the continuation itself converges to.
+//
+// Network (hidden width 64, 3 message-passing layers):
+//   x_i   = [Re/Im psi_k, Re/Im s~, Re/Im q~, mu_new, 1]           (8)
+//           s~ = secant step / rms, q~ = (quadratic - secant) / rms_q
+//   e_ij  = [alpha_e / mean|alpha|, +-p_e / rms p, |e| / mean|e|, 1]  (4)
+//   h0    = relu(x W_enc + b_enc)
+//   layer: A = h W_a, B = h W_b,
+//          M_i = sum_j relu(A_i + B_j + e_ij W_c + b_m),
+//          h  <- h + relu([h, M] W_u + b_u)
+//   y_i   = h W_dec + b_dec                                          (2)
+//   prediction = secant + rms_q * y
+// Node GEMMs run on the tensor cores with BF16 operands and FP32
+// accumulation (mma.sync m16n8k16); edge aggregation, weight gradients and
+// the optimiser are FP32.  Every reduction is deterministic (block partials
+// summed in a fixed order).
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <vector>
+
+#include "mpnn.cuh"
+#include "spmv.cuh"
+
+namespace nosh {
+
+using namespace dev;
+
+namespace {
+
+constexpr int H = 64;      // hidden width
+constexpr int FX = 8;      // node input features
+constexpr int FE = 4;      // edge features
+constexpr int LAYERS = 3;
+
+// flat parameter layout (FP32 master copy)
+struct Layout {
+  int64_t enc_w, enc_b, dec_w, dec_b, total;
+  int64_t wa[LAYERS], wb[LAYERS], wc[LAYERS], bm[LAYERS], wu[LAYERS], bu[LAYERS];
+  Layout() {
+    int64_t o = 0;
+    enc_w = o; o += FX * H;
+    enc_b = o; o += H;
+    for (int l = 0; l < LAYERS; l++) {
+      wa[l] = o; o += H * H;
+      wb[l] = o; o += H * H;
+      wc[l] = o; o += FE * H;
+      bm[l] = o; o += H;
+      wu[l] = o; o += 2 * H * H;
+      bu[l] = o; o += H;
+    }
+    dec_w = o; o += H * 2;
+    dec_b = o; o += 2;
+    total = o;
+  }
+};
+
+// ------------------------------------------------ tensor-core node GEMM
+// out[r, 0:64] = epilogue( [in0[r, 0:K0], in1[r, 0:K1]] @ W ), W stored as
+// Wt[64][K] BF16 (transposed, K = K0 + K1 <= 128, K0, K1 multiples of 16
+// or K1 = 0).  One warp per 16 rows, 4 warps per CTA.
+enum Epi { EPI_LINEAR = 0, EPI_BIAS_RELU = 1, EPI_RESID_RELU = 2, EPI_ACCUM = 3 };
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128) gemm64_kernel(int64_t n, const float *__restrict__ in0, int K0,
+                                                     const float *__restrict__ in1, int K1,
+                                                     const __nv_bfloat16 *__restrict__ Wt,
+                                                     const float *__restrict__ bias, float *__restrict__ out,
+                                                     float *__restrict__ out2) {
+  constexpr int KMAX = 128, LD = KMAX + 8;  // padded rows: conflict-free
+  __shared__ __align__(16) __nv_bfloat16 sW[H * LD];
+  const int K = K0 + K1;
+  for (int q = threadIdx.x; q < H * K; q += blockDim.x) sW[(q / K) * LD + (q % K)] = Wt[q];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tig = lane & 3;
+  const int64_t r0 = (blockIdx.x * 4 + warp) * 16;
+  if (r0 >= n) return;
+  const int64_t ra = r0 + g, rb = r0 + g + 8;
+  float acc[8][4];
+#pragma unroll
+  for (int t = 0; t < 8; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+  for (int kk = 0; kk < K; kk += 16) {
+    const float *src = kk < K0 ? in0 : in1;
+    const int ld = kk < K0 ? K0 : K1, kc = kk < K0 ? kk : kk - K0;
+    float2 a[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    if (ra < n) {
+      a[0] = *reinterpret_cast<const float2 *>(src + ra * ld + kc + tig * 2);
+      a[2] = *reinterpret_cast<const float2 *>(src + ra * ld + kc + tig * 2 + 8);
+    }
+    if (rb < n) {
+      a[1] = *reinterpret_cast<const float2 *>(src + rb * ld + kc + tig * 2);
+      a[3] = *reinterpret_cast<const float2 *>(src + rb * ld + kc + tig * 2 + 8);
+    }
+    const uint32_t a0 = pack_bf16(a[0].x, a[0].y), a1 = pack_bf16(a[1].x, a[1].y);
+    const uint32_t a2 = pack_bf16(a[2].x, a[2].y), a3 = pack_bf16(a[3].x, a[3].y);
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const __nv_bfloat16 *w = sW + (t * 8 + g) * LD + kk + tig * 2;
+      const uint32_t b0 = *reinterpret_cast<const uint32_t *>(w);
+      const uint32_t b1 = *reinterpret_cast<const uint32_t *>(w + 8);
+      mma_bf16(acc[t], a0, a1, a2, a3, b0, b1);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    const int c = t * 8 + tig * 2;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      const int64_t r = half ? rb : ra;
+      if (r >= n) continue;
+      float v0 = acc[t][2 * half], v1 = acc[t][2 * half + 1];
+      float2 *o = reinterpret_cast<float2 *>(out + r * H + c);
+      if (EPI == EPI_LINEAR) {
+        *o = make_float2(v0, v1);
+      } else if (EPI == EPI_ACCUM) {
+        const float2 p = *o;
+        *o = make_float2(p.x + v0, p.y + v1);
+      } else if (EPI == EPI_BIAS_RELU) {
+        *o = make_float2(fmaxf(v0 + bias[c], 0.f), fmaxf(v1 + bias[c + 1], 0.f));
+      } else {  // residual: out2 = relu(acc + b) (kept for the backward pass), out += out2
+        const float u0 = fmaxf(v0 + bias[c], 0.f), u1 = fmaxf(v1 + bias[c + 1], 0.f);
+        *reinterpret_cast<float2 *>(out2 + r * H + c) = make_float2(u0, u1);
+        const float2 p = *o;
+        *o = make_float2(p.x + u0, p.y + u1);
+      }
+    }
+  }
+}
+
+// forward operand: W (K x ncols, row-major FP32 inside the parameter
+// vector) -> Wt[64][K] BF16 with Wt[n][k] = W[k][col0 + n]
+__global__ void to_bf16_t(const float *__restrict__ W, int K, int ncols, int col0, __nv_bfloat16 *__restrict__ Wt) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= H * K) return;
+  const int n = q / K, k = q % K;
+  Wt[q] = __float2bfloat16(W[(int64_t)k * ncols + col0 + n]);
+}
+
+// encoder operand: Wt[n][k] = W[k][n] for k < 8, zero for the padding k < 16
+__global__ void enc_to_bf16(const float *__restrict__ W, __nv_bfloat16 *__restrict__ Wt) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= H * 16) return;
+  const int n = q / 16, k = q % 16;
+  Wt[q] = __float2bfloat16(k < FX ? W[k * H + n] : 0.f);
+}
+
+__global__ void to_bf16_rows(const float *__restrict__ W, int rows, int row0, __nv_bfloat16 *__restrict__ Wt) {
+  // Wt[n][k] = W[row0 + n][k] for a row-major [* x 64] W: the operand of
+  // dIn[:, row0:row0+64] = dOut @ W[row0:row0+64, :]^T
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= H * H) return;
+  const int n = q / H, k = q % H;
+  Wt[q] = __float2bfloat16(W[(int64_t)(row0 + n) * H + k]);
+  (void)rows;
+}
+
+// ----------------------------------------------------------- edge kernels
+// one warp per row i, 2 features per lane
+__global__ void edge_forward(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                             const float *__restrict__ ef, const float *__restrict__ A,
+                             const float *__restrict__ B, const float *__restrict__ Wc,
+                             const float *__restrict__ bm, float *__restrict__ M) {
+  const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const int c = lane * 2;
+  float w[FE][2];
+#pragma unroll
+  for (int f = 0; f < FE; f++) {
+    w[f][0] = Wc[f * H + c];
+    w[f][1] = Wc[f * H + c + 1];
+  }
+  const float2 a = *reinterpret_cast<const float2 *>(A + i * H + c);
+  const float b0 = a.x + bm[c], b1 = a.y + bm[c + 1];
+  float m0 = 0.f, m1 = 0.f;
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
+    const int32_t j = ci[k];
+    const float2 bj = *reinterpret_cast<const float2 *>(B + (int64_t)j * H + c);
+    const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)k * FE);
+    const float p0 = b0 + bj.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
+    const float p1 = b1 + bj.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
+    m0 += fmaxf(p0, 0.f);
+    m1 += fmaxf(p1, 0.f);
+  }
+  *reinterpret_cast<float2 *>(M + i * H + c) = make_float2(m0, m1);
+}
+
+// dA_i = sum_j dM_i [P_ij > 0]; also block partials of dW_c (4 x 64) and
+// db_m (64): rows of the partial buffer hold 5 x 64 floats per CTA
+__global__ void edge_backward_a(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                                const float *__restrict__ ef, const float *__restrict__ A,
+                                const float *__restrict__ B, const float *__restrict__ Wc,
+                                const float *__restrict__ bm, const float *__restrict__ dM,
+                                float *__restrict__ dA, float *__restrict__ part) {
+  __shared__ float red[8][5][H];  // 8 warps per CTA, 8 rows per warp
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = lane * 2;
+  float gw[5][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  for (int rr = 0; rr < 8; rr++) {
+    const int64_t i = ((int64_t)blockIdx.x * 8 + warp) * 8 + rr;
+    if (i >= n) break;
+    float w[FE][2];
+#pragma unroll
+    for (int f = 0; f < FE; f++) {
+      w[f][0] = Wc[f * H + c];
+      w[f][1] = Wc[f * H + c + 1];
+    }
+    const float2 a = *reinterpret_cast<const float2 *>(A + i * H + c);
+    const float2 dm = *reinterpret_cast<const float2 *>(dM + i * H + c);
+    const float b0 = a.x + bm[c], b1 = a.y + bm[c + 1];
+    float s0 = 0.f, s1 = 0.f;
+    for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
+      const int32_t j = ci[k];
+      const float2 bj = *reinterpret_cast<const float2 *>(B + (int64_t)j * H + c);
+      const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)k * FE);
+      const float p0 = b0 + bj.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
+      const float p1 = b1 + bj.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
+      const float g0 = p0 > 0.f ? dm.x : 0.f, g1 = p1 > 0.f ? dm.y : 0.f;
+      s0 += g0;
+      s1 += g1;
+      gw[0][0] += e.x * g0; gw[0][1] += e.x * g1;
+      gw[1][0] += e.y * g0; gw[1][1] += e.y * g1;
+      gw[2][0] += e.z * g0; gw[2][1] += e.z * g1;
+      gw[3][0] += e.w * g0; gw[3][1] += e.w * g1;
+      gw[4][0] += g0; gw[4][1] += g1;
+    }
+    *reinterpret_cast<float2 *>(dA + i * H + c) = make_float2(s0, s1);
+  }
+#pragma unroll
+  for (int f = 0; f < 5; f++) {
+    red[warp][f][c] = gw[f][0];
+    red[warp][f][c + 1] = gw[f][1];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < 5 * H; q += blockDim.x) {
+    float s = 0.f;
+    for (int w8 = 0; w8 < 8; w8++) s += red[w8][q / H][q % H];
+    part[(int64_t)blockIdx.x * 5 * H + q] = s;
+  }
+}
+
+// dB_j = sum over the rows i that receive from j of dM_i [P_ij > 0]: row j
+// of the symmetric graph lists those i; tr[k] is the position of (i, j)
+__global__ void edge_backward_b(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                                const int32_t *__restrict__ tr, const float *__restrict__ ef,
+                                const float *__restrict__ A, const float *__restrict__ B,
+                                const float *__restrict__ Wc, const float *__restrict__ bm,
+                                const float *__restrict__ dM, float *__restrict__ dB) {
+  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= n) return;
+  const int c = lane * 2;
+  float w[FE][2];
+#pragma unroll
+  for (int f = 0; f < FE; f++) {
+    w[f][0] = Wc[f * H + c];
+    w[f][1] = Wc[f * H + c + 1];
+  }
+  const float2 bj = *reinterpret_cast<const float2 *>(B + j * H + c);
+  const float c0 = bj.x + bm[c], c1 = bj.y + bm[c + 1];
+  float s0 = 0.f, s1 = 0.f;
+  for (int32_t k = rp[j]; k < rp[j + 1]; k++) {
+    const int32_t i = ci[k];
+    const float2 ai = *reinterpret_cast<const float2 *>(A + (int64_t)i * H + c);
+    const float2 dm = *reinterpret_cast<const float2 *>(dM + (int64_t)i * H + c);
+    const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)tr[k] * FE);
+    const float p0 = c0 + ai.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
+    const float p1 = c1 + ai.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
+    s0 += p0 > 0.f ? dm.x : 0.f;
+    s1 += p1 > 0.f ? dm.y : 0.f;
+  }
+  *reinterpret_cast<float2 *>(dB + j * H + c) = make_float2(s0, s1);
+}
+
+// ------------------------------------------------- weight gradients (FP32)
+// part[cta][k][c] = sum over the CTA's rows of in[r][k] * dout[r][c] (c <
+// 64) and, in row K, sum of dout[r][c] (bias gradient).  in = [in0 | in1].
+constexpr int WG_ROWS = 1024;
+__global__ void __launch_bounds__(256) wgrad_kernel(int64_t n, const float *__restrict__ in0, int K0,
+                                                    const float *__restrict__ in1, int K1,
+                                                    const float *__restrict__ dout, int ncol,
+                                                    float *__restrict__ part) {
+  __shared__ float sin_[32][129];
+  __shared__ float sd[32][65];
+  const int K = K0 + K1;
+  const int64_t rbeg = (int64_t)blockIdx.x * WG_ROWS, rend = min((int64_t)n, rbeg + WG_ROWS);
+  // each thread owns outputs q = tid + 256 * m over (K + 1) x ncol
+  const int nout = (K + 1) * ncol;
+  float acc[33];
+#pragma unroll
+  for (int m = 0; m < 33; m++) acc[m] = 0.f;
+  for (int64_t r0 = rbeg; r0 < rend; r0 += 32) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < 32 * K; q += blockDim.x) {
+      const int rr = q / K, k = q % K;
+      const int64_t r = r0 + rr;
+      float v = 0.f;
+      if (r < rend) v = k < K0 ? in0[r * K0 + k] : in1[r * K1 + (k - K0)];
+      sin_[rr][k] = v;
+    }
+    for (int q = threadIdx.x; q < 32 * ncol; q += blockDim.x) {
+      const int rr = q / ncol, c = q % ncol;
+      const int64_t r = r0 + rr;
+      sd[rr][c] = r < rend ? dout[r * ncol + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 33; m++) {
+      const int q = threadIdx.x + 256 * m;
+      if (q >= nout) break;
+      const int k = q / ncol, c = q % ncol;
+      float s = 0.f;
+      if (k < K) {
+        for (int rr = 0; rr < 32; rr++) s += sin_[rr][k] * sd[rr][c];
+      } else {
+        for (int rr = 0; rr < 32; rr++) s += sd[rr][c];
+      }
+      acc[m] += s;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 33; m++) {
+    const int q = threadIdx.x + 256 * m;
+    if (q >= nout) break;
+    part[(int64_t)blockIdx.x * nout + q] = acc[m];
+  }
+}
+
+// grad[dst + q] (+)= sum_b part[b][q], fixed order; q < count.  The bias row
+// (q >= bias_from) goes to grad[bias_dst + q - bias_from] when bias_dst >= 0.
+__global__ void reduce_parts(int nparts, int count, const float *__restrict__ part, float *__restrict__ grad,
+                             int64_t dst, int bias_from, int64_t bias_dst, int accumulate) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= count) return;
+  float s = 0.f;
+  for (int b = 0; b < nparts; b++) s += part[(int64_t)b * count + q];
+  int64_t o;
+  if (q >= bias_from) {
+    if (bias_dst < 0) return;
+    o = bias_dst + (q - bias_from);
+  } else {
+    o = dst + q;
+  }
+  grad[o] = accumulate ? grad[o] + s : s;
+}
+
+// ------------------------------------------------------- small node kernels
+__global__ void decoder_forward(int64_t n, const float *__restrict__ h, const float *__restrict__ W,
+                                const float *__restrict__ b, float *__restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float y0 = b[0], y1 = b[1];
+  for (int k = 0; k < H; k++) {
+    const float v = h[i * H + k];
+    y0 += v * W[k * 2];
+    y1 += v * W[k * 2 + 1];
+  }
+  y[2 * i] = y0;
+  y[2 * i + 1] = y1;
+}
+
+// loss = sum |y - t|^2 / n (grid reduction), dy = 2 (y - t) / n
+__global__ void loss_kernel(int64_t n, const float *__restrict__ y, const float *__restrict__ t,
+                            float *__restrict__ dy, double *partials, unsigned *counter, double *loss) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (i < n) {
+    const float e0 = y[2 * i] - t[2 * i], e1 = y[2 * i + 1] - t[2 * i + 1];
+    dy[2 * i] = 2.f * e0 / (float)n;
+    dy[2 * i + 1] = 2.f * e1 / (float)n;
+    v = ((double)e0 * e0 + (double)e1 * e1) / (double)n;
+  }
+  grid_reduce(v, partials, counter, loss);
+}
+
+// dh = dy W_dec^T
+__global__ void decoder_backward(int64_t n, const float *__restrict__ dy, const float *__restrict__ W,
+                                 float *__restrict__ dh) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n * H) return;
+  const int64_t i = q / H;
+  const int k = (int)(q % H);
+  dh[q] = dy[2 * i] * W[k * 2] + dy[2 * i + 1] * W[k * 2 + 1];
+}
+
+// g *= [r > 0] (relu mask from the post-activation)
+__global__ void relu_mask(int64_t n, const float *__restrict__ r, const float *__restrict__ g,
+                          float *__restrict__ out) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < n) out[q] = r[q] > 0.f ? g[q] : 0.f;
+}
+
+
+// Adam (Kingma & Ba 2015), bias-corrected, FP32
+__global__ void adam_kernel(int64_t n, float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                            float *__restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float gq = g[q];
+  const float mq = b1 * m[q] + (1.f - b1) * gq, vq = b2 * v[q] + (1.f - b2) * gq * gq;
+  m[q] = mq;
+  v[q] = vq;
+  p[q] -= lr * (mq / c1) / (sqrtf(vq / c2) + eps);
+}
+
+// ----------------------------------------------------------- features
+// s = x0 - e1 x1 (secant step), q = quadratic - secant extrapolation to t,
+// sums of |s|^2 and |q|^2 into red[0], red[1]
+__global__ void features_a(int64_t n, const double *__restrict__ c, double L0s, double L1s, double L0q,
+                           double L1q, double L2q, const C2<double> *__restrict__ x0,
+                           const C2<double> *__restrict__ x1, const C2<double> *__restrict__ x2,
+                           double *__restrict__ sq, double *partials, unsigned *counter, double *red) {
+  double e1r = 1.0, e1i = 0.0, e2r = 1.0, e2i = 0.0;
+  {
+    const double m1 = sqrt(c[0] * c[0] + c[1] * c[1]), m2 = sqrt(c[2] * c[2] + c[3] * c[3]);
+    if (m1 > 0) { e1r = c[0] / m1; e1i = c[1] / m1; }
+    if (m2 > 0) { e2r = c[2] / m2; e2i = c[3] / m2; }
+  }
+  double as = 0.0, aq = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> a = x0[i], p = x1[i], r = x2[i];
+    const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
+    const double rr = e2r * r.x - e2i * r.y, ri = e2r * r.y + e2i * r.x;
+    const double sr = a.x - pr, si = a.y - pi;
+    const double secr = L0s * a.x + L1s * pr, seci = L0s * a.y + L1s * pi;
+    const double qr = L0q * a.x + L1q * pr + L2q * rr - secr, qi = L0q * a.y + L1q * pi + L2q * ri - seci;
+    sq[4 * i] = sr;
+    sq[4 * i + 1] = si;
+    sq[4 * i + 2] = qr;
+    sq[4 * i + 3] = qi;
+    as += sr * sr + si * si;
+    aq += qr * qr + qi * qi;
+  }
+  grid_reduce(as, partials, counter, red);
+  grid_reduce(aq, partials + gridDim.x, counter + 1, red + 1);
+}
+
+// X = [x0, s / rms_s, q / rms_q, mu_new, 1]; with a target, T = (e_t x_t -
+// secant) / rms_q; red[0..1] hold the sums of squares
+__global__ void features_b(int64_t n, const double *__restrict__ red, double mu_new, const C2<double> *__restrict__ x0,
+                           const double *__restrict__ sq, float *__restrict__ X, const double *__restrict__ ct,
+                           double L0s, double L1s, const C2<double> *__restrict__ x1,
+                           const double *__restrict__ c, const C2<double> *__restrict__ xt,
+                           float *__restrict__ T) {
+  const double rs = sqrt(red[0] / n), rq = sqrt(red[1] / n);
+  const double is = rs > 0 ? 1.0 / rs : 0.0, iq = rq > 0 ? 1.0 / rq : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> a = x0[i];
+    float *xi = X + i * FX;
+    xi[0] = (float)a.x;
+    xi[1] = (float)a.y;
+    xi[2] = (float)(sq[4 * i] * is);
+    xi[3] = (float)(sq[4 * i + 1] * is);
+    xi[4] = (float)(sq[4 * i + 2] * iq);
+    xi[5] = (float)(sq[4 * i + 3] * iq);
+    xi[6] = (float)mu_new;
+    xi[7] = 1.f;
+    if (T) {
+      double e1r = 1.0, e1i = 0.0, etr = 1.0, eti = 0.0;
+      const double m1 = sqrt(c[0] * c[0] + c[1] * c[1]), mt = sqrt(ct[0] * ct[0] + ct[1] * ct[1]);
+      if (m1 > 0) { e1r = c[0] / m1; e1i = c[1] / m1; }
+      if (mt > 0) { etr = ct[0] / mt; eti = ct[1] / mt; }
+      const C2<double> p = x1[i], t = xt[i];
+      const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
+      const double secr = L0s * a.x + L1s * pr, seci = L0s * a.y + L1s * pi;
+      const double tr = etr * t.x - eti * t.y, ti = etr * t.y + eti * t.x;
+      T[2 * i] = (float)((tr - secr) * iq);
+      T[2 * i + 1] = (float)((ti - seci) * iq);
+    }
+  }
+}
+
+// out += rms_q * y
+__global__ void apply_correction(int64_t n, const double *__restrict__ red, const float *__restrict__ y,
+                                 C2<double> *__restrict__ out) {
+  const double rq = sqrt(red[1] / n);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    C2<double> o = out[i];
+    o.x += rq * (double)y[2 * i];
+    o.y += rq * (double)y[2 * i + 1];
+    out[i] = o;
+  }
+}
+
+__global__ void cdot_pair(int64_t n, const C2<double> *__restrict__ a, const C2<double> *__restrict__ b,
+                          double *partials, unsigned *counter, double *out) {
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> x = a[i], y = b[i];
+    re += x.x * y.x + x.y * y.y;
+    im += x.x * y.y - x.y * y.x;
+  }
+  grid_reduce(re, partials, counter, out);
+  grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
+}
+
+// per-nonzero edge features and the transpose map of the symmetric graph
+__global__ void edge_setup(int64_t nnz, const int32_t *__restrict__ nz_edge, const int32_t *__restrict__ pf,
+                           const int32_t *__restrict__ pb, const double *__restrict__ alpha,
+                           const double *__restrict__ p, const double *__restrict__ len, double ia, double ip,
+                           double il, float *__restrict__ ef, int32_t *__restrict__ tr) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nnz) return;
+  const int32_t z = nz_edge[k];
+  const int32_t e = z >= 0 ? z : ~z;
+  const double sgn = z >= 0 ? 1.0 : -1.0;
+  float4 f;
+  f.x = (float)(alpha[e] * ia);
+  f.y = (float)(sgn * p[e] * ip);
+  f.z = (float)(len[e] * il);
+  f.w = 1.f;
+  *reinterpret_cast<float4 *>(ef + k * FE) = f;
+  tr[k] = z >= 0 ? pb[e] : pf[e];
+}
+
+inline int vgrid(int64_t n) { return (int)std::min<int64_t>(div_up(n, 256), kNumSMs * 8); }
+
+// splitmix64 for deterministic initialisation
+inline uint64_t sm64(uint64_t &s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ impl
+struct Mpnn::Impl {
+  NlsImpl &s;
+  Layout L;
+  int64_t N, nnz;
+  DevBuf<float> ef;
+  DevBuf<int32_t> tr;
+  DevBuf<float> params, grads, am, av;
+  int64_t adam_t = 0;
+  // BF16 transposed operands: forward W (enc padded to K=16, wa, wb, wu per
+  // layer) and backward W^T blocks
+  DevBuf<__nv_bfloat16> wt;
+  int64_t wt_enc, wt_a[LAYERS], wt_b[LAYERS], wt_u[LAYERS], wtb_a[LAYERS], wtb_b[LAYERS], wtb_uh[LAYERS],
+      wtb_um[LAYERS];
+  // activations and gradients
+  DevBuf<float> X, Xp, Hs[LAYERS + 1], A[LAYERS], B[LAYERS], Mg[LAYERS], R[LAYERS], Y, T, dY;
+  DevBuf<float> dH, dR, dM, dA, dB, tmp;
+  DevBuf<float> part;
+  DevBuf<double> sq, red, dots;
+  DevBuf<double> loss;
+  explicit Impl(NlsImpl &nls);
+  void refresh_bf16();
+  void forward();
+  double backward_and_step(float lr);
+  void features(const double *x0, const double *x1, const double *x2, double mu0, double mu1, double mu2,
+                double mu_t, const double *target);
+  void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, const float *bias,
+            float *out, float *out2);
+  void wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol, int64_t dst,
+             int64_t bias_dst);
+};
+
+Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
+  cudaStream_t st = s.stream;
+  MeshImpl &m = *s.mesh;
+  // normalisation of the edge features from the mesh and fields
+  std::vector<double> alpha(s.E), p(s.E);
+  s.d_alpha.download(alpha.data(), s.E, st);
+  s.d_p.download(p.data(), s.E, st);
+  s.sync();
+  double sa = 0, sp = 0, sl = 0;
+  for (int64_t e = 0; e < s.E; e++) {
+    sa += std::fabs(alpha[e]);
+    sp += p[e] * p[e];
+    sl += m.h_len[e];
+  }
+  const double ia = sa > 0 ? s.E / sa : 1.0, ip = sp > 0 ? 1.0 / std::sqrt(sp / s.E) : 1.0,
+               il = sl > 0 ? s.E / sl : 1.0;
+  ef.alloc(nnz * FE);
+  tr.alloc(nnz);
+  edge_setup<<<div_up(nnz, 256), 256, 0, st>>>(nnz, m.d_nz_edge.p, m.d_pos_fwd.p, m.d_pos_bwd.p, s.d_alpha.p,
+                                               s.d_p.p, m.d_len.p, ia, ip, il, ef.p, tr.p);
+  NOSH_CUDA(cudaGetLastError());
+  // parameters: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero
+  // biases, a small decoder so the first predictions stay near the secant
+  std::vector<float> h(L.total, 0.f);
+  uint64_t seed = 0x6e6f7368ULL;
+  auto fill = [&](int64_t off, int64_t count, int fan_in, float scale) {
+    const float b = scale / std::sqrt((float)fan_in);
+    for (int64_t q = 0; q < count; q++) h[off + q] = b * (2.f * (float)((sm64(seed) >> 11) * 0x1.0p-53) - 1.f);
+  };
+  fill(L.enc_w, FX * H, FX, 1.f);
+  for (int l = 0; l < LAYERS; l++) {
+    fill(L.wa[l], H * H, H, 1.f);
+    fill(L.wb[l], H * H, H, 1.f);
+    fill(L.wc[l], FE * H, FE, 1.f);
+    fill(L.wu[l], 2 * H * H, 2 * H, 1.f);
+  }
+  fill(L.dec_w, H * 2, H, 0.1f);
+  params.upload(h, st);
+  grads.alloc(L.total);
+  am.alloc(L.total);
+  av.alloc(L.total);
+  am.zero(st);
+  av.zero(st);
+  // BF16 operand offsets
+  int64_t o = 0;
+  wt_enc = o; o += H * 16;
+  for (int l = 0; l < LAYERS; l++) {
+    wt_a[l] = o; o += H * H;
+    wt_b[l] = o; o += H * H;
+    wt_u[l] = o; o += H * 2 * H;
+    wtb_a[l] = o; o += H * H;
+    wtb_b[l] = o; o += H * H;
+    wtb_uh[l] = o; o += H * H;
+    wtb_um[l] = o; o += H * H;
+  }
+  wt.alloc(o);
+  wt.zero(st);
+  X.alloc(N * FX);
+  Xp.alloc(N * 16);
+  Xp.zero(st);
+  for (auto &b : Hs) b.alloc(N * H);
+  for (int l = 0; l < LAYERS; l++) {
+    A[l].alloc(N * H);
+    B[l].alloc(N * H);
+    Mg[l].alloc(N * H);
+    R[l].alloc(N * H);
+  }
+  Y.alloc(2 * N);
+  T.alloc(2 * N);
+  dY.alloc(2 * N);
+  for (DevBuf<float> *b : {&dH, &dR, &dM, &dA, &dB, &tmp}) b->alloc(N * 2 * H);
+  part.alloc(std::max<int64_t>(div_up(N, WG_ROWS) * (2 * H + 1) * H, div_up(N, 64) * 5 * H) + 64);
+  sq.alloc(4 * N);
+  red.alloc(8);
+  dots.alloc(8);
+  loss.alloc(1);
+  refresh_bf16();
+  s.sync();
+}
+
+void Mpnn::Impl::refresh_bf16() {
+  cudaStream_t st = s.stream;
+  const float *P = params.p;
+  // encoder: K = 8 features padded to 16 (the padded columns of Xp are 0)
+  enc_to_bf16<<<div_up(H * 16, 256), 256, 0, st>>>(P + L.enc_w, wt.p + wt_enc);
+  for (int l = 0; l < LAYERS; l++) {
+    to_bf16_t<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wa[l], H, H, 0, wt.p + wt_a[l]);
+    to_bf16_t<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wb[l], H, H, 0, wt.p + wt_b[l]);
+    to_bf16_t<<<div_up(H * 2 * H, 256), 256, 0, st>>>(P + L.wu[l], 2 * H, H, 0, wt.p + wt_u[l]);
+    // backward operands: dIn = dOut W^T  ->  Wt[n][k] = W[n][k]
+    to_bf16_rows<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wa[l], H, 0, wt.p + wtb_a[l]);
+    to_bf16_rows<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wb[l], H, 0, wt.p + wtb_b[l]);
+    to_bf16_rows<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wu[l], 2 * H, 0, wt.p + wtb_uh[l]);
+    to_bf16_rows<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wu[l], 2 * H, H, wt.p + wtb_um[l]);
+  }
+  NOSH_CUDA(cudaGetLastError());
+}
+
+void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off,
+                      const float *bias, float *out, float *out2) {
+  const int grid = div_up(N, 64);
+  cudaStream_t st = s.stream;
+  const __nv_bfloat16 *W = wt.p + wt_off;
+  switch (epi) {
+    case EPI_LINEAR: gemm64_kernel<EPI_LINEAR><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
+    case EPI_BIAS_RELU: gemm64_kernel<EPI_BIAS_RELU><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
+    case EPI_RESID_RELU: gemm64_kernel<EPI_RESID_RELU><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
+    default: gemm64_kernel<EPI_ACCUM><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
+  }
+  ++s.launch_count;
+}
+
+void Mpnn::Impl::forward() {
+  cudaStream_t st = s.stream;
+  const float *P = params.p;
+  MeshImpl &m = *s.mesh;
+  // encoder (features padded to 16 columns)
+  NOSH_CUDA(cudaMemcpy2DAsync(Xp.p, 16 * sizeof(float), X.p, FX * sizeof(float), FX * sizeof(float), N,
+                              cudaMemcpyDeviceToDevice, st));
+  gemm(EPI_BIAS_RELU, Xp.p, 16, nullptr, 0, wt_enc, P + L.enc_b, Hs[0].p, nullptr);
+  for (int l = 0; l < LAYERS; l++) {
+    gemm(EPI_LINEAR, Hs[l].p, H, nullptr, 0, wt_a[l], nullptr, A[l].p, nullptr);
+    gemm(EPI_LINEAR, Hs[l].p, H, nullptr, 0, wt_b[l], nullptr, B[l].p, nullptr);
+    edge_forward<<<div_up(N * 32, 256), 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l],
+                                                     P + L.bm[l], Mg[l].p);
+    ++s.launch_count;
+    NOSH_CUDA(cudaMemcpyAsync(Hs[l + 1].p, Hs[l].p, N * H * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    gemm(EPI_RESID_RELU, Hs[l].p, H, Mg[l].p, H, wt_u[l], P + L.bu[l], Hs[l + 1].p, R[l].p);
+  }
+  decoder_forward<<<div_up(N, 256), 256, 0, st>>>(N, Hs[LAYERS].p, P + L.dec_w, P + L.dec_b, Y.p);
+  ++s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+}
+
+void Mpnn::Impl::wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol,
+                       int64_t dst, int64_t bias_dst) {
+  cudaStream_t st = s.stream;
+  const int nb = div_up(N, WG_ROWS);
+  const int count = (K0 + K1 + 1) * ncol;
+  wgrad_kernel<<<nb, 256, 0, st>>>(N, in0, K0, in1, K1, dout, ncol, part.p);
+  reduce_parts<<<div_up(count, 256), 256, 0, st>>>(nb, count, part.p, grads.p, dst, (K0 + K1) * ncol, bias_dst, 0);
+  s.launch_count += 2;
+}
+
+double Mpnn::Impl::backward_and_step(float lr) {
+  cudaStream_t st = s.stream;
+  const float *P = params.p;
+  MeshImpl &m = *s.mesh;
+  loss_kernel<<<div_up(N, 256), 256, 0, st>>>(N, Y.p, T.p, dY.p, s.red.partials.p, s.red.counter.p, loss.p);
+  // decoder
+  wgrad(Hs[LAYERS].p, H, nullptr, 0, dY.p, 2, L.dec_w, L.dec_b);
+  decoder_backward<<<div_up(N * H, 256), 256, 0, st>>>(N, dY.p, P + L.dec_w, dH.p);
+  s.launch_count += 2;
+  for (int l = LAYERS - 1; l >= 0; l--) {
+    // h_{l+1} = h_l + R_l, R_l = relu([h_l, M_l] W_u + b_u)
+    relu_mask<<<div_up(N * H, 256), 256, 0, st>>>(N * H, R[l].p, dH.p, dR.p);
+    wgrad(Hs[l].p, H, Mg[l].p, H, dR.p, H, L.wu[l], L.bu[l]);
+    // dM = dR W_u[64:128]^T ; dh += dR W_u[0:64]^T (dh already holds the
+    // residual path)
+    gemm(EPI_LINEAR, dR.p, H, nullptr, 0, wtb_um[l], nullptr, dM.p, nullptr);
+    gemm(EPI_ACCUM, dR.p, H, nullptr, 0, wtb_uh[l], nullptr, dH.p, nullptr);
+    // message aggregation
+    const int nb8 = div_up(N, 64);
+    edge_backward_a<<<nb8, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l],
+                                         dM.p, dA.p, part.p);
+    reduce_parts<<<div_up(5 * H, 256), 256, 0, st>>>(nb8, 5 * H, part.p, grads.p, L.wc[l], 4 * H, L.bm[l], 0);
+    edge_backward_b<<<div_up(N * 32, 256), 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, tr.p, ef.p, A[l].p, B[l].p,
+                                                         P + L.wc[l], P + L.bm[l], dM.p, dB.p);
+    s.launch_count += 4;
+    // A = h W_a, B = h W_b
+    wgrad(Hs[l].p, H, nullptr, 0, dA.p, H, L.wa[l], -1);
+    wgrad(Hs[l].p, H, nullptr, 0, dB.p, H, L.wb[l], -1);
+    gemm(EPI_ACCUM, dA.p, H, nullptr, 0, wtb_a[l], nullptr, dH.p, nullptr);
+    gemm(EPI_ACCUM, dB.p, H, nullptr, 0, wtb_b[l], nullptr, dH.p, nullptr);
+  }
+  // encoder: h0 = relu(X W + b)
+  relu_mask<<<div_up(N * H, 256), 256, 0, st>>>(N * H, Hs[0].p, dH.p, dR.p);
+  ++s.launch_count;
+  wgrad(X.p, FX, nullptr, 0, dR.p, H, L.enc_w, L.enc_b);
+  adam_t++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)adam_t), c2 = 1.f - std::pow(b2, (float)adam_t);
+  adam_kernel<<<div_up(L.total, 256), 256, 0, st>>>(L.total, params.p, grads.p, am.p, av.p, lr, b1, b2, 1e-8f, c1, c2);
+  ++s.launch_count;
+  refresh_bf16();
+  double hl = 0.0;
+  loss.download(&hl, 1, st);
+  s.sync();
+  return hl;
+}
+
+void Mpnn::Impl::features(const double *x0, const double *x1, const double *x2, double mu0, double mu1,
+                          double mu2, double t, const double *target) {
+  cudaStream_t st = s.stream;
+  const int G = vgrid(N);
+  const double L0s = (t - mu1) / (mu0 - mu1), L1s = (t - mu0) / (mu1 - mu0);
+  const double L0q = (t - mu1) * (t - mu2) / ((mu0 - mu1) * (mu0 - mu2));
+  const double L1q = (t - mu0) * (t - mu2) / ((mu1 - mu0) * (mu1 - mu2));
+  const double L2q = (t - mu0) * (t - mu1) / ((mu2 - mu0) * (mu2 - mu1));
+  cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)x1, (const C2<double> *)x0, s.red.partials.p, s.red.counter.p,
+                               dots.p);
+  cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)x2, (const C2<double> *)x0, s.red.partials.p, s.red.counter.p,
+                               dots.p + 2);
+  if (target)
+    cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)target, (const C2<double> *)x0, s.red.partials.p,
+                                 s.red.counter.p, dots.p + 4);
+  features_a<<<G, 256, 0, st>>>(N, dots.p, L0s, L1s, L0q, L1q, L2q, (const C2<double> *)x0,
+                                (const C2<double> *)x1, (const C2<double> *)x2, sq.p, s.red.partials.p,
+                                s.red.counter.p, red.p);
+  features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x0, sq.p, X.p, dots.p + 4, L0s, L1s,
+                                (const C2<double> *)x1, dots.p, (const C2<double> *)target,
+                                target ? T.p : nullptr);
+  s.launch_count += target ? 5 : 4;
+  NOSH_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- facade
+Mpnn::Mpnn(NlsImpl &s) : impl(new Impl(s)) {}
+Mpnn::~Mpnn() = default;
+
+void Mpnn::predict(const double *x0, const double *x1, const double *x2, double mu0, double mu1, double mu2,
+                   double mu_new, double *out) {
+  Impl &I = *impl;
+  I.features(x0, x1, x2, mu0, mu1, mu2, mu_new, nullptr);
+  I.forward();
+  apply_correction<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.red.p, I.Y.p, (C2<double> *)out);
+  ++I.s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+}
+
+double Mpnn::train(const double *x0, const double *x1, const double *x2, double mu0, double mu1, double mu2,
+                   const double *target, double mu_t, int iters, double lr) {
+  Impl &I = *impl;
+  I.features(x0, x1, x2, mu0, mu1, mu2, mu_t, target);
+  double l = std::nan("");
+  for (int k = 0; k < iters; k++) {
+    I.forward();
+    l = I.backward_and_step((float)lr);
+  }
+  return l;
+}
+
+// ------------------------------------------ hooks for the gradient checks
+int64_t Mpnn::num_params() const { return impl->L.total; }
+void Mpnn::get_params(float *h) const {
+  impl->params.download(h, impl->L.total, impl->s.stream);
+  impl->s.sync();
+}
+void Mpnn::set_params(const float *h) {
+  impl->params.upload(h, impl->L.total, impl->s.stream);
+  impl->refresh_bf16();
+  impl->s.sync();
+}
+void Mpnn::get_edge_features(float *h) const {
+  impl->ef.download(h, impl->nnz * FE, impl->s.stream);
+  impl->s.sync();
+}
+void Mpnn::forward_features(const float *X, float *Y) {
+  Impl &I = *impl;
+  I.X.upload(X, I.N * FX, I.s.stream);
+  I.forward();
+  I.Y.download(Y, 2 * I.N, I.s.stream);
+  I.s.sync();
+}
+double Mpnn::loss_and_grad(const float *X, const float *T, float *grad) {
+  Impl &I = *impl;
+  I.X.upload(X, I.N * FX, I.s.stream);
+  I.T.upload(T, 2 * I.N, I.s.stream);
+  I.forward();
+  // backward without the optimiser step: reuse backward_and_step with lr 0
+  // and restore the Adam state afterwards
+  std::vector<float> m(I.L.total), v(I.L.total);
+  I.am.download(m.data(), I.L.total, I.s.stream);
+  I.av.download(v.data(), I.L.total, I.s.stream);
+  const int64_t t = I.adam_t;
+  const double l = I.backward_and_step(0.f);
+  I.adam_t = t;
+  I.am.upload(m, I.s.stream);
+  I.av.upload(v, I.s.stream);
+  I.grads.download(grad, I.L.total, I.s.stream);
+  I.s.sync();
+  return l;
+}
+
+}  // namespace nosh

@@ -35,8 +35,14 @@ struct KernelTimer {
   size_t used = 0;
   int64_t launches = 0;
   double bytes = 0.0;
+  static bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus c = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &c) == cudaSuccess && c != cudaStreamCaptureStatusNone;
+  }
+  bool open_pair = false;
   void begin(cudaStream_t s) {
-    if (!on) return;
+    if (!on || capturing(s)) return;
+    open_pair = true;
     if (used + 2 > ev.size()) {
       for (int k = 0; k < 2; k++) {
         cudaEvent_t e;
@@ -47,7 +53,8 @@ struct KernelTimer {
     NOSH_CUDA(cudaEventRecord(ev[used], s));
   }
   void end(cudaStream_t s, double b) {
-    if (!on) return;
+    if (!on || !open_pair) return;
+    open_pair = false;
     NOSH_CUDA(cudaEventRecord(ev[used + 1], s));
     used += 2;
     launches++;

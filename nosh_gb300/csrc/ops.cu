@@ -240,7 +240,7 @@ void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &o
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
     attr_set = true;
   }
-  const int grid = div_up(s.N, kRows);
+  const int grid = row_grid((const void *)row_block_apply<T, Op>, smem, s.N);
   row_block_apply<T, Op><<<grid, kRows, smem, s.stream>>>(
       (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, x, cap, op, s.red.partials.p,
       s.red.counter.p, red_out);
@@ -249,6 +249,22 @@ void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &o
 }
 
 }  // namespace
+
+namespace dev {
+int row_grid(const void *kernel, size_t smem, int64_t n_rows) {
+  static int sms = 0;
+  if (sms == 0) {
+    int d = 0;
+    NOSH_CUDA(cudaGetDevice(&d));
+    NOSH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d));
+  }
+  int per_sm = 0;
+  NOSH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRows, smem));
+  const int64_t blocks = (n_rows + kRows - 1) / kRows;
+  const int64_t cap = (int64_t)std::max(per_sm, 1) * sms;
+  return (int)std::max<int64_t>(1, std::min(blocks, cap));
+}
+}  // namespace dev
 
 void launch_f64_to_f32(const double *a, float *b, int64_t n, cudaStream_t s) {
   if (n) d2f_kernel<<<div_up(n, 256), 256, 0, s>>>(a, b, n);

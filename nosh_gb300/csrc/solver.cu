@@ -41,6 +41,7 @@ __global__ void minres_init(MinresScalars *s, double rtol, int maxit) {
   s->itn = 0;
   s->flag = 0;
   s->done = 0;
+  s->wx_pending = 0;
   s->oldb = 0.0;
   s->dbar = 0.0;
   s->epsln = 0.0;
@@ -63,74 +64,49 @@ __global__ void minres_init(MinresScalars *s, double rtol, int maxit) {
   if (rz == 0.0) s->done = 2;  // b == 0: x = 0
 }
 
-// r_new = J z / beta - (beta/oldb) r1 - (alfa/beta) r2, written over r1
+// u = J z and <z, u>, with the deferred w/x update of the previous Lanczos
+// step folded into the epilogue (element-wise, rows are independent).
 template <typename T>
-__global__ void lanczos_update(int64_t n, const MinresScalars *__restrict__ s, const T *__restrict__ u,
-                               T *__restrict__ r1, const T *__restrict__ r2) {
-  if (s->done) return;
-  const double beta = s->beta, alfa = s->zu / (beta * beta);
-  const T a = (T)(1.0 / beta), c = (T)(alfa / beta);
-  const T bb = s->itn > 0 ? (T)(beta / s->oldb) : (T)0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    r1[i] = a * u[i] - bb * r1[i] - c * r2[i];
-}
+struct JacMinresOp {
+  static constexpr bool kReduce = true;
+  static constexpr bool kHook = true;
+  const T *d;  // Jacobian diagonal blocks, 3 per vertex
+  const C2<T> *x;
+  C2<T> *y;
+  const MinresScalars *s;
+  const T *zprev;
+  T *wa;
+  const T *wb, *wc;
+  T *xsol;
+  __device__ double finish(int i, T sr, T si) const {
+    const C2<T> xi = x[i];
+    const T d0r = d[3 * i], d0i = d[3 * i + 1], d1b = d[3 * i + 2];
+    const T yr = sr + d0r * xi.x + d1b * xi.y;
+    const T yi = si + d1b * xi.x + d0i * xi.y;
+    y[i] = C2<T>{yr, yi};
+    if (s->wx_pending) {
+      const T *c = wx_coef<T>(s);
+      minres_wx_elem<T>(c, 2 * (int64_t)i, zprev, wa, wb, wc, xsol);
+      minres_wx_elem<T>(c, 2 * (int64_t)i + 1, zprev, wa, wb, wc, xsol);
+    }
+    return (double)(xi.x * yr + xi.y * yi);
+  }
+  // the finishing thread turns <z, J z> into the Lanczos coefficients
+  __device__ void hook(double total) const { minres_lanczos_coefs(const_cast<MinresScalars *>(s), total); }
+};
 
-// Givens recurrence (scipy / Paige-Saunders variable names)
-__global__ void minres_scalars(MinresScalars *s) {
-  if (s->done) {
-    s->done = 2;  // 2: frozen, 1: converged during the last update
-    return;
-  }
-  const double beta = s->beta;
-  const double alfa = s->zu / (beta * beta);
-  const double rz = s->rz;
-  s->alfa = alfa;
-  s->oldb = beta;
-  if (!(rz >= 0.0) || isinf(rz) || isnan(alfa)) {
-    s->flag = (isnan(rz) || isinf(rz) || isnan(alfa)) ? NOSH_ERR_NAN : NOSH_ERR_BREAKDOWN;
-    s->done = 2;
-    return;
-  }
-  const double nb = sqrt(rz);
-  s->beta = nb;
-  s->oldeps = s->epsln;
-  const double delta = s->cs * s->dbar + s->sn * alfa;
-  const double gbar = s->sn * s->dbar - s->cs * alfa;
-  s->epsln = s->sn * nb;
-  s->dbar = -s->cs * nb;
-  double gamma = hypot(gbar, nb);
-  if (gamma == 0.0) gamma = 2.2e-16;
-  s->cs = gbar / gamma;
-  s->sn = nb / gamma;
-  s->phi = s->cs * s->phibar;
-  s->phibar = s->sn * s->phibar;
-  s->gamma = gamma;
-  s->delta = delta;
-  s->itn += 1;
-  if (s->phibar <= s->rtol * s->beta1 || nb == 0.0) s->done = 1;
-  else if (s->itn >= s->maxit) {
-    s->done = 1;
-    s->flag = NOSH_ERR_NOT_CONVERGED;
-  }
-}
-
-// w_new = (z/oldb - oldeps w2 - delta w) / gamma over the w1 buffer;
-// x += phi w_new
 template <typename T>
 __global__ void minres_wx(int64_t n, const MinresScalars *__restrict__ s, const T *__restrict__ z,
                           T *__restrict__ wa, const T *__restrict__ wb, const T *__restrict__ wc,
                           T *__restrict__ x) {
-  if (s->done == 2) return;
-  const T iv = (T)(1.0 / s->oldb), e = (T)s->oldeps, d = (T)s->delta, ig = (T)(1.0 / s->gamma),
-          ph = (T)s->phi;
+  if (!s->wx_pending) return;
+  const T *c = wx_coef<T>(s);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const T w = (z[i] * iv - e * wb[i] - d * wc[i]) * ig;
-    wa[i] = w;
-    x[i] += ph * w;
-  }
+       i += (int64_t)gridDim.x * blockDim.x)
+    minres_wx_elem<T>(c, i, z, wa, wb, wc, x);
 }
+
+__global__ void clear_wx_pending(MinresScalars *s) { s->wx_pending = 0; }
 
 template <typename T>
 __global__ void neg_cast(int64_t n, const double *__restrict__ f, T *__restrict__ b) {
@@ -152,14 +128,57 @@ inline int vec_grid(int64_t n) { return std::min<int64_t>(div_up(n, 256), kNumSM
 
 template <typename T>
 Minres<T>::Minres(NlsImpl &nls) : s(nls), n2(2 * nls.N) {
-  for (DevBuf<T> *b : {&r1, &r2, &z0, &z1, &u, &w0, &w1, &w2, &x}) b->alloc(n2);
+  for (DevBuf<T> *b : {&r[0], &r[1], &z[0], &z[1], &w[0], &w[1], &w[2], &u, &x}) b->alloc(n2);
   sc.alloc(1);
   NOSH_CUDA(cudaMallocHost(&h_sc, sizeof(MinresScalars)));
+  NOSH_CUDA(cudaMallocHost(&h_err, sizeof(int)));
+  NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, JacMinresOp<T>>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
 }
 
 template <typename T>
 Minres<T>::~Minres() {
+  if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
   if (h_sc) cudaFreeHost(h_sc);
+  if (h_err) cudaFreeHost(h_err);
+}
+
+// Iteration j of a chunk.  Buffer roles rotate with period 2 (z, r) and 3
+// (w: the (w1, w2, w) triple of the recurrence), so a chunk of 6 iterations
+// always starts from the same assignment.
+template <typename T>
+void Minres<T>::iteration(int j) {
+  cudaStream_t st = s.stream;
+  MinresScalars *d = sc.p;
+  T *zc = z[j % 2].p, *zn = z[(j + 1) % 2].p;
+  T *r_old = r[j % 2].p, *r_cur = r[(j + 1) % 2].p;
+  // deferred w/x update of step j-1: its z is zn, its (w1, w2, w) buffers
+  const int jm = (j + kChunk - 1) % 3;
+  T *wa = w[jm].p, *wb = w[(jm + 1) % 3].p, *wc = w[(jm + 2) % 3].p;
+  const int cap = sizeof(T) == 4 ? s.cap32 : s.cap64;
+  const C2<T> *val = sizeof(T) == 4 ? (const C2<T> *)s.d_keo32.p : (const C2<T> *)s.d_keo64.p;
+  const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
+  JacMinresOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, d, zn, wa, wb, wc, x.p};
+  s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
+  const size_t smem = (size_t)cap * (4 + sizeof(C2<T>));
+  row_block_apply<T, JacMinresOp<T>><<<row_grid((const void *)row_block_apply<T, JacMinresOp<T>>, smem, s.N),
+                                       kRows, smem, st>>>(
+      (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, (const C2<T> *)zc, cap, op, s.red.partials.p,
+      s.red.counter.p, &d->zu);
+  ++s.launch_count;
+  // bytes per vertex: z, diag block, u (+ the fused w/x update: z_prev, w2,
+  // w, x read; w1, x written)
+  s.timers[NOSH_KERNEL_JACOBIAN].end(st, s.spmv_bytes(2 * sizeof(T), 13 * sizeof(T)));
+  s.amg->apply_minres<T>(d, u.p, r_old, r_cur, zn);
+}
+
+template <typename T>
+void Minres<T>::wx_final() {
+  // step kChunk-1 = 5: z = z[1], (w1, w2, w) = (w[2], w[0], w[1])
+  const int G = std::min<int64_t>(div_up(n2, 256), kNumSMs * 8);
+  minres_wx<T><<<G, 256, 0, s.stream>>>(n2, sc.p, z[1].p, w[2].p, w[0].p, w[1].p, x.p);
+  clear_wx_pending<<<1, 1, 0, s.stream>>>(sc.p);
+  s.launch_count += 2;
 }
 
 template <typename T>
@@ -168,48 +187,45 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
   const int G = vec_grid(n2);
   const size_t bytes = n2 * sizeof(T);
   MinresScalars *d = sc.p;
-  // r1 = r2 = b, x = w = 0, z = M b, beta1^2 = <b, z>
-  NOSH_CUDA(cudaMemcpyAsync(r2.p, b, bytes, cudaMemcpyDeviceToDevice, st));
-  NOSH_CUDA(cudaMemcpyAsync(r1.p, b, bytes, cudaMemcpyDeviceToDevice, st));
-  for (DevBuf<T> *q : {&x, &w0, &w1, &w2}) NOSH_CUDA(cudaMemsetAsync(q->p, 0, bytes, st));
-  T *zc = z0.p, *zn = z1.p, *pr1 = r1.p, *pr2 = r2.p;
-  T *wa = w0.p, *wb = w1.p, *wc = w2.p;  // (w1, w2, w) of the recurrence
-  s.amg->apply<T>(pr2, zc);
-  dot_kernel<T><<<G, 256, 0, st>>>(n2, pr2, zc, s.red.partials.p, s.red.counter.p, &d->rz);
-  ++s.launch_count;
+  // r_old = r_cur = b, x = w = 0, z = M b, beta1^2 = <b, z>
+  NOSH_CUDA(cudaMemcpyAsync(r[0].p, b, bytes, cudaMemcpyDeviceToDevice, st));
+  NOSH_CUDA(cudaMemcpyAsync(r[1].p, b, bytes, cudaMemcpyDeviceToDevice, st));
+  for (DevBuf<T> *q : {&x, &w[0], &w[1], &w[2]}) NOSH_CUDA(cudaMemsetAsync(q->p, 0, bytes, st));
+  s.amg->apply<T>(r[1].p, z[0].p);
+  dot_kernel<T><<<G, 256, 0, st>>>(n2, r[1].p, z[0].p, s.red.partials.p, s.red.counter.p, &d->rz);
   minres_init<<<1, 1, 0, st>>>(d, rtol, maxit);
-  ++s.launch_count;
+  s.launch_count += 2;
   NOSH_CUDA(cudaGetLastError());
-  const int check_every = 4;
+  // graphs are used unless kernel timing is on (event pairs per launch)
+  const bool graphs = !s.timers[NOSH_KERNEL_JACOBIAN].on;
+  if (graphs && !chunk_exec) {
+    cudaGraph_t g;
+    const int64_t before = s.launch_count;
+    NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int j = 0; j < kChunk; j++) iteration(j);
+    NOSH_CUDA(cudaStreamEndCapture(st, &g));
+    chunk_kernels = s.launch_count - before;
+    s.launch_count = before;
+    NOSH_CUDA(cudaGraphInstantiate(&chunk_exec, g, 0));
+    NOSH_CUDA(cudaGraphDestroy(g));
+  }
   int it = 0;
   for (;;) {
-    for (int k = 0; k < check_every; k++, it++) {
-      // u = J z, <z, u>   (bytes per vertex: x, diag block, y)
-      s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
-      s.jac_apply<T>(zc, u.p, &d->zu);
-      s.timers[NOSH_KERNEL_JACOBIAN].end(st, s.spmv_bytes(2 * sizeof(T), 7 * sizeof(T)));
-      lanczos_update<T><<<G, 256, 0, st>>>(n2, d, u.p, pr1, pr2);
-      ++s.launch_count;
-      std::swap(pr1, pr2);  // r2 = r_new, r1 = previous r2
-      s.amg->apply<T>(pr2, zn);
-      dot_kernel<T><<<G, 256, 0, st>>>(n2, pr2, zn, s.red.partials.p, s.red.counter.p, &d->rz);
-      ++s.launch_count;
-      minres_scalars<<<1, 1, 0, st>>>(d);
-      ++s.launch_count;
-      minres_wx<T><<<G, 256, 0, st>>>(n2, d, zc, wa, wb, wc, x.p);
-      ++s.launch_count;
-      // (w1, w2, w) <- (w2, w, w_new)
-      T *t = wa;
-      wa = wb;
-      wb = wc;
-      wc = t;
-      std::swap(zc, zn);
+    if (graphs) {
+      NOSH_CUDA(cudaGraphLaunch(chunk_exec, st));
+      s.launch_count += chunk_kernels;
+    } else {
+      for (int j = 0; j < kChunk; j++) iteration(j);
     }
+    it += kChunk;
     NOSH_CUDA(cudaGetLastError());
     NOSH_CUDA(cudaMemcpyAsync(h_sc, d, sizeof(MinresScalars), cudaMemcpyDeviceToHost, st));
+    NOSH_CUDA(cudaMemcpyAsync(h_err, s.amg->error_flag_ptr(), sizeof(int), cudaMemcpyDeviceToHost, st));
     NOSH_CUDA(cudaStreamSynchronize(st));
-    if (h_sc->done || it >= maxit + check_every) break;
+    if (h_sc->done || it >= maxit + kChunk) break;
   }
+  if (h_sc->wx_pending) wx_final();  // converged on the chunk's last step
+  NOSH_CHECK(*h_err == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
   status = h_sc->flag;
   rel_res = h_sc->beta1 > 0 ? h_sc->phibar / h_sc->beta1 : 0.0;
   return h_sc->itn;
@@ -220,14 +236,6 @@ template struct Minres<double>;
 
 // ------------------------------------------------------------------ Newton
 namespace {
-struct NewtonState {
-  DevBuf<double> psi, f, xc, xp, tmp;  // working state, residual, staged inputs
-  DevBuf<float> b32;
-  DevBuf<double> b64;
-  DevBuf<double> red2;  // complex reduction (phase alignment)
-  std::unique_ptr<Minres<float>> m32;
-  std::unique_ptr<Minres<double>> m64;
-};
 
 // c = sum conj(a_i) b_i (complex), deterministic two-slot reduction
 __global__ void cdot_kernel(int64_t n, const C2<double> *__restrict__ a,
@@ -269,7 +277,7 @@ __global__ void axpy_to(int64_t n, double a, const T *__restrict__ t, const doub
 }
 }  // namespace
 
-static NewtonState &state_of(NlsImpl &s) {
+NewtonState &state_of(NlsImpl &s) {
   if (!s.solver_state) {
     auto *ns = new NewtonState();
     for (DevBuf<double> *b : {&ns->psi, &ns->f, &ns->xc, &ns->xp, &ns->tmp}) b->alloc(2 * s.N);
@@ -279,7 +287,7 @@ static NewtonState &state_of(NlsImpl &s) {
   return *(NewtonState *)s.solver_state.get();
 }
 
-static double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f) {
+double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f) {
   s.compute_f64(psi, g, mu, f, 0);
   double n2 = 0.0;
   s.red.out.download(&n2, 1, s.stream);
@@ -363,8 +371,8 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
   }
 }
 
-static void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
-                        nosh_newton_stats &st) {
+void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
+                 nosh_newton_stats &st) {
   st = nosh_newton_stats{};
   st.f_norm0 = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
   st.f_norm = st.f_norm0;

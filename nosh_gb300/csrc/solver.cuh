@@ -2,32 +2,51 @@
 #pragma once
 
 #include "amg.cuh"
+#include "minres_state.cuh"
 #include "nls.cuh"
 
 namespace nosh {
 
-// MINRES recurrence state, resident in device memory (FP64 scalars).
-struct MinresScalars {
-  double beta1, beta, oldb, alfa, dbar, epsln, oldeps, phibar, phi, cs, sn, gamma, delta;
-  double zu, rz;  // reduction slots: <z, J z>, <r, M r>
-  int itn, done, flag, maxit;
-  double rtol;
-};
-
 // Preconditioned MINRES (Paige-Saunders) on J dx = b with the AMG V-cycle as
-// the SPD preconditioner, vectors in T, scalars in FP64.
+// the SPD preconditioner, vectors in T, scalars in FP64 (minres_state.cuh).
+// Iterations run in chunks of kChunk, each captured once as a CUDA graph and
+// replayed; the host polls the convergence flag once per chunk.
 template <typename T>
 struct Minres {
+  static constexpr int kChunk = 6;  // multiple of the 2- and 3-buffer rotations
   NlsImpl &s;
   int64_t n2;  // real length (2N)
-  DevBuf<T> r1, r2, z0, z1, u, w0, w1, w2, x;
+  DevBuf<T> r[2], z[2], w[3], u, x;
   DevBuf<MinresScalars> sc;
   MinresScalars *h_sc = nullptr;  // pinned host mirror
+  int *h_err = nullptr;
+  cudaGraphExec_t chunk_exec = nullptr;
+  int64_t chunk_kernels = 0;
   explicit Minres(NlsImpl &nls);
   ~Minres();
   // b: device vector of T (2N); returns iterations; x holds the solution
   int solve(const T *b, double rtol, int maxit, int &status, double &rel_res);
+
+ private:
+  void iteration(int j);   // issue iteration j (0..kChunk-1) of a chunk
+  void wx_final();         // deferred w/x update of the chunk's last step
 };
+
+// Newton work space of an nls handle (solver.cu)
+struct NewtonState {
+  DevBuf<double> psi, f, xc, xp, tmp;  // working state, residual, staged inputs
+  DevBuf<float> b32;
+  DevBuf<double> b64;
+  DevBuf<double> red2;  // complex reduction (phase alignment)
+  std::unique_ptr<Minres<float>> m32;
+  std::unique_ptr<Minres<double>> m64;
+};
+NewtonState &state_of(NlsImpl &s);
+// ||F(psi)||_2 (writes F into f; synchronises)
+double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f);
+// Newton on state_of(s).psi in place
+void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
+                 nosh_newton_stats &st);
 
 void newton_solve(NlsImpl &s, double *x_user, double g, double mu,
                   const nosh_newton_options &opt, nosh_newton_stats &st);

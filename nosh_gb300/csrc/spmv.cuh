@@ -9,6 +9,8 @@
 // staging capacity reads them directly.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace nosh {
@@ -22,9 +24,11 @@ template <> struct Acc<float> { using type = float; };
 template <> struct Acc<double> { using type = double; };
 
 // Grid-wide deterministic sum of one double per thread: block partials, then
-// the last CTA to arrive adds them in fixed order and stores *out.
-__device__ __forceinline__ void grid_reduce(double v, double *partials,
-                                            unsigned *counter, double *out) {
+// the last CTA to arrive adds them in fixed order and stores *out.  Returns
+// true in exactly one thread (thread 0 of that last CTA), with the sum in
+// *total, so callers can continue with scalar work on the result.
+__device__ __forceinline__ bool grid_reduce(double v, double *partials, unsigned *counter,
+                                            double *out, double *total = nullptr) {
   __shared__ double s32[32];
   __shared__ bool last;
   const double b = block_sum(v, s32);
@@ -35,22 +39,55 @@ __device__ __forceinline__ void grid_reduce(double v, double *partials,
     last = (t == gridDim.x - 1);
   }
   __syncthreads();
+  bool finisher = false;
   if (last) {
     __threadfence();
-    double s = 0.0;
-    for (unsigned j = threadIdx.x; j < gridDim.x; j += blockDim.x) s += __ldcg(partials + j);
-    s = block_sum(s, s32);
+    // four independent accumulators so the partial loads overlap (fixed
+    // order per thread: deterministic)
+    const unsigned G = gridDim.x, st = blockDim.x;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    unsigned j = threadIdx.x;
+    for (; j + 3 * st < G; j += 4 * st) {
+      a0 += __ldcg(partials + j);
+      a1 += __ldcg(partials + j + st);
+      a2 += __ldcg(partials + j + 2 * st);
+      a3 += __ldcg(partials + j + 3 * st);
+    }
+    for (; j < G; j += st) a0 += __ldcg(partials + j);
+    double s = block_sum((a0 + a1) + (a2 + a3), s32);
     if (threadIdx.x == 0) {
       *out = s;
       *counter = 0u;
+      if (total) *total = s;
+      finisher = true;
     }
   }
+  return finisher;
 }
 
 // Op must provide:
 //   static constexpr bool kReduce;
-//   __device__ double finish(int row, C2<acc> sum) -- writes y[row], returns
-//                                                     the thread's partial
+//   __device__ double finish(int row, acc sr, acc si) -- writes y[row],
+//                                                       returns the thread's
+//                                                       partial
+// and, when kReduce, may provide kHook + hook(total): scalar work done by one
+// thread once the grid sum is known.
+template <class Op, class = void>
+struct HasHook {
+  static constexpr bool value = false;
+};
+template <class Op>
+struct HasHook<Op, decltype((void)Op::kHook, void())> {
+  static constexpr bool value = Op::kHook;
+};
+template <class Op>
+__device__ __forceinline__ typename std::enable_if<HasHook<Op>::value>::type run_hook(const Op &op,
+                                                                                     double t) {
+  op.hook(t);
+}
+template <class Op>
+__device__ __forceinline__ typename std::enable_if<!HasHook<Op>::value>::type run_hook(const Op &,
+                                                                                      double) {}
 template <typename T, class Op>
 __global__ void __launch_bounds__(kRows)
     row_block_apply(int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
@@ -58,47 +95,60 @@ __global__ void __launch_bounds__(kRows)
                     Op op, double *partials, unsigned *counter, double *red_out) {
   using A = typename Acc<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int r0 = blockIdx.x * kRows;
-  const int r1 = min(N, r0 + kRows);
-  const int k0 = __ldg(rp + r0), k1 = __ldg(rp + r1);
-  const int ks = k0 & ~3;  // 16-byte aligned start for both arrays
-  const int n = k1 - ks;
-  const bool staged = n <= cap;
   int32_t *s_col = reinterpret_cast<int32_t *>(smem_raw);
   C2<T> *s_val = reinterpret_cast<C2<T> *>(smem_raw + (size_t)cap * sizeof(int32_t));
-  if (staged) {
-    const int n4 = (n + 3) >> 2;
-    const int4 *c4 = reinterpret_cast<const int4 *>(ci + ks);
-    for (int j = threadIdx.x; j < n4; j += kRows) reinterpret_cast<int4 *>(s_col)[j] = __ldg(c4 + j);
-    const int nv = (int)((n * sizeof(C2<T>) + 15) / 16);
-    const uint4 *v4 = reinterpret_cast<const uint4 *>(val + ks);
-    for (int j = threadIdx.x; j < nv; j += kRows) reinterpret_cast<uint4 *>(s_val)[j] = __ldg(v4 + j);
-  }
-  __syncthreads();
-  const int row = r0 + threadIdx.x;
-  double part = 0.0;
-  if (row < N) {
-    A sr = 0, si = 0;
-    const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+  const int nblocks = (N + kRows - 1) / kRows;
+  A part = 0;
+  // persistent: the grid is sized to the resident capacity and each CTA
+  // walks row blocks with a grid stride (whole waves, fewer partial sums)
+  for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x) {
+    const int r0 = rb * kRows;
+    const int r1 = min(N, r0 + kRows);
+    const int k0 = __ldg(rp + r0), k1 = __ldg(rp + r1);
+    const int ks = k0 & ~3;  // 16-byte aligned start for both arrays
+    const int n = k1 - ks;
+    const bool staged = n <= cap;
     if (staged) {
-      for (int k = b - ks; k < e - ks; k++) {
-        const C2<T> v = s_val[k];
-        const C2<T> xv = ldg(x + s_col[k]);
-        sr += v.x * xv.x - v.y * xv.y;
-        si += v.x * xv.y + v.y * xv.x;
-      }
-    } else {
-      for (int k = b; k < e; k++) {
-        const C2<T> v = ldg(val + k);
-        const C2<T> xv = ldg(x + __ldg(ci + k));
-        sr += v.x * xv.x - v.y * xv.y;
-        si += v.x * xv.y + v.y * xv.x;
-      }
+      const int n4 = (n + 3) >> 2;
+      const int4 *c4 = reinterpret_cast<const int4 *>(ci + ks);
+      for (int j = threadIdx.x; j < n4; j += kRows) reinterpret_cast<int4 *>(s_col)[j] = __ldg(c4 + j);
+      const int nv = (int)((n * sizeof(C2<T>) + 15) / 16);
+      const uint4 *v4 = reinterpret_cast<const uint4 *>(val + ks);
+      for (int j = threadIdx.x; j < nv; j += kRows) reinterpret_cast<uint4 *>(s_val)[j] = __ldg(v4 + j);
     }
-    part = op.finish(row, sr, si);
+    __syncthreads();
+    const int row = r0 + threadIdx.x;
+    if (row < N) {
+      A sr = 0, si = 0;
+      const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+      if (staged) {
+        for (int k = b - ks; k < e - ks; k++) {
+          const C2<T> v = s_val[k];
+          const C2<T> xv = ldg(x + s_col[k]);
+          sr += v.x * xv.x - v.y * xv.y;
+          si += v.x * xv.y + v.y * xv.x;
+        }
+      } else {
+        for (int k = b; k < e; k++) {
+          const C2<T> v = ldg(val + k);
+          const C2<T> xv = ldg(x + __ldg(ci + k));
+          sr += v.x * xv.x - v.y * xv.y;
+          si += v.x * xv.y + v.y * xv.x;
+        }
+      }
+      part += (A)op.finish(row, sr, si);
+    }
+    __syncthreads();  // the staging buffer is reused by the next row block
   }
-  if (Op::kReduce) grid_reduce(part, partials, counter, red_out);
+  if (Op::kReduce) {
+    double total = 0.0;
+    if (grid_reduce((double)part, partials, counter, red_out, &total)) run_hook(op, total);
+  }
 }
+
+// Grid for a persistent row kernel: the resident capacity of the device for
+// this kernel and shared-memory size, capped by the number of row blocks.
+int row_grid(const void *kernel, size_t smem, int64_t n_rows);
 
 // ---- epilogues --------------------------------------------------------
 // y = K x : diagonal K_ii = sum of incident alpha (real)

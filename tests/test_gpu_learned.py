@@ -1,0 +1,180 @@
+"""Continuation driver and learned predictor on the GPU.
+
+* the device-resident continuation reproduces the oracle's converged states
+  (exact-LU Newton, modulo the global phase);
+* the message-passing network's forward pass and parameter gradient match a
+  torch FP32 CPU reference of the same network that rounds the GEMM operands
+  to BF16 as the tensor-core path does (gradient tolerance accounts for the
+  BF16 operands of the backward GEMMs);
+* trained online on the first steps of a continuation, the learned predictor
+  starts Newton from a smaller residual than the secant predictor.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+H, FX, FE, LAYERS = 64, 8, 4, 3
+
+
+def _layout():
+    o, L = 0, {}
+
+    def take(name, n):
+        nonlocal o
+        L[name] = (o, n)
+        o += n
+
+    take("enc_w", FX * H)
+    take("enc_b", H)
+    for l in range(LAYERS):
+        take(f"wa{l}", H * H)
+        take(f"wb{l}", H * H)
+        take(f"wc{l}", FE * H)
+        take(f"bm{l}", H)
+        take(f"wu{l}", 2 * H * H)
+        take(f"bu{l}", H)
+    take("dec_w", H * 2)
+    take("dec_b", 2)
+    return L, o
+
+
+def torch_reference(p, ef, rp, ci, X, T):
+    """The network in torch (CPU, FP32), GEMM operands rounded to BF16."""
+    import torch
+
+    L, total = _layout()
+    P = torch.tensor(p, dtype=torch.float32, requires_grad=True)
+
+    def w(name, shape):
+        o, n = L[name]
+        return P[o : o + n].reshape(shape)
+
+    def bf(t):
+        return t.to(torch.bfloat16).float()
+
+    N = X.shape[0]
+    rows = torch.tensor(np.repeat(np.arange(N), np.diff(rp)), dtype=torch.long)
+    cols = torch.tensor(ci, dtype=torch.long)
+    E = torch.tensor(ef, dtype=torch.float32)
+    Xt = torch.tensor(X, dtype=torch.float32)
+    h = torch.relu(bf(Xt) @ bf(w("enc_w", (FX, H))) + w("enc_b", (H,)))
+    for l in range(LAYERS):
+        A = bf(h) @ bf(w(f"wa{l}", (H, H)))
+        B = bf(h) @ bf(w(f"wb{l}", (H, H)))
+        Pij = A[rows] + B[cols] + E @ w(f"wc{l}", (FE, H)) + w(f"bm{l}", (H,))
+        M = torch.zeros(N, H).index_add_(0, rows, torch.relu(Pij))
+        R = torch.relu(bf(torch.cat([h, M], dim=1)) @ bf(w(f"wu{l}", (2 * H, H))) + w(f"bu{l}", (H,)))
+        h = h + R
+    Y = h @ w("dec_w", (H, 2)) + w("dec_b", (2,))
+    loss = ((Y - torch.tensor(T)) ** 2).sum() / N
+    loss.backward()
+    return Y.detach().numpy(), float(loss), P.grad.numpy()
+
+
+@pytest.fixture(scope="module")
+def net():
+    import nosh_gb300 as ng
+
+    x, c, psi0 = O.gen_cube(6, 3)
+    gm = ng.mesh(x, c)
+    model = ng.nls(gm, O.mvp_constant_curl(x), -1.0, 1.0, 1.0, mu=0.3)
+    return gm, model, ng.mpnn(model)
+
+
+def test_mpnn_parameter_layout(net):
+    gm, model, mp = net
+    assert mp.num_params == _layout()[1]
+
+
+def test_mpnn_forward_and_gradient_match_torch(net):
+    pytest.importorskip("torch")
+    gm, model, mp = net
+    rng = np.random.default_rng(7)
+    N = gm.num_vertices
+    # a parameter set with well-populated ReLUs (the decoder starts small)
+    p = mp.params()
+    L, _ = _layout()
+    o, n = L["dec_w"]
+    p[o : o + n] = rng.uniform(-0.3, 0.3, n)
+    mp.params(p)
+    X = rng.standard_normal((N, FX)).astype(np.float32)
+    X[:, 7] = 1.0
+    T = rng.standard_normal((N, 2)).astype(np.float32)
+    rp, ci = gm.build_complex_graph()
+    rows = np.repeat(np.arange(N), np.diff(rp))
+    keep = ci != rows
+    rp_od = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=N))]).astype(np.int64)
+    ci_od = ci[keep]
+    ef = mp.edge_features()
+    Y_ref, loss_ref, g_ref = torch_reference(p, ef, rp_od, ci_od, X, T)
+    Y = mp.forward(X)
+    assert np.abs(Y - Y_ref).max() <= 2e-3 * np.abs(Y_ref).max()
+    loss, g = mp.loss_grad(X, T)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    cos = float(g @ g_ref / (np.linalg.norm(g) * np.linalg.norm(g_ref)))
+    rel = float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref))
+    assert cos > 0.999 and rel < 3e-2, (cos, rel)
+    # the loss-gradient query does not change the parameters
+    np.testing.assert_array_equal(mp.params(), p)
+
+
+def _square(s=33, seed=4):
+    x, c, psi0 = O.gen_square(s, seed)
+    m = O.finish_mesh(x, c)
+    return m, O.Problem(m, O.mvp_constant_curl(m.x)), psi0
+
+
+@pytest.mark.parametrize("predictor", ["secant", "quadratic"])
+def test_continuation_driver_matches_oracle(predictor):
+    import nosh_gb300 as ng
+
+    m, P, psi0 = _square()
+    mu0 = 0.2
+    x0, _ = O.newton_exact(P, psi0, 1.0, mu0)
+    gm = ng.mesh(m.x, m.cells)
+    model = ng.nls(gm, P.A, -1.0, 1.0, 1.0, mu=mu0)
+    cont = ng.continuation(model, x0, mu0)
+    pred = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC}[predictor]
+    f0 = []
+    mu = mu0
+    for k in range(5):
+        mu += 0.01
+        st = cont.advance(mu, predictor=pred)
+        assert st["status"] == 0 and st["f_norm"] <= 1e-10
+        f0.append(st["f_norm0"])
+    x, mu_c = cont.state()
+    assert abs(mu_c - mu) < 1e-15
+    ref, _ = O.newton_exact(P, x, 1.0, mu)
+    assert np.abs(O.align_phase(x, ref) - ref).max() < 1e-8
+    assert np.linalg.norm(P.compute_f(x, 1.0, mu)) <= 1.5e-10
+    if predictor == "quadratic":
+        # from the third step on the 3-point predictor is active
+        assert f0[-1] < 0.5 * f0[1]
+
+
+def test_learned_predictor_gains_over_secant():
+    import nosh_gb300 as ng
+
+    m, P, psi0 = _square(33, 5)
+    mu0 = 0.0
+    gm = ng.mesh(m.x, m.cells)
+    model = ng.nls(gm, P.A, -1.0, 1.0, 1.0, mu=mu0)
+    x0 = psi0.copy()
+    model.newton(x0, {"mu": mu0})
+    cont = ng.continuation(model, x0, mu0)
+    cont.learning(train_steps=16, iters_per_step=40, learning_rate=2e-3)
+    mu, gains = mu0, []
+    for k in range(30):
+        mu += 0.01
+        st = cont.advance(mu, predictor=ng.PREDICT_LEARNED)
+        assert st["status"] == 0 and st["f_norm"] <= 1e-10
+        lp = cont.last_prediction()
+        if k >= 22:  # after the training window (+3 history steps)
+            assert np.isfinite(lp["f_learned"]) and np.isfinite(lp["f_secant"])
+            gains.append(lp["f_secant"] / lp["f_learned"])
+    assert np.isfinite(lp["train_loss"])
+    # the trained network's prediction starts Newton closer than the secant
+    assert np.median(gains) > 2.0, gains
