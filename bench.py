@@ -5,10 +5,18 @@ Workload (one "step" = one natural continuation step): unit cube, 64^3 cubes
 x 6 Kuhn tetrahedra (274,625 vertices, 1,572,864 tets), interior vertices
 jittered +-0.1h (seed 2), A = 1/2 (-y, x, 0) sampled per vertex (B = (0,0,mu)),
 V = -1, g = 1, thickness 1; mu advances by 0.005 per step from mu = 0.5;
-each step predicts the state (phase-aligned secant predictor) and
-Newton-corrects it to ||F||_2 <= 1e-10 with AMG-preconditioned MINRES, in the
-mixed FP32 (operators, Krylov, AMG) / FP64 (residual, scalars) path.
-The synthetic mesh stands in for the reference's .h5m inputs.
+each step predicts the state and Newton-corrects it to ||F||_2 <= 1e-10 with
+AMG-preconditioned MINRES, in the mixed FP32 (operators, Krylov, AMG) / FP64
+(residual, scalars) path.  The synthetic mesh stands in for the reference's
+.h5m inputs.
+
+The headline ("value") uses the learned predictor: a message-passing network
+trained online during the first --train-steps steps (untimed, part of the
+warm-up) that combines phase-aligned history extrapolants; it falls back to
+the secant whenever its prediction has the larger residual.  The plain
+predictor (the reference's secant) is timed on the same workload
+("plain_predictor"), and the 3-point polynomial predictor as an ablation
+("quadratic_predictor").
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
 
@@ -272,7 +280,7 @@ def run_gb300(args):
         mu = args.mu0
         if pred == ng.PREDICT_LEARNED:
             cont.learning(args.train_steps, args.train_iters, args.lr)
-            warmup = warmup + args.train_steps + 3
+            warmup = warmup + args.train_steps + 4
         for _ in range(warmup):
             mu += args.dmu
             s = cont.advance(mu, predictor=pred)
@@ -322,6 +330,7 @@ def run_gb300(args):
     clocks.start()
     plain = run("secant", args.steps, args.warmup)
     head = run(args.predictor, args.steps, args.warmup) if args.predictor != "secant" else plain
+    quad = run("quadratic", args.steps, args.warmup) if args.predictor != "quadratic" else head
     clk = clocks.stop()
     ms = maxrank(head["ms"])
     value = world * 1000.0 / ms
@@ -378,6 +387,9 @@ def run_gb300(args):
                                     "parallelism": f"replicas x{world}"},
         "plain_predictor": {"predictor": "secant", "value": world * 1000.0 / plain_ms, "ms_per_step": plain_ms,
                             "newton_krylov_per_step": plain["newton_krylov_per_step"]},
+        "quadratic_predictor": {"predictor": "quadratic", "value": world * 1000.0 / maxrank(quad["ms"]),
+                                "ms_per_step": maxrank(quad["ms"]),
+                                "newton_krylov_per_step": quad["newton_krylov_per_step"]},
         "learned_vs_plain": plain_ms / ms,
         "newton_krylov_per_step": head["newton_krylov_per_step"],
         "learned_used_steps": head["learned_used"],

@@ -273,12 +273,15 @@ int nosh_continuation_last_prediction(nosh_continuation c, int *used,
                                       double *train_loss);
 
 /* The learned predictor's network, for inspection and gradient checks (the
- * continuation handle owns its own instance).  Parameters are one flat FP32
- * vector: encoder W [8x64] (row-major), b [64]; per layer l = 0..2:
- * W_a [64x64], W_b [64x64], W_c [4x64], b_m [64], W_u [128x64], b_u [64];
- * decoder W [64x2], b [2].  Node features are N x 8, outputs N x 2, edge
- * features 2E x 4 in the order of the off-diagonal KEO graph (the complex
- * graph of nosh_mesh_complex_graph without its diagonal). */
+ * continuation handle owns its own instance).  From the four newest states
+ * it predicts two global coefficients (w_q, w_c) and the prediction is
+ * secant + w_q q + w_c c, q = quadratic - secant and c = cubic - quadratic
+ * extrapolation.  Parameters are one flat FP32 vector: encoder W [10x64]
+ * (row-major), b [64]; per layer l = 0..2: W_a [64x64], W_b [64x64],
+ * W_c [4x64], b_m [64], W_u [128x64], b_u [64]; readout W_1 [64x32],
+ * b_1 [32], W_2 [32x2], b_2 [2].  Node features are N x 10, edge features
+ * 2E x 4 in the order of the off-diagonal KEO graph (the complex graph of
+ * nosh_mesh_complex_graph without its diagonal). */
 typedef struct nosh_mpnn_s *nosh_mpnn;
 int nosh_mpnn_create(nosh_nls nls, nosh_mpnn *out);
 int nosh_mpnn_destroy(nosh_mpnn net);
@@ -286,9 +289,13 @@ int nosh_mpnn_num_params(nosh_mpnn net, int64_t *n);
 /* copies the parameters out (get != NULL) and/or in (set != NULL) */
 int nosh_mpnn_params(nosh_mpnn net, float *get, const float *set);
 int nosh_mpnn_edge_features(nosh_mpnn net, float *ef);
-int nosh_mpnn_forward(nosh_mpnn net, const float *X, float *Y);
-/* mean-squared loss against targets T (N x 2) and its parameter gradient */
-int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const float *T,
+/* the readout coefficients w[2] = (w_q, w_c) for node features X (N x 10) */
+int nosh_mpnn_forward(nosh_mpnn net, const float *X, double *w);
+/* the training loss (w^T G w - 2 w.b + dd) / qq for the cv-weighted Gram
+ * scalars gram = [qq, qc, cc, qd, cd, dd] of (q, c, d = target - secant),
+ * G = [[qq, qc], [qc, cc]], b = (qd, cd), and its parameter gradient; the
+ * parameters are not changed */
+int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const double *gram,
                         double *loss, float *grad);
 
 /* ------------------------------------------------------ kernel timing */

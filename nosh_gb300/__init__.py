@@ -507,15 +507,18 @@ class mpnn:
         return out
 
     def forward(self, X):
+        """The readout coefficients (w_q, w_c) for node features X (N x 10)."""
         X = np.ascontiguousarray(X, np.float32)
-        Y = np.empty((X.shape[0], 2), np.float32)
-        _check(_lib.nosh_mpnn_forward(self._h, _ptr(X), _ptr(Y)))
-        return Y
+        w = np.empty(2, np.float64)
+        _check(_lib.nosh_mpnn_forward(self._h, _ptr(X), _ptr(w)))
+        return w
 
-    def loss_grad(self, X, T):
+    def loss_grad(self, X, gram):
+        """Training loss and parameter gradient for node features X and the
+        cv-weighted Gram scalars [qq, qc, cc, qd, cd, dd]."""
         X = np.ascontiguousarray(X, np.float32)
-        T = np.ascontiguousarray(T, np.float32)
+        gram = np.ascontiguousarray(gram, np.float64)
         g = np.empty(self.num_params, np.float32)
         loss = C.c_double()
-        _check(_lib.nosh_mpnn_loss_grad(self._h, _ptr(X), _ptr(T), C.byref(loss), _ptr(g)))
+        _check(_lib.nosh_mpnn_loss_grad(self._h, _ptr(X), _ptr(gram), C.byref(loss), _ptr(g)))
         return loss.value, g

@@ -670,17 +670,17 @@ int nosh_mpnn_edge_features(nosh_mpnn net, float *ef) {
   });
 }
 
-int nosh_mpnn_forward(nosh_mpnn net, const float *X, float *Y) {
+int nosh_mpnn_forward(nosh_mpnn net, const float *X, double *w) {
   return guarded([&] {
-    require(net && net->impl && X && Y, "null argument");
-    net->impl->forward_features(X, Y);
+    require(net && net->impl && X && w, "null argument");
+    net->impl->forward_features(X, w);
   });
 }
 
-int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const float *T, double *loss, float *grad) {
+int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const double *gram, double *loss, float *grad) {
   return guarded([&] {
-    require(net && net->impl && X && T && grad, "null argument");
-    const double l = net->impl->loss_and_grad(X, T, grad);
+    require(net && net->impl && X && gram && grad, "null argument");
+    const double l = net->impl->loss_and_grad(X, gram, grad);
     if (loss) *loss = l;
   });
 }

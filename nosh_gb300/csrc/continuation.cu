@@ -124,12 +124,14 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   f_learned = std::nan("");
   f_secant = std::nan("");
   extrapolate(order, mu_new, ns.psi.p);
-  if (predictor == NOSH_PREDICT_LEARNED && net && net->trained() && count >= 3) {
+  if (predictor == NOSH_PREDICT_LEARNED && net && net->trained() && count >= 4) {
     // learned correction of the secant prediction; keep whichever starts
     // Newton from the smaller residual (the secant is the fallback)
     f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.f.p);
     NOSH_CUDA(cudaMemcpyAsync(ns.tmp.p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
-    net->predict(slot(0), slot(1), slot(2), mu_of(0), mu_of(1), mu_of(2), mu_new, ns.tmp.p);
+    const double *x[4] = {slot(0), slot(1), slot(2), slot(3)};
+    const double m[4] = {mu_of(0), mu_of(1), mu_of(2), mu_of(3)};
+    net->predict(x, m, mu_new, ns.tmp.p);
     f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
     if (f_learned < f_secant) {
       std::swap(ns.psi, ns.tmp);
@@ -144,10 +146,11 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
                             s.stream));
   mu[head] = mu_new;
   count = std::min(count + 1, kHist);
-  // online training on the transition (x_{k-2}, x_{k-1}, x_k) -> x_{k+1}
-  if (net && train_left > 0 && count >= 4) {
-    train_loss = net->train(slot(1), slot(2), slot(3), mu_of(1), mu_of(2), mu_of(3), slot(0), mu_of(0),
-                            iters_per_step, learning_rate);
+  // online training on the transition (x_{k-3}, ..., x_k) -> x_{k+1}
+  if (net && train_left > 0 && count >= 5) {
+    const double *x[4] = {slot(1), slot(2), slot(3), slot(4)};
+    const double m[4] = {mu_of(1), mu_of(2), mu_of(3), mu_of(4)};
+    train_loss = net->train(x, m, slot(0), mu_of(0), iters_per_step, learning_rate);
     train_left--;
     if (train_left == 0) net->set_trained(true);
   }

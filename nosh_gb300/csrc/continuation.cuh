@@ -10,10 +10,10 @@ namespace nosh {
 struct Mpnn;  // learned predictor (mpnn.cu)
 
 struct ContinuationImpl {
-  static constexpr int kHist = 4;  // newest converged states kept in HBM
+  static constexpr int kHist = 5;  // newest converged states kept in HBM
   NlsImpl &s;
   DevBuf<double> hist[kHist];
-  double mu[kHist] = {0, 0, 0, 0};
+  double mu[kHist] = {0, 0, 0, 0, 0};
   int head = 0;   // slot of the newest state
   int count = 0;  // valid states
   DevBuf<double> dots;

@@ -1,17 +1,24 @@
-// Learned continuation predictor: an edge message-passing network that
-// corrects the secant prediction of the next continuation state, trained
-// online on the states the continuation itself converges to.
+// Learned continuation predictor: an edge message-passing network that reads
+// the newest converged states and the mesh geometry and predicts how to
+// extrapolate to the next parameter value; trained online on the states the
+// continuation itself converges to.
 //
 // Network (hidden width 64, 3 message-passing layers):
-//   x_i   = [Re/Im psi_k, Re/Im s~, Re/Im q~, mu_new, 1]           (8)
-//           s~ = secant step / rms, q~ = (quadratic - secant) / rms_q
+//   x_i   = [Re/Im psi_k, Re/Im s~, Re/Im q~, Re/Im c~, mu_new, 1]     (10)
+//           s = psi_k - psi_{k-1}, q = quadratic - secant extrapolation,
+//           c = cubic - quadratic extrapolation (phase aligned), ~ = / rms
 //   e_ij  = [alpha_e / mean|alpha|, +-p_e / rms p, |e| / mean|e|, 1]  (4)
 //   h0    = relu(x W_enc + b_enc)
 //   layer: A = h W_a, B = h W_b,
 //          M_i = sum_j relu(A_i + B_j + e_ij W_c + b_m),
 //          h  <- h + relu([h, M] W_u + b_u)
-//   y_i   = h W_dec + b_dec                                          (2)
-//   prediction = secant + rms_q * y
+//   z     = mean_i h_i; (w_q, w_c) = relu(z W_r1 + b_r1) W_r2 + b_r2
+//   prediction = secant + w_q q + w_c c
+// The readout is global: the correction is a combination of smooth
+// history-difference fields, so node-level rounding noise (which the KEO
+// amplifies) never enters the predicted state.  The loss is the
+// cv-weighted squared state error relative to |q|^2, exact from six Gram
+// scalars of the fields.
 // Node GEMMs run on the tensor cores with BF16 operands and FP32
 // accumulation (mma.sync m16n8k16); edge aggregation, weight gradients and
 // the optimiser are FP32.  Every reduction is deterministic (block partials
@@ -31,13 +38,14 @@ using namespace dev;
 namespace {
 
 constexpr int H = 64;      // hidden width
-constexpr int FX = 8;      // node input features
+constexpr int FX = 10;     // node input features
+constexpr int RH = 32;     // readout hidden width
 constexpr int FE = 4;      // edge features
 constexpr int LAYERS = 3;
 
 // flat parameter layout (FP32 master copy)
 struct Layout {
-  int64_t enc_w, enc_b, dec_w, dec_b, total;
+  int64_t enc_w, enc_b, r1_w, r1_b, r2_w, r2_b, total;
   int64_t wa[LAYERS], wb[LAYERS], wc[LAYERS], bm[LAYERS], wu[LAYERS], bu[LAYERS];
   Layout() {
     int64_t o = 0;
@@ -51,8 +59,10 @@ struct Layout {
       wu[l] = o; o += 2 * H * H;
       bu[l] = o; o += H;
     }
-    dec_w = o; o += H * 2;
-    dec_b = o; o += 2;
+    r1_w = o; o += H * RH;
+    r1_b = o; o += RH;
+    r2_w = o; o += RH * 2;
+    r2_b = o; o += 2;
     total = o;
   }
 };
@@ -361,45 +371,6 @@ __global__ void reduce_parts(int nparts, int count, const float *__restrict__ pa
   grad[o] = accumulate ? grad[o] + s : s;
 }
 
-// ------------------------------------------------------- small node kernels
-__global__ void decoder_forward(int64_t n, const float *__restrict__ h, const float *__restrict__ W,
-                                const float *__restrict__ b, float *__restrict__ y) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float y0 = b[0], y1 = b[1];
-  for (int k = 0; k < H; k++) {
-    const float v = h[i * H + k];
-    y0 += v * W[k * 2];
-    y1 += v * W[k * 2 + 1];
-  }
-  y[2 * i] = y0;
-  y[2 * i + 1] = y1;
-}
-
-// loss = sum |y - t|^2 / n (grid reduction), dy = 2 (y - t) / n
-__global__ void loss_kernel(int64_t n, const float *__restrict__ y, const float *__restrict__ t,
-                            float *__restrict__ dy, double *partials, unsigned *counter, double *loss) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double v = 0.0;
-  if (i < n) {
-    const float e0 = y[2 * i] - t[2 * i], e1 = y[2 * i + 1] - t[2 * i + 1];
-    dy[2 * i] = 2.f * e0 / (float)n;
-    dy[2 * i + 1] = 2.f * e1 / (float)n;
-    v = ((double)e0 * e0 + (double)e1 * e1) / (double)n;
-  }
-  grid_reduce(v, partials, counter, loss);
-}
-
-// dh = dy W_dec^T
-__global__ void decoder_backward(int64_t n, const float *__restrict__ dy, const float *__restrict__ W,
-                                 float *__restrict__ dh) {
-  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q >= n * H) return;
-  const int64_t i = q / H;
-  const int k = (int)(q % H);
-  dh[q] = dy[2 * i] * W[k * 2] + dy[2 * i + 1] * W[k * 2 + 1];
-}
-
 // g *= [r > 0] (relu mask from the post-activation)
 __global__ void relu_mask(int64_t n, const float *__restrict__ r, const float *__restrict__ g,
                           float *__restrict__ out) {
@@ -421,82 +392,192 @@ __global__ void adam_kernel(int64_t n, float *__restrict__ p, const float *__res
 }
 
 // ----------------------------------------------------------- features
-// s = x0 - e1 x1 (secant step), q = quadratic - secant extrapolation to t,
-// sums of |s|^2 and |q|^2 into red[0], red[1]
-__global__ void features_a(int64_t n, const double *__restrict__ c, double L0s, double L1s, double L0q,
-                           double L1q, double L2q, const C2<double> *__restrict__ x0,
-                           const C2<double> *__restrict__ x1, const C2<double> *__restrict__ x2,
+struct Phases {
+  double er[4], ei[4];  // phase factors aligning x1, x2, x3, target with x0
+};
+__device__ __forceinline__ void phases(const double *c, int k, double &er, double &ei) {
+  const double m = sqrt(c[2 * k] * c[2 * k] + c[2 * k + 1] * c[2 * k + 1]);
+  er = m > 0 ? c[2 * k] / m : 1.0;
+  ei = m > 0 ? c[2 * k + 1] / m : 0.0;
+}
+
+// per node: s = x0 - x1, q = quad - sec, c = cubic - quad at t (fields in
+// sq, 6 doubles per node), and the sums of |s|^2, |q|^2, |c|^2 into red[0..2]
+__global__ void features_a(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
+                           const C2<double> *__restrict__ x0, const C2<double> *__restrict__ x1,
+                           const C2<double> *__restrict__ x2, const C2<double> *__restrict__ x3,
                            double *__restrict__ sq, double *partials, unsigned *counter, double *red) {
-  double e1r = 1.0, e1i = 0.0, e2r = 1.0, e2i = 0.0;
-  {
-    const double m1 = sqrt(c[0] * c[0] + c[1] * c[1]), m2 = sqrt(c[2] * c[2] + c[3] * c[3]);
-    if (m1 > 0) { e1r = c[0] / m1; e1i = c[1] / m1; }
-    if (m2 > 0) { e2r = c[2] / m2; e2i = c[3] / m2; }
-  }
-  double as = 0.0, aq = 0.0;
+  double er[3], ei[3];
+  for (int k = 0; k < 3; k++) phases(dots, k, er[k], ei[k]);
+  double as = 0.0, aq = 0.0, ac = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const C2<double> a = x0[i], p = x1[i], r = x2[i];
-    const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
-    const double rr = e2r * r.x - e2i * r.y, ri = e2r * r.y + e2i * r.x;
-    const double sr = a.x - pr, si = a.y - pi;
-    const double secr = L0s * a.x + L1s * pr, seci = L0s * a.y + L1s * pi;
-    const double qr = L0q * a.x + L1q * pr + L2q * rr - secr, qi = L0q * a.y + L1q * pi + L2q * ri - seci;
-    sq[4 * i] = sr;
-    sq[4 * i + 1] = si;
-    sq[4 * i + 2] = qr;
-    sq[4 * i + 3] = qi;
-    as += sr * sr + si * si;
-    aq += qr * qr + qi * qi;
+    double xr[4], xi[4];
+    xr[0] = x0[i].x;
+    xi[0] = x0[i].y;
+    const C2<double> *xs[3] = {x1, x2, x3};
+    for (int k = 0; k < 3; k++) {
+      const C2<double> p = xs[k][i];
+      xr[k + 1] = er[k] * p.x - ei[k] * p.y;
+      xi[k + 1] = er[k] * p.y + ei[k] * p.x;
+    }
+    // Ls: secant (2), quadratic (3), cubic (4) Lagrange weights
+    const double secr = Ls[0] * xr[0] + Ls[1] * xr[1], seci = Ls[0] * xi[0] + Ls[1] * xi[1];
+    const double qdr = Ls[2] * xr[0] + Ls[3] * xr[1] + Ls[4] * xr[2];
+    const double qdi = Ls[2] * xi[0] + Ls[3] * xi[1] + Ls[4] * xi[2];
+    const double cbr = Ls[5] * xr[0] + Ls[6] * xr[1] + Ls[7] * xr[2] + Ls[8] * xr[3];
+    const double cbi = Ls[5] * xi[0] + Ls[6] * xi[1] + Ls[7] * xi[2] + Ls[8] * xi[3];
+    double *o = sq + 6 * i;
+    o[0] = xr[0] - xr[1];
+    o[1] = xi[0] - xi[1];
+    o[2] = qdr - secr;
+    o[3] = qdi - seci;
+    o[4] = cbr - qdr;
+    o[5] = cbi - qdi;
+    as += o[0] * o[0] + o[1] * o[1];
+    aq += o[2] * o[2] + o[3] * o[3];
+    ac += o[4] * o[4] + o[5] * o[5];
   }
   grid_reduce(as, partials, counter, red);
   grid_reduce(aq, partials + gridDim.x, counter + 1, red + 1);
+  grid_reduce(ac, partials + 2 * gridDim.x, counter + 2, red + 2);
 }
 
-// X = [x0, s / rms_s, q / rms_q, mu_new, 1]; with a target, T = (e_t x_t -
-// secant) / rms_q; red[0..1] hold the sums of squares
-__global__ void features_b(int64_t n, const double *__restrict__ red, double mu_new, const C2<double> *__restrict__ x0,
-                           const double *__restrict__ sq, float *__restrict__ X, const double *__restrict__ ct,
-                           double L0s, double L1s, const C2<double> *__restrict__ x1,
-                           const double *__restrict__ c, const C2<double> *__restrict__ xt,
-                           float *__restrict__ T) {
-  const double rs = sqrt(red[0] / n), rq = sqrt(red[1] / n);
-  const double is = rs > 0 ? 1.0 / rs : 0.0, iq = rq > 0 ? 1.0 / rq : 0.0;
+// X = [x0, s~, q~, c~, mu_new, 1]
+__global__ void features_b(int64_t n, const double *__restrict__ red, double mu_new,
+                           const C2<double> *__restrict__ x0, const double *__restrict__ sq,
+                           float *__restrict__ X) {
+  const double rs = sqrt(red[0] / n), rq = sqrt(red[1] / n), rc = sqrt(red[2] / n);
+  const double is = rs > 0 ? 1.0 / rs : 0.0, iq = rq > 0 ? 1.0 / rq : 0.0, ic = rc > 0 ? 1.0 / rc : 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const C2<double> a = x0[i];
+    const double *f = sq + 6 * i;
     float *xi = X + i * FX;
     xi[0] = (float)a.x;
     xi[1] = (float)a.y;
-    xi[2] = (float)(sq[4 * i] * is);
-    xi[3] = (float)(sq[4 * i + 1] * is);
-    xi[4] = (float)(sq[4 * i + 2] * iq);
-    xi[5] = (float)(sq[4 * i + 3] * iq);
-    xi[6] = (float)mu_new;
-    xi[7] = 1.f;
-    if (T) {
-      double e1r = 1.0, e1i = 0.0, etr = 1.0, eti = 0.0;
-      const double m1 = sqrt(c[0] * c[0] + c[1] * c[1]), mt = sqrt(ct[0] * ct[0] + ct[1] * ct[1]);
-      if (m1 > 0) { e1r = c[0] / m1; e1i = c[1] / m1; }
-      if (mt > 0) { etr = ct[0] / mt; eti = ct[1] / mt; }
-      const C2<double> p = x1[i], t = xt[i];
-      const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
-      const double secr = L0s * a.x + L1s * pr, seci = L0s * a.y + L1s * pi;
-      const double tr = etr * t.x - eti * t.y, ti = etr * t.y + eti * t.x;
-      T[2 * i] = (float)((tr - secr) * iq);
-      T[2 * i + 1] = (float)((ti - seci) * iq);
-    }
+    xi[2] = (float)(f[0] * is);
+    xi[3] = (float)(f[1] * is);
+    xi[4] = (float)(f[2] * iq);
+    xi[5] = (float)(f[3] * iq);
+    xi[6] = (float)(f[4] * ic);
+    xi[7] = (float)(f[5] * ic);
+    xi[8] = (float)mu_new;
+    xi[9] = 1.f;
   }
 }
 
-// out += rms_q * y
-__global__ void apply_correction(int64_t n, const double *__restrict__ red, const float *__restrict__ y,
-                                 C2<double> *__restrict__ out) {
-  const double rq = sqrt(red[1] / n);
+// cv-weighted Gram scalars of (q, c, d) with d = e_t x_t - secant:
+// g = [<q,q>, <q,c>, <c,c>, <q,d>, <c,d>, <d,d>]
+__global__ void gram_kernel(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
+                            const C2<double> *__restrict__ x0, const C2<double> *__restrict__ x1,
+                            const C2<double> *__restrict__ xt, const double *__restrict__ cv,
+                            const double *__restrict__ sq, double *partials, unsigned *counter, double *g) {
+  double e1r, e1i, etr, eti;
+  phases(dots, 0, e1r, e1i);
+  phases(dots, 3, etr, eti);
+  double acc[6] = {0, 0, 0, 0, 0, 0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> a = x0[i], p = x1[i], t = xt[i];
+    const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
+    const double secr = Ls[0] * a.x + Ls[1] * pr, seci = Ls[0] * a.y + Ls[1] * pi;
+    const double dr = etr * t.x - eti * t.y - secr, di = etr * t.y + eti * t.x - seci;
+    const double *f = sq + 6 * i;
+    const double w = cv[i];
+    acc[0] += w * (f[2] * f[2] + f[3] * f[3]);
+    acc[1] += w * (f[2] * f[4] + f[3] * f[5]);
+    acc[2] += w * (f[4] * f[4] + f[5] * f[5]);
+    acc[3] += w * (f[2] * dr + f[3] * di);
+    acc[4] += w * (f[4] * dr + f[5] * di);
+    acc[5] += w * (dr * dr + di * di);
+  }
+  for (int k = 0; k < 6; k++) grid_reduce(acc[k], partials + k * gridDim.x, counter + k, g + k);
+}
+
+// out (the secant prediction) += w_q q + w_c c
+__global__ void combine_kernel(int64_t n, const double *__restrict__ w, const double *__restrict__ sq,
+                               C2<double> *__restrict__ out) {
+  const double wq = w[0], wc = w[1];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double *f = sq + 6 * i;
     C2<double> o = out[i];
-    o.x += rq * (double)y[2 * i];
-    o.y += rq * (double)y[2 * i + 1];
+    o.x += wq * f[2] + wc * f[4];
+    o.y += wq * f[3] + wc * f[5];
     out[i] = o;
   }
+}
+
+// ------------------------------------------------------------- readout
+// column sums of h (n x 64): one partial row of 64 per CTA
+__global__ void pool_partial(int64_t n, const float *__restrict__ h, float *__restrict__ part) {
+  __shared__ float s[4][H];
+  const int c = threadIdx.x & 63, rgrp = threadIdx.x >> 6;  // 256 threads: 4 row groups
+  float a = 0.f;
+  for (int64_t r = (int64_t)blockIdx.x * 4 + rgrp; r < n; r += (int64_t)gridDim.x * 4) a += h[r * H + c];
+  s[rgrp][c] = a;
+  __syncthreads();
+  if (threadIdx.x < H) part[(int64_t)blockIdx.x * H + c] = (s[0][c] + s[1][c]) + (s[2][c] + s[3][c]);
+}
+
+// z = sum of the partials / n; (w_q, w_c) = relu(z W1 + b1) W2 + b2.  With
+// a Gram vector: loss (relative state error) and the backward pass of the
+// readout into grad, dz into dz.  One CTA of 64 threads.
+__global__ void readout(int nparts, int64_t n, const float *__restrict__ part, const float *__restrict__ P,
+                        int64_t o_w1, int64_t o_b1, int64_t o_w2, int64_t o_b2, double *__restrict__ wout,
+                        const double *__restrict__ gram, float *__restrict__ grad, float *__restrict__ dz,
+                        double *__restrict__ loss) {
+  __shared__ float z[H], h1[RH], dh1[RH];
+  __shared__ double w[2], dw[2];
+  const int t = threadIdx.x;
+  {
+    float a = 0.f;
+    for (int b = 0; b < nparts; b++) a += part[(int64_t)b * H + t];
+    z[t] = a / (float)n;
+  }
+  __syncthreads();
+  if (t < RH) {
+    float a = P[o_b1 + t];
+    for (int k = 0; k < H; k++) a += z[k] * P[o_w1 + k * RH + t];
+    h1[t] = fmaxf(a, 0.f);
+  }
+  __syncthreads();
+  if (t < 2) {
+    double a = P[o_b2 + t];
+    for (int k = 0; k < RH; k++) a += (double)h1[k] * P[o_w2 + k * 2 + t];
+    w[t] = a;
+    wout[t] = a;
+  }
+  __syncthreads();
+  if (!gram) return;
+  // loss = (w^T G w - 2 w.b + dd) / qq with G = [[qq, qc], [qc, cc]]
+  if (t == 0) {
+    const double qq = gram[0] > 0 ? gram[0] : 1.0;
+    const double L = (w[0] * w[0] * gram[0] + 2 * w[0] * w[1] * gram[1] + w[1] * w[1] * gram[2] -
+                      2 * w[0] * gram[3] - 2 * w[1] * gram[4] + gram[5]) / qq;
+    *loss = L;
+    dw[0] = 2 * (w[0] * gram[0] + w[1] * gram[1] - gram[3]) / qq;
+    dw[1] = 2 * (w[0] * gram[1] + w[1] * gram[2] - gram[4]) / qq;
+  }
+  __syncthreads();
+  if (t < RH) {
+    // W2, b2 gradients and dh1
+    grad[o_w2 + t * 2] = (float)(h1[t] * dw[0]);
+    grad[o_w2 + t * 2 + 1] = (float)(h1[t] * dw[1]);
+    const float g = (float)(dw[0] * P[o_w2 + t * 2] + dw[1] * P[o_w2 + t * 2 + 1]);
+    dh1[t] = h1[t] > 0.f ? g : 0.f;
+  }
+  if (t < 2) grad[o_b2 + t] = (float)dw[t];
+  __syncthreads();
+  // W1, b1 gradients and dz
+  for (int q = t; q < H * RH; q += blockDim.x) grad[o_w1 + q] = z[q / RH] * dh1[q % RH];
+  if (t < RH) grad[o_b1 + t] = dh1[t];
+  float a = 0.f;
+  for (int k = 0; k < RH; k++) a += dh1[k] * P[o_w1 + t * RH + k];
+  dz[t] = a;
+}
+
+// dh[i][c] = dz[c] / n (gradient of the mean pool)
+__global__ void pool_backward(int64_t n, const float *__restrict__ dz, float *__restrict__ dh) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < n * H) dh[q] = dz[q % H] / (float)n;
 }
 
 __global__ void cdot_pair(int64_t n, const C2<double> *__restrict__ a, const C2<double> *__restrict__ b,
@@ -552,26 +633,26 @@ struct Mpnn::Impl {
   DevBuf<float> params, grads, am, av;
   int64_t adam_t = 0;
   // BF16 transposed operands: forward W (enc padded to K=16, wa, wb, wu per
-  // layer) and backward W^T blocks
+  // layer) and the W^T blocks of the backward pass
   DevBuf<__nv_bfloat16> wt;
   int64_t wt_enc, wt_a[LAYERS], wt_b[LAYERS], wt_u[LAYERS], wtb_a[LAYERS], wtb_b[LAYERS], wtb_uh[LAYERS],
       wtb_um[LAYERS];
   // activations and gradients
-  DevBuf<float> X, Xp, Hs[LAYERS + 1], A[LAYERS], B[LAYERS], Mg[LAYERS], R[LAYERS], Y, T, dY;
-  DevBuf<float> dH, dR, dM, dA, dB, tmp;
-  DevBuf<float> part;
-  DevBuf<double> sq, red, dots;
-  DevBuf<double> loss;
+  DevBuf<float> X, Xp, Hs[LAYERS + 1], A[LAYERS], B[LAYERS], Mg[LAYERS], R[LAYERS];
+  DevBuf<float> dH, dR, dM, dA, dB, dz;
+  DevBuf<float> part, pool;
+  int pool_blocks = 0;
+  DevBuf<double> sq, red, dots, Ls, gram, w, loss;
   explicit Impl(NlsImpl &nls);
   void refresh_bf16();
-  void forward();
-  double backward_and_step(float lr);
-  void features(const double *x0, const double *x1, const double *x2, double mu0, double mu1, double mu2,
-                double mu_t, const double *target);
+  void forward();                         // X -> H -> w
+  double backward_and_step(float lr);     // needs gram
+  void features(const double *const x[4], const double mu[4], double mu_t, const double *target);
   void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, const float *bias,
             float *out, float *out2);
   void wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol, int64_t dst,
              int64_t bias_dst);
+  void readout_launch(bool train);
 };
 
 Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
@@ -596,7 +677,7 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
                                                s.d_p.p, m.d_len.p, ia, ip, il, ef.p, tr.p);
   NOSH_CUDA(cudaGetLastError());
   // parameters: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero
-  // biases, a small decoder so the first predictions stay near the secant
+  // biases; the readout starts at zero output (secant prediction)
   std::vector<float> h(L.total, 0.f);
   uint64_t seed = 0x6e6f7368ULL;
   auto fill = [&](int64_t off, int64_t count, int fan_in, float scale) {
@@ -610,14 +691,15 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
     fill(L.wc[l], FE * H, FE, 1.f);
     fill(L.wu[l], 2 * H * H, 2 * H, 1.f);
   }
-  fill(L.dec_w, H * 2, H, 0.1f);
+  fill(L.r1_w, H * RH, H, 1.f);
+  fill(L.r2_w, RH * 2, RH, 0.1f);
   params.upload(h, st);
   grads.alloc(L.total);
+  grads.zero(st);
   am.alloc(L.total);
   av.alloc(L.total);
   am.zero(st);
   av.zero(st);
-  // BF16 operand offsets
   int64_t o = 0;
   wt_enc = o; o += H * 16;
   for (int l = 0; l < LAYERS; l++) {
@@ -641,14 +723,18 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
     Mg[l].alloc(N * H);
     R[l].alloc(N * H);
   }
-  Y.alloc(2 * N);
-  T.alloc(2 * N);
-  dY.alloc(2 * N);
-  for (DevBuf<float> *b : {&dH, &dR, &dM, &dA, &dB, &tmp}) b->alloc(N * 2 * H);
+  for (DevBuf<float> *b : {&dH, &dR, &dM, &dA, &dB}) b->alloc(N * H);
+  dz.alloc(H);
   part.alloc(std::max<int64_t>(div_up(N, WG_ROWS) * (2 * H + 1) * H, div_up(N, 64) * 5 * H) + 64);
-  sq.alloc(4 * N);
+  pool_blocks = (int)std::min<int64_t>(div_up(N, 4), 1024);
+  pool.alloc((int64_t)pool_blocks * H);
+  sq.alloc(6 * N);
   red.alloc(8);
   dots.alloc(8);
+  Ls.alloc(9);
+  gram.alloc(6);
+  w.alloc(2);
+  w.zero(st);
   loss.alloc(1);
   refresh_bf16();
   s.sync();
@@ -657,7 +743,7 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
 void Mpnn::Impl::refresh_bf16() {
   cudaStream_t st = s.stream;
   const float *P = params.p;
-  // encoder: K = 8 features padded to 16 (the padded columns of Xp are 0)
+  // encoder: K = 10 features padded to 16 (the padded columns of Xp are 0)
   enc_to_bf16<<<div_up(H * 16, 256), 256, 0, st>>>(P + L.enc_w, wt.p + wt_enc);
   for (int l = 0; l < LAYERS; l++) {
     to_bf16_t<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wa[l], H, H, 0, wt.p + wt_a[l]);
@@ -669,6 +755,7 @@ void Mpnn::Impl::refresh_bf16() {
     to_bf16_rows<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wu[l], 2 * H, 0, wt.p + wtb_uh[l]);
     to_bf16_rows<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wu[l], 2 * H, H, wt.p + wtb_um[l]);
   }
+  s.launch_count += 1 + 7 * LAYERS;
   NOSH_CUDA(cudaGetLastError());
 }
 
@@ -686,11 +773,18 @@ void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K
   ++s.launch_count;
 }
 
+void Mpnn::Impl::readout_launch(bool train) {
+  cudaStream_t st = s.stream;
+  pool_partial<<<pool_blocks, 256, 0, st>>>(N, Hs[LAYERS].p, pool.p);
+  readout<<<1, H, 0, st>>>(pool_blocks, N, pool.p, params.p, L.r1_w, L.r1_b, L.r2_w, L.r2_b, w.p,
+                           train ? gram.p : nullptr, grads.p, dz.p, loss.p);
+  s.launch_count += 2;
+}
+
 void Mpnn::Impl::forward() {
   cudaStream_t st = s.stream;
   const float *P = params.p;
   MeshImpl &m = *s.mesh;
-  // encoder (features padded to 16 columns)
   NOSH_CUDA(cudaMemcpy2DAsync(Xp.p, 16 * sizeof(float), X.p, FX * sizeof(float), FX * sizeof(float), N,
                               cudaMemcpyDeviceToDevice, st));
   gemm(EPI_BIAS_RELU, Xp.p, 16, nullptr, 0, wt_enc, P + L.enc_b, Hs[0].p, nullptr);
@@ -703,8 +797,6 @@ void Mpnn::Impl::forward() {
     NOSH_CUDA(cudaMemcpyAsync(Hs[l + 1].p, Hs[l].p, N * H * sizeof(float), cudaMemcpyDeviceToDevice, st));
     gemm(EPI_RESID_RELU, Hs[l].p, H, Mg[l].p, H, wt_u[l], P + L.bu[l], Hs[l + 1].p, R[l].p);
   }
-  decoder_forward<<<div_up(N, 256), 256, 0, st>>>(N, Hs[LAYERS].p, P + L.dec_w, P + L.dec_b, Y.p);
-  ++s.launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
 
@@ -718,31 +810,29 @@ void Mpnn::Impl::wgrad(const float *in0, int K0, const float *in1, int K1, const
   s.launch_count += 2;
 }
 
+// forward must have run; gram holds the sample's Gram scalars
 double Mpnn::Impl::backward_and_step(float lr) {
   cudaStream_t st = s.stream;
   const float *P = params.p;
   MeshImpl &m = *s.mesh;
-  loss_kernel<<<div_up(N, 256), 256, 0, st>>>(N, Y.p, T.p, dY.p, s.red.partials.p, s.red.counter.p, loss.p);
-  // decoder
-  wgrad(Hs[LAYERS].p, H, nullptr, 0, dY.p, 2, L.dec_w, L.dec_b);
-  decoder_backward<<<div_up(N * H, 256), 256, 0, st>>>(N, dY.p, P + L.dec_w, dH.p);
-  s.launch_count += 2;
+  readout_launch(true);  // loss, readout gradients, dz
+  pool_backward<<<div_up(N * H, 256), 256, 0, st>>>(N, dz.p, dH.p);
+  ++s.launch_count;
   for (int l = LAYERS - 1; l >= 0; l--) {
     // h_{l+1} = h_l + R_l, R_l = relu([h_l, M_l] W_u + b_u)
     relu_mask<<<div_up(N * H, 256), 256, 0, st>>>(N * H, R[l].p, dH.p, dR.p);
+    ++s.launch_count;
     wgrad(Hs[l].p, H, Mg[l].p, H, dR.p, H, L.wu[l], L.bu[l]);
-    // dM = dR W_u[64:128]^T ; dh += dR W_u[0:64]^T (dh already holds the
-    // residual path)
+    // dM = dR W_u[64:128]^T ; dh += dR W_u[0:64]^T (dh holds the residual path)
     gemm(EPI_LINEAR, dR.p, H, nullptr, 0, wtb_um[l], nullptr, dM.p, nullptr);
     gemm(EPI_ACCUM, dR.p, H, nullptr, 0, wtb_uh[l], nullptr, dH.p, nullptr);
-    // message aggregation
-    const int nb8 = div_up(N, 64);
-    edge_backward_a<<<nb8, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l],
-                                         dM.p, dA.p, part.p);
-    reduce_parts<<<div_up(5 * H, 256), 256, 0, st>>>(nb8, 5 * H, part.p, grads.p, L.wc[l], 4 * H, L.bm[l], 0);
+    const int nb = div_up(N, 64);
+    edge_backward_a<<<nb, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l],
+                                        dM.p, dA.p, part.p);
+    reduce_parts<<<div_up(5 * H, 256), 256, 0, st>>>(nb, 5 * H, part.p, grads.p, L.wc[l], 4 * H, L.bm[l], 0);
     edge_backward_b<<<div_up(N * 32, 256), 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, tr.p, ef.p, A[l].p, B[l].p,
                                                          P + L.wc[l], P + L.bm[l], dM.p, dB.p);
-    s.launch_count += 4;
+    s.launch_count += 3;
     // A = h W_a, B = h W_b
     wgrad(Hs[l].p, H, nullptr, 0, dA.p, H, L.wa[l], -1);
     wgrad(Hs[l].p, H, nullptr, 0, dB.p, H, L.wb[l], -1);
@@ -753,40 +843,63 @@ double Mpnn::Impl::backward_and_step(float lr) {
   relu_mask<<<div_up(N * H, 256), 256, 0, st>>>(N * H, Hs[0].p, dH.p, dR.p);
   ++s.launch_count;
   wgrad(X.p, FX, nullptr, 0, dR.p, H, L.enc_w, L.enc_b);
-  adam_t++;
-  const float b1 = 0.9f, b2 = 0.999f;
-  const float c1 = 1.f - std::pow(b1, (float)adam_t), c2 = 1.f - std::pow(b2, (float)adam_t);
-  adam_kernel<<<div_up(L.total, 256), 256, 0, st>>>(L.total, params.p, grads.p, am.p, av.p, lr, b1, b2, 1e-8f, c1, c2);
-  ++s.launch_count;
-  refresh_bf16();
+  if (lr > 0.f) {
+    adam_t++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)adam_t), c2 = 1.f - std::pow(b2, (float)adam_t);
+    adam_kernel<<<div_up(L.total, 256), 256, 0, st>>>(L.total, params.p, grads.p, am.p, av.p, lr, b1, b2, 1e-8f,
+                                                      c1, c2);
+    ++s.launch_count;
+    refresh_bf16();
+  }
   double hl = 0.0;
   loss.download(&hl, 1, st);
   s.sync();
   return hl;
 }
 
-void Mpnn::Impl::features(const double *x0, const double *x1, const double *x2, double mu0, double mu1,
-                          double mu2, double t, const double *target) {
+// node features at mu_t from the newest states x[0..3] (mu[0..3]) and, with
+// a target (the converged state at mu_t), the sample's Gram scalars
+void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target) {
   cudaStream_t st = s.stream;
   const int G = vgrid(N);
-  const double L0s = (t - mu1) / (mu0 - mu1), L1s = (t - mu0) / (mu1 - mu0);
-  const double L0q = (t - mu1) * (t - mu2) / ((mu0 - mu1) * (mu0 - mu2));
-  const double L1q = (t - mu0) * (t - mu2) / ((mu1 - mu0) * (mu1 - mu2));
-  const double L2q = (t - mu0) * (t - mu1) / ((mu2 - mu0) * (mu2 - mu1));
-  cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)x1, (const C2<double> *)x0, s.red.partials.p, s.red.counter.p,
-                               dots.p);
-  cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)x2, (const C2<double> *)x0, s.red.partials.p, s.red.counter.p,
-                               dots.p + 2);
-  if (target)
-    cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)target, (const C2<double> *)x0, s.red.partials.p,
-                                 s.red.counter.p, dots.p + 4);
-  features_a<<<G, 256, 0, st>>>(N, dots.p, L0s, L1s, L0q, L1q, L2q, (const C2<double> *)x0,
-                                (const C2<double> *)x1, (const C2<double> *)x2, sq.p, s.red.partials.p,
+  double Lh[9];
+  Lh[0] = (t - mu[1]) / (mu[0] - mu[1]);
+  Lh[1] = (t - mu[0]) / (mu[1] - mu[0]);
+  for (int k = 0; k < 3; k++) {
+    double v = 1.0;
+    for (int q = 0; q < 3; q++)
+      if (q != k) v *= (t - mu[q]) / (mu[k] - mu[q]);
+    Lh[2 + k] = v;
+  }
+  for (int k = 0; k < 4; k++) {
+    double v = 1.0;
+    for (int q = 0; q < 4; q++)
+      if (q != k) v *= (t - mu[q]) / (mu[k] - mu[q]);
+    Lh[5 + k] = v;
+  }
+  Ls.upload(Lh, 9, st);
+  for (int k = 1; k < 4; k++) {
+    cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)x[k], (const C2<double> *)x[0], s.red.partials.p,
+                                 s.red.counter.p, dots.p + 2 * (k - 1));
+    ++s.launch_count;
+  }
+  if (target) {
+    cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)target, (const C2<double> *)x[0], s.red.partials.p,
+                                 s.red.counter.p, dots.p + 6);
+    ++s.launch_count;
+  }
+  features_a<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
+                                (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, s.red.partials.p,
                                 s.red.counter.p, red.p);
-  features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x0, sq.p, X.p, dots.p + 4, L0s, L1s,
-                                (const C2<double> *)x1, dots.p, (const C2<double> *)target,
-                                target ? T.p : nullptr);
-  s.launch_count += target ? 5 : 4;
+  features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x[0], sq.p, X.p);
+  s.launch_count += 2;
+  if (target) {
+    gram_kernel<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
+                                   (const C2<double> *)target, s.mesh->d_cv.p, sq.p, s.red.partials.p,
+                                   s.red.counter.p, gram.p);
+    ++s.launch_count;
+  }
   NOSH_CUDA(cudaGetLastError());
 }
 
@@ -794,20 +907,20 @@ void Mpnn::Impl::features(const double *x0, const double *x1, const double *x2, 
 Mpnn::Mpnn(NlsImpl &s) : impl(new Impl(s)) {}
 Mpnn::~Mpnn() = default;
 
-void Mpnn::predict(const double *x0, const double *x1, const double *x2, double mu0, double mu1, double mu2,
-                   double mu_new, double *out) {
+void Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, double *out) {
   Impl &I = *impl;
-  I.features(x0, x1, x2, mu0, mu1, mu2, mu_new, nullptr);
+  I.features(x, mu, mu_new, nullptr);
   I.forward();
-  apply_correction<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.red.p, I.Y.p, (C2<double> *)out);
+  I.readout_launch(false);
+  combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (C2<double> *)out);
   ++I.s.launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
 
-double Mpnn::train(const double *x0, const double *x1, const double *x2, double mu0, double mu1, double mu2,
-                   const double *target, double mu_t, int iters, double lr) {
+double Mpnn::train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,
+                   double lr) {
   Impl &I = *impl;
-  I.features(x0, x1, x2, mu0, mu1, mu2, mu_t, target);
+  I.features(x, mu, mu_t, target);
   double l = std::nan("");
   for (int k = 0; k < iters; k++) {
     I.forward();
@@ -831,28 +944,20 @@ void Mpnn::get_edge_features(float *h) const {
   impl->ef.download(h, impl->nnz * FE, impl->s.stream);
   impl->s.sync();
 }
-void Mpnn::forward_features(const float *X, float *Y) {
+void Mpnn::forward_features(const float *X, double *w) {
   Impl &I = *impl;
   I.X.upload(X, I.N * FX, I.s.stream);
   I.forward();
-  I.Y.download(Y, 2 * I.N, I.s.stream);
+  I.readout_launch(false);
+  I.w.download(w, 2, I.s.stream);
   I.s.sync();
 }
-double Mpnn::loss_and_grad(const float *X, const float *T, float *grad) {
+double Mpnn::loss_and_grad(const float *X, const double *gram, float *grad) {
   Impl &I = *impl;
   I.X.upload(X, I.N * FX, I.s.stream);
-  I.T.upload(T, 2 * I.N, I.s.stream);
+  I.gram.upload(gram, 6, I.s.stream);
   I.forward();
-  // backward without the optimiser step: reuse backward_and_step with lr 0
-  // and restore the Adam state afterwards
-  std::vector<float> m(I.L.total), v(I.L.total);
-  I.am.download(m.data(), I.L.total, I.s.stream);
-  I.av.download(v.data(), I.L.total, I.s.stream);
-  const int64_t t = I.adam_t;
-  const double l = I.backward_and_step(0.f);
-  I.adam_t = t;
-  I.am.upload(m, I.s.stream);
-  I.av.upload(v, I.s.stream);
+  const double l = I.backward_and_step(0.f);  // gradient only, no step
   I.grads.download(grad, I.L.total, I.s.stream);
   I.s.sync();
   return l;

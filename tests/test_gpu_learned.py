@@ -2,10 +2,10 @@
 
 * the device-resident continuation reproduces the oracle's converged states
   (exact-LU Newton, modulo the global phase);
-* the message-passing network's forward pass and parameter gradient match a
-  torch FP32 CPU reference of the same network that rounds the GEMM operands
-  to BF16 as the tensor-core path does (gradient tolerance accounts for the
-  BF16 operands of the backward GEMMs);
+* the message-passing network's readout coefficients and parameter gradient
+  match a torch FP32 CPU reference of the same network that rounds the node
+  GEMM operands to BF16 as the tensor-core path does (gradient tolerance
+  accounts for the BF16 operands of the backward GEMMs);
 * trained online on the first steps of a continuation, the learned predictor
   starts Newton from a smaller residual than the secant predictor.
 """
@@ -16,7 +16,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-H, FX, FE, LAYERS = 64, 8, 4, 3
+H, FX, FE, LAYERS, RH = 64, 10, 4, 3, 32
 
 
 def _layout():
@@ -36,13 +36,16 @@ def _layout():
         take(f"bm{l}", H)
         take(f"wu{l}", 2 * H * H)
         take(f"bu{l}", H)
-    take("dec_w", H * 2)
-    take("dec_b", 2)
+    take("r1_w", H * RH)
+    take("r1_b", RH)
+    take("r2_w", RH * 2)
+    take("r2_b", 2)
     return L, o
 
 
-def torch_reference(p, ef, rp, ci, X, T):
-    """The network in torch (CPU, FP32), GEMM operands rounded to BF16."""
+def torch_reference(p, ef, rp, ci, X, gram):
+    """The network in torch (CPU, FP32), node GEMM operands rounded to BF16;
+    returns the readout coefficients, the loss and the parameter gradient."""
     import torch
 
     L, total = _layout()
@@ -68,10 +71,15 @@ def torch_reference(p, ef, rp, ci, X, T):
         M = torch.zeros(N, H).index_add_(0, rows, torch.relu(Pij))
         R = torch.relu(bf(torch.cat([h, M], dim=1)) @ bf(w(f"wu{l}", (2 * H, H))) + w(f"bu{l}", (H,)))
         h = h + R
-    Y = h @ w("dec_w", (H, 2)) + w("dec_b", (2,))
-    loss = ((Y - torch.tensor(T)) ** 2).sum() / N
+    z = h.mean(dim=0)
+    h1 = torch.relu(z @ w("r1_w", (H, RH)) + w("r1_b", (RH,)))
+    wq = (h1 @ w("r2_w", (RH, 2)) + w("r2_b", (2,))).double()
+    g = torch.tensor(gram, dtype=torch.float64)
+    G = torch.stack([torch.stack([g[0], g[1]]), torch.stack([g[1], g[2]])])
+    b = torch.stack([g[3], g[4]])
+    loss = (wq @ G @ wq - 2 * wq @ b + g[5]) / g[0]
     loss.backward()
-    return Y.detach().numpy(), float(loss), P.grad.numpy()
+    return wq.detach().numpy(), float(loss), P.grad.numpy()
 
 
 @pytest.fixture(scope="module")
@@ -94,29 +102,40 @@ def test_mpnn_forward_and_gradient_match_torch(net):
     gm, model, mp = net
     rng = np.random.default_rng(7)
     N = gm.num_vertices
-    # a parameter set with well-populated ReLUs (the decoder starts small)
+    # a parameter set with well-populated ReLUs and an O(1) readout (the
+    # readout starts near zero)
     p = mp.params()
     L, _ = _layout()
-    o, n = L["dec_w"]
-    p[o : o + n] = rng.uniform(-0.3, 0.3, n)
+    for name, a in (("r1_b", 0.2), ("r2_w", 0.5), ("r2_b", 0.5)):
+        o, n = L[name]
+        p[o : o + n] = rng.uniform(-a, a, n)
     mp.params(p)
     X = rng.standard_normal((N, FX)).astype(np.float32)
-    X[:, 7] = 1.0
-    T = rng.standard_normal((N, 2)).astype(np.float32)
+    X[:, FX - 1] = 1.0
+    # Gram scalars of three random fields (q, c, d)
+    q, c, d = rng.standard_normal((3, 2 * N))
+    gram = np.array([q @ q, q @ c, c @ c, q @ d, c @ d, d @ d])
     rp, ci = gm.build_complex_graph()
     rows = np.repeat(np.arange(N), np.diff(rp))
     keep = ci != rows
     rp_od = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=N))]).astype(np.int64)
     ci_od = ci[keep]
     ef = mp.edge_features()
-    Y_ref, loss_ref, g_ref = torch_reference(p, ef, rp_od, ci_od, X, T)
-    Y = mp.forward(X)
-    assert np.abs(Y - Y_ref).max() <= 2e-3 * np.abs(Y_ref).max()
-    loss, g = mp.loss_grad(X, T)
+    w_ref, loss_ref, g_ref = torch_reference(p, ef, rp_od, ci_od, X, gram)
+    w = mp.forward(X)
+    assert np.abs(w - w_ref).max() <= 2e-3 * np.abs(w_ref).max(), (w, w_ref)
+    loss, g = mp.loss_grad(X, gram)
     assert abs(loss - loss_ref) <= 1e-4 * loss_ref
     cos = float(g @ g_ref / (np.linalg.norm(g) * np.linalg.norm(g_ref)))
     rel = float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref))
     assert cos > 0.999 and rel < 3e-2, (cos, rel)
+    # the message-passing part on its own (its gradient is much smaller than
+    # the readout's and runs through the BF16 backward GEMMs)
+    mp_end = L["r1_w"][0]
+    gm_, gr_ = g[:mp_end], g_ref[:mp_end]
+    cos = float(gm_ @ gr_ / (np.linalg.norm(gm_) * np.linalg.norm(gr_)))
+    rel = float(np.linalg.norm(gm_ - gr_) / np.linalg.norm(gr_))
+    assert cos > 0.998 and rel < 6e-2, (cos, rel)
     # the loss-gradient query does not change the parameters
     np.testing.assert_array_equal(mp.params(), p)
 
@@ -172,7 +191,7 @@ def test_learned_predictor_gains_over_secant():
         st = cont.advance(mu, predictor=ng.PREDICT_LEARNED)
         assert st["status"] == 0 and st["f_norm"] <= 1e-10
         lp = cont.last_prediction()
-        if k >= 22:  # after the training window (+3 history steps)
+        if k >= 22:  # after the training window (+4 history steps)
             assert np.isfinite(lp["f_learned"]) and np.isfinite(lp["f_secant"])
             gains.append(lp["f_secant"] / lp["f_learned"])
     assert np.isfinite(lp["train_loss"])
