@@ -267,7 +267,8 @@ int nosh_continuation_learning(nosh_continuation c, int train_steps,
                                int iters_per_step, double learning_rate);
 /* Predictor telemetry: which predictor the last advance used
  * (NOSH_PREDICT_*), the learned prediction's residual and the secant one's
- * (NaN when not evaluated), and the last training loss. */
+ * (NaN when not evaluated: the secant is only evaluated when the learned
+ * prediction misses the tolerance), and the last training loss. */
 int nosh_continuation_last_prediction(nosh_continuation c, int *used,
                                       double *f_learned, double *f_secant,
                                       double *train_loss);

@@ -330,7 +330,7 @@ __global__ void lanczos_first(int64_t n, const MinresScalars *__restrict__ s,
                               const C2<T> *__restrict__ r_cur, const T *__restrict__ dinv,
                               const T *__restrict__ coef, C2<T> *__restrict__ d, C2<T> *__restrict__ x) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || s->done >= 2) return;
   const T *la = lanczos_coef<T>(s);
   const T a = la[0], bb = la[1], c = la[2];
   const C2<T> ui = u[i], ro = r_old[i], rc = r_cur[i];
@@ -347,6 +347,7 @@ struct ChebOp {
   int step;
   const C2<T> *b, *xin;
   C2<T> *d, *xout;
+  const int *halt = nullptr;
   __device__ double finish(int i, T sr, T si) const {
     cheb_elem<T>(i, step, sr, si, dia, dinv, coef, b, xin, d, xout);
     return 0.0;
@@ -364,6 +365,7 @@ struct ChebMinresOp {
   const C2<T> *b, *xin;
   C2<T> *d, *xout;
   MinresScalars *s;
+  const int *halt = nullptr;
   __device__ double finish(int i, T sr, T si) const {
     const C2<T> z = cheb_elem<T>(i, step, sr, si, dia, dinv, coef, b, xin, d, xout);
     const C2<T> bi = b[i];
@@ -379,6 +381,7 @@ struct ResidOp {
   const T *dia;
   const C2<T> *b, *x;
   C2<T> *res;
+  const int *halt = nullptr;
   __device__ double finish(int i, T sr, T si) const {
     const C2<T> xi = x[i], bi = b[i];
     const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
@@ -390,9 +393,9 @@ struct ResidOp {
 template <typename T>
 __global__ void restrict_kernel(int64_t na, const int32_t *__restrict__ mptr,
                                 const int32_t *__restrict__ midx, const C2<T> *__restrict__ r,
-                                C2<T> *__restrict__ rc) {
+                                C2<T> *__restrict__ rc, const int *halt) {
   const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (a >= na) return;
+  if (a >= na || (halt && *halt >= 2)) return;
   T sr = 0, si = 0;
   for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
     const C2<T> v = r[midx[q]];
@@ -408,9 +411,9 @@ __global__ void restrict_first(int64_t na, const int32_t *__restrict__ mptr,
                                const int32_t *__restrict__ midx, const C2<T> *__restrict__ r,
                                C2<T> *__restrict__ rc, const T *__restrict__ dinv,
                                const T *__restrict__ coef, C2<T> *__restrict__ d,
-                               C2<T> *__restrict__ x) {
+                               C2<T> *__restrict__ x, const int *halt) {
   const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (a >= na) return;
+  if (a >= na || (halt && *halt >= 2)) return;
   T sr = 0, si = 0;
   for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
     const C2<T> v = r[midx[q]];
@@ -424,9 +427,9 @@ __global__ void restrict_first(int64_t na, const int32_t *__restrict__ mptr,
 
 template <typename T>
 __global__ void prolong_kernel(int64_t n, const int32_t *__restrict__ agg,
-                               const C2<T> *__restrict__ xc, C2<T> *__restrict__ x) {
+                               const C2<T> *__restrict__ xc, C2<T> *__restrict__ x, const int *halt) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || (halt && *halt >= 2)) return;
   const C2<T> c = xc[agg[i]];
   C2<T> v = x[i];
   v.x += c.x;
@@ -556,7 +559,8 @@ __device__ __forceinline__ void tail_row_sum(const LevelDesc<T> &A, int64_t i, c
 
 template <typename T>
 __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restrict__ lv, int lt, int L,
-                                                    int deg, const T *__restrict__ Ainv) {
+                                                    int deg, const T *__restrict__ Ainv, const int *halt) {
+  if (halt && *halt >= 2) return;
   const int tid = threadIdx.x, bs = blockDim.x;
   for (int l = lt; l < L - 1; l++) {
     const LevelDesc<T> A = lv[l];
@@ -712,6 +716,9 @@ struct Amg::Impl {
   template <typename T> const T *dense_inv();
   template <typename T, class Op> void rows(int l, const C2<T> *x, const Op &op);
   template <typename T> void descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *ms);
+  // the MINRES state's `done` while a MINRES V-cycle is being issued: its
+  // launches return at once once the solve has converged
+  const int *halt = nullptr;
   template <typename T> void prime();
 };
 
@@ -967,13 +974,13 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
   const double cheb_bytes = nls.spmv_bytes(2 * vb, 16 * vb);
   const double res_bytes = nls.spmv_bytes(2 * vb, 9 * vb);
   for (int k = 1; k < deg; k++) {
-    ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
+    ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, halt};
     if (tm) tm->begin(st);
     rows<T>(l, cur, op);
     if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
-  ResidOp<T> rop{dv, b, x, V.res[l].p};
+  ResidOp<T> rop{dv, b, x, V.res[l].p, halt};
   if (tm) tm->begin(st);
   rows<T>(l, x, rop);
   if (tm) tm->end(st, res_bytes);
@@ -984,27 +991,27 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     C2<T> *first = (deg % 2 == 1) ? V.x[l + 1].p : V.x2[l + 1].p;
     restrict_first<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
                                                       V.b[l + 1].p, V.dinv[l + 1].p, V.coef[l + 1].p,
-                                                      V.d[l + 1].p, first);
+                                                      V.d[l + 1].p, first, halt);
     ++nls.launch_count;
     descend_ascend<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p, nullptr);
   } else {
     restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
-                                                       V.b[l + 1].p);
+                                                       V.b[l + 1].p, halt);
     ++nls.launch_count;
-    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>());
+    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), halt);
     ++nls.launch_count;
   }
-  prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x);
+  prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x, halt);
   ++nls.launch_count;
   cur = x;
   oth = V.x2[l].p;
   for (int k = 0; k < deg; k++) {
     if (tm) tm->begin(st);
     if (ms && k == deg - 1) {
-      ChebMinresOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, ms};
+      ChebMinresOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, ms, halt};
       rows<T>(l, cur, op);
     } else {
-      ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth};
+      ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, halt};
       rows<T>(l, cur, op);
     }
     if (tm) tm->end(st, cheb_bytes);
@@ -1066,7 +1073,9 @@ void Amg::apply_minres(MinresScalars *ms, const T *u, T *r_old, const T *r_cur, 
                                                      (const C2<T> *)r_cur, V.dinv[0].p, V.coef[0].p,
                                                      V.d[0].p, first);
   ++I.nls.launch_count;
+  I.halt = &ms->done;
   I.descend_ascend<T>(0, (const C2<T> *)r_old, (C2<T> *)z_out, ms);
+  I.halt = nullptr;
   NOSH_CUDA(cudaGetLastError());
 }
 

@@ -124,21 +124,27 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   f_learned = std::nan("");
   f_secant = std::nan("");
   extrapolate(order, mu_new, ns.psi.p);
+  double f0 = -1.0;
   if (predictor == NOSH_PREDICT_LEARNED && net && net->trained() && count >= 4) {
-    // learned correction of the secant prediction; keep whichever starts
-    // Newton from the smaller residual (the secant is the fallback)
-    f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.f.p);
+    // learned correction of the secant prediction; a prediction that already
+    // meets the tolerance is taken as is, otherwise the one with the smaller
+    // residual starts Newton (the secant is the fallback)
     NOSH_CUDA(cudaMemcpyAsync(ns.tmp.p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
     const double *x[4] = {slot(0), slot(1), slot(2), slot(3)};
     const double m[4] = {mu_of(0), mu_of(1), mu_of(2), mu_of(3)};
     net->predict(x, m, mu_new, ns.tmp.p);
     f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
-    if (f_learned < f_secant) {
+    if (!(f_learned <= opt.tol)) f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.xc.p);
+    if (f_learned <= opt.tol || f_learned < f_secant) {
       std::swap(ns.psi, ns.tmp);
       last_used = NOSH_PREDICT_LEARNED;
+      f0 = f_learned;  // ns.f holds F of the learned prediction
+    } else {
+      std::swap(ns.f, ns.xc);
+      f0 = f_secant;
     }
   }
-  newton_core(s, ns, g, mu_new, opt, st);
+  newton_core(s, ns, g, mu_new, opt, st, f0);
   if (st.status != NOSH_OK) return;
   // push the converged state
   head = (head + 1) % kHist;

@@ -43,8 +43,16 @@ __device__ __forceinline__ const double *wx_coef<double>(const MinresScalars *s)
   return s->wx64;
 }
 
-// Lanczos coefficients once <z, J z> (zu) is known.  Single thread.
+// Lanczos coefficients once <z, J z> (zu) is known.  Single thread.  After
+// convergence (done == 1) the launch has applied the last deferred w/x
+// update, and the recurrence is frozen (done = 2): the remaining launches of
+// the chunk return at once.
 __device__ __forceinline__ void minres_lanczos_coefs(MinresScalars *s, double zu) {
+  if (s->done) {
+    s->done = 2;
+    s->wx_pending = 0;
+    return;
+  }
   s->zu = zu;
   const double beta = s->beta, alfa = zu / (beta * beta);
   const double c[3] = {1.0 / beta, s->itn > 0 ? beta / s->oldb : 0.0, alfa / beta};

@@ -68,10 +68,11 @@ struct Layout {
 };
 
 // ------------------------------------------------ tensor-core node GEMM
-// out[r, 0:64] = epilogue( [in0[r, 0:K0], in1[r, 0:K1]] @ W ), W stored as
+// out[r, 0:64] (=, +=) [in0[r, 0:K0], in1[r, 0:K1]] @ W, W stored as
 // Wt[64][K] BF16 (transposed, K = K0 + K1 <= 128, K0, K1 multiples of 16
-// or K1 = 0).  One warp per 16 rows, 4 warps per CTA.
-enum Epi { EPI_LINEAR = 0, EPI_BIAS_RELU = 1, EPI_RESID_RELU = 2, EPI_ACCUM = 3 };
+// or K1 = 0).  One warp per 16 rows, 4 warps per CTA.  Used by the backward
+// pass (the forward runs in the fused layer kernels below).
+enum Epi { EPI_LINEAR = 0, EPI_ACCUM = 1 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -91,8 +92,7 @@ template <int EPI>
 __global__ void __launch_bounds__(128) gemm64_kernel(int64_t n, const float *__restrict__ in0, int K0,
                                                      const float *__restrict__ in1, int K1,
                                                      const __nv_bfloat16 *__restrict__ Wt,
-                                                     const float *__restrict__ bias, float *__restrict__ out,
-                                                     float *__restrict__ out2) {
+                                                     float *__restrict__ out) {
   constexpr int KMAX = 128, LD = KMAX + 8;  // padded rows: conflict-free
   __shared__ __align__(16) __nv_bfloat16 sW[H * LD];
   const int K = K0 + K1;
@@ -135,20 +135,13 @@ __global__ void __launch_bounds__(128) gemm64_kernel(int64_t n, const float *__r
     for (int half = 0; half < 2; half++) {
       const int64_t r = half ? rb : ra;
       if (r >= n) continue;
-      float v0 = acc[t][2 * half], v1 = acc[t][2 * half + 1];
+      const float v0 = acc[t][2 * half], v1 = acc[t][2 * half + 1];
       float2 *o = reinterpret_cast<float2 *>(out + r * H + c);
       if (EPI == EPI_LINEAR) {
         *o = make_float2(v0, v1);
-      } else if (EPI == EPI_ACCUM) {
+      } else {
         const float2 p = *o;
         *o = make_float2(p.x + v0, p.y + v1);
-      } else if (EPI == EPI_BIAS_RELU) {
-        *o = make_float2(fmaxf(v0 + bias[c], 0.f), fmaxf(v1 + bias[c + 1], 0.f));
-      } else {  // residual: out2 = relu(acc + b) (kept for the backward pass), out += out2
-        const float u0 = fmaxf(v0 + bias[c], 0.f), u1 = fmaxf(v1 + bias[c + 1], 0.f);
-        *reinterpret_cast<float2 *>(out2 + r * H + c) = make_float2(u0, u1);
-        const float2 p = *o;
-        *o = make_float2(p.x + u0, p.y + u1);
       }
     }
   }
@@ -181,42 +174,325 @@ __global__ void to_bf16_rows(const float *__restrict__ W, int rows, int row0, __
   (void)rows;
 }
 
-// ----------------------------------------------------------- edge kernels
-// one warp per row i, 2 features per lane
-__global__ void edge_forward(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                             const float *__restrict__ ef, const float *__restrict__ A,
-                             const float *__restrict__ B, const float *__restrict__ Wc,
-                             const float *__restrict__ bm, float *__restrict__ M) {
-  const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (i >= n) return;
-  const int c = lane * 2;
-  float w[FE][2];
+// ------------------------------------------------- fused forward layers
+// A CTA of 4 warps owns tiles of 64 consecutive rows (16 per warp); each CTA
+// walks a contiguous range of tiles, so the neighbour rows a tile gathers
+// (mesh-ordered graphs: bands at fixed index offsets) are largely the rows
+// its previous tiles gathered.  Per tile and warp, the FP32 16 x 64 state
+// lives in registers in the mma accumulator layout: v[t][0..1] = row g,
+// columns 8t + 2q, 8t + 2q + 1; v[t][2..3] = the same columns of row g + 8
+// (g = lane / 4, q = lane % 4), which is also the A-operand layout of the
+// next m16n8k16 (k-step kk takes column tiles 2kk and 2kk + 1).
+constexpr int TILE = 64;
+constexpr int LDU = 2 * H + 8;  // smem row strides (BF16), padded: conflict-free fragment loads
+constexpr int LDAB = H + 8;
+constexpr int LDM = H + 8;
+constexpr int LDE = 16 + 8;
+constexpr size_t kLayerSmem = (size_t)(H * LDU + 2 * H * LDAB + 4 * 16 * LDM) * sizeof(__nv_bfloat16) +
+                              4 * H * sizeof(float);
+constexpr size_t kEncSmem = (size_t)(H * LDE + 2 * H * LDAB) * sizeof(__nv_bfloat16);
+
+__device__ __forceinline__ void frag_from_c(const float (&v)[8][4], int kk, uint32_t &a0, uint32_t &a1,
+                                            uint32_t &a2, uint32_t &a3) {
+  a0 = pack_bf16(v[2 * kk][0], v[2 * kk][1]);
+  a1 = pack_bf16(v[2 * kk][2], v[2 * kk][3]);
+  a2 = pack_bf16(v[2 * kk + 1][0], v[2 * kk + 1][1]);
+  a3 = pack_bf16(v[2 * kk + 1][2], v[2 * kk + 1][3]);
+}
+
+// BF16 [rows][K] (global, K a multiple of 8) -> smem rows of stride ld
+__device__ __forceinline__ void stage_w(__nv_bfloat16 *dst, const __nv_bfloat16 *__restrict__ src, int rows, int K,
+                                        int ld) {
+  const int per_row = K / 8;
+  for (int q = threadIdx.x; q < rows * per_row; q += blockDim.x) {
+    const int r = q / per_row, k = (q % per_row) * 8;
+    *reinterpret_cast<uint4 *>(dst + r * ld + k) = *reinterpret_cast<const uint4 *>(src + r * K + k);
+  }
+}
+
+// [A | B] = bf16(v) @ [W_a | W_b] for the warp's 16 rows; BF16 stores
+__device__ __forceinline__ void emit_ab(const float (&v)[8][4], const __nv_bfloat16 *sW, int64_t ra, int64_t rb,
+                                        int64_t n, __nv_bfloat16 *__restrict__ A, __nv_bfloat16 *__restrict__ B,
+                                        int g, int q) {
+#pragma unroll
+  for (int part = 0; part < 2; part++) {
+    float acc[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++) {
+      uint32_t a0, a1, a2, a3;
+      frag_from_c(v, kk, a0, a1, a2, a3);
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const __nv_bfloat16 *w = sW + (part * H + t * 8 + g) * LDAB + kk * 16 + q * 2;
+        mma_bf16(acc[t], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(w),
+                 *reinterpret_cast<const uint32_t *>(w + 8));
+      }
+    }
+    __nv_bfloat16 *dst = part ? B : A;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t * 8 + q * 2;
+      if (ra < n) *reinterpret_cast<__nv_bfloat162 *>(dst + ra * H + c) = __floats2bfloat162_rn(acc[t][0], acc[t][1]);
+      if (rb < n) *reinterpret_cast<__nv_bfloat162 *>(dst + rb * H + c) = __floats2bfloat162_rn(acc[t][2], acc[t][3]);
+    }
+  }
+}
+
+__device__ __forceinline__ void tile_range(int64_t tiles, int64_t &t0, int64_t &t1) {
+  t0 = tiles * blockIdx.x / gridDim.x;
+  t1 = tiles * (blockIdx.x + 1) / gridDim.x;
+}
+
+// h0 = relu(X W_enc + b_enc) (X: n x 10, K padded to 16 with zeros), then
+// layer 0's A, B
+__global__ void __launch_bounds__(128) encode_kernel(int64_t n, const float *__restrict__ X,
+                                                     const __nv_bfloat16 *__restrict__ We,
+                                                     const float *__restrict__ be,
+                                                     const __nv_bfloat16 *__restrict__ Wab, float *__restrict__ h,
+                                                     __nv_bfloat16 *__restrict__ A, __nv_bfloat16 *__restrict__ B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16 *sWe = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+  __nv_bfloat16 *sWab = sWe + H * LDE;
+  stage_w(sWe, We, H, 16, LDE);
+  stage_w(sWab, Wab, 2 * H, H, LDAB);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+  int64_t t0, t1;
+  tile_range((n + TILE - 1) / TILE, t0, t1);
+  for (int64_t tile = t0; tile < t1; tile++) {
+    const int64_t r0 = tile * TILE + warp * 16;
+    if (r0 >= n) continue;
+    const int64_t ra = r0 + g, rb = r0 + g + 8;
+    float2 x[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    // columns 2q, 2q + 1 (< 8) and 8 + 2q, 9 + 2q (only q = 0 is < FX = 10)
+    if (ra < n) {
+      x[0] = *reinterpret_cast<const float2 *>(X + ra * FX + 2 * q);
+      if (q == 0) x[2] = *reinterpret_cast<const float2 *>(X + ra * FX + 8);
+    }
+    if (rb < n) {
+      x[1] = *reinterpret_cast<const float2 *>(X + rb * FX + 2 * q);
+      if (q == 0) x[3] = *reinterpret_cast<const float2 *>(X + rb * FX + 8);
+    }
+    const uint32_t a0 = pack_bf16(x[0].x, x[0].y), a1 = pack_bf16(x[1].x, x[1].y);
+    const uint32_t a2 = pack_bf16(x[2].x, x[2].y), a3 = pack_bf16(x[3].x, x[3].y);
+    float v[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      v[t][0] = v[t][1] = v[t][2] = v[t][3] = 0.f;
+      const __nv_bfloat16 *w = sWe + (t * 8 + g) * LDE + q * 2;
+      mma_bf16(v[t], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(w),
+               *reinterpret_cast<const uint32_t *>(w + 8));
+    }
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t * 8 + q * 2;
+      const float b0 = be[c], b1 = be[c + 1];
+      v[t][0] = ra < n ? fmaxf(v[t][0] + b0, 0.f) : 0.f;
+      v[t][1] = ra < n ? fmaxf(v[t][1] + b1, 0.f) : 0.f;
+      v[t][2] = rb < n ? fmaxf(v[t][2] + b0, 0.f) : 0.f;
+      v[t][3] = rb < n ? fmaxf(v[t][3] + b1, 0.f) : 0.f;
+      if (ra < n) *reinterpret_cast<float2 *>(h + ra * H + c) = make_float2(v[t][0], v[t][1]);
+      if (rb < n) *reinterpret_cast<float2 *>(h + rb * H + c) = make_float2(v[t][2], v[t][3]);
+    }
+    emit_ab(v, sWab, ra, rb, n, A, B, g, q);
+  }
+}
+
+// One message-passing layer:
+//   M_i = sum_j relu(A_i + B_j + e_ij W_c + b_m)          (FP32 sums)
+//   R   = relu(bf16([h, M]) @ bf16(W_u) + b_u),  h' = h + R
+// then, for all but the last layer, the next layer's A, B from h'; the last
+// layer writes per-CTA column sums of h' (the mean-pool partials) instead of
+// h'.  TRAIN also stores M and R (FP32) for the backward pass.
+template <bool TRAIN, bool LAST>
+__global__ void __launch_bounds__(128, 3) mp_layer_kernel(
+    int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const float4 *__restrict__ ef,
+    const float *__restrict__ h, const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B,
+    const float *__restrict__ Wc, const float *__restrict__ bm, const __nv_bfloat16 *__restrict__ Wu,
+    const float *__restrict__ bu, const __nv_bfloat16 *__restrict__ Wab, float *__restrict__ h_out,
+    __nv_bfloat16 *__restrict__ A_out, __nv_bfloat16 *__restrict__ B_out, float *__restrict__ M_out,
+    float *__restrict__ R_out, float *__restrict__ pool) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16 *sWu = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+  __nv_bfloat16 *sWab = sWu + H * LDU;
+  __nv_bfloat16 *sM = sWab + 2 * H * LDAB;
+  float *sPool = reinterpret_cast<float *>(sM + 4 * 16 * LDM);
+  stage_w(sWu, Wu, H, 2 * H, LDU);
+  if (!LAST) stage_w(sWab, Wab, 2 * H, H, LDAB);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+  __nv_bfloat16 *sMw = sM + warp * 16 * LDM;
+  // aggregation: a half-warp per row, 4 channels per lane
+  const int hl = lane & 15, half = lane >> 4, c4 = hl * 4;
+  float wc[FE][4], bmv[4];
 #pragma unroll
   for (int f = 0; f < FE; f++) {
-    w[f][0] = Wc[f * H + c];
-    w[f][1] = Wc[f * H + c + 1];
+    const float4 w = *reinterpret_cast<const float4 *>(Wc + f * H + c4);
+    wc[f][0] = w.x; wc[f][1] = w.y; wc[f][2] = w.z; wc[f][3] = w.w;
   }
-  const float2 a = *reinterpret_cast<const float2 *>(A + i * H + c);
-  const float b0 = a.x + bm[c], b1 = a.y + bm[c + 1];
-  float m0 = 0.f, m1 = 0.f;
-  for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
-    const int32_t j = ci[k];
-    const float2 bj = *reinterpret_cast<const float2 *>(B + (int64_t)j * H + c);
-    const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)k * FE);
-    const float p0 = b0 + bj.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
-    const float p1 = b1 + bj.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
-    m0 += fmaxf(p0, 0.f);
-    m1 += fmaxf(p1, 0.f);
+  {
+    const float4 b = *reinterpret_cast<const float4 *>(bm + c4);
+    bmv[0] = b.x; bmv[1] = b.y; bmv[2] = b.z; bmv[3] = b.w;
   }
-  *reinterpret_cast<float2 *>(M + i * H + c) = make_float2(m0, m1);
+  float psum[8][2];
+#pragma unroll
+  for (int t = 0; t < 8; t++) psum[t][0] = psum[t][1] = 0.f;
+  int64_t t0, t1;
+  tile_range((n + TILE - 1) / TILE, t0, t1);
+  for (int64_t tile = t0; tile < t1; tile++) {
+    const int64_t r0 = tile * TILE + warp * 16;
+    if (r0 >= n) continue;
+    for (int p = 0; p < 8; p++) {
+      const int rr = 2 * p + half;
+      const int64_t r = r0 + rr;
+      int32_t beg = 0, deg = 0;
+      float m[4] = {0.f, 0.f, 0.f, 0.f}, a[4] = {0.f, 0.f, 0.f, 0.f};
+      if (r < n) {
+        beg = rp[r];
+        deg = rp[r + 1] - beg;
+        const uint2 av = *reinterpret_cast<const uint2 *>(A + r * H + c4);
+        const float2 a01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&av.x));
+        const float2 a23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&av.y));
+        a[0] = a01.x + bmv[0]; a[1] = a01.y + bmv[1]; a[2] = a23.x + bmv[2]; a[3] = a23.y + bmv[3];
+      }
+      const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+      for (int k0 = 0; k0 < maxdeg; k0 += 16) {
+        // each lane fetches one neighbour index and its edge features; the
+        // gathers below are unconditional (row 0 stands in for missing
+        // neighbours, masked out of the sum) so all 16 are in flight at once
+        const bool ok = k0 + hl < deg;
+        const int32_t jl = ok ? ci[beg + k0 + hl] : 0;
+        const float4 el = ok ? ef[beg + k0 + hl] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int cnt = deg - k0;  // this half's remaining neighbours (may be <= 0)
+        uint2 bv[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+          const int32_t j = __shfl_sync(0xffffffffu, jl, (half << 4) + u);
+          bv[u] = *reinterpret_cast<const uint2 *>(B + (int64_t)j * H + c4);
+        }
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+          const int src = (half << 4) + u;
+          const float ex = __shfl_sync(0xffffffffu, el.x, src), ey = __shfl_sync(0xffffffffu, el.y, src);
+          const float ez = __shfl_sync(0xffffffffu, el.z, src), ew = __shfl_sync(0xffffffffu, el.w, src);
+          const float2 b01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&bv[u].x));
+          const float2 b23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&bv[u].y));
+          const float bb[4] = {b01.x, b01.y, b23.x, b23.y};
+          const bool live = u < cnt;
+#pragma unroll
+          for (int cc = 0; cc < 4; cc++) {
+            const float pv = a[cc] + bb[cc] + ex * wc[0][cc] + ey * wc[1][cc] + ez * wc[2][cc] + ew * wc[3][cc];
+            m[cc] += live ? fmaxf(pv, 0.f) : 0.f;
+          }
+        }
+      }
+      uint2 mv;
+      *reinterpret_cast<__nv_bfloat162 *>(&mv.x) = __floats2bfloat162_rn(m[0], m[1]);
+      *reinterpret_cast<__nv_bfloat162 *>(&mv.y) = __floats2bfloat162_rn(m[2], m[3]);
+      *reinterpret_cast<uint2 *>(sMw + rr * LDM + c4) = mv;
+      if (TRAIN && r < n) *reinterpret_cast<float4 *>(M_out + r * H + c4) = make_float4(m[0], m[1], m[2], m[3]);
+    }
+    __syncwarp();
+    // update GEMM: K = 128 = [h (registers) | M (shared memory)]
+    const int64_t ra = r0 + g, rb = r0 + g + 8;
+    float v[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t * 8 + q * 2;
+      const float2 x0 = ra < n ? *reinterpret_cast<const float2 *>(h + ra * H + c) : make_float2(0.f, 0.f);
+      const float2 x1 = rb < n ? *reinterpret_cast<const float2 *>(h + rb * H + c) : make_float2(0.f, 0.f);
+      v[t][0] = x0.x; v[t][1] = x0.y; v[t][2] = x1.x; v[t][3] = x1.y;
+    }
+    float acc[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++) {
+      uint32_t a0, a1, a2, a3;
+      frag_from_c(v, kk, a0, a1, a2, a3);
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const __nv_bfloat16 *w = sWu + (t * 8 + g) * LDU + kk * 16 + q * 2;
+        mma_bf16(acc[t], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(w),
+                 *reinterpret_cast<const uint32_t *>(w + 8));
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++) {
+      const __nv_bfloat16 *mrow = sMw + kk * 16 + q * 2;
+      const uint32_t a0 = *reinterpret_cast<const uint32_t *>(mrow + g * LDM);
+      const uint32_t a1 = *reinterpret_cast<const uint32_t *>(mrow + (g + 8) * LDM);
+      const uint32_t a2 = *reinterpret_cast<const uint32_t *>(mrow + g * LDM + 8);
+      const uint32_t a3 = *reinterpret_cast<const uint32_t *>(mrow + (g + 8) * LDM + 8);
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const __nv_bfloat16 *w = sWu + (t * 8 + g) * LDU + H + kk * 16 + q * 2;
+        mma_bf16(acc[t], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(w),
+                 *reinterpret_cast<const uint32_t *>(w + 8));
+      }
+    }
+    __syncwarp();  // sMw is rewritten by the next tile
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t * 8 + q * 2;
+      const float b0 = bu[c], b1 = bu[c + 1];
+      const float u0 = fmaxf(acc[t][0] + b0, 0.f), u1 = fmaxf(acc[t][1] + b1, 0.f);
+      const float u2 = fmaxf(acc[t][2] + b0, 0.f), u3 = fmaxf(acc[t][3] + b1, 0.f);
+      v[t][0] = ra < n ? v[t][0] + u0 : 0.f;
+      v[t][1] = ra < n ? v[t][1] + u1 : 0.f;
+      v[t][2] = rb < n ? v[t][2] + u2 : 0.f;
+      v[t][3] = rb < n ? v[t][3] + u3 : 0.f;
+      if (TRAIN) {
+        if (ra < n) *reinterpret_cast<float2 *>(R_out + ra * H + c) = make_float2(u0, u1);
+        if (rb < n) *reinterpret_cast<float2 *>(R_out + rb * H + c) = make_float2(u2, u3);
+      }
+      if (!LAST) {
+        if (ra < n) *reinterpret_cast<float2 *>(h_out + ra * H + c) = make_float2(v[t][0], v[t][1]);
+        if (rb < n) *reinterpret_cast<float2 *>(h_out + rb * H + c) = make_float2(v[t][2], v[t][3]);
+      }
+    }
+    if (LAST) {
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        psum[t][0] += v[t][0] + v[t][2];
+        psum[t][1] += v[t][1] + v[t][3];
+      }
+    } else {
+      emit_ab(v, sWab, ra, rb, n, A_out, B_out, g, q);
+    }
+  }
+  if (LAST) {
+    // column sums over the lanes of equal q, then over the 4 warps
+#pragma unroll
+    for (int t = 0; t < 8; t++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        float x = psum[t][k];
+        x += __shfl_xor_sync(0xffffffffu, x, 4);
+        x += __shfl_xor_sync(0xffffffffu, x, 8);
+        x += __shfl_xor_sync(0xffffffffu, x, 16);
+        psum[t][k] = x;
+      }
+    if (g == 0)
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        sPool[warp * H + t * 8 + q * 2] = psum[t][0];
+        sPool[warp * H + t * 8 + q * 2 + 1] = psum[t][1];
+      }
+    __syncthreads();
+    if (threadIdx.x < H)
+      pool[(int64_t)blockIdx.x * H + threadIdx.x] =
+          (sPool[threadIdx.x] + sPool[H + threadIdx.x]) + (sPool[2 * H + threadIdx.x] + sPool[3 * H + threadIdx.x]);
+  }
 }
 
 // dA_i = sum_j dM_i [P_ij > 0]; also block partials of dW_c (4 x 64) and
 // db_m (64): rows of the partial buffer hold 5 x 64 floats per CTA
 __global__ void edge_backward_a(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                                const float *__restrict__ ef, const float *__restrict__ A,
-                                const float *__restrict__ B, const float *__restrict__ Wc,
+                                const float *__restrict__ ef, const __nv_bfloat16 *__restrict__ A,
+                                const __nv_bfloat16 *__restrict__ B, const float *__restrict__ Wc,
                                 const float *__restrict__ bm, const float *__restrict__ dM,
                                 float *__restrict__ dA, float *__restrict__ part) {
   __shared__ float red[8][5][H];  // 8 warps per CTA, 8 rows per warp
@@ -232,13 +508,13 @@ __global__ void edge_backward_a(int64_t n, const int32_t *__restrict__ rp, const
       w[f][0] = Wc[f * H + c];
       w[f][1] = Wc[f * H + c + 1];
     }
-    const float2 a = *reinterpret_cast<const float2 *>(A + i * H + c);
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(A + i * H + c));
     const float2 dm = *reinterpret_cast<const float2 *>(dM + i * H + c);
     const float b0 = a.x + bm[c], b1 = a.y + bm[c + 1];
     float s0 = 0.f, s1 = 0.f;
     for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
       const int32_t j = ci[k];
-      const float2 bj = *reinterpret_cast<const float2 *>(B + (int64_t)j * H + c);
+      const float2 bj = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(B + (int64_t)j * H + c));
       const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)k * FE);
       const float p0 = b0 + bj.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
       const float p1 = b1 + bj.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
@@ -270,7 +546,7 @@ __global__ void edge_backward_a(int64_t n, const int32_t *__restrict__ rp, const
 // of the symmetric graph lists those i; tr[k] is the position of (i, j)
 __global__ void edge_backward_b(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                                 const int32_t *__restrict__ tr, const float *__restrict__ ef,
-                                const float *__restrict__ A, const float *__restrict__ B,
+                                const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B,
                                 const float *__restrict__ Wc, const float *__restrict__ bm,
                                 const float *__restrict__ dM, float *__restrict__ dB) {
   const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -283,12 +559,12 @@ __global__ void edge_backward_b(int64_t n, const int32_t *__restrict__ rp, const
     w[f][0] = Wc[f * H + c];
     w[f][1] = Wc[f * H + c + 1];
   }
-  const float2 bj = *reinterpret_cast<const float2 *>(B + j * H + c);
+  const float2 bj = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(B + j * H + c));
   const float c0 = bj.x + bm[c], c1 = bj.y + bm[c + 1];
   float s0 = 0.f, s1 = 0.f;
   for (int32_t k = rp[j]; k < rp[j + 1]; k++) {
     const int32_t i = ci[k];
-    const float2 ai = *reinterpret_cast<const float2 *>(A + (int64_t)i * H + c);
+    const float2 ai = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(A + (int64_t)i * H + c));
     const float2 dm = *reinterpret_cast<const float2 *>(dM + (int64_t)i * H + c);
     const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)tr[k] * FE);
     const float p0 = c0 + ai.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
@@ -506,32 +782,29 @@ __global__ void combine_kernel(int64_t n, const double *__restrict__ w, const do
 }
 
 // ------------------------------------------------------------- readout
-// column sums of h (n x 64): one partial row of 64 per CTA
-__global__ void pool_partial(int64_t n, const float *__restrict__ h, float *__restrict__ part) {
-  __shared__ float s[4][H];
-  const int c = threadIdx.x & 63, rgrp = threadIdx.x >> 6;  // 256 threads: 4 row groups
-  float a = 0.f;
-  for (int64_t r = (int64_t)blockIdx.x * 4 + rgrp; r < n; r += (int64_t)gridDim.x * 4) a += h[r * H + c];
-  s[rgrp][c] = a;
-  __syncthreads();
-  if (threadIdx.x < H) part[(int64_t)blockIdx.x * H + c] = (s[0][c] + s[1][c]) + (s[2][c] + s[3][c]);
-}
-
-// z = sum of the partials / n; (w_q, w_c) = relu(z W1 + b1) W2 + b2.  With
-// a Gram vector: loss (relative state error) and the backward pass of the
-// readout into grad, dz into dz.  One CTA of 64 threads.
+// z = sum of the pool partials / n; (w_q, w_c) = relu(z W1 + b1) W2 + b2.
+// With a Gram vector: loss (relative state error) and the backward pass of
+// the readout into grad, dz into dz.  One CTA of 256 threads.
 __global__ void readout(int nparts, int64_t n, const float *__restrict__ part, const float *__restrict__ P,
                         int64_t o_w1, int64_t o_b1, int64_t o_w2, int64_t o_b2, double *__restrict__ wout,
                         const double *__restrict__ gram, float *__restrict__ grad, float *__restrict__ dz,
                         double *__restrict__ loss) {
-  __shared__ float z[H], h1[RH], dh1[RH];
+  __shared__ float z[H], zs[4][H], h1[RH], dh1[RH];
   __shared__ double w[2], dw[2];
   const int t = threadIdx.x;
   {
-    float a = 0.f;
-    for (int b = 0; b < nparts; b++) a += part[(int64_t)b * H + t];
-    z[t] = a / (float)n;
+    const int c = t & (H - 1), grp = t / H;  // 4 groups of 64 channels
+    float a0 = 0.f, a1 = 0.f;
+    int b = grp;
+    for (; b + 4 < nparts; b += 8) {
+      a0 += part[(int64_t)b * H + c];
+      a1 += part[(int64_t)(b + 4) * H + c];
+    }
+    for (; b < nparts; b += 4) a0 += part[(int64_t)b * H + c];
+    zs[grp][c] = a0 + a1;
   }
+  __syncthreads();
+  if (t < H) z[t] = ((zs[0][t] + zs[1][t]) + (zs[2][t] + zs[3][t])) / (float)n;
   __syncthreads();
   if (t < RH) {
     float a = P[o_b1 + t];
@@ -569,9 +842,11 @@ __global__ void readout(int nparts, int64_t n, const float *__restrict__ part, c
   // W1, b1 gradients and dz
   for (int q = t; q < H * RH; q += blockDim.x) grad[o_w1 + q] = z[q / RH] * dh1[q % RH];
   if (t < RH) grad[o_b1 + t] = dh1[t];
-  float a = 0.f;
-  for (int k = 0; k < RH; k++) a += dh1[k] * P[o_w1 + t * RH + k];
-  dz[t] = a;
+  if (t < H) {
+    float a = 0.f;
+    for (int k = 0; k < RH; k++) a += dh1[k] * P[o_w1 + t * RH + k];
+    dz[t] = a;
+  }
 }
 
 // dh[i][c] = dz[c] / n (gradient of the mean pool)
@@ -613,6 +888,16 @@ __global__ void edge_setup(int64_t nnz, const int32_t *__restrict__ nz_edge, con
 
 inline int vgrid(int64_t n) { return (int)std::min<int64_t>(div_up(n, 256), kNumSMs * 8); }
 
+// resident CTAs of a 128-thread kernel on the whole device, capped by the
+// number of tiles
+int persistent_grid(const void *kernel, size_t smem, int64_t tiles) {
+  int d = 0, sms = 0, per_sm = 0;
+  NOSH_CUDA(cudaGetDevice(&d));
+  NOSH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d));
+  NOSH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)std::max(per_sm, 1) * sms));
+}
+
 // splitmix64 for deterministic initialisation
 inline uint64_t sm64(uint64_t &s) {
   uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
@@ -637,19 +922,19 @@ struct Mpnn::Impl {
   DevBuf<__nv_bfloat16> wt;
   int64_t wt_enc, wt_a[LAYERS], wt_b[LAYERS], wt_u[LAYERS], wtb_a[LAYERS], wtb_b[LAYERS], wtb_uh[LAYERS],
       wtb_um[LAYERS];
-  // activations and gradients
-  DevBuf<float> X, Xp, Hs[LAYERS + 1], A[LAYERS], B[LAYERS], Mg[LAYERS], R[LAYERS];
+  // activations (A, B in BF16: the message operands) and gradients
+  DevBuf<float> X, Hs[LAYERS], Mg[LAYERS], R[LAYERS];
+  DevBuf<__nv_bfloat16> A[LAYERS], B[LAYERS];
   DevBuf<float> dH, dR, dM, dA, dB, dz;
   DevBuf<float> part, pool;
-  int pool_blocks = 0;
+  int enc_grid = 0, layer_grid = 0;
   DevBuf<double> sq, red, dots, Ls, gram, w, loss;
   explicit Impl(NlsImpl &nls);
   void refresh_bf16();
-  void forward();                         // X -> H -> w
+  void forward(bool train);               // X -> pooled embedding
   double backward_and_step(float lr);     // needs gram
   void features(const double *const x[4], const double mu[4], double mu_t, const double *target);
-  void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, const float *bias,
-            float *out, float *out2);
+  void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, float *out);
   void wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol, int64_t dst,
              int64_t bias_dst);
   void readout_launch(bool train);
@@ -714,10 +999,8 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
   wt.alloc(o);
   wt.zero(st);
   X.alloc(N * FX);
-  Xp.alloc(N * 16);
-  Xp.zero(st);
-  for (auto &b : Hs) b.alloc(N * H);
   for (int l = 0; l < LAYERS; l++) {
+    Hs[l].alloc(N * H);
     A[l].alloc(N * H);
     B[l].alloc(N * H);
     Mg[l].alloc(N * H);
@@ -726,8 +1009,13 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
   for (DevBuf<float> *b : {&dH, &dR, &dM, &dA, &dB}) b->alloc(N * H);
   dz.alloc(H);
   part.alloc(std::max<int64_t>(div_up(N, WG_ROWS) * (2 * H + 1) * H, div_up(N, 64) * 5 * H) + 64);
-  pool_blocks = (int)std::min<int64_t>(div_up(N, 4), 1024);
-  pool.alloc((int64_t)pool_blocks * H);
+  const int64_t tiles = div_up(N, (int64_t)TILE);
+  enc_grid = persistent_grid((const void *)encode_kernel, kEncSmem, tiles);
+  layer_grid = persistent_grid((const void *)mp_layer_kernel<true, true>, kLayerSmem, tiles);
+  for (const void *k : {(const void *)mp_layer_kernel<false, false>, (const void *)mp_layer_kernel<false, true>,
+                        (const void *)mp_layer_kernel<true, false>})
+    layer_grid = std::min(layer_grid, persistent_grid(k, kLayerSmem, tiles));
+  pool.alloc((int64_t)layer_grid * H);
   sq.alloc(6 * N);
   red.alloc(8);
   dots.alloc(8);
@@ -743,7 +1031,7 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
 void Mpnn::Impl::refresh_bf16() {
   cudaStream_t st = s.stream;
   const float *P = params.p;
-  // encoder: K = 10 features padded to 16 (the padded columns of Xp are 0)
+  // encoder: K = 10 features padded to 16 (zero weights in the padding)
   enc_to_bf16<<<div_up(H * 16, 256), 256, 0, st>>>(P + L.enc_w, wt.p + wt_enc);
   for (int l = 0; l < LAYERS; l++) {
     to_bf16_t<<<div_up(H * H, 256), 256, 0, st>>>(P + L.wa[l], H, H, 0, wt.p + wt_a[l]);
@@ -759,43 +1047,41 @@ void Mpnn::Impl::refresh_bf16() {
   NOSH_CUDA(cudaGetLastError());
 }
 
-void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off,
-                      const float *bias, float *out, float *out2) {
+void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, float *out) {
   const int grid = div_up(N, 64);
   cudaStream_t st = s.stream;
   const __nv_bfloat16 *W = wt.p + wt_off;
   switch (epi) {
-    case EPI_LINEAR: gemm64_kernel<EPI_LINEAR><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
-    case EPI_BIAS_RELU: gemm64_kernel<EPI_BIAS_RELU><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
-    case EPI_RESID_RELU: gemm64_kernel<EPI_RESID_RELU><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
-    default: gemm64_kernel<EPI_ACCUM><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, bias, out, out2); break;
+    case EPI_LINEAR: gemm64_kernel<EPI_LINEAR><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, out); break;
+    default: gemm64_kernel<EPI_ACCUM><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, out); break;
   }
   ++s.launch_count;
 }
 
 void Mpnn::Impl::readout_launch(bool train) {
   cudaStream_t st = s.stream;
-  pool_partial<<<pool_blocks, 256, 0, st>>>(N, Hs[LAYERS].p, pool.p);
-  readout<<<1, H, 0, st>>>(pool_blocks, N, pool.p, params.p, L.r1_w, L.r1_b, L.r2_w, L.r2_b, w.p,
-                           train ? gram.p : nullptr, grads.p, dz.p, loss.p);
-  s.launch_count += 2;
+  readout<<<1, 4 * H, 0, st>>>(layer_grid, N, pool.p, params.p, L.r1_w, L.r1_b, L.r2_w, L.r2_b, w.p,
+                               train ? gram.p : nullptr, grads.p, dz.p, loss.p);
+  ++s.launch_count;
 }
 
-void Mpnn::Impl::forward() {
+void Mpnn::Impl::forward(bool train) {
   cudaStream_t st = s.stream;
   const float *P = params.p;
   MeshImpl &m = *s.mesh;
-  NOSH_CUDA(cudaMemcpy2DAsync(Xp.p, 16 * sizeof(float), X.p, FX * sizeof(float), FX * sizeof(float), N,
-                              cudaMemcpyDeviceToDevice, st));
-  gemm(EPI_BIAS_RELU, Xp.p, 16, nullptr, 0, wt_enc, P + L.enc_b, Hs[0].p, nullptr);
+  const float4 *ef4 = reinterpret_cast<const float4 *>(ef.p);
+  encode_kernel<<<enc_grid, 128, kEncSmem, st>>>(N, X.p, wt.p + wt_enc, P + L.enc_b, wt.p + wt_a[0], Hs[0].p,
+                                                 A[0].p, B[0].p);
+  ++s.launch_count;
   for (int l = 0; l < LAYERS; l++) {
-    gemm(EPI_LINEAR, Hs[l].p, H, nullptr, 0, wt_a[l], nullptr, A[l].p, nullptr);
-    gemm(EPI_LINEAR, Hs[l].p, H, nullptr, 0, wt_b[l], nullptr, B[l].p, nullptr);
-    edge_forward<<<div_up(N * 32, 256), 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l],
-                                                     P + L.bm[l], Mg[l].p);
+    const bool last = l == LAYERS - 1;
+    auto kernel = train ? (last ? mp_layer_kernel<true, true> : mp_layer_kernel<true, false>)
+                        : (last ? mp_layer_kernel<false, true> : mp_layer_kernel<false, false>);
+    kernel<<<layer_grid, 128, kLayerSmem, st>>>(
+        N, m.d_rp.p, m.d_ci.p, ef4, Hs[l].p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l], wt.p + wt_u[l],
+        P + L.bu[l], last ? nullptr : wt.p + wt_a[l + 1], last ? nullptr : Hs[l + 1].p,
+        last ? nullptr : A[l + 1].p, last ? nullptr : B[l + 1].p, Mg[l].p, R[l].p, pool.p);
     ++s.launch_count;
-    NOSH_CUDA(cudaMemcpyAsync(Hs[l + 1].p, Hs[l].p, N * H * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    gemm(EPI_RESID_RELU, Hs[l].p, H, Mg[l].p, H, wt_u[l], P + L.bu[l], Hs[l + 1].p, R[l].p);
   }
   NOSH_CUDA(cudaGetLastError());
 }
@@ -824,8 +1110,8 @@ double Mpnn::Impl::backward_and_step(float lr) {
     ++s.launch_count;
     wgrad(Hs[l].p, H, Mg[l].p, H, dR.p, H, L.wu[l], L.bu[l]);
     // dM = dR W_u[64:128]^T ; dh += dR W_u[0:64]^T (dh holds the residual path)
-    gemm(EPI_LINEAR, dR.p, H, nullptr, 0, wtb_um[l], nullptr, dM.p, nullptr);
-    gemm(EPI_ACCUM, dR.p, H, nullptr, 0, wtb_uh[l], nullptr, dH.p, nullptr);
+    gemm(EPI_LINEAR, dR.p, H, nullptr, 0, wtb_um[l], dM.p);
+    gemm(EPI_ACCUM, dR.p, H, nullptr, 0, wtb_uh[l], dH.p);
     const int nb = div_up(N, 64);
     edge_backward_a<<<nb, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l],
                                         dM.p, dA.p, part.p);
@@ -836,8 +1122,8 @@ double Mpnn::Impl::backward_and_step(float lr) {
     // A = h W_a, B = h W_b
     wgrad(Hs[l].p, H, nullptr, 0, dA.p, H, L.wa[l], -1);
     wgrad(Hs[l].p, H, nullptr, 0, dB.p, H, L.wb[l], -1);
-    gemm(EPI_ACCUM, dA.p, H, nullptr, 0, wtb_a[l], nullptr, dH.p, nullptr);
-    gemm(EPI_ACCUM, dB.p, H, nullptr, 0, wtb_b[l], nullptr, dH.p, nullptr);
+    gemm(EPI_ACCUM, dA.p, H, nullptr, 0, wtb_a[l], dH.p);
+    gemm(EPI_ACCUM, dB.p, H, nullptr, 0, wtb_b[l], dH.p);
   }
   // encoder: h0 = relu(X W + b)
   relu_mask<<<div_up(N * H, 256), 256, 0, st>>>(N * H, Hs[0].p, dH.p, dR.p);
@@ -910,7 +1196,7 @@ Mpnn::~Mpnn() = default;
 void Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, double *out) {
   Impl &I = *impl;
   I.features(x, mu, mu_new, nullptr);
-  I.forward();
+  I.forward(false);
   I.readout_launch(false);
   combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (C2<double> *)out);
   ++I.s.launch_count;
@@ -923,7 +1209,7 @@ double Mpnn::train(const double *const x[4], const double mu[4], const double *t
   I.features(x, mu, mu_t, target);
   double l = std::nan("");
   for (int k = 0; k < iters; k++) {
-    I.forward();
+    I.forward(true);
     l = I.backward_and_step((float)lr);
   }
   return l;
@@ -947,7 +1233,7 @@ void Mpnn::get_edge_features(float *h) const {
 void Mpnn::forward_features(const float *X, double *w) {
   Impl &I = *impl;
   I.X.upload(X, I.N * FX, I.s.stream);
-  I.forward();
+  I.forward(false);
   I.readout_launch(false);
   I.w.download(w, 2, I.s.stream);
   I.s.sync();
@@ -956,7 +1242,7 @@ double Mpnn::loss_and_grad(const float *X, const double *gram, float *grad) {
   Impl &I = *impl;
   I.X.upload(X, I.N * FX, I.s.stream);
   I.gram.upload(gram, 6, I.s.stream);
-  I.forward();
+  I.forward(true);
   const double l = I.backward_and_step(0.f);  // gradient only, no step
   I.grads.download(grad, I.L.total, I.s.stream);
   I.s.sync();

@@ -78,6 +78,7 @@ struct JacMinresOp {
   T *wa;
   const T *wb, *wc;
   T *xsol;
+  const int *halt;  // &s->done
   __device__ double finish(int i, T sr, T si) const {
     const C2<T> xi = x[i];
     const T d0r = d[3 * i], d0i = d[3 * i + 1], d1b = d[3 * i + 2];
@@ -158,7 +159,7 @@ void Minres<T>::iteration(int j) {
   const int cap = sizeof(T) == 4 ? s.cap32 : s.cap64;
   const C2<T> *val = sizeof(T) == 4 ? (const C2<T> *)s.d_keo32.p : (const C2<T> *)s.d_keo64.p;
   const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
-  JacMinresOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, d, zn, wa, wb, wc, x.p};
+  JacMinresOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, d, zn, wa, wb, wc, x.p, &d->done};
   s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
   const size_t smem = (size_t)cap * (4 + sizeof(C2<T>));
   row_block_apply<T, JacMinresOp<T>><<<row_grid((const void *)row_block_apply<T, JacMinresOp<T>>, smem, s.N),
@@ -372,9 +373,9 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
 }
 
 void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
-                 nosh_newton_stats &st) {
+                 nosh_newton_stats &st, double f0) {
   st = nosh_newton_stats{};
-  st.f_norm0 = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+  st.f_norm0 = f0 >= 0.0 ? f0 : residual_norm(s, ns.psi.p, g, mu, ns.f.p);
   st.f_norm = st.f_norm0;
   NOSH_CHECK(!std::isnan(st.f_norm0), NOSH_ERR_NAN, "initial residual is NaN");
   if (opt.precision == NOSH_PREC_FP64) newton_loop<double>(s, ns, g, mu, opt, st);

@@ -44,9 +44,10 @@ struct NewtonState {
 NewtonState &state_of(NlsImpl &s);
 // ||F(psi)||_2 (writes F into f; synchronises)
 double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f);
-// Newton on state_of(s).psi in place
+// Newton on state_of(s).psi in place.  With f0 >= 0, ns.f already holds
+// F(psi) and f0 is its norm (no re-evaluation).
 void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
-                 nosh_newton_stats &st);
+                 nosh_newton_stats &st, double f0 = -1.0);
 
 void newton_solve(NlsImpl &s, double *x_user, double g, double mu,
                   const nosh_newton_options &opt, nosh_newton_stats &st);

@@ -9,6 +9,8 @@
 // staging capacity reads them directly.
 #pragma once
 
+#include <utility>
+
 #include <type_traits>
 
 #include "common.cuh"
@@ -88,12 +90,32 @@ __device__ __forceinline__ typename std::enable_if<HasHook<Op>::value>::type run
 template <class Op>
 __device__ __forceinline__ typename std::enable_if<!HasHook<Op>::value>::type run_hook(const Op &,
                                                                                       double) {}
+// An Op may also carry `const int *halt`: when it points at a value >= 2
+// the whole launch returns at once (MINRES iterations of a captured chunk
+// that follow convergence).
+template <class Op, class = void>
+struct HasHalt {
+  static constexpr bool value = false;
+};
+template <class Op>
+struct HasHalt<Op, decltype((void)std::declval<Op>().halt, void())> {
+  static constexpr bool value = true;
+};
+template <class Op>
+__device__ __forceinline__ bool halted(const Op &op) {
+  if constexpr (HasHalt<Op>::value) {
+    return op.halt != nullptr && *op.halt >= 2;
+  } else {
+    return false;
+  }
+}
 template <typename T, class Op>
 __global__ void __launch_bounds__(kRows)
     row_block_apply(int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                     const C2<T> *__restrict__ val, const C2<T> *__restrict__ x, int cap,
                     Op op, double *partials, unsigned *counter, double *red_out) {
   using A = typename Acc<T>::type;
+  if (halted(op)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int32_t *s_col = reinterpret_cast<int32_t *>(smem_raw);
   C2<T> *s_val = reinterpret_cast<C2<T> *>(smem_raw + (size_t)cap * sizeof(int32_t));
