@@ -12,11 +12,14 @@ AMG-preconditioned MINRES, in the mixed FP32 (operators, Krylov, AMG) / FP64
 
 The headline ("value") uses the learned predictor: a message-passing network
 trained online during the first --train-steps steps (untimed, part of the
-warm-up) that combines phase-aligned history extrapolants; it falls back to
-the secant whenever its prediction has the larger residual.  The plain
-predictor (the reference's secant) is timed on the same workload
-("plain_predictor"), and the 3-point polynomial predictor as an ablation
-("quadratic_predictor").
+warm-up) that sets the weight of the cubic-minus-quadratic extrapolation
+field; it falls back to the secant whenever its prediction has the larger
+residual.  Under it the Newton steps aim at --refine (1e-12), so the stored
+states feed the 4-point extrapolants; a step whose prediction already meets
+||F|| <= 1e-10 takes no Newton iteration.  Also timed on the same workload:
+the plain predictor (the reference's secant, mixed precision:
+"plain_predictor"), the plain FP64 GPU path ("plain_fp64") and the
+polynomial predictors as ablations ("ablations").
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
 
@@ -54,7 +57,9 @@ def parse():
     ap.add_argument("--mu0", type=float, default=0.5)
     ap.add_argument("--dmu", type=float, default=0.005)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--predictor", default="learned", choices=["learned", "secant", "quadratic", "none"])
+    ap.add_argument("--predictor", default="learned", choices=["learned", "secant", "quadratic", "cubic", "none"])
+    ap.add_argument("--refine", type=float, default=1e-12,
+                    help="residual the Newton steps aim at under the learned and cubic predictors")
     ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
     ap.add_argument("--train-iters", type=int, default=40, help="optimiser iterations per training step")
     ap.add_argument("--lr", type=float, default=2e-3)
@@ -266,10 +271,11 @@ def run_gb300(args):
     st = model.newton(x0, {"mu": args.mu0})
     assert st["status"] == 0, st
 
-    preds = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC, "learned": ng.PREDICT_LEARNED,
-             "none": ng.PREDICT_NONE}
+    preds = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC, "cubic": ng.PREDICT_CUBIC,
+             "learned": ng.PREDICT_LEARNED, "none": ng.PREDICT_NONE}
+    refine_of = {"learned": args.refine, "cubic": args.refine}
 
-    def run(pred_name, steps, warmup, profile=False, e2e=False):
+    def run(pred_name, steps, warmup, profile=False, e2e=False, precision=None):
         """A continuation handle from x0; `warmup` untimed steps (for the
         learned predictor: its online-training window first), then `steps`
         steps timed with CUDA events on the library stream, L2 flushed before
@@ -277,13 +283,14 @@ def run_gb300(args):
         memory inside the timed region."""
         cont = ng.continuation(model, x0, args.mu0)
         pred = preds[pred_name]
+        refine = refine_of.get(pred_name, 0.0)
         mu = args.mu0
         if pred == ng.PREDICT_LEARNED:
             cont.learning(args.train_steps, args.train_iters, args.lr)
             warmup = warmup + args.train_steps + 4
         for _ in range(warmup):
             mu += args.dmu
-            s = cont.advance(mu, predictor=pred)
+            s = cont.advance(mu, predictor=pred, refine=refine, precision=precision)
             assert s["status"] == 0, s
         if profile:
             model.profile(True)
@@ -299,7 +306,7 @@ def run_gb300(args):
             mu += args.dmu
             t0 = time.perf_counter()
             ev[k][0].record(stream)
-            s = cont.advance(mu, predictor=pred)
+            s = cont.advance(mu, predictor=pred, refine=refine, precision=precision)
             if e2e:
                 cont.state(host)
             ev[k][1].record(stream)
@@ -312,6 +319,7 @@ def run_gb300(args):
                "launches": model.profile_read(ng.KERNEL_ALL)[0],
                "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
                "learned_used": int(sum(1 for u in used if u == ng.PREDICT_LEARNED)),
+               "zero_newton_steps": int(sum(1 for a, b in its if a == 0)),
                "train_loss": cont.last_prediction()["train_loss"]}
         if profile:
             out["jac"] = model.profile_read(ng.KERNEL_JACOBIAN)
@@ -330,7 +338,9 @@ def run_gb300(args):
     clocks.start()
     plain = run("secant", args.steps, args.warmup)
     head = run(args.predictor, args.steps, args.warmup) if args.predictor != "secant" else plain
-    quad = run("quadratic", args.steps, args.warmup) if args.predictor != "quadratic" else head
+    ablations = {name: run(name, args.steps, args.warmup) for name in ("quadratic", "cubic")
+                 if name != args.predictor}
+    fp64 = run("secant", args.steps, args.warmup, precision=ng.PREC_FP64)
     clk = clocks.stop()
     ms = maxrank(head["ms"])
     value = world * 1000.0 / ms
@@ -387,10 +397,17 @@ def run_gb300(args):
                                     "parallelism": f"replicas x{world}"},
         "plain_predictor": {"predictor": "secant", "value": world * 1000.0 / plain_ms, "ms_per_step": plain_ms,
                             "newton_krylov_per_step": plain["newton_krylov_per_step"]},
-        "quadratic_predictor": {"predictor": "quadratic", "value": world * 1000.0 / maxrank(quad["ms"]),
-                                "ms_per_step": maxrank(quad["ms"]),
-                                "newton_krylov_per_step": quad["newton_krylov_per_step"]},
+        "plain_fp64": {"predictor": "secant", "precision": "fp64", "value": world * 1000.0 / maxrank(fp64["ms"]),
+                       "ms_per_step": maxrank(fp64["ms"]),
+                       "newton_krylov_per_step": fp64["newton_krylov_per_step"]},
+        "ablations": {name: {"value": world * 1000.0 / maxrank(r["ms"]), "ms_per_step": maxrank(r["ms"]),
+                             "refine": refine_of.get(name, 0.0),
+                             "newton_krylov_per_step": r["newton_krylov_per_step"],
+                             "zero_newton_steps": r["zero_newton_steps"]} for name, r in ablations.items()},
         "learned_vs_plain": plain_ms / ms,
+        "learned_mixed_vs_plain_fp64": maxrank(fp64["ms"]) / ms,
+        "refine": refine_of.get(args.predictor, 0.0),
+        "zero_newton_steps": head["zero_newton_steps"],
         "newton_krylov_per_step": head["newton_krylov_per_step"],
         "learned_used_steps": head["learned_used"],
         "train_loss": head["train_loss"],

@@ -200,6 +200,11 @@ typedef struct {
   int max_krylov;         /* per linear solve; default 1000 (conf.xml:127)*/
   int precision;          /* NOSH_PREC_*                                  */
   int verbose;            /* 0 = silent                                   */
+  double refine;          /* residual norm the Eisenstat-Walker forcing
+                             aims the Newton steps at (<= tol; 0 = tol).
+                             Converged states well below tol make
+                             high-order continuation predictors exact to
+                             their truncation error; default 0            */
 } nosh_newton_options;
 
 typedef struct {
@@ -228,6 +233,7 @@ int nosh_newton_solve(nosh_nls nls, double *x, const double *p,
 #define NOSH_PREDICT_LEARNED 4   /* edge message-passing network on top of the
                                     secant, trained online; falls back to the
                                     secant when its residual is larger       */
+#define NOSH_PREDICT_CUBIC 5     /* 4-point polynomial extrapolation       */
 
 /* One natural-parameter continuation step (LOCA stepper semantics,
  * examples/conf.xml:35-75; driven by executables/nosh-cont/nosh-cont.cpp:
@@ -275,14 +281,14 @@ int nosh_continuation_last_prediction(nosh_continuation c, int *used,
 
 /* The learned predictor's network, for inspection and gradient checks (the
  * continuation handle owns its own instance).  From the four newest states
- * it predicts two global coefficients (w_q, w_c) and the prediction is
- * secant + w_q q + w_c c, q = quadratic - secant and c = cubic - quadratic
- * extrapolation.  Parameters are one flat FP32 vector: encoder W [10x64]
- * (row-major), b [64]; per layer l = 0..2: W_a [64x64], W_b [64x64],
- * W_c [4x64], b_m [64], W_u [128x64], b_u [64]; readout W_1 [64x32],
- * b_1 [32], W_2 [32x2], b_2 [2].  Node features are N x 10, edge features
- * 2E x 4 in the order of the off-diagonal KEO graph (the complex graph of
- * nosh_mesh_complex_graph without its diagonal). */
+ * it predicts one global coefficient w and the prediction is
+ * quadratic + w c, c = cubic - quadratic extrapolation (w = 1 is the cubic
+ * extrapolation, where the readout starts).  Parameters are one flat FP32
+ * vector: encoder W [10x64] (row-major), b [64]; per layer l = 0..2:
+ * W_a [64x64], W_b [64x64], W_c [4x64], b_m [64], W_u [128x64], b_u [64];
+ * readout W_1 [64x32], b_1 [32], W_2 [32x1], b_2 [1].  Node features are
+ * N x 10, edge features 2E x 4 in the order of the off-diagonal KEO graph
+ * (the complex graph of nosh_mesh_complex_graph without its diagonal). */
 typedef struct nosh_mpnn_s *nosh_mpnn;
 int nosh_mpnn_create(nosh_nls nls, nosh_mpnn *out);
 int nosh_mpnn_destroy(nosh_mpnn net);
@@ -290,12 +296,11 @@ int nosh_mpnn_num_params(nosh_mpnn net, int64_t *n);
 /* copies the parameters out (get != NULL) and/or in (set != NULL) */
 int nosh_mpnn_params(nosh_mpnn net, float *get, const float *set);
 int nosh_mpnn_edge_features(nosh_mpnn net, float *ef);
-/* the readout coefficients w[2] = (w_q, w_c) for node features X (N x 10) */
+/* the readout coefficient *w for node features X (N x 10) */
 int nosh_mpnn_forward(nosh_mpnn net, const float *X, double *w);
-/* the training loss (w^T G w - 2 w.b + dd) / qq for the cv-weighted Gram
- * scalars gram = [qq, qc, cc, qd, cd, dd] of (q, c, d = target - secant),
- * G = [[qq, qc], [qc, cc]], b = (qd, cd), and its parameter gradient; the
- * parameters are not changed */
+/* the training loss (w^2 cc - 2 w cd + dd) / dd for the cv-weighted Gram
+ * scalars gram = [cc, cd, dd] of c and d = target - quadratic, and its
+ * parameter gradient; the parameters are not changed */
 int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const double *gram,
                         double *loss, float *grad);
 

@@ -44,7 +44,7 @@ ERR_INVALID, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN = 1, 2, 3, 4, 5
 ERR_UNSUPPORTED, ERR_MESH, ERR_NO_MEMORY = 6, 7, 8
 PREC_FP64, PREC_MIXED = 0, 1
 NO_TRANS, TRANS = 0, 1
-PREDICT_NONE, PREDICT_SECANT, PREDICT_TANGENT, PREDICT_QUADRATIC, PREDICT_LEARNED = 0, 1, 2, 3, 4
+PREDICT_NONE, PREDICT_SECANT, PREDICT_TANGENT, PREDICT_QUADRATIC, PREDICT_LEARNED, PREDICT_CUBIC = 0, 1, 2, 3, 4, 5
 KERNEL_JACOBIAN, KERNEL_SMOOTHER, KERNEL_ALL = 0, 1, 2
 
 
@@ -62,6 +62,7 @@ class NewtonOptions(C.Structure):
         ("max_krylov", C.c_int),
         ("precision", C.c_int),
         ("verbose", C.c_int),
+        ("refine", C.c_double),
     ]
 
 
@@ -391,10 +392,11 @@ class nls:
         return n.value, ms.value, b.value
 
     # -- solvers
-    def _options(self, tol, max_newton, forcing, max_krylov, precision, verbose):
+    def _options(self, tol, max_newton, forcing, max_krylov, precision, verbose, refine=0.0):
         o = NewtonOptions()
         _lib.nosh_newton_default_options(C.byref(o))
         o.tol, o.max_newton, o.forcing, o.max_krylov = tol, max_newton, forcing, max_krylov
+        o.refine = refine
         o.precision = self.precision if precision is None else precision
         o.verbose = verbose
         return o
@@ -452,8 +454,11 @@ class continuation:
             self._h = None
 
     def advance(self, mu_new, predictor=PREDICT_SECANT, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000,
-                precision=None, verbose=0):
-        o = self.model._options(tol, max_newton, forcing, max_krylov, precision, verbose)
+                precision=None, verbose=0, refine=0.0):
+        """One step to ``mu_new``; ``refine`` (<= tol) is the residual the
+        Newton steps aim at, so that the stored states serve high-order
+        predictors."""
+        o = self.model._options(tol, max_newton, forcing, max_krylov, precision, verbose, refine)
         st = NewtonStats()
         rc = _lib.nosh_continuation_advance(self._h, mu_new, predictor, C.byref(o), C.byref(st))
         _check(rc, allow=(ERR_NOT_CONVERGED,))
@@ -507,15 +512,15 @@ class mpnn:
         return out
 
     def forward(self, X):
-        """The readout coefficients (w_q, w_c) for node features X (N x 10)."""
+        """The readout coefficient w for node features X (N x 10)."""
         X = np.ascontiguousarray(X, np.float32)
-        w = np.empty(2, np.float64)
-        _check(_lib.nosh_mpnn_forward(self._h, _ptr(X), _ptr(w)))
-        return w
+        w = C.c_double()
+        _check(_lib.nosh_mpnn_forward(self._h, _ptr(X), C.byref(w)))
+        return w.value
 
     def loss_grad(self, X, gram):
         """Training loss and parameter gradient for node features X and the
-        cv-weighted Gram scalars [qq, qc, cc, qd, cd, dd]."""
+        cv-weighted Gram scalars [cc, cd, dd]."""
         X = np.ascontiguousarray(X, np.float32)
         gram = np.ascontiguousarray(gram, np.float64)
         g = np.empty(self.num_params, np.float32)

@@ -670,8 +670,7 @@ int staging_cap_of(const std::vector<int32_t> &rp, int64_t n) {
     mx = std::max<int64_t>(mx, rp[r1] - (rp[r0] & ~(int64_t)3));
   }
   mx = (mx + 3) & ~(int64_t)3;
-  const int64_t limit = (96 * 1024) / (sizeof(int32_t) + sizeof(C2<T>));
-  return (int)std::min<int64_t>(mx, limit & ~(int64_t)3);
+  return (int)std::min<int64_t>(mx, stage_limit<T>());
 }
 
 }  // namespace
@@ -947,7 +946,7 @@ template <typename T, class Op>
 void Amg::Impl::rows(int l, const C2<T> *x, const Op &op) {
   const AmgLevel &A = lev[l];
   const int cap = sizeof(T) == 4 ? A.cap32 : A.cap64;
-  const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
+  const size_t smem = 2 * stage_bytes<T>(cap);
   row_block_apply<T, Op><<<row_grid((const void *)row_block_apply<T, Op>, smem, A.n), kRows, smem,
                             nls.stream>>>(
       (int)A.n, A.rp, A.ci, off<T>(l), x, cap, op, nls.red.partials.p, nls.red.counter.p,

@@ -509,6 +509,7 @@ void nosh_newton_default_options(nosh_newton_options *opt) {
   opt->max_krylov = 1000;
   opt->precision = NOSH_PREC_MIXED;
   opt->verbose = 0;
+  opt->refine = 0.0;
 }
 
 int nosh_newton_solve(nosh_nls nls, double *x, const double *p, const nosh_newton_options *opt,
@@ -521,7 +522,8 @@ int nosh_newton_solve(nosh_nls nls, double *x, const double *p, const nosh_newto
     nosh_newton_options o;
     nosh_newton_default_options(&o);
     if (opt) o = *opt;
-    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0, "bad solver options");
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0 && o.refine >= 0 && o.refine <= o.tol,
+            "bad solver options");
     require(x != nullptr, "null state");
     nosh::newton_solve(s, x, g, mu, o, st);
   });
@@ -544,7 +546,8 @@ int nosh_continuation_step(nosh_nls nls, double *x, double *x_prev, const double
     nosh_newton_options o;
     nosh_newton_default_options(&o);
     if (opt) o = *opt;
-    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0, "bad solver options");
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0 && o.refine >= 0 && o.refine <= o.tol,
+            "bad solver options");
     nosh::continuation_step(s, x, x_prev, g, mu, mu_cur, mu_prev, predictor, o, st);
   });
   if (rc == NOSH_OK) rc = st.status;
@@ -584,7 +587,8 @@ int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
     nosh_newton_options o;
     nosh_newton_default_options(&o);
     if (opt) o = *opt;
-    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0, "bad solver options");
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0 && o.refine >= 0 && o.refine <= o.tol,
+            "bad solver options");
     c->impl->advance(mu_new, predictor, o, st);
   });
   if (rc == NOSH_OK) rc = st.status;

@@ -34,28 +34,24 @@ __device__ __forceinline__ void unit_phase(const double *c, double &er, double &
   ei = m > 0 ? c[1] / m : 0.0;
 }
 
-// out = L0 x0 + L1 e^{i phi1} x1 + L2 e^{i phi2} x2, the phases aligning x1
-// and x2 with x0 (solutions are defined up to a global U(1) phase)
+// out = sum_k L_k e^{i phi_k} x_k (k <= order), the phases aligning x_k with
+// x0 (solutions are defined up to a global U(1) phase)
 __global__ void extrapolate_kernel(int64_t n, int order, const double *__restrict__ c, double L0, double L1,
-                                   double L2, const C2<double> *__restrict__ x0,
+                                   double L2, double L3, const C2<double> *__restrict__ x0,
                                    const C2<double> *__restrict__ x1, const C2<double> *__restrict__ x2,
-                                   C2<double> *__restrict__ out) {
-  double e1r = 1.0, e1i = 0.0, e2r = 1.0, e2i = 0.0;
-  if (order >= 1) unit_phase(c, e1r, e1i);
-  if (order >= 2) unit_phase(c + 2, e2r, e2i);
+                                   const C2<double> *__restrict__ x3, C2<double> *__restrict__ out) {
+  double er[3] = {1.0, 1.0, 1.0}, ei[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < order; k++) unit_phase(c + 2 * k, er[k], ei[k]);
+  const double L[3] = {L1, L2, L3};
+  const C2<double> *xs[3] = {x1, x2, x3};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const C2<double> a = x0[i];
     double r = L0 * a.x, im = L0 * a.y;
-    if (order >= 1) {
-      const C2<double> p = x1[i];
-      r += L1 * (e1r * p.x - e1i * p.y);
-      im += L1 * (e1r * p.y + e1i * p.x);
-    }
-    if (order >= 2) {
-      const C2<double> p = x2[i];
-      r += L2 * (e2r * p.x - e2i * p.y);
-      im += L2 * (e2r * p.y + e2i * p.x);
+    for (int k = 0; k < order; k++) {
+      const C2<double> p = xs[k][i];
+      r += L[k] * (er[k] * p.x - ei[k] * p.y);
+      im += L[k] * (er[k] * p.y + ei[k] * p.x);
     }
     out[i] = C2<double>{r, im};
   }
@@ -80,30 +76,24 @@ ContinuationImpl::~ContinuationImpl() = default;
 // phase-aligned Lagrange extrapolation of the newest (order+1) states to mu_new
 void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
   cudaStream_t st = s.stream;
-  const double *x0 = slot(0), *x1 = order >= 1 ? slot(1) : slot(0), *x2 = order >= 2 ? slot(2) : slot(0);
-  const double t = mu_new, t0 = mu_of(0), t1 = order >= 1 ? mu_of(1) : 0.0, t2 = order >= 2 ? mu_of(2) : 0.0;
-  double L0 = 1.0, L1 = 0.0, L2 = 0.0;
-  if (order == 1) {
-    L0 = (t - t1) / (t0 - t1);
-    L1 = (t - t0) / (t1 - t0);
-  } else if (order == 2) {
-    L0 = (t - t1) * (t - t2) / ((t0 - t1) * (t0 - t2));
-    L1 = (t - t0) * (t - t2) / ((t1 - t0) * (t1 - t2));
-    L2 = (t - t0) * (t - t1) / ((t2 - t0) * (t2 - t1));
+  double L[4] = {1.0, 0.0, 0.0, 0.0};
+  for (int k = 0; k <= order; k++) {
+    double v = 1.0;
+    for (int q = 0; q <= order; q++)
+      if (q != k) v *= (mu_new - mu_of(q)) / (mu_of(k) - mu_of(q));
+    L[k] = v;
   }
   const int G = vgrid(s.N);
-  if (order >= 1) {
-    cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)x1, (const C2<double> *)x0, s.red.partials.p,
-                                    s.red.counter.p, dots.p);
+  for (int k = 1; k <= order; k++) {
+    cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)slot(k), (const C2<double> *)slot(0),
+                                    s.red.partials.p, s.red.counter.p, dots.p + 2 * (k - 1));
     ++s.launch_count;
   }
-  if (order >= 2) {
-    cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)x2, (const C2<double> *)x0, s.red.partials.p,
-                                    s.red.counter.p, dots.p + 2);
-    ++s.launch_count;
-  }
-  extrapolate_kernel<<<G, 256, 0, st>>>(s.N, order, dots.p, L0, L1, L2, (const C2<double> *)x0,
-                                        (const C2<double> *)x1, (const C2<double> *)x2, (C2<double> *)out);
+  const double *x1 = order >= 1 ? slot(1) : slot(0), *x2 = order >= 2 ? slot(2) : slot(0),
+               *x3 = order >= 3 ? slot(3) : slot(0);
+  extrapolate_kernel<<<G, 256, 0, st>>>(s.N, order, dots.p, L[0], L[1], L[2], L[3], (const C2<double> *)slot(0),
+                                        (const C2<double> *)x1, (const C2<double> *)x2, (const C2<double> *)x3,
+                                        (C2<double> *)out);
   ++s.launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
@@ -111,21 +101,24 @@ void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
 void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_options &opt,
                                nosh_newton_stats &st) {
   NOSH_CHECK(predictor == NOSH_PREDICT_NONE || predictor == NOSH_PREDICT_SECANT ||
-                 predictor == NOSH_PREDICT_QUADRATIC || predictor == NOSH_PREDICT_LEARNED,
-             NOSH_ERR_INVALID, "continuation handles predict NONE, SECANT, QUADRATIC or LEARNED");
+                 predictor == NOSH_PREDICT_QUADRATIC || predictor == NOSH_PREDICT_CUBIC ||
+                 predictor == NOSH_PREDICT_LEARNED,
+             NOSH_ERR_INVALID, "continuation handles predict NONE, SECANT, QUADRATIC, CUBIC or LEARNED");
   NOSH_CHECK(mu_new != mu_of(0), NOSH_ERR_INVALID, "mu_new equals the current mu");
   NewtonState &ns = state_of(s);
   const double g = s.g0;
   int order = 0;
   if (predictor == NOSH_PREDICT_SECANT || predictor == NOSH_PREDICT_LEARNED) order = 1;
   if (predictor == NOSH_PREDICT_QUADRATIC) order = 2;
+  if (predictor == NOSH_PREDICT_CUBIC) order = 3;
   order = std::min(order, count - 1);
-  last_used = order == 0 ? NOSH_PREDICT_NONE : (order == 1 ? NOSH_PREDICT_SECANT : NOSH_PREDICT_QUADRATIC);
+  const int used_of[4] = {NOSH_PREDICT_NONE, NOSH_PREDICT_SECANT, NOSH_PREDICT_QUADRATIC, NOSH_PREDICT_CUBIC};
+  last_used = used_of[order];
   f_learned = std::nan("");
   f_secant = std::nan("");
   extrapolate(order, mu_new, ns.psi.p);
   double f0 = -1.0;
-  if (predictor == NOSH_PREDICT_LEARNED && net && net->trained() && count >= 4) {
+  if (predictor == NOSH_PREDICT_LEARNED && net && count >= 4) {
     // learned correction of the secant prediction; a prediction that already
     // meets the tolerance is taken as is, otherwise the one with the smaller
     // residual starts Newton (the secant is the fallback)
@@ -158,7 +151,6 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
     const double m[4] = {mu_of(1), mu_of(2), mu_of(3), mu_of(4)};
     train_loss = net->train(x, m, slot(0), mu_of(0), iters_per_step, learning_rate);
     train_left--;
-    if (train_left == 0) net->set_trained(true);
   }
   s.sync();
 }
@@ -168,7 +160,6 @@ void ContinuationImpl::enable_learning(int train_steps, int iters, double lr) {
   train_left = train_steps;
   iters_per_step = iters;
   learning_rate = lr;
-  net->set_trained(train_steps == 0);
 }
 
 }  // namespace nosh

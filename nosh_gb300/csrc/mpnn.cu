@@ -12,13 +12,15 @@
 //   layer: A = h W_a, B = h W_b,
 //          M_i = sum_j relu(A_i + B_j + e_ij W_c + b_m),
 //          h  <- h + relu([h, M] W_u + b_u)
-//   z     = mean_i h_i; (w_q, w_c) = relu(z W_r1 + b_r1) W_r2 + b_r2
-//   prediction = secant + w_q q + w_c c
-// The readout is global: the correction is a combination of smooth
-// history-difference fields, so node-level rounding noise (which the KEO
-// amplifies) never enters the predicted state.  The loss is the
-// cv-weighted squared state error relative to |q|^2, exact from six Gram
-// scalars of the fields.
+//   z     = mean_i h_i; w = relu(z W_r1 + b_r1) W_r2 + b_r2   (a scalar)
+//   prediction = quadratic + w c  (w = 0: quadratic, w = 1: cubic
+//   extrapolation; the readout starts near the cubic)
+// The readout is global: the correction is a multiple of a smooth
+// history-difference field, so node-level rounding noise (which the KEO
+// amplifies) never enters the predicted state, and an error in w is scaled
+// by |c|, the difference of two extrapolants.  The loss is the cv-weighted
+// squared error of the prediction relative to the quadratic's, exact from
+// three Gram scalars.
 // Node GEMMs run on the tensor cores with BF16 operands and FP32
 // accumulation (mma.sync m16n8k16); edge aggregation, weight gradients and
 // the optimiser are FP32.  Every reduction is deterministic (block partials
@@ -61,8 +63,8 @@ struct Layout {
     }
     r1_w = o; o += H * RH;
     r1_b = o; o += RH;
-    r2_w = o; o += RH * 2;
-    r2_b = o; o += 2;
+    r2_w = o; o += RH;
+    r2_b = o; o += 1;
     total = o;
   }
 };
@@ -741,8 +743,8 @@ __global__ void features_b(int64_t n, const double *__restrict__ red, double mu_
   }
 }
 
-// cv-weighted Gram scalars of (q, c, d) with d = e_t x_t - secant:
-// g = [<q,q>, <q,c>, <c,c>, <q,d>, <c,d>, <d,d>]
+// cv-weighted Gram scalars of c and d = e_t x_t - quadratic (the quadratic
+// prediction's error): g = [<c,c>, <c,d>, <d,d>]
 __global__ void gram_kernel(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
                             const C2<double> *__restrict__ x0, const C2<double> *__restrict__ x1,
                             const C2<double> *__restrict__ xt, const double *__restrict__ cv,
@@ -750,47 +752,44 @@ __global__ void gram_kernel(int64_t n, const double *__restrict__ dots, const do
   double e1r, e1i, etr, eti;
   phases(dots, 0, e1r, e1i);
   phases(dots, 3, etr, eti);
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  double acc[3] = {0, 0, 0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const C2<double> a = x0[i], p = x1[i], t = xt[i];
     const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
-    const double secr = Ls[0] * a.x + Ls[1] * pr, seci = Ls[0] * a.y + Ls[1] * pi;
-    const double dr = etr * t.x - eti * t.y - secr, di = etr * t.y + eti * t.x - seci;
     const double *f = sq + 6 * i;
+    const double qr = Ls[0] * a.x + Ls[1] * pr + f[2], qi = Ls[0] * a.y + Ls[1] * pi + f[3];
+    const double dr = etr * t.x - eti * t.y - qr, di = etr * t.y + eti * t.x - qi;
     const double w = cv[i];
-    acc[0] += w * (f[2] * f[2] + f[3] * f[3]);
-    acc[1] += w * (f[2] * f[4] + f[3] * f[5]);
-    acc[2] += w * (f[4] * f[4] + f[5] * f[5]);
-    acc[3] += w * (f[2] * dr + f[3] * di);
-    acc[4] += w * (f[4] * dr + f[5] * di);
-    acc[5] += w * (dr * dr + di * di);
+    acc[0] += w * (f[4] * f[4] + f[5] * f[5]);
+    acc[1] += w * (f[4] * dr + f[5] * di);
+    acc[2] += w * (dr * dr + di * di);
   }
-  for (int k = 0; k < 6; k++) grid_reduce(acc[k], partials + k * gridDim.x, counter + k, g + k);
+  for (int k = 0; k < 3; k++) grid_reduce(acc[k], partials + k * gridDim.x, counter + k, g + k);
 }
 
-// out (the secant prediction) += w_q q + w_c c
+// out (the secant prediction) += q + w c
 __global__ void combine_kernel(int64_t n, const double *__restrict__ w, const double *__restrict__ sq,
                                C2<double> *__restrict__ out) {
-  const double wq = w[0], wc = w[1];
+  const double wc = w[0];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double *f = sq + 6 * i;
     C2<double> o = out[i];
-    o.x += wq * f[2] + wc * f[4];
-    o.y += wq * f[3] + wc * f[5];
+    o.x += f[2] + wc * f[4];
+    o.y += f[3] + wc * f[5];
     out[i] = o;
   }
 }
 
 // ------------------------------------------------------------- readout
-// z = sum of the pool partials / n; (w_q, w_c) = relu(z W1 + b1) W2 + b2.
-// With a Gram vector: loss (relative state error) and the backward pass of
-// the readout into grad, dz into dz.  One CTA of 256 threads.
+// z = sum of the pool partials / n; w = relu(z W1 + b1) W2 + b2.  With a
+// Gram vector [cc, cd, dd]: the loss (w^2 cc - 2 w cd + dd) / dd, the
+// backward pass of the readout into grad and dz.  One CTA of 256 threads.
 __global__ void readout(int nparts, int64_t n, const float *__restrict__ part, const float *__restrict__ P,
                         int64_t o_w1, int64_t o_b1, int64_t o_w2, int64_t o_b2, double *__restrict__ wout,
                         const double *__restrict__ gram, float *__restrict__ grad, float *__restrict__ dz,
                         double *__restrict__ loss) {
   __shared__ float z[H], zs[4][H], h1[RH], dh1[RH];
-  __shared__ double w[2], dw[2];
+  __shared__ double w, dw;
   const int t = threadIdx.x;
   {
     const int c = t & (H - 1), grp = t / H;  // 4 groups of 64 channels
@@ -812,32 +811,26 @@ __global__ void readout(int nparts, int64_t n, const float *__restrict__ part, c
     h1[t] = fmaxf(a, 0.f);
   }
   __syncthreads();
-  if (t < 2) {
-    double a = P[o_b2 + t];
-    for (int k = 0; k < RH; k++) a += (double)h1[k] * P[o_w2 + k * 2 + t];
-    w[t] = a;
-    wout[t] = a;
+  if (t == 0) {
+    double a = P[o_b2];
+    for (int k = 0; k < RH; k++) a += (double)h1[k] * P[o_w2 + k];
+    w = a;
+    *wout = a;
+    if (gram) {
+      const double dd = gram[2] > 0 ? gram[2] : 1.0;
+      *loss = (a * a * gram[0] - 2 * a * gram[1] + gram[2]) / dd;
+      dw = 2 * (a * gram[0] - gram[1]) / dd;
+    }
   }
   __syncthreads();
   if (!gram) return;
-  // loss = (w^T G w - 2 w.b + dd) / qq with G = [[qq, qc], [qc, cc]]
-  if (t == 0) {
-    const double qq = gram[0] > 0 ? gram[0] : 1.0;
-    const double L = (w[0] * w[0] * gram[0] + 2 * w[0] * w[1] * gram[1] + w[1] * w[1] * gram[2] -
-                      2 * w[0] * gram[3] - 2 * w[1] * gram[4] + gram[5]) / qq;
-    *loss = L;
-    dw[0] = 2 * (w[0] * gram[0] + w[1] * gram[1] - gram[3]) / qq;
-    dw[1] = 2 * (w[0] * gram[1] + w[1] * gram[2] - gram[4]) / qq;
-  }
-  __syncthreads();
   if (t < RH) {
     // W2, b2 gradients and dh1
-    grad[o_w2 + t * 2] = (float)(h1[t] * dw[0]);
-    grad[o_w2 + t * 2 + 1] = (float)(h1[t] * dw[1]);
-    const float g = (float)(dw[0] * P[o_w2 + t * 2] + dw[1] * P[o_w2 + t * 2 + 1]);
+    grad[o_w2 + t] = (float)(h1[t] * dw);
+    const float g = (float)(dw * P[o_w2 + t]);
     dh1[t] = h1[t] > 0.f ? g : 0.f;
   }
-  if (t < 2) grad[o_b2 + t] = (float)dw[t];
+  if (t == 0) grad[o_b2] = (float)dw;
   __syncthreads();
   // W1, b1 gradients and dz
   for (int q = t; q < H * RH; q += blockDim.x) grad[o_w1 + q] = z[q / RH] * dh1[q % RH];
@@ -962,7 +955,8 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
                                                s.d_p.p, m.d_len.p, ia, ip, il, ef.p, tr.p);
   NOSH_CUDA(cudaGetLastError());
   // parameters: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero
-  // biases; the readout starts at zero output (secant prediction)
+  // biases; the readout starts near w = (1, 1), the cubic extrapolation
+  // (the Lagrange combination of the four states), with small weights
   std::vector<float> h(L.total, 0.f);
   uint64_t seed = 0x6e6f7368ULL;
   auto fill = [&](int64_t off, int64_t count, int fan_in, float scale) {
@@ -977,7 +971,8 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
     fill(L.wu[l], 2 * H * H, 2 * H, 1.f);
   }
   fill(L.r1_w, H * RH, H, 1.f);
-  fill(L.r2_w, RH * 2, RH, 0.1f);
+  fill(L.r2_w, RH, RH, 0.01f);
+  h[L.r2_b] = 1.f;
   params.upload(h, st);
   grads.alloc(L.total);
   grads.zero(st);
@@ -1020,8 +1015,8 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
   red.alloc(8);
   dots.alloc(8);
   Ls.alloc(9);
-  gram.alloc(6);
-  w.alloc(2);
+  gram.alloc(3);
+  w.alloc(1);
   w.zero(st);
   loss.alloc(1);
   refresh_bf16();
@@ -1235,13 +1230,13 @@ void Mpnn::forward_features(const float *X, double *w) {
   I.X.upload(X, I.N * FX, I.s.stream);
   I.forward(false);
   I.readout_launch(false);
-  I.w.download(w, 2, I.s.stream);
+  I.w.download(w, 1, I.s.stream);
   I.s.sync();
 }
 double Mpnn::loss_and_grad(const float *X, const double *gram, float *grad) {
   Impl &I = *impl;
   I.X.upload(X, I.N * FX, I.s.stream);
-  I.gram.upload(gram, 6, I.s.stream);
+  I.gram.upload(gram, 3, I.s.stream);
   I.forward(true);
   const double l = I.backward_and_step(0.f);  // gradient only, no step
   I.grads.download(grad, I.L.total, I.s.stream);

@@ -9,10 +9,9 @@ namespace nosh {
 struct Mpnn {
   explicit Mpnn(NlsImpl &s);
   ~Mpnn();
-  bool trained() const { return trained_; }
-  void set_trained(bool t) { trained_ = t; }
-  // out (in: the secant prediction to mu_new) += learned combination of the
-  // history-difference fields, from the newest states x[0..3] at mu[0..3]
+  // out (in: the secant prediction to mu_new) += q + w c, the learned
+  // multiple of the cubic-minus-quadratic field, from the newest states
+  // x[0..3] at mu[0..3]
   void predict(const double *const x[4], const double mu[4], double mu_new, double *out);
   // optimiser iterations on the transition x[0..3] -> target at mu_t;
   // returns the last relative loss
@@ -20,9 +19,9 @@ struct Mpnn {
                double lr);
 
   // inspection (gradient checks): flat FP32 parameters, per-nonzero edge
-  // features (adjacency-CSR order), the readout coefficients for given node
+  // features (adjacency-CSR order), the readout coefficient for given node
   // features, and loss + parameter gradient for given features and Gram
-  // scalars [<q,q>, <q,c>, <c,c>, <q,d>, <c,d>, <d,d>]
+  // scalars [<c,c>, <c,d>, <d,d>]
   int64_t num_params() const;
   void get_params(float *h) const;
   void set_params(const float *h);
@@ -32,9 +31,6 @@ struct Mpnn {
 
   struct Impl;
   std::unique_ptr<Impl> impl;
-
- private:
-  bool trained_ = false;
 };
 
 }  // namespace nosh

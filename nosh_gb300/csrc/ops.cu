@@ -226,14 +226,13 @@ int staging_cap(const MeshImpl &m) {
     mx = std::max<int64_t>(mx, m.rp[r1] - (m.rp[r0] & ~(int64_t)3));
   }
   mx = (mx + 3) & ~(int64_t)3;
-  const int64_t limit = (96 * 1024) / (sizeof(int32_t) + sizeof(C2<T>));
-  return (int)std::min<int64_t>(mx, limit & ~(int64_t)3);
+  return (int)std::min<int64_t>(mx, stage_limit<T>());
 }
 
 template <typename T, class Op>
 void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &op, int cap,
                  double *red_out) {
-  const size_t smem = (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
+  const size_t smem = 2 * stage_bytes<T>(cap);
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
     NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>,

@@ -132,7 +132,7 @@ Minres<T>::Minres(NlsImpl &nls) : s(nls), n2(2 * nls.N) {
   for (DevBuf<T> *b : {&r[0], &r[1], &z[0], &z[1], &w[0], &w[1], &w[2], &u, &x}) b->alloc(n2);
   sc.alloc(1);
   NOSH_CUDA(cudaMallocHost(&h_sc, sizeof(MinresScalars)));
-  NOSH_CUDA(cudaMallocHost(&h_err, sizeof(int)));
+  NOSH_CUDA(cudaMallocHost(&h_err, 2 * sizeof(int)));
   NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, JacMinresOp<T>>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
 }
@@ -161,7 +161,7 @@ void Minres<T>::iteration(int j) {
   const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
   JacMinresOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, d, zn, wa, wb, wc, x.p, &d->done};
   s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
-  const size_t smem = (size_t)cap * (4 + sizeof(C2<T>));
+  const size_t smem = 2 * stage_bytes<T>(cap);
   row_block_apply<T, JacMinresOp<T>><<<row_grid((const void *)row_block_apply<T, JacMinresOp<T>>, smem, s.N),
                                        kRows, smem, st>>>(
       (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, (const C2<T> *)zc, cap, op, s.red.partials.p,
@@ -222,11 +222,14 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     NOSH_CUDA(cudaGetLastError());
     NOSH_CUDA(cudaMemcpyAsync(h_sc, d, sizeof(MinresScalars), cudaMemcpyDeviceToHost, st));
     NOSH_CUDA(cudaMemcpyAsync(h_err, s.amg->error_flag_ptr(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    NOSH_CUDA(cudaMemcpyAsync(h_err + 1, s.red.counter.p + kStageErrorSlot, sizeof(int), cudaMemcpyDeviceToHost,
+                              st));
     NOSH_CUDA(cudaStreamSynchronize(st));
     if (h_sc->done || it >= maxit + kChunk) break;
   }
   if (h_sc->wx_pending) wx_final();  // converged on the chunk's last step
-  NOSH_CHECK(*h_err == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
+  NOSH_CHECK(h_err[1] == 0, NOSH_ERR_CUDA, "an SpMV staging copy did not complete");
+  NOSH_CHECK(h_err[0] == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
   status = h_sc->flag;
   rel_res = h_sc->beta1 > 0 ? h_sc->phibar / h_sc->beta1 : 0.0;
   return h_sc->itn;
@@ -343,9 +346,10 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
       eta = opt.forcing;
     } else {
       // Eisenstat-Walker choice 2 (gamma 0.9, alpha 2), safeguarded, and no
-      // tighter than needed to reach the target in one step
+      // tighter than needed to reach the target (refine, else tol) in one step
+      const double target = opt.refine > 0.0 ? opt.refine : opt.tol;
       const double ew = it == 0 ? 1e-2 : 0.9 * (fn / fn_prev) * (fn / fn_prev);
-      eta = std::min(0.1, std::max(ew, 0.5 * opt.tol / fn));
+      eta = std::min(0.1, std::max(ew, 0.5 * target / fn));
     }
     eta = std::max(eta, eta_min);
     int status = 0;

@@ -1,12 +1,14 @@
 // Row-block SpMV over the off-diagonal KEO graph with a fused per-vertex
 // epilogue (diagonal 2x2 block, residual nonlinearity, reductions).
 //
-// One CTA = kRows consecutive rows = kRows threads.  The CTA's nonzeros
-// [rp[r0], rp[r1]) are contiguous; they are staged into shared memory with
-// 128-bit coalesced loads (int4 for column ids, 16-byte chunks of the complex
-// values), then every thread reduces its own row out of shared memory and
-// gathers x through the read-only path.  A CTA whose nonzeros exceed the
-// staging capacity reads them directly.
+// One CTA = kRows consecutive rows = kRows threads, persistent over row
+// blocks.  A row block's nonzeros [rp[r0], rp[r1]) are contiguous: one
+// thread stages them into shared memory with two bulk asynchronous copies
+// (TMA, cp.async.bulk: column ids and complex values) completing on an
+// mbarrier, double-buffered so that the copy of the CTA's next row block
+// overlaps the current one's arithmetic.  Every thread then reduces its own
+// row out of shared memory and gathers x through the read-only path.  A
+// row block whose nonzeros exceed the staging capacity reads them directly.
 #pragma once
 
 #include <utility>
@@ -109,6 +111,55 @@ __device__ __forceinline__ bool halted(const Op &op) {
     return false;
   }
 }
+// ---- bulk-copy staging (TMA + mbarrier) ------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+// global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Bounded wait for the phase with the given parity; false after the limit.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  for (int it = 0; it < (1 << 20); it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Shared memory of one staging buffer (column ids, then complex values) for
+// a capacity of cap nonzeros (a multiple of 4); the kernel uses two.
+template <typename T>
+__host__ __device__ constexpr size_t stage_bytes(int cap) {
+  return (size_t)cap * (sizeof(int32_t) + sizeof(C2<T>));
+}
+// Largest staging capacity: two buffers within 96 KB.
+template <typename T>
+__host__ __device__ constexpr int stage_limit() {
+  return (int)((48 * 1024) / (sizeof(int32_t) + sizeof(C2<T>))) & ~3;
+}
+// Slot of the per-stream reduction counters that records a staging copy
+// that never completed (checked by the host after each linear solve).
+constexpr int kStageErrorSlot = 7;
+
 template <typename T, class Op>
 __global__ void __launch_bounds__(kRows)
     row_block_apply(int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
@@ -116,34 +167,62 @@ __global__ void __launch_bounds__(kRows)
                     Op op, double *partials, unsigned *counter, double *red_out) {
   using A = typename Acc<T>::type;
   if (halted(op)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  int32_t *s_col = reinterpret_cast<int32_t *>(smem_raw);
-  C2<T> *s_val = reinterpret_cast<C2<T> *>(smem_raw + (size_t)cap * sizeof(int32_t));
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar[2];
+  const size_t buf = stage_bytes<T>(cap);
   const int nblocks = (N + kRows - 1) / kRows;
-  A part = 0;
-  // persistent: the grid is sized to the resident capacity and each CTA
-  // walks row blocks with a grid stride (whole waves, fewer partial sums)
-  for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x) {
-    const int r0 = rb * kRows;
-    const int r1 = min(N, r0 + kRows);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0]);
+    mbar_init(&bar[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  }
+  __syncthreads();
+  // row block -> its aligned nonzero range; staged when it fits
+  auto range = [&](int rb, int &ks, int &n) {
+    const int r0 = rb * kRows, r1 = min(N, r0 + kRows);
     const int k0 = __ldg(rp + r0), k1 = __ldg(rp + r1);
-    const int ks = k0 & ~3;  // 16-byte aligned start for both arrays
-    const int n = k1 - ks;
-    const bool staged = n <= cap;
-    if (staged) {
-      const int n4 = (n + 3) >> 2;
-      const int4 *c4 = reinterpret_cast<const int4 *>(ci + ks);
-      for (int j = threadIdx.x; j < n4; j += kRows) reinterpret_cast<int4 *>(s_col)[j] = __ldg(c4 + j);
-      const int nv = (int)((n * sizeof(C2<T>) + 15) / 16);
-      const uint4 *v4 = reinterpret_cast<const uint4 *>(val + ks);
-      for (int j = threadIdx.x; j < nv; j += kRows) reinterpret_cast<uint4 *>(s_val)[j] = __ldg(v4 + j);
+    ks = k0 & ~3;  // 16-byte aligned start for both arrays
+    n = k1 - ks;
+  };
+  auto issue = [&](int rb, int stage) {
+    int ks, n;
+    range(rb, ks, n);
+    if (n > 0 && n <= cap) {
+      unsigned char *base = smem_raw + stage * buf;
+      const uint32_t cb = (uint32_t)(((n + 3) >> 2) * 16);                   // column ids
+      const uint32_t vb = (uint32_t)(((size_t)n * sizeof(C2<T>) + 15) / 16 * 16);  // values
+      mbar_expect_tx(&bar[stage], cb + vb);
+      bulk_g2s(base, ci + ks, cb, &bar[stage]);
+      bulk_g2s(base + (size_t)cap * sizeof(int32_t), val + ks, vb, &bar[stage]);
     }
-    __syncthreads();
-    const int row = r0 + threadIdx.x;
+  };
+  A part = 0;
+  uint32_t parity[2] = {0u, 0u};
+  bool ok = true;
+  if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue(blockIdx.x, 0);
+  int stage = 0;
+  for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, stage ^= 1) {
+    // the other buffer was released by the barrier that ended the previous
+    // iteration: start the next row block's copy into it
+    if (threadIdx.x == 0 && rb + (int)gridDim.x < nblocks) issue(rb + gridDim.x, stage ^ 1);
+    int ks, n;
+    range(rb, ks, n);
+    const bool staged = n > 0 && n <= cap;
+    const bool arrived = staged ? mbar_wait(&bar[stage], parity[stage]) : true;
+    if (__syncthreads_or(!arrived)) {  // the CTA leaves together
+      ok = false;
+      break;
+    }
+    if (staged) parity[stage] ^= 1u;
+    const int32_t *s_col = reinterpret_cast<const int32_t *>(smem_raw + stage * buf);
+    const C2<T> *s_val = reinterpret_cast<const C2<T> *>(smem_raw + stage * buf + (size_t)cap * sizeof(int32_t));
+    const int row = rb * kRows + threadIdx.x;
     if (row < N) {
       A sr = 0, si = 0;
       const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
       if (staged) {
+#pragma unroll 4
         for (int k = b - ks; k < e - ks; k++) {
           const C2<T> v = s_val[k];
           const C2<T> xv = ldg(x + s_col[k]);
@@ -160,7 +239,15 @@ __global__ void __launch_bounds__(kRows)
       }
       part += (A)op.finish(row, sr, si);
     }
-    __syncthreads();  // the staging buffer is reused by the next row block
+    __syncthreads();  // this buffer is refilled two row blocks later
+  }
+  if (!ok) {
+    // a copy never completed: record it, give the copies in flight a last
+    // bounded wait, and leave (the results of this launch are invalid)
+    atomicOr(counter + kStageErrorSlot, 1u);
+    mbar_wait(&bar[0], parity[0]);
+    mbar_wait(&bar[1], parity[1]);
+    return;
   }
   if (Op::kReduce) {
     double total = 0.0;

@@ -2,13 +2,15 @@
 
 * the device-resident continuation reproduces the oracle's converged states
   (exact-LU Newton, modulo the global phase);
-* the message-passing network's readout coefficients and parameter gradient
+* the message-passing network's readout coefficient and parameter gradient
   match a torch FP32 CPU reference of the same network that rounds the node
   GEMM operands and the stored message operands A, B to BF16 as the
   tensor-core path does (gradient tolerance accounts for the BF16 operands
   of the backward GEMMs);
 * trained online on the first steps of a continuation, the learned predictor
-  starts Newton from a smaller residual than the secant predictor.
+  starts Newton from a much smaller residual than the secant predictor (the
+  plain method), and beats the quadratic extrapolation on the transitions it
+  was trained on (training loss < 1).
 """
 import numpy as np
 import pytest
@@ -39,14 +41,14 @@ def _layout():
         take(f"bu{l}", H)
     take("r1_w", H * RH)
     take("r1_b", RH)
-    take("r2_w", RH * 2)
-    take("r2_b", 2)
+    take("r2_w", RH)
+    take("r2_b", 1)
     return L, o
 
 
 def torch_reference(p, ef, rp, ci, X, gram):
     """The network in torch (CPU, FP32), node GEMM operands rounded to BF16;
-    returns the readout coefficients, the loss and the parameter gradient."""
+    returns the readout coefficient, the loss and the parameter gradient."""
     import torch
 
     L, total = _layout()
@@ -75,13 +77,11 @@ def torch_reference(p, ef, rp, ci, X, gram):
         h = h + R
     z = h.mean(dim=0)
     h1 = torch.relu(z @ w("r1_w", (H, RH)) + w("r1_b", (RH,)))
-    wq = (h1 @ w("r2_w", (RH, 2)) + w("r2_b", (2,))).double()
+    wc = (h1 @ w("r2_w", (RH, 1)) + w("r2_b", (1,))).double()[0]
     g = torch.tensor(gram, dtype=torch.float64)
-    G = torch.stack([torch.stack([g[0], g[1]]), torch.stack([g[1], g[2]])])
-    b = torch.stack([g[3], g[4]])
-    loss = (wq @ G @ wq - 2 * wq @ b + g[5]) / g[0]
+    loss = (wc * wc * g[0] - 2 * wc * g[1] + g[2]) / g[2]
     loss.backward()
-    return wq.detach().numpy(), float(loss), P.grad.numpy()
+    return float(wc.detach()), float(loss), P.grad.numpy()
 
 
 @pytest.fixture(scope="module")
@@ -104,19 +104,19 @@ def test_mpnn_forward_and_gradient_match_torch(net):
     gm, model, mp = net
     rng = np.random.default_rng(7)
     N = gm.num_vertices
-    # a parameter set with well-populated ReLUs and an O(1) readout (the
-    # readout starts near zero)
+    # a parameter set with well-populated ReLUs and an O(1) readout slope
+    # (the readout starts with small weights)
     p = mp.params()
     L, _ = _layout()
-    for name, a in (("r1_b", 0.2), ("r2_w", 0.5), ("r2_b", 0.5)):
+    for name, a in (("r1_b", 0.2), ("r2_w", 0.5)):
         o, n = L[name]
         p[o : o + n] = rng.uniform(-a, a, n)
     mp.params(p)
     X = rng.standard_normal((N, FX)).astype(np.float32)
     X[:, FX - 1] = 1.0
-    # Gram scalars of three random fields (q, c, d)
-    q, c, d = rng.standard_normal((3, 2 * N))
-    gram = np.array([q @ q, q @ c, c @ c, q @ d, c @ d, d @ d])
+    # Gram scalars of two random fields (c, d)
+    c, d = rng.standard_normal((2, 2 * N))
+    gram = np.array([c @ c, c @ d, d @ d])
     rp, ci = gm.build_complex_graph()
     rows = np.repeat(np.arange(N), np.diff(rp))
     keep = ci != rows
@@ -125,7 +125,7 @@ def test_mpnn_forward_and_gradient_match_torch(net):
     ef = mp.edge_features()
     w_ref, loss_ref, g_ref = torch_reference(p, ef, rp_od, ci_od, X, gram)
     w = mp.forward(X)
-    assert np.abs(w - w_ref).max() <= 2e-3 * np.abs(w_ref).max(), (w, w_ref)
+    assert abs(w - w_ref) <= 2e-3 * abs(w_ref), (w, w_ref)
     loss, g = mp.loss_grad(X, gram)
     assert abs(loss - loss_ref) <= 1e-4 * loss_ref
     cos = float(g @ g_ref / (np.linalg.norm(g) * np.linalg.norm(g_ref)))
@@ -148,7 +148,7 @@ def _square(s=33, seed=4):
     return m, O.Problem(m, O.mvp_constant_curl(m.x)), psi0
 
 
-@pytest.mark.parametrize("predictor", ["secant", "quadratic"])
+@pytest.mark.parametrize("predictor", ["secant", "quadratic", "cubic"])
 def test_continuation_driver_matches_oracle(predictor):
     import nosh_gb300 as ng
 
@@ -158,7 +158,7 @@ def test_continuation_driver_matches_oracle(predictor):
     gm = ng.mesh(m.x, m.cells)
     model = ng.nls(gm, P.A, -1.0, 1.0, 1.0, mu=mu0)
     cont = ng.continuation(model, x0, mu0)
-    pred = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC}[predictor]
+    pred = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC, "cubic": ng.PREDICT_CUBIC}[predictor]
     f0 = []
     mu = mu0
     for k in range(5):
@@ -171,8 +171,9 @@ def test_continuation_driver_matches_oracle(predictor):
     ref, _ = O.newton_exact(P, x, 1.0, mu)
     assert np.abs(O.align_phase(x, ref) - ref).max() < 1e-8
     assert np.linalg.norm(P.compute_f(x, 1.0, mu)) <= 1.5e-10
-    if predictor == "quadratic":
-        # from the third step on the 3-point predictor is active
+    if predictor != "secant":
+        # from the third (fourth) step on the 3-point (4-point) predictor is
+        # active
         assert f0[-1] < 0.5 * f0[1]
 
 
@@ -187,20 +188,24 @@ def test_learned_predictor_gains_over_secant():
     model.newton(x0, {"mu": mu0})
     cont = ng.continuation(model, x0, mu0)
     cont.learning(train_steps=16, iters_per_step=40, learning_rate=2e-3)
-    mu, gains = mu0, []
+    mu, gains, zero_newton = mu0, [], 0
     for k in range(30):
         mu += 0.01
-        st = cont.advance(mu, predictor=ng.PREDICT_LEARNED)
+        # converged states well below the tolerance serve the 4-point
+        # extrapolants the network combines
+        st = cont.advance(mu, predictor=ng.PREDICT_LEARNED, refine=1e-12)
         assert st["status"] == 0 and st["f_norm"] <= 1e-10
         lp = cont.last_prediction()
         if k >= 22:  # after the training window (+4 history steps)
-            assert np.isfinite(lp["f_learned"])
+            assert lp["used"] == ng.PREDICT_LEARNED and np.isfinite(lp["f_learned"])
             if np.isnan(lp["f_secant"]):
                 # the learned prediction met the tolerance: no comparison
                 assert lp["f_learned"] <= 1e-10 and st["newton_iters"] == 0
+                zero_newton += 1
                 gains.append(np.inf)
             else:
                 gains.append(lp["f_secant"] / lp["f_learned"])
-    assert np.isfinite(lp["train_loss"])
-    # the trained network's prediction starts Newton closer than the secant
-    assert np.median(gains) > 2.0, gains
+    # the trained network beats the quadratic extrapolation on its last
+    # training transition, and starts Newton far closer than the secant
+    assert 0.0 <= lp["train_loss"] < 1.0, lp
+    assert np.median(gains) > 10.0, gains
