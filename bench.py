@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--refine", type=float, default=1e-12,
                     help="residual the Newton steps aim at under the learned and cubic predictors")
     ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
-    ap.add_argument("--train-iters", type=int, default=40, help="optimiser iterations per training step")
+    ap.add_argument("--train-iters", type=int, default=10, help="optimiser iterations per training step")
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -268,7 +268,7 @@ def run_gb300(args):
 
     # converged state at mu0 (untimed set-up)
     x0 = torch.tensor(psi0, dtype=torch.float64, device=dev)
-    st = model.newton(x0, {"mu": args.mu0})
+    st = model.newton(x0, {"mu": args.mu0}, refine=args.refine)
     assert st["status"] == 0, st
 
     preds = {"secant": ng.PREDICT_SECANT, "quadratic": ng.PREDICT_QUADRATIC, "cubic": ng.PREDICT_CUBIC,
@@ -288,10 +288,14 @@ def run_gb300(args):
         if pred == ng.PREDICT_LEARNED:
             cont.learning(args.train_steps, args.train_iters, args.lr)
             warmup = warmup + args.train_steps + 4
+        torch.cuda.synchronize()
+        t_warm = time.perf_counter()
         for _ in range(warmup):
             mu += args.dmu
             s = cont.advance(mu, predictor=pred, refine=refine, precision=precision)
             assert s["status"] == 0, s
+        torch.cuda.synchronize()
+        t_warm = time.perf_counter() - t_warm
         if profile:
             model.profile(True)
             model.profile_read(ng.KERNEL_JACOBIAN)
@@ -320,7 +324,8 @@ def run_gb300(args):
                "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
                "learned_used": int(sum(1 for u in used if u == ng.PREDICT_LEARNED)),
                "zero_newton_steps": int(sum(1 for a, b in its if a == 0)),
-               "train_loss": cont.last_prediction()["train_loss"]}
+               "train_loss": cont.last_prediction()["train_loss"], "warmup_steps": warmup,
+               "warmup_seconds": t_warm}
         if profile:
             out["jac"] = model.profile_read(ng.KERNEL_JACOBIAN)
             out["smo"] = model.profile_read(ng.KERNEL_SMOOTHER)
@@ -410,6 +415,11 @@ def run_gb300(args):
         "zero_newton_steps": head["zero_newton_steps"],
         "newton_krylov_per_step": head["newton_krylov_per_step"],
         "learned_used_steps": head["learned_used"],
+        "training_window": {"steps": head["warmup_steps"], "seconds": head["warmup_seconds"],
+                            "amortized_steps_per_s": (head["warmup_steps"] + args.steps)
+                            / (head["warmup_seconds"] + args.steps * ms / 1000.0),
+                            "note": "untimed warm-up steps that include the online training of the "
+                                    "learned predictor; amortized = all steps of the run / their time"},
         "train_loss": head["train_loss"],
         "e2e": e2e,
         "gpu_launches": int(head["launches"]),

@@ -200,11 +200,14 @@ typedef struct {
   int max_krylov;         /* per linear solve; default 1000 (conf.xml:127)*/
   int precision;          /* NOSH_PREC_*                                  */
   int verbose;            /* 0 = silent                                   */
-  double refine;          /* residual norm the Eisenstat-Walker forcing
-                             aims the Newton steps at (<= tol; 0 = tol).
-                             Converged states well below tol make
-                             high-order continuation predictors exact to
-                             their truncation error; default 0            */
+  double refine;          /* 0 (default) or a residual norm <= tol that
+                             the solve aims at: a state with ||F|| above
+                             4 refine gets at least one Newton step, whose
+                             Eisenstat-Walker forcing aims at refine, and
+                             iteration continues while ||F|| > tol.
+                             States converged well below tol keep
+                             high-order continuation predictors at their
+                             truncation error                             */
 } nosh_newton_options;
 
 typedef struct {
@@ -266,18 +269,21 @@ int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
                               nosh_newton_stats *stats);
 /* The current state (2N doubles, host or device) and its mu. */
 int nosh_continuation_state(nosh_continuation c, double *x, double *mu);
-/* Learned predictor: train on the transitions of the next `train_steps`
- * steps (online, `iters_per_step` optimiser iterations each), then predict.
- * Returns the last training loss (relative) in *loss when not NULL. */
+/* Learned predictor: creates the network (its readout starts at the cubic
+ * extrapolation) and trains it online on the transitions of the next
+ * `train_steps` steps, `iters_per_step` Adam iterations each, the step size
+ * decaying linearly from `learning_rate` over the window.  NOSH_PREDICT_
+ * LEARNED predicts with it once four states are known. */
 int nosh_continuation_learning(nosh_continuation c, int train_steps,
                                int iters_per_step, double learning_rate);
 /* Predictor telemetry: which predictor the last advance used
  * (NOSH_PREDICT_*), the learned prediction's residual and the secant one's
  * (NaN when not evaluated: the secant is only evaluated when the learned
- * prediction misses the tolerance), and the last training loss. */
+ * prediction misses the tolerance), the last training loss, and the
+ * learned coefficient w of the last learned prediction (NaN if none). */
 int nosh_continuation_last_prediction(nosh_continuation c, int *used,
                                       double *f_learned, double *f_secant,
-                                      double *train_loss);
+                                      double *train_loss, double *coef);
 
 /* The learned predictor's network, for inspection and gradient checks (the
  * continuation handle owns its own instance).  From the four newest states

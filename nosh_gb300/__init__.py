@@ -120,7 +120,8 @@ _SIGS = {
     "nosh_continuation_advance": (_I, [_P, _D, _I, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "nosh_continuation_state": (_I, [_P, _P, C.POINTER(_D)]),
     "nosh_continuation_learning": (_I, [_P, _I, _I, _D]),
-    "nosh_continuation_last_prediction": (_I, [_P, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), C.POINTER(_D)]),
+    "nosh_continuation_last_prediction": (_I, [_P, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), C.POINTER(_D),
+                                               C.POINTER(_D)]),
     "nosh_mpnn_create": (_I, [_P, C.POINTER(_P)]),
     "nosh_mpnn_destroy": (_I, [_P]),
     "nosh_mpnn_num_params": (_I, [_P, C.POINTER(_I64)]),
@@ -426,10 +427,10 @@ class nls:
         return self._stats(st)
 
     def newton(self, x, params, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000, precision=None,
-               verbose=0):
+               verbose=0, refine=0.0):
         """Full-step inexact Newton with AMG-preconditioned MINRES; ``x`` is
         updated in place (numpy array or device tensor).  Returns stats."""
-        o = self._options(tol, max_newton, forcing, max_krylov, precision, verbose)
+        o = self._options(tol, max_newton, forcing, max_krylov, precision, verbose, refine)
         st = NewtonStats()
         rc = _lib.nosh_newton_solve(self._h, _ptr(x), _ptr(self._pvec(params)), C.byref(o), C.byref(st))
         _check(rc, allow=(ERR_NOT_CONVERGED,))
@@ -474,9 +475,11 @@ class continuation:
         _check(_lib.nosh_continuation_learning(self._h, train_steps, iters_per_step, learning_rate))
 
     def last_prediction(self):
-        u, fl, fs, tl = C.c_int(), C.c_double(), C.c_double(), C.c_double()
-        _check(_lib.nosh_continuation_last_prediction(self._h, C.byref(u), C.byref(fl), C.byref(fs), C.byref(tl)))
-        return {"used": u.value, "f_learned": fl.value, "f_secant": fs.value, "train_loss": tl.value}
+        u, fl, fs, tl, w = C.c_int(), C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        _check(_lib.nosh_continuation_last_prediction(self._h, C.byref(u), C.byref(fl), C.byref(fs), C.byref(tl),
+                                                      C.byref(w)))
+        return {"used": u.value, "f_learned": fl.value, "f_secant": fs.value, "train_loss": tl.value,
+                "coef": w.value}
 
 
 class mpnn:

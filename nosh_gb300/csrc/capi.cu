@@ -617,7 +617,7 @@ int nosh_continuation_learning(nosh_continuation c, int train_steps, int iters_p
 }
 
 int nosh_continuation_last_prediction(nosh_continuation c, int *used, double *f_learned, double *f_secant,
-                                      double *train_loss) {
+                                      double *train_loss, double *coef) {
   return guarded([&] {
     require(c && c->impl, "null continuation handle");
     auto &C = *c->impl;
@@ -625,6 +625,7 @@ int nosh_continuation_last_prediction(nosh_continuation c, int *used, double *f_
     if (f_learned) *f_learned = C.f_learned;
     if (f_secant) *f_secant = C.f_secant;
     if (train_loss) *train_loss = C.train_loss;
+    if (coef) *coef = C.coef;
   });
 }
 

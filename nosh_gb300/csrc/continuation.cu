@@ -116,6 +116,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   last_used = used_of[order];
   f_learned = std::nan("");
   f_secant = std::nan("");
+  coef = std::nan("");
   extrapolate(order, mu_new, ns.psi.p);
   double f0 = -1.0;
   if (predictor == NOSH_PREDICT_LEARNED && net && count >= 4) {
@@ -125,7 +126,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
     NOSH_CUDA(cudaMemcpyAsync(ns.tmp.p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
     const double *x[4] = {slot(0), slot(1), slot(2), slot(3)};
     const double m[4] = {mu_of(0), mu_of(1), mu_of(2), mu_of(3)};
-    net->predict(x, m, mu_new, ns.tmp.p);
+    coef = net->predict(x, m, mu_new, ns.tmp.p);
     f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
     if (!(f_learned <= opt.tol)) f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.xc.p);
     if (f_learned <= opt.tol || f_learned < f_secant) {
@@ -149,7 +150,9 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   if (net && train_left > 0 && count >= 5) {
     const double *x[4] = {slot(1), slot(2), slot(3), slot(4)};
     const double m[4] = {mu_of(1), mu_of(2), mu_of(3), mu_of(4)};
-    train_loss = net->train(x, m, slot(0), mu_of(0), iters_per_step, learning_rate);
+    // the step size decays linearly over the training window
+    const double lr = learning_rate * train_left / std::max(train_steps, 1);
+    train_loss = net->train(x, m, slot(0), mu_of(0), iters_per_step, lr);
     train_left--;
   }
   s.sync();
@@ -158,6 +161,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
 void ContinuationImpl::enable_learning(int train_steps, int iters, double lr) {
   if (!net) net.reset(new Mpnn(s));
   train_left = train_steps;
+  this->train_steps = train_steps;
   iters_per_step = iters;
   learning_rate = lr;
 }

@@ -18,10 +18,10 @@ struct ContinuationImpl {
   int count = 0;  // valid states
   DevBuf<double> dots;
   std::unique_ptr<Mpnn> net;
-  int train_left = 0, iters_per_step = 0;
+  int train_left = 0, train_steps = 0, iters_per_step = 0;
   double learning_rate = 0.0, train_loss = std::nan("");
   int last_used = NOSH_PREDICT_NONE;
-  double f_learned = std::nan(""), f_secant = std::nan("");
+  double f_learned = std::nan(""), f_secant = std::nan(""), coef = std::nan("");
 
   ContinuationImpl(NlsImpl &nls, const double *x0, double mu0);
   ~ContinuationImpl();

@@ -1188,7 +1188,7 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
 Mpnn::Mpnn(NlsImpl &s) : impl(new Impl(s)) {}
 Mpnn::~Mpnn() = default;
 
-void Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, double *out) {
+double Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, double *out) {
   Impl &I = *impl;
   I.features(x, mu, mu_new, nullptr);
   I.forward(false);
@@ -1196,6 +1196,9 @@ void Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, 
   combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (C2<double> *)out);
   ++I.s.launch_count;
   NOSH_CUDA(cudaGetLastError());
+  double w = 0.0;
+  I.w.download(&w, 1, I.s.stream);  // pageable destination: returns once copied
+  return w;
 }
 
 double Mpnn::train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,

@@ -12,7 +12,8 @@ struct Mpnn {
   // out (in: the secant prediction to mu_new) += q + w c, the learned
   // multiple of the cubic-minus-quadratic field, from the newest states
   // x[0..3] at mu[0..3]
-  void predict(const double *const x[4], const double mu[4], double mu_new, double *out);
+  // (returns w)
+  double predict(const double *const x[4], const double mu[4], double mu_new, double *out);
   // optimiser iterations on the transition x[0..3] -> target at mu_t;
   // returns the last relative loss
   double train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,

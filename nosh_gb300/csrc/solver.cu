@@ -337,7 +337,9 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
   // FP32 Krylov cannot resolve relative residuals much below ~1e-6
   const double eta_min = sizeof(T) == 4 ? 1e-6 : 1e-12;
   double fn = st.f_norm0, fn_prev = fn;
-  for (int it = 0; it < opt.max_newton && fn > opt.tol; it++) {
+  // with a refine target, a state above 4 refine gets at least one step
+  const bool polish = opt.refine > 0.0 && fn > 4.0 * opt.refine;
+  for (int it = 0; it < opt.max_newton && (fn > opt.tol || (it == 0 && polish)); it++) {
     rebuild_operators<T>(s, ns.psi.p, g, mu);
     neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.f.p, b.p);
     ++s.launch_count;

@@ -222,12 +222,26 @@ __global__ void __launch_bounds__(kRows)
       A sr = 0, si = 0;
       const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
       if (staged) {
-#pragma unroll 4
-        for (int k = b - ks; k < e - ks; k++) {
-          const C2<T> v = s_val[k];
-          const C2<T> xv = ldg(x + s_col[k]);
-          sr += v.x * xv.x - v.y * xv.y;
-          si += v.x * xv.y + v.y * xv.x;
+        // batches of kBatch nonzeros: all gathers of a batch are issued
+        // before the first is used (rows of the mesh graph fit one batch)
+        constexpr int kBatch = sizeof(T) == 4 ? 16 : 8;
+        for (int k0 = b - ks; k0 < e - ks; k0 += kBatch) {
+          const int cnt = e - ks - k0;
+          C2<T> v[kBatch], xv[kBatch];
+#pragma unroll
+          for (int u = 0; u < kBatch; u++) {
+            if (u < cnt) {
+              v[u] = s_val[k0 + u];
+              xv[u] = ldg(x + s_col[k0 + u]);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < kBatch; u++) {
+            if (u < cnt) {
+              sr += v[u].x * xv[u].x - v[u].y * xv[u].y;
+              si += v[u].x * xv[u].y + v[u].y * xv[u].x;
+            }
+          }
         }
       } else {
         for (int k = b; k < e; k++) {

@@ -185,10 +185,10 @@ def test_learned_predictor_gains_over_secant():
     gm = ng.mesh(m.x, m.cells)
     model = ng.nls(gm, P.A, -1.0, 1.0, 1.0, mu=mu0)
     x0 = psi0.copy()
-    model.newton(x0, {"mu": mu0})
+    model.newton(x0, {"mu": mu0}, refine=1e-12)
     cont = ng.continuation(model, x0, mu0)
-    cont.learning(train_steps=16, iters_per_step=40, learning_rate=2e-3)
-    mu, gains, zero_newton = mu0, [], 0
+    cont.learning(train_steps=16, iters_per_step=20, learning_rate=2e-3)
+    mu, gains = mu0, []
     for k in range(30):
         mu += 0.01
         # converged states well below the tolerance serve the 4-point
@@ -200,8 +200,8 @@ def test_learned_predictor_gains_over_secant():
             assert lp["used"] == ng.PREDICT_LEARNED and np.isfinite(lp["f_learned"])
             if np.isnan(lp["f_secant"]):
                 # the learned prediction met the tolerance: no comparison
-                assert lp["f_learned"] <= 1e-10 and st["newton_iters"] == 0
-                zero_newton += 1
+                # (Newton may still polish it towards the refine target)
+                assert lp["f_learned"] <= 1e-10
                 gains.append(np.inf)
             else:
                 gains.append(lp["f_secant"] / lp["f_learned"])
