@@ -121,6 +121,15 @@ int nosh_nls_num_params(nosh_nls nls, int *num);
 int nosh_nls_param_name(nosh_nls nls, int index, char *buf, size_t len);
 /* Precision of J/K_reg applies and of the Krylov solver: NOSH_PREC_*. */
 int nosh_nls_set_precision(nosh_nls nls, int precision);
+/* Preconditioner options (the MueLu parameter list of
+ * src/keo_regularized.cpp:296-315): maximum levels, coarsest size (nodes),
+ * Chebyshev degree of pre- and post-smoothing, and the reuse period: the
+ * numeric refreshes between two full Galerkin refreshes (1 = refresh every
+ * level at every rebuild; the ones in between update the fine level only,
+ * like MueLu "reuse: type full").  Defaults 10, 64, 2, 8.  Drops the current
+ * hierarchy; the next rebuild builds a new one. */
+int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size,
+                             int smooth_degree, int reuse_period);
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int nosh_nls_stream(nosh_nls nls, void **stream);
 

@@ -94,6 +94,7 @@ _SIGS = {
     "nosh_nls_num_params": (_I, [_P, C.POINTER(_I)]),
     "nosh_nls_param_name": (_I, [_P, _I, C.c_char_p, C.c_size_t]),
     "nosh_nls_set_precision": (_I, [_P, _I]),
+    "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I]),
     "nosh_nls_stream": (_I, [_P, C.POINTER(_P)]),
     "nosh_nls_compute_f": (_I, [_P, _P, _P, _P]),
     "nosh_nls_compute_f_norm": (_I, [_P, _P, _P, _P, C.POINTER(_D)]),
@@ -345,6 +346,11 @@ class nls:
             p = {**self.nominal, **params}
             return np.array([p["g"], p["mu"]], np.float64)
         return np.ascontiguousarray(params, np.float64)
+
+    def set_amg_options(self, max_levels=10, coarse_size=64, smooth_degree=2, reuse_period=8):
+        """Preconditioner options (MueLu parameter list of the reference);
+        the hierarchy is rebuilt at the next Newton step."""
+        _check(_lib.nosh_nls_set_amg_options(self._h, max_levels, coarse_size, smooth_degree, reuse_period))
 
     def stream(self) -> int:
         s = C.c_void_p()

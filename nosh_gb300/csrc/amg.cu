@@ -289,27 +289,48 @@ __device__ __forceinline__ void cheb_first_elem(int64_t i, const T *dinv, T c0, 
 // Chebyshev step k given (sr, si) = (offdiag A x_in)_i:
 // r = D^-1 (b - A x_in), d = c1 d + c2 r (d = c0 r for k == 0), x_out = x_in + d
 template <typename T>
-__device__ __forceinline__ C2<T> cheb_elem(int64_t i, int k, T sr, T si, const T *dia, const T *dinv,
-                                           const T *coef, const C2<T> *b, const C2<T> *xin, C2<T> *d,
-                                           C2<T> *xout) {
-  const C2<T> xi = xin[i], bi = b[i];
-  const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
-  const T rr = bi.x - (sr + d0r * xi.x + d1b * xi.y);
-  const T ri = bi.y - (si + d1b * xi.x + d0i * xi.y);
-  const T a = dinv[3 * i], e = dinv[3 * i + 1], f = dinv[3 * i + 2];
-  const T zr = a * rr + f * ri, zi = f * rr + e * ri;
+struct ChebPre {
+  C2<T> xi, bi, dold;
+  T d0r, d0i, d1b, a, e, f;
+};
+template <typename T>
+__device__ __forceinline__ ChebPre<T> cheb_load(int64_t i, int k, const T *dia, const T *dinv, const C2<T> *b,
+                                                const C2<T> *xin, const C2<T> *d) {
+  ChebPre<T> p;
+  p.xi = xin[i];
+  p.bi = b[i];
+  p.d0r = dia[3 * i];
+  p.d0i = dia[3 * i + 1];
+  p.d1b = dia[3 * i + 2];
+  p.a = dinv[3 * i];
+  p.e = dinv[3 * i + 1];
+  p.f = dinv[3 * i + 2];
+  p.dold = k == 0 ? C2<T>{0, 0} : d[i];
+  return p;
+}
+template <typename T>
+__device__ __forceinline__ C2<T> cheb_apply(int64_t i, int k, T sr, T si, const ChebPre<T> &p, const T *coef,
+                                            C2<T> *d, C2<T> *xout) {
+  const T rr = p.bi.x - (sr + p.d0r * p.xi.x + p.d1b * p.xi.y);
+  const T ri = p.bi.y - (si + p.d1b * p.xi.x + p.d0i * p.xi.y);
+  const T zr = p.a * rr + p.f * ri, zi = p.f * rr + p.e * ri;
   C2<T> dn;
   if (k == 0) {
     dn = C2<T>{coef[0] * zr, coef[0] * zi};
   } else {
-    const C2<T> dold = d[i];
     const T c1 = coef[2 * k], c2 = coef[2 * k + 1];
-    dn = C2<T>{c1 * dold.x + c2 * zr, c1 * dold.y + c2 * zi};
+    dn = C2<T>{c1 * p.dold.x + c2 * zr, c1 * p.dold.y + c2 * zi};
   }
   d[i] = dn;
-  const C2<T> xo{xi.x + dn.x, xi.y + dn.y};
+  const C2<T> xo{p.xi.x + dn.x, p.xi.y + dn.y};
   xout[i] = xo;
   return xo;
+}
+template <typename T>
+__device__ __forceinline__ C2<T> cheb_elem(int64_t i, int k, T sr, T si, const T *dia, const T *dinv,
+                                           const T *coef, const C2<T> *b, const C2<T> *xin, C2<T> *d,
+                                           C2<T> *xout) {
+  return cheb_apply<T>(i, k, sr, si, cheb_load<T>(i, k, dia, dinv, b, xin, d), coef, d, xout);
 }
 
 template <typename T>
@@ -348,8 +369,10 @@ struct ChebOp {
   const C2<T> *b, *xin;
   C2<T> *d, *xout;
   const int *halt = nullptr;
-  __device__ double finish(int i, T sr, T si) const {
-    cheb_elem<T>(i, step, sr, si, dia, dinv, coef, b, xin, d, xout);
+  using Pre = ChebPre<T>;
+  __device__ Pre load(int i) const { return cheb_load<T>(i, step, dia, dinv, b, xin, d); }
+  __device__ double finish(int i, T sr, T si, const Pre &p) const {
+    cheb_apply<T>(i, step, sr, si, p, coef, d, xout);
     return 0.0;
   }
 };
@@ -366,10 +389,11 @@ struct ChebMinresOp {
   C2<T> *d, *xout;
   MinresScalars *s;
   const int *halt = nullptr;
-  __device__ double finish(int i, T sr, T si) const {
-    const C2<T> z = cheb_elem<T>(i, step, sr, si, dia, dinv, coef, b, xin, d, xout);
-    const C2<T> bi = b[i];
-    return (double)bi.x * (double)z.x + (double)bi.y * (double)z.y;
+  using Pre = ChebPre<T>;
+  __device__ Pre load(int i) const { return cheb_load<T>(i, step, dia, dinv, b, xin, d); }
+  __device__ double finish(int i, T sr, T si, const Pre &p) const {
+    const C2<T> z = cheb_apply<T>(i, step, sr, si, p, coef, d, xout);
+    return (double)p.bi.x * (double)z.x + (double)p.bi.y * (double)z.y;
   }
   __device__ void hook(double total) const { minres_advance(s, total); }
 };
@@ -382,10 +406,14 @@ struct ResidOp {
   const C2<T> *b, *x;
   C2<T> *res;
   const int *halt = nullptr;
-  __device__ double finish(int i, T sr, T si) const {
-    const C2<T> xi = x[i], bi = b[i];
-    const T d0r = dia[3 * i], d0i = dia[3 * i + 1], d1b = dia[3 * i + 2];
-    res[i] = C2<T>{bi.x - (sr + d0r * xi.x + d1b * xi.y), bi.y - (si + d1b * xi.x + d0i * xi.y)};
+  struct Pre {
+    C2<T> xi, bi;
+    T d0r, d0i, d1b;
+  };
+  __device__ Pre load(int i) const { return Pre{x[i], b[i], dia[3 * i], dia[3 * i + 1], dia[3 * i + 2]}; }
+  __device__ double finish(int i, T sr, T si, const Pre &p) const {
+    res[i] = C2<T>{p.bi.x - (sr + p.d0r * p.xi.x + p.d1b * p.xi.y),
+                   p.bi.y - (si + p.d1b * p.xi.x + p.d0i * p.xi.y)};
     return 0.0;
   }
 };
@@ -688,6 +716,7 @@ struct AmgLevel {
 template <typename T>
 struct AmgVals {
   bool ready = false;
+  int64_t refreshes = 0;  // numeric refreshes so far
   std::vector<DevBuf<C2<T>>> off;  // level >= 1
   std::vector<DevBuf<T>> dia;      // level >= 1
   std::vector<DevBuf<T>> dinv, coef;
@@ -895,6 +924,22 @@ void Amg::refresh() {
   AmgVals<T> &V = I.vals<T>();
   cudaStream_t st = I.nls.stream;
   const int L = (int)I.lev.size();
+  const bool partial = I.opt.reuse_period > 1 && L > 1 && V.refreshes % I.opt.reuse_period != 0;
+  ++V.refreshes;
+  if (partial) {
+    // hierarchy reuse (MueLu "reuse: type full", src/keo_regularized.cpp:
+    // 298-330): the fine level reads the current operator directly; only its
+    // block-Jacobi inverse and Chebyshev bounds follow it, the coarse
+    // operators keep their last Galerkin values (SPD, so the V-cycle stays
+    // an SPD preconditioner)
+    NOSH_CUDA(cudaMemsetAsync(I.lmax_bits.p, 0, sizeof(unsigned long long), st));
+    dinv_gershgorin<T><<<div_up(I.lev[0].n, 256), 256, 0, st>>>(I.lev[0].n, I.lev[0].rp, I.off<T>(0), I.dia<T>(0),
+                                                                V.dinv[0].p, I.lmax_bits.p);
+    cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p, std::max(I.opt.smooth_degree, 1), V.coef[0].p, I.lmax.p);
+    I.nls.launch_count += 2;
+    NOSH_CUDA(cudaGetLastError());
+    return;
+  }
   NOSH_CUDA(cudaMemsetAsync(I.lmax_bits.p, 0, L * sizeof(unsigned long long), st));
   for (int l = 0; l < L; l++) {
     AmgLevel &A = I.lev[l];

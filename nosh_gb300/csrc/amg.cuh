@@ -13,8 +13,9 @@ struct AmgOptions {
   int max_levels = 10;
   int coarse_size = 64;  // stop coarsening at or below this many nodes
   int smooth_degree = 2; // Chebyshev degree of pre- and post-smoothing
-  bool smoothed = true;  // smoothed (true) or plain (false) aggregation
-  double omega_scale = 4.0 / 3.0;  // prolongator damping / lambda_max
+  // refreshes between full Galerkin refreshes; the ones in between update
+  // the fine level only (hierarchy reuse)
+  int reuse_period = 8;
 };
 
 struct Amg {

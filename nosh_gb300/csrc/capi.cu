@@ -295,6 +295,21 @@ int nosh_nls_set_precision(nosh_nls nls, int precision) {
   });
 }
 
+int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size, int smooth_degree,
+                             int reuse_period) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(max_levels >= 1 && max_levels <= 16 && coarse_size >= 1 && coarse_size <= 512 &&
+                smooth_degree >= 1 && smooth_degree <= 8 && reuse_period >= 1,
+            "AMG options out of range");
+    s.amg_max_levels = max_levels;
+    s.amg_coarse_size = coarse_size;
+    s.amg_smooth_degree = smooth_degree;
+    s.amg_reuse_period = reuse_period;
+    nosh::reset_preconditioner(s);
+  });
+}
+
 int nosh_nls_stream(nosh_nls nls, void **stream) {
   return guarded([&] {
     require(stream != nullptr, "null output");

@@ -109,6 +109,12 @@ void parallel_for(int64_t n, F &&f, int64_t grain = 1 << 14) {
 // ------------------------------------------------------------ launch math
 constexpr int kPad = 8;        // tail padding of nonzero arrays (elements)
 constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time)
+
+// In place: each of the first n complex values c[2k], c[2k+1] (a dot
+// product <x_k, x_0>) becomes the unit phase factor c / |c| (1 when c = 0)
+// that aligns x_k with x_0.  One launch of 32 threads: the FP64 square root
+// and divisions run once per factor, not once per vector element.
+__global__ void normalize_phases(int n, double *c);
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 }  // namespace nosh

@@ -28,20 +28,18 @@ __global__ void cdot2_kernel(int64_t n, const C2<double> *__restrict__ a, const 
   grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
 }
 
-__device__ __forceinline__ void unit_phase(const double *c, double &er, double &ei) {
-  const double m = sqrt(c[0] * c[0] + c[1] * c[1]);
-  er = m > 0 ? c[0] / m : 1.0;
-  ei = m > 0 ? c[1] / m : 0.0;
-}
-
-// out = sum_k L_k e^{i phi_k} x_k (k <= order), the phases aligning x_k with
-// x0 (solutions are defined up to a global U(1) phase)
+// out = sum_k L_k e^{i phi_k} x_k (k <= order), the unit phase factors c
+// (normalize_phases) aligning x_k with x0 (solutions are defined up to a
+// global U(1) phase)
 __global__ void extrapolate_kernel(int64_t n, int order, const double *__restrict__ c, double L0, double L1,
                                    double L2, double L3, const C2<double> *__restrict__ x0,
                                    const C2<double> *__restrict__ x1, const C2<double> *__restrict__ x2,
                                    const C2<double> *__restrict__ x3, C2<double> *__restrict__ out) {
   double er[3] = {1.0, 1.0, 1.0}, ei[3] = {0.0, 0.0, 0.0};
-  for (int k = 0; k < order; k++) unit_phase(c + 2 * k, er[k], ei[k]);
+  for (int k = 0; k < order; k++) {
+    er[k] = c[2 * k];
+    ei[k] = c[2 * k + 1];
+  }
   const double L[3] = {L1, L2, L3};
   const C2<double> *xs[3] = {x1, x2, x3};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -87,6 +85,10 @@ void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
   for (int k = 1; k <= order; k++) {
     cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)slot(k), (const C2<double> *)slot(0),
                                     s.red.partials.p, s.red.counter.p, dots.p + 2 * (k - 1));
+    ++s.launch_count;
+  }
+  if (order >= 1) {
+    normalize_phases<<<1, 32, 0, st>>>(order, dots.p);
     ++s.launch_count;
   }
   const double *x1 = order >= 1 ? slot(1) : slot(0), *x2 = order >= 2 ? slot(2) : slot(0),

@@ -670,13 +670,10 @@ __global__ void adam_kernel(int64_t n, float *__restrict__ p, const float *__res
 }
 
 // ----------------------------------------------------------- features
-struct Phases {
-  double er[4], ei[4];  // phase factors aligning x1, x2, x3, target with x0
-};
+// unit phase factor k (normalized in place by normalize_phases)
 __device__ __forceinline__ void phases(const double *c, int k, double &er, double &ei) {
-  const double m = sqrt(c[2 * k] * c[2 * k] + c[2 * k + 1] * c[2 * k + 1]);
-  er = m > 0 ? c[2 * k] / m : 1.0;
-  ei = m > 0 ? c[2 * k + 1] / m : 0.0;
+  er = c[2 * k];
+  ei = c[2 * k + 1];
 }
 
 // per node: s = x0 - x1, q = quad - sec, c = cubic - quad at t (fields in
@@ -1170,6 +1167,8 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
                                  s.red.counter.p, dots.p + 6);
     ++s.launch_count;
   }
+  normalize_phases<<<1, 32, 0, st>>>(target ? 4 : 3, dots.p);
+  ++s.launch_count;
   features_a<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
                                 (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, s.red.partials.p,
                                 s.red.counter.p, red.p);

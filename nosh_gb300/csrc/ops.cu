@@ -249,6 +249,15 @@ void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &o
 
 }  // namespace
 
+__global__ void normalize_phases(int n, double *c) {
+  const int k = threadIdx.x;
+  if (k >= n) return;
+  const double re = c[2 * k], im = c[2 * k + 1];
+  const double m = sqrt(re * re + im * im);
+  c[2 * k] = m > 0 ? re / m : 1.0;
+  c[2 * k + 1] = m > 0 ? im / m : 0.0;
+}
+
 namespace dev {
 int row_grid(const void *kernel, size_t smem, int64_t n_rows) {
   static int sms = 0;

@@ -79,18 +79,40 @@ struct JacMinresOp {
   const T *wb, *wc;
   T *xsol;
   const int *halt;  // &s->done
-  __device__ double finish(int i, T sr, T si) const {
-    const C2<T> xi = x[i];
-    const T d0r = d[3 * i], d0i = d[3 * i + 1], d1b = d[3 * i + 2];
-    const T yr = sr + d0r * xi.x + d1b * xi.y;
-    const T yi = si + d1b * xi.x + d0i * xi.y;
-    y[i] = C2<T>{yr, yi};
-    if (s->wx_pending) {
-      const T *c = wx_coef<T>(s);
-      minres_wx_elem<T>(c, 2 * (int64_t)i, zprev, wa, wb, wc, xsol);
-      minres_wx_elem<T>(c, 2 * (int64_t)i + 1, zprev, wa, wb, wc, xsol);
+  struct Pre {
+    C2<T> xi;
+    T d0r, d0i, d1b;
+    C2<T> zp, wbv, wcv, xs;  // deferred w/x update operands (when pending)
+    bool wx;
+  };
+  __device__ Pre load(int i) const {
+    Pre p;
+    p.xi = x[i];
+    p.d0r = d[3 * i];
+    p.d0i = d[3 * i + 1];
+    p.d1b = d[3 * i + 2];
+    p.wx = s->wx_pending != 0;
+    if (p.wx) {
+      p.zp = reinterpret_cast<const C2<T> *>(zprev)[i];
+      p.wbv = reinterpret_cast<const C2<T> *>(wb)[i];
+      p.wcv = reinterpret_cast<const C2<T> *>(wc)[i];
+      p.xs = reinterpret_cast<const C2<T> *>(xsol)[i];
     }
-    return (double)(xi.x * yr + xi.y * yi);
+    return p;
+  }
+  __device__ double finish(int i, T sr, T si, const Pre &p) const {
+    const T yr = sr + p.d0r * p.xi.x + p.d1b * p.xi.y;
+    const T yi = si + p.d1b * p.xi.x + p.d0i * p.xi.y;
+    y[i] = C2<T>{yr, yi};
+    if (p.wx) {
+      // w = (z c0 - c1 w2 - c2 w) c3 over the w1 buffer, x += c4 w
+      const T *c = wx_coef<T>(s);
+      const C2<T> w{(p.zp.x * c[0] - c[1] * p.wbv.x - c[2] * p.wcv.x) * c[3],
+                    (p.zp.y * c[0] - c[1] * p.wbv.y - c[2] * p.wcv.y) * c[3]};
+      reinterpret_cast<C2<T> *>(wa)[i] = w;
+      reinterpret_cast<C2<T> *>(xsol)[i] = C2<T>{p.xs.x + c[4] * w.x, p.xs.y + c[4] * w.y};
+    }
+    return (double)(p.xi.x * yr + p.xi.y * yi);
   }
   // the finishing thread turns <z, J z> into the Lanczos coefficients
   __device__ void hook(double total) const { minres_lanczos_coefs(const_cast<MinresScalars *>(s), total); }
@@ -139,7 +161,8 @@ Minres<T>::Minres(NlsImpl &nls) : s(nls), n2(2 * nls.N) {
 
 template <typename T>
 Minres<T>::~Minres() {
-  if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+  for (cudaGraphExec_t &e : half_exec)
+    if (e) cudaGraphExecDestroy(e);
   if (h_sc) cudaFreeHost(h_sc);
   if (h_err) cudaFreeHost(h_err);
 }
@@ -174,10 +197,12 @@ void Minres<T>::iteration(int j) {
 }
 
 template <typename T>
-void Minres<T>::wx_final() {
-  // step kChunk-1 = 5: z = z[1], (w1, w2, w) = (w[2], w[0], w[1])
+void Minres<T>::wx_final(int j) {
+  // the update iteration j + 1 would have fused: z = z[j % 2], (w1, w2, w) =
+  // (w[j % 3], w[(j + 1) % 3], w[(j + 2) % 3])
   const int G = std::min<int64_t>(div_up(n2, 256), kNumSMs * 8);
-  minres_wx<T><<<G, 256, 0, s.stream>>>(n2, sc.p, z[1].p, w[2].p, w[0].p, w[1].p, x.p);
+  minres_wx<T><<<G, 256, 0, s.stream>>>(n2, sc.p, z[j % 2].p, w[j % 3].p, w[(j + 1) % 3].p, w[(j + 2) % 3].p,
+                                        x.p);
   clear_wx_pending<<<1, 1, 0, s.stream>>>(sc.p);
   s.launch_count += 2;
 }
@@ -199,26 +224,33 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
   NOSH_CUDA(cudaGetLastError());
   // graphs are used unless kernel timing is on (event pairs per launch)
   const bool graphs = !s.timers[NOSH_KERNEL_JACOBIAN].on;
-  if (graphs && !chunk_exec) {
-    cudaGraph_t g;
-    const int64_t before = s.launch_count;
-    NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int j = 0; j < kChunk; j++) iteration(j);
-    NOSH_CUDA(cudaStreamEndCapture(st, &g));
-    chunk_kernels = s.launch_count - before;
-    s.launch_count = before;
-    NOSH_CUDA(cudaGraphInstantiate(&chunk_exec, g, 0));
-    NOSH_CUDA(cudaGraphDestroy(g));
-  }
-  int it = 0;
-  for (;;) {
-    if (graphs) {
-      NOSH_CUDA(cudaGraphLaunch(chunk_exec, st));
-      s.launch_count += chunk_kernels;
-    } else {
-      for (int j = 0; j < kChunk; j++) iteration(j);
+  if (graphs && !half_exec[0]) {
+    for (int h = 0; h < 2; h++) {
+      cudaGraph_t g;
+      const int64_t before = s.launch_count;
+      NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (int j = h * kHalf; j < (h + 1) * kHalf; j++) iteration(j);
+      NOSH_CUDA(cudaStreamEndCapture(st, &g));
+      half_kernels[h] = s.launch_count - before;
+      s.launch_count = before;
+      NOSH_CUDA(cudaGraphInstantiate(&half_exec[h], g, 0));
+      NOSH_CUDA(cudaGraphDestroy(g));
     }
-    it += kChunk;
+  }
+  auto launch_half = [&](int h) {
+    if (graphs) {
+      NOSH_CUDA(cudaGraphLaunch(half_exec[h], st));
+      s.launch_count += half_kernels[h];
+    } else {
+      for (int j = h * kHalf; j < (h + 1) * kHalf; j++) iteration(j);
+    }
+  };
+  // first batch: as many half-chunks as the previous solve used (two at first)
+  int batch = last_its > 0 ? (last_its + kHalf - 1) / kHalf : 2;
+  int it = 0, h = 0;
+  for (;;) {
+    for (int q = 0; q < batch; q++, h ^= 1, it += kHalf) launch_half(h);
+    batch = 1;
     NOSH_CUDA(cudaGetLastError());
     NOSH_CUDA(cudaMemcpyAsync(h_sc, d, sizeof(MinresScalars), cudaMemcpyDeviceToHost, st));
     NOSH_CUDA(cudaMemcpyAsync(h_err, s.amg->error_flag_ptr(), sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -227,11 +259,13 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     NOSH_CUDA(cudaStreamSynchronize(st));
     if (h_sc->done || it >= maxit + kChunk) break;
   }
-  if (h_sc->wx_pending) wx_final();  // converged on the chunk's last step
+  // converged on the last issued iteration: its w/x update is still due
+  if (h_sc->wx_pending) wx_final(h == 1 ? kHalf - 1 : kChunk - 1);
   NOSH_CHECK(h_err[1] == 0, NOSH_ERR_CUDA, "an SpMV staging copy did not complete");
   NOSH_CHECK(h_err[0] == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
   status = h_sc->flag;
   rel_res = h_sc->beta1 > 0 ? h_sc->phibar / h_sc->beta1 : 0.0;
+  last_its = h_sc->itn;
   return h_sc->itn;
 }
 
@@ -256,13 +290,12 @@ __global__ void cdot_kernel(int64_t n, const C2<double> *__restrict__ a,
   grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
 }
 
-// secant prediction x_new = x + r (x - e^{i phi} x_prev), phi aligning
-// x_prev to x; x_prev <- x
+// secant prediction x_new = x + r (x - e^{i phi} x_prev), e^{i phi} = c (the
+// unit phase factor aligning x_prev to x); x_prev <- x
 __global__ void secant_kernel(int64_t n, const double *__restrict__ c, double r,
                               C2<double> *__restrict__ xn, C2<double> *__restrict__ x,
                               C2<double> *__restrict__ xp) {
-  const double m = sqrt(c[0] * c[0] + c[1] * c[1]);
-  const double er = m > 0 ? c[0] / m : 1.0, ei = m > 0 ? c[1] / m : 0.0;
+  const double er = c[0], ei = c[1];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const C2<double> a = x[i], p = xp[i];
@@ -280,6 +313,16 @@ __global__ void axpy_to(int64_t n, double a, const T *__restrict__ t, const doub
     y[i] = x[i] + a * (double)t[i];
 }
 }  // namespace
+
+void reset_preconditioner(NlsImpl &s) {
+  // the MINRES graphs capture the hierarchy's buffers: drop them with it
+  if (s.solver_state) {
+    NewtonState &ns = *(NewtonState *)s.solver_state.get();
+    ns.m32.reset();
+    ns.m64.reset();
+  }
+  s.amg.reset();
+}
 
 NewtonState &state_of(NlsImpl &s) {
   if (!s.solver_state) {
@@ -304,7 +347,14 @@ template <typename T>
 static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu) {
   s.jac_rebuild(psi, g, mu);
   s.reg_rebuild(psi, g, mu);
-  if (!s.amg) s.amg.reset(new Amg(s));
+  if (!s.amg) {
+    AmgOptions o;
+    o.max_levels = s.amg_max_levels;
+    o.coarse_size = s.amg_coarse_size;
+    o.smooth_degree = s.amg_smooth_degree;
+    o.reuse_period = s.amg_reuse_period;
+    s.amg.reset(new Amg(s, o));
+  }
   s.amg->refresh<T>();
 }
 
@@ -434,7 +484,8 @@ void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double m
     NOSH_CUDA(cudaMemcpyAsync(ns.xp.p, x_prev, bytes, cudaMemcpyDefault, st_));
     cdot_kernel<<<G, 256, 0, st_>>>(s.N, (const C2<double> *)ns.xp.p, (const C2<double> *)ns.xc.p,
                                     s.red.partials.p, s.red.counter.p, ns.red2.p);
-    ++s.launch_count;
+    normalize_phases<<<1, 32, 0, st_>>>(1, ns.red2.p);
+    s.launch_count += 2;
     secant_kernel<<<G, 256, 0, st_>>>(s.N, ns.red2.p, (mu_new - mu_cur) / (mu_cur - mu_prev),
                                       (C2<double> *)ns.psi.p, (C2<double> *)ns.xc.p,
                                       (C2<double> *)ns.xp.p);

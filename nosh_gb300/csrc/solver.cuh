@@ -9,19 +9,24 @@ namespace nosh {
 
 // Preconditioned MINRES (Paige-Saunders) on J dx = b with the AMG V-cycle as
 // the SPD preconditioner, vectors in T, scalars in FP64 (minres_state.cuh).
-// Iterations run in chunks of kChunk, each captured once as a CUDA graph and
-// replayed; the host polls the convergence flag once per chunk.
+// Buffer roles repeat every kChunk iterations; the chunk is captured once as
+// two CUDA graphs of kChunk / 2 iterations (half-chunks, replayed
+// alternately).  A solve launches as many half-chunks as the previous solve
+// needed before the host first polls the convergence flag, then one at a
+// time; launches after convergence return at once.
 template <typename T>
 struct Minres {
   static constexpr int kChunk = 6;  // multiple of the 2- and 3-buffer rotations
+  static constexpr int kHalf = kChunk / 2;
   NlsImpl &s;
   int64_t n2;  // real length (2N)
   DevBuf<T> r[2], z[2], w[3], u, x;
   DevBuf<MinresScalars> sc;
   MinresScalars *h_sc = nullptr;  // pinned host mirror
   int *h_err = nullptr;
-  cudaGraphExec_t chunk_exec = nullptr;
-  int64_t chunk_kernels = 0;
+  cudaGraphExec_t half_exec[2] = {nullptr, nullptr};
+  int64_t half_kernels[2] = {0, 0};
+  int last_its = 0;  // iterations of the previous solve
   explicit Minres(NlsImpl &nls);
   ~Minres();
   // b: device vector of T (2N); returns iterations; x holds the solution
@@ -29,7 +34,7 @@ struct Minres {
 
  private:
   void iteration(int j);   // issue iteration j (0..kChunk-1) of a chunk
-  void wx_final();         // deferred w/x update of the chunk's last step
+  void wx_final(int j);    // deferred w/x update of iteration j, the last issued
 };
 
 // Newton work space of an nls handle (solver.cu)
@@ -42,6 +47,9 @@ struct NewtonState {
   std::unique_ptr<Minres<double>> m64;
 };
 NewtonState &state_of(NlsImpl &s);
+// drop the AMG hierarchy (and the MINRES graphs that reference it); the next
+// rebuild constructs it from the current options
+void reset_preconditioner(NlsImpl &s);
 // ||F(psi)||_2 (writes F into f; synchronises)
 double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f);
 // Newton on state_of(s).psi in place.  With f0 >= 0, ns.f already holds

@@ -71,9 +71,14 @@ __device__ __forceinline__ bool grid_reduce(double v, double *partials, unsigned
 
 // Op must provide:
 //   static constexpr bool kReduce;
-//   __device__ double finish(int row, acc sr, acc si) -- writes y[row],
-//                                                       returns the thread's
-//                                                       partial
+//   struct Pre;                                  -- the row's epilogue operands
+//   __device__ Pre load(int row)                 -- issued before the row's
+//                                                   nonzeros arrive, so the
+//                                                   epilogue loads overlap the
+//                                                   staging and the gathers
+//   __device__ double finish(int row, acc sr, acc si, const Pre &)
+//                                                -- writes y[row], returns the
+//                                                   thread's partial
 // and, when kReduce, may provide kHook + hook(total): scalar work done by one
 // thread once the grid sum is known.
 template <class Op, class = void>
@@ -208,6 +213,9 @@ __global__ void __launch_bounds__(kRows)
     if (threadIdx.x == 0 && rb + (int)gridDim.x < nblocks) issue(rb + gridDim.x, stage ^ 1);
     int ks, n;
     range(rb, ks, n);
+    const int row = rb * kRows + threadIdx.x;
+    typename Op::Pre pre{};
+    if (row < N) pre = op.load(row);
     const bool staged = n > 0 && n <= cap;
     const bool arrived = staged ? mbar_wait(&bar[stage], parity[stage]) : true;
     if (__syncthreads_or(!arrived)) {  // the CTA leaves together
@@ -217,7 +225,6 @@ __global__ void __launch_bounds__(kRows)
     if (staged) parity[stage] ^= 1u;
     const int32_t *s_col = reinterpret_cast<const int32_t *>(smem_raw + stage * buf);
     const C2<T> *s_val = reinterpret_cast<const C2<T> *>(smem_raw + stage * buf + (size_t)cap * sizeof(int32_t));
-    const int row = rb * kRows + threadIdx.x;
     if (row < N) {
       A sr = 0, si = 0;
       const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
@@ -251,7 +258,7 @@ __global__ void __launch_bounds__(kRows)
           si += v.x * xv.y + v.y * xv.x;
         }
       }
-      part += (A)op.finish(row, sr, si);
+      part += (A)op.finish(row, sr, si, pre);
     }
     __syncthreads();  // this buffer is refilled two row blocks later
   }
@@ -281,10 +288,13 @@ struct KeoOp {
   const T *kdiag;
   const C2<T> *x;
   C2<T> *y;
-  __device__ double finish(int i, T sr, T si) const {
-    const C2<T> xi = x[i];
-    const T d = kdiag[i];
-    y[i] = C2<T>{sr + d * xi.x, si + d * xi.y};
+  struct Pre {
+    C2<T> xi;
+    T d;
+  };
+  __device__ Pre load(int i) const { return Pre{x[i], kdiag[i]}; }
+  __device__ double finish(int i, T sr, T si, const Pre &p) const {
+    y[i] = C2<T>{sr + p.d * p.xi.x, si + p.d * p.xi.y};
     return 0.0;
   }
 };
@@ -294,7 +304,9 @@ template <typename T>
 struct PlainOp {
   static constexpr bool kReduce = false;
   C2<T> *y;
-  __device__ double finish(int i, T sr, T si) const {
+  struct Pre {};
+  __device__ Pre load(int) const { return Pre{}; }
+  __device__ double finish(int i, T sr, T si, const Pre &) const {
     y[i] = C2<T>{sr, si};
     return 0.0;
   }
@@ -308,13 +320,16 @@ struct BlockDiagOp {
   const T *d;  // 3 per vertex
   const C2<T> *x;
   C2<T> *y;
-  __device__ double finish(int i, T sr, T si) const {
-    const C2<T> xi = x[i];
-    const T d0r = d[3 * i], d0i = d[3 * i + 1], d1b = d[3 * i + 2];
-    const T yr = sr + d0r * xi.x + d1b * xi.y;
-    const T yi = si + d1b * xi.x + d0i * xi.y;
+  struct Pre {
+    C2<T> xi;
+    T d0r, d0i, d1b;
+  };
+  __device__ Pre load(int i) const { return Pre{x[i], d[3 * i], d[3 * i + 1], d[3 * i + 2]}; }
+  __device__ double finish(int i, T sr, T si, const Pre &p) const {
+    const T yr = sr + p.d0r * p.xi.x + p.d1b * p.xi.y;
+    const T yi = si + p.d1b * p.xi.x + p.d0i * p.xi.y;
     y[i] = C2<T>{yr, yi};
-    return kDot ? (double)xi.x * (double)yr + (double)xi.y * (double)yi : 0.0;
+    return kDot ? (double)p.xi.x * (double)yr + (double)p.xi.y * (double)yi : 0.0;
   }
 };
 
@@ -326,10 +341,14 @@ struct ResidualOp {
   double g;
   const C2<double> *x;
   C2<double> *y;
-  __device__ double finish(int i, double sr, double si) const {
-    const C2<double> p = x[i];
-    const double a = kdiag[i] + cvt[i] * (V[i] + g * (p.x * p.x + p.y * p.y));
-    const double fr = sr + a * p.x, fi = si + a * p.y;
+  struct Pre {
+    C2<double> p;
+    double kd, ct, v;
+  };
+  __device__ Pre load(int i) const { return Pre{x[i], kdiag[i], cvt[i], V[i]}; }
+  __device__ double finish(int i, double sr, double si, const Pre &q) const {
+    const double a = q.kd + q.ct * (q.v + g * (q.p.x * q.p.x + q.p.y * q.p.y));
+    const double fr = sr + a * q.p.x, fi = si + a * q.p.y;
     y[i] = C2<double>{fr, fi};
     return kNorm ? fr * fr + fi * fi : 0.0;
   }
