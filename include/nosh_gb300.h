@@ -130,6 +130,15 @@ int nosh_nls_set_precision(nosh_nls nls, int precision);
  * hierarchy; the next rebuild builds a new one. */
 int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size,
                              int smooth_degree, int reuse_period);
+/* SpMV schedule of the handle's operators: NOSH_SPMV_AUTO (default: each
+ * matrix times both schedules once and keeps the faster), NOSH_SPMV_STAGED
+ * (128-row blocks staged into shared memory by bulk copies) or
+ * NOSH_SPMV_WARP (warp-cooperative, a half-warp per row).  Drops the
+ * preconditioner hierarchy. */
+#define NOSH_SPMV_AUTO 0
+#define NOSH_SPMV_STAGED 1
+#define NOSH_SPMV_WARP 2
+int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule);
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int nosh_nls_stream(nosh_nls nls, void **stream);
 

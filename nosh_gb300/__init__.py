@@ -43,6 +43,7 @@ OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN = 1, 2, 3, 4, 5
 ERR_UNSUPPORTED, ERR_MESH, ERR_NO_MEMORY = 6, 7, 8
 PREC_FP64, PREC_MIXED = 0, 1
+SPMV_AUTO, SPMV_STAGED, SPMV_WARP = 0, 1, 2
 NO_TRANS, TRANS = 0, 1
 PREDICT_NONE, PREDICT_SECANT, PREDICT_TANGENT, PREDICT_QUADRATIC, PREDICT_LEARNED, PREDICT_CUBIC = 0, 1, 2, 3, 4, 5
 KERNEL_JACOBIAN, KERNEL_SMOOTHER, KERNEL_ALL = 0, 1, 2
@@ -95,6 +96,7 @@ _SIGS = {
     "nosh_nls_param_name": (_I, [_P, _I, C.c_char_p, C.c_size_t]),
     "nosh_nls_set_precision": (_I, [_P, _I]),
     "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I]),
+    "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
     "nosh_nls_stream": (_I, [_P, C.POINTER(_P)]),
     "nosh_nls_compute_f": (_I, [_P, _P, _P, _P]),
     "nosh_nls_compute_f_norm": (_I, [_P, _P, _P, _P, C.POINTER(_D)]),
@@ -351,6 +353,10 @@ class nls:
         """Preconditioner options (MueLu parameter list of the reference);
         the hierarchy is rebuilt at the next Newton step."""
         _check(_lib.nosh_nls_set_amg_options(self._h, max_levels, coarse_size, smooth_degree, reuse_period))
+
+    def set_spmv_schedule(self, schedule):
+        """SPMV_AUTO, SPMV_STAGED or SPMV_WARP (see nosh_gb300.h)."""
+        _check(_lib.nosh_nls_set_spmv_schedule(self._h, schedule))
 
     def stream(self) -> int:
         s = C.c_void_p()

@@ -709,6 +709,8 @@ struct AmgLevel {
   const int32_t *rp = nullptr, *ci = nullptr;  // level 0: the mesh graph
   DevBuf<int32_t> rp_own, ci_own;
   int cap32 = 0, cap64 = 0;
+  bool warp32 = false, warp64 = false;  // SpMV schedule (tuned on the first refresh)
+  bool tuned32 = false, tuned64 = false;
   // transfer to the next level
   DevBuf<int32_t> agg, mem_ptr, mem_idx, seg_ptr, seg_idx, intra_ptr, intra_idx;
 };
@@ -962,6 +964,19 @@ void Amg::refresh() {
       ++I.nls.launch_count;
     }
   }
+  // SpMV schedule per coarse level, once (needs the level's values)
+  for (int l = 1; l < L; l++) {
+    AmgLevel &A = I.lev[l];
+    bool &tuned = sizeof(T) == 4 ? A.tuned32 : A.tuned64;
+    if (tuned) continue;
+    bool &warp = sizeof(T) == 4 ? A.warp32 : A.warp64;
+    if (I.nls.spmv_schedule == 0)
+      warp = pick_warp_schedule<T>((int)A.n, A.rp, A.ci, I.off<T>(l), sizeof(T) == 4 ? A.cap32 : A.cap64,
+                                   I.nls.red.partials.p, I.nls.red.counter.p, st);
+    else
+      warp = I.nls.spmv_schedule == 2;
+    tuned = true;
+  }
   const AmgLevel &C = I.lev.back();
   const int m2 = (int)(2 * C.n);
   coarse_dense<T><<<div_up(C.n, 128), 128, 0, st>>>(C.n, C.rp, C.ci, I.off<T>(L - 1), I.dia<T>(L - 1),
@@ -991,11 +1006,9 @@ template <typename T, class Op>
 void Amg::Impl::rows(int l, const C2<T> *x, const Op &op) {
   const AmgLevel &A = lev[l];
   const int cap = sizeof(T) == 4 ? A.cap32 : A.cap64;
-  const size_t smem = 2 * stage_bytes<T>(cap);
-  row_block_apply<T, Op><<<row_grid((const void *)row_block_apply<T, Op>, smem, A.n), kRows, smem,
-                            nls.stream>>>(
-      (int)A.n, A.rp, A.ci, off<T>(l), x, cap, op, nls.red.partials.p, nls.red.counter.p,
-      Op::kReduce ? &nls.red.out.p[32] : nullptr);
+  const bool warp = l == 0 ? (sizeof(T) == 4 ? nls.warp32 : nls.warp64) : (sizeof(T) == 4 ? A.warp32 : A.warp64);
+  launch_spmv<T, Op>(warp, (int)A.n, A.rp, A.ci, off<T>(l), x, cap, op, nls.red.partials.p, nls.red.counter.p,
+                     Op::kReduce ? &nls.red.out.p[32] : nullptr, nls.stream);
   ++nls.launch_count;
 }
 

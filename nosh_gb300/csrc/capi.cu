@@ -310,6 +310,16 @@ int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size, int 
   });
 }
 
+int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(schedule >= 0 && schedule <= 2, "unknown SpMV schedule");
+    s.spmv_schedule = schedule;
+    s.tune_schedules();
+    nosh::reset_preconditioner(s);
+  });
+}
+
 int nosh_nls_stream(nosh_nls nls, void **stream) {
   return guarded([&] {
     require(stream != nullptr, "null output");

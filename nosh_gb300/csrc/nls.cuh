@@ -112,6 +112,11 @@ struct NlsImpl {
 
   Reducer red;
   int cap32 = 0, cap64 = 0;  // staged nonzeros per row block (FP32 / FP64)
+  // SpMV schedule of the fine-level operators (spmv.cuh): 0 autotuned, 1
+  // staged row blocks, 2 warp-cooperative; warp32/64 hold the choice
+  int spmv_schedule = 0;
+  bool warp32 = false, warp64 = false;
+  void tune_schedules();
 
   std::unique_ptr<Amg> amg;
   // preconditioner options (amg.cuh AmgOptions), applied when the hierarchy

@@ -232,19 +232,9 @@ int staging_cap(const MeshImpl &m) {
 template <typename T, class Op>
 void launch_rows(const NlsImpl &s, const C2<T> *val, const C2<T> *x, const Op &op, int cap,
                  double *red_out) {
-  const size_t smem = 2 * stage_bytes<T>(cap);
-  static bool attr_set = false;  // per instantiation
-  if (!attr_set) {
-    NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-    attr_set = true;
-  }
-  const int grid = row_grid((const void *)row_block_apply<T, Op>, smem, s.N);
-  row_block_apply<T, Op><<<grid, kRows, smem, s.stream>>>(
-      (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, x, cap, op, s.red.partials.p,
-      s.red.counter.p, red_out);
+  launch_spmv<T, Op>(sizeof(T) == 4 ? s.warp32 : s.warp64, (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, x, cap,
+                     op, s.red.partials.p, s.red.counter.p, red_out, s.stream);
   ++s.launch_count;
-  NOSH_CUDA(cudaGetLastError());
 }
 
 }  // namespace
@@ -259,6 +249,50 @@ __global__ void normalize_phases(int n, double *c) {
 }
 
 namespace dev {
+template <typename T>
+bool pick_warp_schedule(int N, const int32_t *rp, const int32_t *ci, const C2<T> *val, int cap, double *partials,
+                        unsigned *counter, cudaStream_t st) {
+  if (N <= 0) return false;
+  DevBuf<C2<T>> xb, yb;
+  xb.alloc(N);
+  yb.alloc(N);
+  xb.zero(st);
+  PlainOp<T> op{yb.p};
+  cudaEvent_t e0, e1;
+  NOSH_CUDA(cudaEventCreate(&e0));
+  NOSH_CUDA(cudaEventCreate(&e1));
+  float ms[2] = {0.f, 0.f};
+  for (int w = 0; w < 2; w++) {
+    for (int r = 0; r < 2; r++) launch_spmv<T>(w == 1, N, rp, ci, val, xb.p, cap, op, partials, counter, nullptr, st);
+    NOSH_CUDA(cudaEventRecord(e0, st));
+    for (int r = 0; r < 5; r++) launch_spmv<T>(w == 1, N, rp, ci, val, xb.p, cap, op, partials, counter, nullptr, st);
+    NOSH_CUDA(cudaEventRecord(e1, st));
+    NOSH_CUDA(cudaEventSynchronize(e1));
+    NOSH_CUDA(cudaEventElapsedTime(&ms[w], e0, e1));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms[1] < ms[0];
+}
+template bool pick_warp_schedule<float>(int, const int32_t *, const int32_t *, const C2<float> *, int, double *,
+                                        unsigned *, cudaStream_t);
+template bool pick_warp_schedule<double>(int, const int32_t *, const int32_t *, const C2<double> *, int, double *,
+                                         unsigned *, cudaStream_t);
+
+int warp_grid(const void *kernel, int64_t n_rows) {
+  static int sms = 0;
+  if (sms == 0) {
+    int d = 0;
+    NOSH_CUDA(cudaGetDevice(&d));
+    NOSH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d));
+  }
+  int per_sm = 0;
+  NOSH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpThreads, 0));
+  const int64_t blocks = (n_rows + kWarpThreads - 1) / kWarpThreads;
+  const int64_t cap = (int64_t)std::max(per_sm, 1) * sms;
+  return (int)std::max<int64_t>(1, std::min(blocks, cap));
+}
+
 int row_grid(const void *kernel, size_t smem, int64_t n_rows) {
   static int sms = 0;
   if (sms == 0) {
@@ -329,8 +363,23 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
   red.init(div_up(N, kRows) + div_up(N, 256) + 1024, 64, s);
   cap32 = staging_cap<float>(*m);
   cap64 = staging_cap<double>(*m);
+  tune_schedules();
   for (double c : m->h_cv) cv_sum += c;
   sync();
+}
+
+void NlsImpl::tune_schedules() {
+  sync();
+  if (spmv_schedule == 1) {
+    warp32 = warp64 = false;
+  } else if (spmv_schedule == 2) {
+    warp32 = warp64 = true;
+  } else {
+    warp32 = pick_warp_schedule<float>((int)N, mesh->d_rp.p, mesh->d_ci.p, d_keo32.p, cap32, red.partials.p,
+                                       red.counter.p, stream);
+    warp64 = pick_warp_schedule<double>((int)N, mesh->d_rp.p, mesh->d_ci.p, d_keo64.p, cap64, red.partials.p,
+                                        red.counter.p, stream);
+  }
 }
 
 NlsImpl::~NlsImpl() {

@@ -184,11 +184,8 @@ void Minres<T>::iteration(int j) {
   const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
   JacMinresOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, d, zn, wa, wb, wc, x.p, &d->done};
   s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
-  const size_t smem = 2 * stage_bytes<T>(cap);
-  row_block_apply<T, JacMinresOp<T>><<<row_grid((const void *)row_block_apply<T, JacMinresOp<T>>, smem, s.N),
-                                       kRows, smem, st>>>(
-      (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, (const C2<T> *)zc, cap, op, s.red.partials.p,
-      s.red.counter.p, &d->zu);
+  launch_spmv<T>(sizeof(T) == 4 ? s.warp32 : s.warp64, (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val,
+                 (const C2<T> *)zc, cap, op, s.red.partials.p, s.red.counter.p, &d->zu, st);
   ++s.launch_count;
   // bytes per vertex: z, diag block, u (+ the fused w/x update: z_prev, w2,
   // w, x read; w1, x written)

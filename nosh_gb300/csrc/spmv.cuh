@@ -276,9 +276,128 @@ __global__ void __launch_bounds__(kRows)
   }
 }
 
+// Warp-cooperative schedule of the same SpMV + epilogue (no staging): a
+// warp owns 32 consecutive rows and walks them in 16 pairs, a half-warp per
+// row, each lane loading one nonzero (coalesced: a row's nonzeros are
+// contiguous) and gathering its x; half-warp shuffles reduce the row and
+// hand the sum to the row's own lane, so the epilogue runs on all 32 lanes
+// with coalesced accesses.  Few registers and no shared memory: high
+// occupancy for latency hiding.  kWarpThreads threads per CTA, persistent.
+constexpr int kWarpThreads = 256;
+template <typename T, class Op>
+__global__ void __launch_bounds__(kWarpThreads)
+    row_warp_apply(int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                   const C2<T> *__restrict__ val, const C2<T> *__restrict__ x, Op op, double *partials,
+                   unsigned *counter, double *red_out) {
+  using A = typename Acc<T>::type;
+  if (halted(op)) return;
+  const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4;
+  const int nwb = (N + 31) / 32;
+  const int wpb = kWarpThreads / 32;
+  A part = 0;
+  for (int wb = blockIdx.x * wpb + (threadIdx.x >> 5); wb < nwb; wb += gridDim.x * wpb) {
+    const int r0 = wb * 32;
+    const int row = r0 + lane;
+    typename Op::Pre pre{};
+    if (row < N) pre = op.load(row);
+    // row pointers of the 32 rows and the block end
+    const int beg = __ldg(rp + min(row, N));
+    const int bend = __ldg(rp + min(r0 + 32, N));
+    A msr = 0, msi = 0;
+    // two batches of 8 row pairs: the column ids and values of a batch are
+    // loaded together, then all its x gathers, so a batch costs two memory
+    // round trips; rows longer than 16 nonzeros finish in a tail loop
+#pragma unroll
+    for (int p0 = 0; p0 < 16; p0 += 8) {
+      int k[8], e[8];
+      int32_t c[8];
+      C2<T> v[8], xv[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int rr = 2 * (p0 + q) + half;
+        const int b = __shfl_sync(0xffffffffu, beg, rr);
+        const int e1 = __shfl_sync(0xffffffffu, beg, (rr + 1) & 31);
+        e[q] = rr < 31 ? e1 : bend;
+        k[q] = b + hl;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        c[q] = 0;
+        v[q] = C2<T>{0, 0};
+        if (k[q] < e[q]) {
+          c[q] = __ldg(ci + k[q]);
+          v[q] = ldg(val + k[q]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) xv[q] = k[q] < e[q] ? ldg(x + c[q]) : C2<T>{0, 0};
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        A sr = v[q].x * xv[q].x - v[q].y * xv[q].y;
+        A si = v[q].x * xv[q].y + v[q].y * xv[q].x;
+        for (int kk = k[q] + 16; kk < e[q]; kk += 16) {
+          const C2<T> vv = ldg(val + kk);
+          const C2<T> xx = ldg(x + __ldg(ci + kk));
+          sr += vv.x * xx.x - vv.y * xx.y;
+          si += vv.x * xx.y + vv.y * xx.x;
+        }
+#pragma unroll
+        for (int off = 8; off > 0; off >>= 1) {
+          sr += __shfl_xor_sync(0xffffffffu, sr, off);
+          si += __shfl_xor_sync(0xffffffffu, si, off);
+        }
+        // lanes 2p and 2p+1 take the sums of halves 0 and 1
+        const A tr = __shfl_sync(0xffffffffu, sr, (lane & 1) << 4);
+        const A ti = __shfl_sync(0xffffffffu, si, (lane & 1) << 4);
+        if ((lane >> 1) == p0 + q) {
+          msr = tr;
+          msi = ti;
+        }
+      }
+    }
+    if (row < N) part += (A)op.finish(row, msr, msi, pre);
+  }
+  if (Op::kReduce) {
+    double total = 0.0;
+    if (grid_reduce((double)part, partials, counter, red_out, &total)) run_hook(op, total);
+  }
+}
+
+// Resident CTAs of row_warp_apply on the device, capped by the work.
+int warp_grid(const void *kernel, int64_t n_rows);
+
 // Grid for a persistent row kernel: the resident capacity of the device for
 // this kernel and shared-memory size, capped by the number of row blocks.
 int row_grid(const void *kernel, size_t smem, int64_t n_rows);
+
+// Launch the SpMV + epilogue over an off-diagonal CSR with one of the two
+// schedules (warp: row_warp_apply, else the staged row_block_apply with
+// staging capacity cap).
+template <typename T, class Op>
+void launch_spmv(bool warp, int N, const int32_t *rp, const int32_t *ci, const C2<T> *val, const C2<T> *x,
+                 int cap, const Op &op, double *partials, unsigned *counter, double *red_out, cudaStream_t st) {
+  if (warp) {
+    const int grid = warp_grid((const void *)row_warp_apply<T, Op>, N);
+    row_warp_apply<T, Op><<<grid, kWarpThreads, 0, st>>>(N, rp, ci, val, x, op, partials, counter, red_out);
+  } else {
+    static bool attr_set = false;  // per instantiation; first call precedes any capture
+    if (!attr_set) {
+      NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     100 * 1024));
+      attr_set = true;
+    }
+    const size_t smem = 2 * stage_bytes<T>(cap);
+    row_block_apply<T, Op><<<row_grid((const void *)row_block_apply<T, Op>, smem, N), kRows, smem, st>>>(
+        N, rp, ci, val, x, cap, op, partials, counter, red_out);
+  }
+  NOSH_CUDA(cudaGetLastError());
+}
+
+// The faster schedule for one matrix: both are timed on y = A x (CUDA
+// events, after a warm-up) once, when the matrix structure is set up.
+template <typename T>
+bool pick_warp_schedule(int N, const int32_t *rp, const int32_t *ci, const C2<T> *val, int cap, double *partials,
+                        unsigned *counter, cudaStream_t st);
 
 // ---- epilogues --------------------------------------------------------
 // y = K x : diagonal K_ii = sum of incident alpha (real)
