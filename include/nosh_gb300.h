@@ -130,6 +130,21 @@ int nosh_nls_set_precision(nosh_nls nls, int precision);
  * hierarchy; the next rebuild builds a new one. */
 int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size,
                              int smooth_degree, int reuse_period);
+/* Batched independent solves (many meshes in one handle): the handle's
+ * mesh is the disjoint union of num_systems meshes, system s owning the
+ * vertices [vertex_offsets[s], vertex_offsets[s+1]) (no edge may join two
+ * systems).  System s uses mu[s] in its KEO; the mu entry of the parameter
+ * vector is then unused.  Every kernel runs over all systems at once, the
+ * residual norms are per system (one CTA each), a Newton solve ends when
+ * every system reaches ||F_s|| <= tol (stats->f_norm is the largest) and
+ * converged systems receive zero Newton updates.  The AMG hierarchy keeps
+ * systems apart (its coarsest level is block diagonal, one dense block per
+ * system).  Continuation handles reject a batched handle: the gauge phase of
+ * each system is its own. */
+int nosh_nls_set_systems(nosh_nls nls, int64_t num_systems,
+                         const int64_t *vertex_offsets, const double *mu);
+/* Per-system ||F_s||_2 of the last residual a Newton solve evaluated. */
+int nosh_nls_system_norms(nosh_nls nls, double *norms);
 /* SpMV schedule of the handle's operators: NOSH_SPMV_AUTO (default: each
  * matrix times both schedules once and keeps the faster), NOSH_SPMV_STAGED
  * (128-row blocks staged into shared memory by bulk copies) or

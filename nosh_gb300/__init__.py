@@ -97,6 +97,8 @@ _SIGS = {
     "nosh_nls_set_precision": (_I, [_P, _I]),
     "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I]),
     "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
+    "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
+    "nosh_nls_system_norms": (_I, [_P, _P]),
     "nosh_nls_stream": (_I, [_P, C.POINTER(_P)]),
     "nosh_nls_compute_f": (_I, [_P, _P, _P, _P]),
     "nosh_nls_compute_f_norm": (_I, [_P, _P, _P, _P, C.POINTER(_D)]),
@@ -353,6 +355,23 @@ class nls:
         """Preconditioner options (MueLu parameter list of the reference);
         the hierarchy is rebuilt at the next Newton step."""
         _check(_lib.nosh_nls_set_amg_options(self._h, max_levels, coarse_size, smooth_degree, reuse_period))
+
+    def set_systems(self, vertex_offsets, mu):
+        """Batched independent solves: the mesh is the disjoint union of
+        len(mu) systems, system s owning vertices [offsets[s], offsets[s+1])
+        and using its own mu (see nosh_nls_set_systems)."""
+        off = np.ascontiguousarray(vertex_offsets, np.int64)
+        mu = np.ascontiguousarray(mu, np.float64)
+        if off.size != mu.size + 1:
+            raise ValueError("need len(mu) + 1 offsets")
+        _check(_lib.nosh_nls_set_systems(self._h, mu.size, _ptr(off), _ptr(mu)))
+        self.num_systems = mu.size
+
+    def system_norms(self):
+        """Per-system ||F_s|| of the last residual a Newton solve evaluated."""
+        out = np.empty(self.num_systems)
+        _check(_lib.nosh_nls_system_norms(self._h, _ptr(out)))
+        return out
 
     def set_spmv_schedule(self, schedule):
         """SPMV_AUTO, SPMV_STAGED or SPMV_WARP (see nosh_gb300.h)."""

@@ -44,7 +44,16 @@ struct HostLevel {
   std::vector<int32_t> mem_ptr, mem_idx;  // coarse node -> fine nodes
   std::vector<int32_t> seg_ptr, seg_idx;  // coarse nonzero -> fine nonzeros
   std::vector<int32_t> intra_ptr, intra_idx;  // coarse node -> fine intra nnz
+  // independent systems (batched solves): nodes of system s are
+  // [soff[s], soff[s+1]); a single system has soff = {0, n}
+  std::vector<int64_t> soff;
 };
+
+int64_t max_block(const HostLevel &L) {
+  int64_t m = 0;
+  for (size_t s = 0; s + 1 < L.soff.size(); s++) m = std::max(m, L.soff[s + 1] - L.soff[s]);
+  return m;
+}
 
 // Greedy aggregation on the strong graph (deterministic, vertex order):
 // 1) a vertex whose strong neighbours are all free roots an aggregate with
@@ -96,6 +105,23 @@ void coarsen(HostLevel &F, HostLevel &C) {
   const int64_t n = F.n;
   const int64_t na = aggregate(F, F.agg);
   C.n = na;
+  // aggregates never cross systems (no edges between them); number them
+  // system by system so every level keeps contiguous system ranges
+  {
+    const int64_t ns = (int64_t)F.soff.size() - 1;
+    std::vector<int32_t> asys(na, 0);
+    for (int64_t sy = 0; sy < ns; sy++)
+      for (int64_t i = F.soff[sy]; i < F.soff[sy + 1]; i++) asys[F.agg[i]] = (int32_t)sy;
+    std::vector<int32_t> order(na);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return asys[a] < asys[b]; });
+    std::vector<int32_t> renum(na);
+    for (int64_t q = 0; q < na; q++) renum[order[q]] = (int32_t)q;
+    for (int64_t i = 0; i < n; i++) F.agg[i] = renum[F.agg[i]];
+    C.soff.assign(ns + 1, 0);
+    for (int64_t a = 0; a < na; a++) C.soff[asys[order[a]] + 1]++;
+    for (int64_t sy = 0; sy < ns; sy++) C.soff[sy + 1] += C.soff[sy];
+  }
   // members
   F.mem_ptr.assign(na + 1, 0);
   for (int64_t i = 0; i < n; i++) F.mem_ptr[F.agg[i] + 1]++;
@@ -468,26 +494,32 @@ __global__ void prolong_kernel(int64_t n, const int32_t *__restrict__ agg,
 // Dense real matrix (m = 2n) of the coarsest level from its compact form.
 template <typename T>
 __global__ void coarse_dense(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                             const C2<T> *__restrict__ off, const T *__restrict__ dia, double *A) {
+                             const C2<T> *__restrict__ off, const T *__restrict__ dia,
+                             const int32_t *__restrict__ bstart, const int64_t *__restrict__ rowoff,
+                             const int32_t *__restrict__ bdim, double *A) {
+  // the coarsest level is block diagonal (one block per system): node i's
+  // two real rows live in its block's packed dense matrix
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t m = 2 * n;
-  double *r0 = A + (2 * i) * m, *r1 = A + (2 * i + 1) * m;
+  const int64_t m = bdim[2 * i];
+  const int64_t s0 = bstart[2 * i];  // first real row of the block
+  double *r0 = A + rowoff[2 * i], *r1 = A + rowoff[2 * i + 1];
   for (int64_t j = 0; j < m; j++) {
     r0[j] = 0.0;
     r1[j] = 0.0;
   }
-  r0[2 * i] = dia[3 * i];
-  r0[2 * i + 1] = dia[3 * i + 2];
-  r1[2 * i] = dia[3 * i + 2];
-  r1[2 * i + 1] = dia[3 * i + 1];
+  const int64_t li = 2 * i - s0;
+  r0[li] = dia[3 * i];
+  r0[li + 1] = dia[3 * i + 2];
+  r1[li] = dia[3 * i + 2];
+  r1[li + 1] = dia[3 * i + 1];
   for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
-    const int32_t j = ci[k];
+    const int64_t lj = 2 * (int64_t)ci[k] - s0;
     const C2<T> v = off[k];  // block [[re, -im], [im, re]]
-    r0[2 * j] = v.x;
-    r0[2 * j + 1] = -v.y;
-    r1[2 * j] = v.y;
-    r1[2 * j + 1] = v.x;
+    r0[lj] = v.x;
+    r0[lj + 1] = -v.y;
+    r1[lj] = v.y;
+    r1[lj + 1] = v.x;
   }
 }
 
@@ -497,7 +529,12 @@ __global__ void coarse_dense(int64_t n, const int32_t *__restrict__ rp, const in
 // is well conditioned); writes the FP64 and FP32 copies.
 constexpr int kDenseSmem = 128;
 template <typename C>
-__global__ void gauss_jordan_spd_smem(int m, double *A, float *Af, int *err) {
+__global__ void gauss_jordan_spd_smem(const int64_t *__restrict__ boff, const int32_t *__restrict__ bd, double *Ag,
+                                      float *Afg, int *err) {
+  // one CTA per diagonal block of the coarsest level
+  const int m = bd[blockIdx.x];
+  double *A = Ag + boff[blockIdx.x];
+  float *Af = Afg + boff[blockIdx.x];
   extern __shared__ __align__(16) unsigned char gj_raw[];
   C *S = reinterpret_cast<C *>(gj_raw);
   __shared__ C ip_s;
@@ -529,8 +566,12 @@ __global__ void gauss_jordan_spd_smem(int m, double *A, float *Af, int *err) {
   }
 }
 
-// The same in global memory for larger coarsest levels.
-__global__ void gauss_jordan_spd(int m, double *A, float *Af, int *err) {
+// The same in global memory for larger blocks.
+__global__ void gauss_jordan_spd(const int64_t *__restrict__ boff, const int32_t *__restrict__ bd, double *Ag,
+                                 float *Afg, int *err) {
+  const int m = bd[blockIdx.x];
+  double *A = Ag + boff[blockIdx.x];
+  float *Af = Afg + boff[blockIdx.x];
   for (int k = 0; k < m; k++) {
     __syncthreads();
     const double piv = A[(int64_t)k * m + k];
@@ -553,13 +594,29 @@ __global__ void gauss_jordan_spd(int m, double *A, float *Af, int *err) {
   for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += blockDim.x) Af[q] = (float)A[q];
 }
 
+// Packed block-diagonal dense inverse: real row i of the coarsest level is
+// row rowoff[i] of the packed array, its block starts at real row bstart[i]
+// and has bdim[i] columns.
+struct DenseMap {
+  const int64_t *rowoff;
+  const int32_t *bstart, *bdim;
+};
 template <typename T>
-__global__ void dense_matvec(int m, const T *__restrict__ Ainv, const T *__restrict__ b, T *__restrict__ x) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    T s = 0;
-    for (int j = 0; j < m; j++) s += Ainv[(int64_t)i * m + j] * b[j];
-    x[i] = s;
-  }
+__device__ __forceinline__ T dense_row(const DenseMap &D, const T *__restrict__ Ainv, int64_t i,
+                                       const T *__restrict__ b) {
+  const T *a = Ainv + D.rowoff[i];
+  const T *bb = b + D.bstart[i];
+  const int m = D.bdim[i];
+  T s = 0;
+  for (int j = 0; j < m; j++) s += a[j] * bb[j];
+  return s;
+}
+
+template <typename T>
+__global__ void dense_matvec(int m, const T *__restrict__ Ainv, DenseMap D, const T *__restrict__ b,
+                             T *__restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    x[i] = dense_row(D, Ainv, i, b);
 }
 
 // ---- single-CTA tail: every level from `lt` down, in one launch
@@ -587,7 +644,8 @@ __device__ __forceinline__ void tail_row_sum(const LevelDesc<T> &A, int64_t i, c
 
 template <typename T>
 __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restrict__ lv, int lt, int L,
-                                                    int deg, const T *__restrict__ Ainv, const int *halt) {
+                                                    int deg, const T *__restrict__ Ainv, DenseMap D,
+                                                    const int *halt) {
   if (halt && *halt >= 2) return;
   const int tid = threadIdx.x, bs = blockDim.x;
   for (int l = lt; l < L - 1; l++) {
@@ -631,11 +689,7 @@ __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restri
     const int m = (int)(2 * C.n);
     const T *b = reinterpret_cast<const T *>(C.b);
     T *x = reinterpret_cast<T *>(C.x);
-    for (int i = tid; i < m; i += bs) {
-      T s = 0;
-      for (int j = 0; j < m; j++) s += Ainv[(int64_t)i * m + j] * b[j];
-      x[i] = s;
-    }
+    for (int i = tid; i < m; i += bs) x[i] = dense_row(D, Ainv, i, b);
     __syncthreads();
   }
   for (int l = L - 2; l >= lt; l--) {
@@ -737,6 +791,12 @@ struct Amg::Impl {
   DevBuf<double> lmax;
   DevBuf<double> dense;  // coarsest (2n)^2 FP64
   DevBuf<float> densef;
+  // packed block-diagonal coarsest inverse: per block (offset, dim), per real
+  // row (offset, block start, dim)
+  DevBuf<int64_t> blk_off, row_off;
+  DevBuf<int32_t> blk_dim, row_start, row_dim;
+  int nblk = 0, max_dim = 0;
+  DenseMap dmap() const { return DenseMap{row_off.p, row_start.p, row_dim.p}; }
   DevBuf<int> err;
   Impl(NlsImpl &s, const AmgOptions &o) : nls(s), opt(o) {}
   template <typename T> AmgVals<T> &vals();
@@ -783,7 +843,13 @@ Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
     H[0].off.resize(2 * m.E);
     for (int64_t k = 0; k < 2 * m.E; k++) H[0].off[k] = {off[k].x, off[k].y};
   }
-  while ((int)H.size() < o.max_levels && H.back().n > o.coarse_size) {
+  if (s.sys_off.empty())
+    H[0].soff = {0, (int64_t)m.N};
+  else
+    H[0].soff = s.sys_off;
+  // coarsen until every system's coarsest block is small (one system: the
+  // whole level)
+  while ((int)H.size() < o.max_levels && max_block(H.back()) > o.coarse_size) {
     HostLevel C;
     coarsen(H.back(), C);
     if (C.n >= H.back().n) {  // no coarsening progress: stop here
@@ -792,8 +858,8 @@ Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
     }
     H.push_back(std::move(C));
   }
-  NOSH_CHECK(H.back().n <= 512, NOSH_ERR_INVALID,
-             "AMG coarsening stalled at " + std::to_string(H.back().n) + " nodes");
+  NOSH_CHECK(max_block(H.back()) <= 512, NOSH_ERR_INVALID,
+             "AMG coarsening stalled at " + std::to_string(max_block(H.back())) + " nodes per system");
   const int L = (int)H.size();
   I.lev.resize(L);
   for (int l = 0; l < L; l++) {
@@ -836,9 +902,36 @@ Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
   if (I.lt < 1) I.lt = L - 1;
   I.lmax_bits.alloc(L);
   I.lmax.alloc(L);
-  const int64_t m2 = 2 * I.lev.back().n;
-  I.dense.alloc(m2 * m2);
-  I.densef.alloc(m2 * m2);
+  {
+    // the coarsest level's dense inverse: one packed block per system
+    const HostLevel &Hc = H.back();
+    const int64_t ns = (int64_t)Hc.soff.size() - 1;
+    std::vector<int64_t> boff, roff;
+    std::vector<int32_t> bdim, rstart, rdim;
+    int64_t total = 0;
+    for (int64_t sy = 0; sy < ns; sy++) {
+      const int64_t n0 = Hc.soff[sy], nb = Hc.soff[sy + 1] - n0;
+      if (nb == 0) continue;
+      const int32_t m = (int32_t)(2 * nb);
+      boff.push_back(total);
+      bdim.push_back(m);
+      for (int32_t r = 0; r < m; r++) {
+        roff.push_back(total + (int64_t)r * m);
+        rstart.push_back((int32_t)(2 * n0));
+        rdim.push_back(m);
+      }
+      total += (int64_t)m * m;
+      I.max_dim = std::max<int>(I.max_dim, m);
+    }
+    I.nblk = (int)boff.size();
+    I.blk_off.upload(boff, st);
+    I.blk_dim.upload(bdim, st);
+    I.row_off.upload(roff, st);
+    I.row_start.upload(rstart, st);
+    I.row_dim.upload(rdim, st);
+    I.dense.alloc(total);
+    I.densef.alloc(total);
+  }
   I.err.alloc(1);
   I.err.zero(st);
   NOSH_CUDA(cudaFuncSetAttribute(gauss_jordan_spd_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -978,14 +1071,14 @@ void Amg::refresh() {
     tuned = true;
   }
   const AmgLevel &C = I.lev.back();
-  const int m2 = (int)(2 * C.n);
   coarse_dense<T><<<div_up(C.n, 128), 128, 0, st>>>(C.n, C.rp, C.ci, I.off<T>(L - 1), I.dia<T>(L - 1),
-                                                     I.dense.p);
+                                                     I.row_start.p, I.row_off.p, I.row_dim.p, I.dense.p);
   ++I.nls.launch_count;
-  if (m2 <= kDenseSmem)
-    gauss_jordan_spd_smem<T><<<1, 1024, m2 * m2 * sizeof(T), st>>>(m2, I.dense.p, I.densef.p, I.err.p);
+  if (I.max_dim <= kDenseSmem)
+    gauss_jordan_spd_smem<T><<<I.nblk, 1024, (size_t)I.max_dim * I.max_dim * sizeof(T), st>>>(
+        I.blk_off.p, I.blk_dim.p, I.dense.p, I.densef.p, I.err.p);
   else
-    gauss_jordan_spd<<<1, 1024, 0, st>>>(m2, I.dense.p, I.densef.p, I.err.p);
+    gauss_jordan_spd<<<I.nblk, 1024, 0, st>>>(I.blk_off.p, I.blk_dim.p, I.dense.p, I.densef.p, I.err.p);
   ++I.nls.launch_count;
   NOSH_CUDA(cudaGetLastError());
 }
@@ -1055,7 +1148,7 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
                                                        V.b[l + 1].p, halt);
     ++nls.launch_count;
-    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), halt);
+    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), halt);
     ++nls.launch_count;
   }
   prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x, halt);
@@ -1089,7 +1182,7 @@ void Amg::apply(const T *r, T *z) {
   const AmgLevel &A = I.lev[0];
   if (L == 1) {
     const int m2 = (int)(2 * A.n);
-    dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, I.dense_inv<T>(), r, z);
+    dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, I.dense_inv<T>(), I.dmap(), r, z);
     ++I.nls.launch_count;
     NOSH_CUDA(cudaGetLastError());
     return;

@@ -310,6 +310,24 @@ int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size, int 
   });
 }
 
+int nosh_nls_set_systems(nosh_nls nls, int64_t num_systems, const int64_t *vertex_offsets, const double *mu) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(num_systems >= 1 && vertex_offsets && mu, "null argument");
+    s.set_systems(vertex_offsets, num_systems, mu);
+    nosh::reset_preconditioner(s);
+  });
+}
+
+int nosh_nls_system_norms(nosh_nls nls, double *norms) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(norms != nullptr, "null argument");
+    require(!s.sys_off.empty(), "no systems set");
+    std::copy(s.h_sys_norm.begin(), s.h_sys_norm.end(), norms);
+  });
+}
+
 int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule) {
   return guarded([&] {
     auto &s = N(nls);
@@ -584,6 +602,7 @@ int nosh_continuation_create(nosh_nls nls, const double *x0, double mu0, nosh_co
   return guarded([&] {
     auto &s = N(nls);
     require(out != nullptr && x0 != nullptr, "null argument");
+    require(s.sys_off.empty(), "continuation needs a single-system handle");
     *out = nullptr;
     auto *h = new nosh_continuation_s{nullptr};
     try {

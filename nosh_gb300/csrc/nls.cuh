@@ -118,6 +118,21 @@ struct NlsImpl {
   bool warp32 = false, warp64 = false;
   void tune_schedules();
 
+  // independent systems (batched solves): vertices [sys_off[s], sys_off[s+1])
+  // form system s, which uses its own mu (d_mu_sys) in the KEO; empty for
+  // one system.  Edges never join two systems.
+  std::vector<int64_t> sys_off;
+  DevBuf<int64_t> d_sys_off;
+  DevBuf<int32_t> d_esys;          // E: system of each edge
+  DevBuf<double> d_mu_sys, d_sys_norm;  // per system
+  std::vector<double> h_sys_norm;
+  int64_t nsys() const { return sys_off.empty() ? 1 : (int64_t)sys_off.size() - 1; }
+  void set_systems(const int64_t *offsets, int64_t num, const double *mu);
+  // per-system ||F_s|| of f (2N) into h_sys_norm; returns the largest
+  double system_norms(const double *f);
+  // zero the rows of f that belong to systems with ||F_s|| <= tol
+  void mask_converged(double *f, double tol);
+
   std::unique_ptr<Amg> amg;
   // preconditioner options (amg.cuh AmgOptions), applied when the hierarchy
   // is next built

@@ -4,6 +4,8 @@
 #include <cstring>
 
 #include "amg.cuh"
+#include <algorithm>
+
 #include "nls.cuh"
 #include "spmv.cuh"
 
@@ -60,14 +62,17 @@ __global__ void vertex_fields_kernel(int64_t N, const int32_t *__restrict__ rp,
 // a = mu p_e, complex coefficient -alpha e^{-ia} at (v0,v1) and its
 // conjugate at (v1,v0), written through the edge -> nonzero scatter map.
 // The diagonal (sum alpha) is mu-independent and kept separately.
+// mu_sys / esys (optional): the edge's system supplies its own mu
 __global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha,
                                const double *__restrict__ p, double mu,
                                const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
-                               C2<double> *__restrict__ val) {
+                               C2<double> *__restrict__ val, const double *__restrict__ mu_sys,
+                               const int32_t *__restrict__ esys) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= E) return;
+  const double m = mu_sys ? mu_sys[esys[e]] : mu;
   double s, c;
-  sincos(mu * p[e], &s, &c);
+  sincos(m * p[e], &s, &c);
   const double al = alpha[e];
   val[pf[e]] = C2<double>{-al * c, al * s};
   val[pb[e]] = C2<double>{-al * c, -al * s};
@@ -76,11 +81,13 @@ __global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha,
 __global__ void keo_assemble32(int64_t E, const float *__restrict__ alpha,
                                const float *__restrict__ p, float mu,
                                const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
-                               C2<float> *__restrict__ val) {
+                               C2<float> *__restrict__ val, const double *__restrict__ mu_sys,
+                               const int32_t *__restrict__ esys) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= E) return;
+  const float m = mu_sys ? (float)mu_sys[esys[e]] : mu;
   float s, c;
-  sincosf(mu * p[e], &s, &c);
+  sincosf(m * p[e], &s, &c);
   const float al = alpha[e];
   val[pf[e]] = C2<float>{-al * c, al * s};
   val[pb[e]] = C2<float>{-al * c, -al * s};
@@ -93,11 +100,13 @@ __global__ void keo_assemble32(int64_t E, const float *__restrict__ alpha,
 __global__ void dkeo_assemble64(int64_t E, const double *__restrict__ alpha,
                                 const double *__restrict__ p, double mu, double dscale,
                                 const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
-                                C2<double> *__restrict__ val) {
+                                C2<double> *__restrict__ val, const double *__restrict__ mu_sys,
+                                const int32_t *__restrict__ esys) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= E) return;
+  const double m = mu_sys ? mu_sys[esys[e]] : mu;
   double s, c;
-  sincos(mu * p[e], &s, &c);
+  sincos(m * p[e], &s, &c);
   const double w = alpha[e] * p[e] * dscale;
   // complex v0 - i v1 at (v0,v1): w sin a + i w cos a; conjugate at (v1,v0)
   val[pf[e]] = C2<double>{w * s, w * c};
@@ -368,6 +377,72 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
   sync();
 }
 
+void NlsImpl::set_systems(const int64_t *offsets, int64_t num, const double *mu) {
+  NOSH_CHECK(num >= 1 && offsets[0] == 0 && offsets[num] == N, NOSH_ERR_INVALID,
+             "system offsets must run from 0 to the number of vertices");
+  for (int64_t q = 0; q < num; q++)
+    NOSH_CHECK(offsets[q + 1] > offsets[q], NOSH_ERR_INVALID, "every system needs at least one vertex");
+  // edge -> system, and no edge between two systems
+  std::vector<int32_t> es(E);
+  const std::vector<int32_t> &ed = mesh->edges;  // 2E, sorted pairs
+  for (int64_t e = 0; e < E; e++) {
+    const int64_t a = ed[2 * e], b = ed[2 * e + 1];
+    const int64_t sa = std::upper_bound(offsets, offsets + num + 1, a) - offsets - 1;
+    const int64_t sb = std::upper_bound(offsets, offsets + num + 1, b) - offsets - 1;
+    NOSH_CHECK(sa == sb, NOSH_ERR_INVALID, "an edge joins two systems");
+    es[e] = (int32_t)sa;
+  }
+  sys_off.assign(offsets, offsets + num + 1);
+  d_sys_off.upload(sys_off, stream);
+  d_esys.upload(es, stream);
+  d_mu_sys.upload(mu, num, stream);
+  d_sys_norm.alloc(num);
+  h_sys_norm.assign(num, 0.0);
+  keo_mu = std::nan("");
+  dkeo_mu = std::nan("");
+  sync();
+}
+
+namespace {
+// ||F_s||^2 of each system: one CTA per system (its rows are contiguous)
+__global__ void system_norms_kernel(const int64_t *__restrict__ off, const C2<double> *__restrict__ f,
+                                    double *__restrict__ out) {
+  __shared__ double s32[32];
+  const int64_t r0 = off[blockIdx.x], r1 = off[blockIdx.x + 1];
+  double a = 0.0;
+  for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    const C2<double> v = f[i];
+    a += v.x * v.x + v.y * v.y;
+  }
+  a = dev::block_sum(a, s32);
+  if (threadIdx.x == 0) out[blockIdx.x] = sqrt(a);
+}
+__global__ void mask_systems_kernel(const int64_t *__restrict__ off, const double *__restrict__ nrm, double tol,
+                                    C2<double> *__restrict__ f) {
+  if (!(nrm[blockIdx.x] <= tol)) return;
+  for (int64_t i = off[blockIdx.x] + threadIdx.x; i < off[blockIdx.x + 1]; i += blockDim.x)
+    f[i] = C2<double>{0.0, 0.0};
+}
+}  // namespace
+
+double NlsImpl::system_norms(const double *f) {
+  const int64_t ns = nsys();
+  system_norms_kernel<<<(unsigned)ns, 256, 0, stream>>>(d_sys_off.p, (const C2<double> *)f, d_sys_norm.p);
+  ++launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  d_sys_norm.download(h_sys_norm.data(), ns, stream);
+  sync();
+  double mx = 0.0;
+  for (double v : h_sys_norm) mx = std::max(mx, v);
+  return mx;
+}
+
+void NlsImpl::mask_converged(double *f, double tol) {
+  mask_systems_kernel<<<(unsigned)nsys(), 256, 0, stream>>>(d_sys_off.p, d_sys_norm.p, tol, (C2<double> *)f);
+  ++launch_count;
+  NOSH_CUDA(cudaGetLastError());
+}
+
 void NlsImpl::tune_schedules() {
   sync();
   if (spmv_schedule == 1) {
@@ -389,12 +464,13 @@ NlsImpl::~NlsImpl() {
 }
 
 void NlsImpl::keo_refill(double mu) {
+  const double *ms = sys_off.empty() ? nullptr : d_mu_sys.p;
   keo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, mesh->d_pos_fwd.p,
-                                                      mesh->d_pos_bwd.p, d_keo64.p);
+                                                      mesh->d_pos_bwd.p, d_keo64.p, ms, d_esys.p);
   ++launch_count;
   keo_assemble32<<<div_up(E, 256), 256, 0, stream>>>(E, d_alphaf.p, d_pf.p, (float)mu,
                                                       mesh->d_pos_fwd.p, mesh->d_pos_bwd.p,
-                                                      d_keo32.p);
+                                                      d_keo32.p, ms, d_esys.p);
   ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   keo_mu = mu;
@@ -403,7 +479,7 @@ void NlsImpl::keo_refill(double mu) {
 void NlsImpl::dkeo_refill(double mu) {
   dkeo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(
       E, d_alpha.p, d_p.p, mu, deriv_param == "mu" ? 1.0 : 0.0, mesh->d_pos_fwd.p,
-      mesh->d_pos_bwd.p, d_dkeo64.p);
+      mesh->d_pos_bwd.p, d_dkeo64.p, sys_off.empty() ? nullptr : d_mu_sys.p, d_esys.p);
   ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   dkeo_mu = mu;

@@ -388,6 +388,9 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
   const bool polish = opt.refine > 0.0 && fn > 4.0 * opt.refine;
   for (int it = 0; it < opt.max_newton && (fn > opt.tol || (it == 0 && polish)); it++) {
     rebuild_operators<T>(s, ns.psi.p, g, mu);
+    // batched systems: converged ones get a zero right-hand side (their
+    // Newton update is zero: the Jacobian is block diagonal)
+    if (!s.sys_off.empty()) s.mask_converged(ns.f.p, opt.tol);
     neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.f.p, b.p);
     ++s.launch_count;
     double eta;
@@ -413,6 +416,7 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     ++s.launch_count;
     fn_prev = fn;
     fn = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+    if (!s.sys_off.empty()) fn = s.system_norms(ns.f.p);
     st.newton_iters = it + 1;
     st.f_norm = fn;
     if (opt.verbose)
@@ -429,6 +433,8 @@ void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_ne
                  nosh_newton_stats &st, double f0) {
   st = nosh_newton_stats{};
   st.f_norm0 = f0 >= 0.0 ? f0 : residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+  // batched systems: the largest per-system norm decides convergence
+  if (!s.sys_off.empty()) st.f_norm0 = s.system_norms(ns.f.p);
   st.f_norm = st.f_norm0;
   NOSH_CHECK(!std::isnan(st.f_norm0), NOSH_ERR_NAN, "initial residual is NaN");
   if (opt.precision == NOSH_PREC_FP64) newton_loop<double>(s, ns, g, mu, opt, st);
