@@ -490,155 +490,297 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
   }
 }
 
-// dA_i = sum_j dM_i [P_ij > 0]; also block partials of dW_c (4 x 64) and
-// db_m (64): rows of the partial buffer hold 5 x 64 floats per CTA
-__global__ void edge_backward_a(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                                const float *__restrict__ ef, const __nv_bfloat16 *__restrict__ A,
-                                const __nv_bfloat16 *__restrict__ B, const float *__restrict__ Wc,
-                                const float *__restrict__ bm, const float *__restrict__ dM,
-                                float *__restrict__ dA, float *__restrict__ part) {
-  __shared__ float red[8][5][H];  // 8 warps per CTA, 8 rows per warp
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = lane * 2;
-  float gw[5][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-  for (int rr = 0; rr < 8; rr++) {
-    const int64_t i = ((int64_t)blockIdx.x * 8 + warp) * 8 + rr;
-    if (i >= n) break;
-    float w[FE][2];
+// ------------------------------------------------- edge backward kernels
+// Both walk rows with a half-warp per row (4 channels per lane) and gather
+// the 16 neighbours of a batch before using any (as the forward layer does).
+constexpr int EB_ROWS = 64;  // rows per CTA (16 half-warps x 4)
+
+__device__ __forceinline__ float4 bf16x4_to_float4(uint2 u) {
+  const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.x));
+  const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// dA_i = sum_j dM_i [P_ij > 0] (P_ij = A_i + B_j + e_ij W_c + b_m), and the
+// CTA's partials of dW_c (4 x 64) and db_m (64): 5 x 64 floats per CTA
+__global__ void __launch_bounds__(256) edge_backward_a(int64_t n, const int32_t *__restrict__ rp,
+                                                       const int32_t *__restrict__ ci, const float4 *__restrict__ ef,
+                                                       const __nv_bfloat16 *__restrict__ A,
+                                                       const __nv_bfloat16 *__restrict__ B,
+                                                       const float *__restrict__ Wc, const float *__restrict__ bm,
+                                                       const float *__restrict__ dM, float *__restrict__ dA,
+                                                       float *__restrict__ part) {
+  __shared__ float red[16][5][H];
+  const int lane = threadIdx.x & 31, hw = threadIdx.x >> 4, hl = lane & 15, half = lane >> 4, c4 = hl * 4;
+  float wc[FE][4], bmv[4];
 #pragma unroll
-    for (int f = 0; f < FE; f++) {
-      w[f][0] = Wc[f * H + c];
-      w[f][1] = Wc[f * H + c + 1];
+  for (int f = 0; f < FE; f++) {
+    const float4 w = *reinterpret_cast<const float4 *>(Wc + f * H + c4);
+    wc[f][0] = w.x; wc[f][1] = w.y; wc[f][2] = w.z; wc[f][3] = w.w;
+  }
+  {
+    const float4 b = *reinterpret_cast<const float4 *>(bm + c4);
+    bmv[0] = b.x; bmv[1] = b.y; bmv[2] = b.z; bmv[3] = b.w;
+  }
+  float gw[5][4];
+#pragma unroll
+  for (int f = 0; f < 5; f++) gw[f][0] = gw[f][1] = gw[f][2] = gw[f][3] = 0.f;
+  for (int rr = 0; rr < EB_ROWS / 16; rr++) {
+    const int64_t i = (int64_t)blockIdx.x * EB_ROWS + hw * (EB_ROWS / 16) + rr;
+    int32_t beg = 0, deg = 0;
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, dm[4] = {0.f, 0.f, 0.f, 0.f};
+    if (i < n) {
+      beg = rp[i];
+      deg = rp[i + 1] - beg;
+      const float4 av = bf16x4_to_float4(*reinterpret_cast<const uint2 *>(A + i * H + c4));
+      const float4 d = *reinterpret_cast<const float4 *>(dM + i * H + c4);
+      a[0] = av.x + bmv[0]; a[1] = av.y + bmv[1]; a[2] = av.z + bmv[2]; a[3] = av.w + bmv[3];
+      dm[0] = d.x; dm[1] = d.y; dm[2] = d.z; dm[3] = d.w;
     }
-    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(A + i * H + c));
-    const float2 dm = *reinterpret_cast<const float2 *>(dM + i * H + c);
-    const float b0 = a.x + bm[c], b1 = a.y + bm[c + 1];
-    float s0 = 0.f, s1 = 0.f;
-    for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
-      const int32_t j = ci[k];
-      const float2 bj = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(B + (int64_t)j * H + c));
-      const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)k * FE);
-      const float p0 = b0 + bj.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
-      const float p1 = b1 + bj.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
-      const float g0 = p0 > 0.f ? dm.x : 0.f, g1 = p1 > 0.f ? dm.y : 0.f;
-      s0 += g0;
-      s1 += g1;
-      gw[0][0] += e.x * g0; gw[0][1] += e.x * g1;
-      gw[1][0] += e.y * g0; gw[1][1] += e.y * g1;
-      gw[2][0] += e.z * g0; gw[2][1] += e.z * g1;
-      gw[3][0] += e.w * g0; gw[3][1] += e.w * g1;
-      gw[4][0] += g0; gw[4][1] += g1;
+    float sacc[4] = {0.f, 0.f, 0.f, 0.f};
+    const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+    for (int k0 = 0; k0 < maxdeg; k0 += 16) {
+      const bool ok = k0 + hl < deg;
+      const int32_t jl = ok ? ci[beg + k0 + hl] : 0;
+      const float4 el = ok ? ef[beg + k0 + hl] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const int cnt = deg - k0;
+      uint2 bv[16];
+#pragma unroll
+      for (int u = 0; u < 16; u++) {
+        const int32_t j = __shfl_sync(0xffffffffu, jl, (half << 4) + u);
+        bv[u] = *reinterpret_cast<const uint2 *>(B + (int64_t)j * H + c4);
+      }
+#pragma unroll
+      for (int u = 0; u < 16; u++) {
+        const int src = (half << 4) + u;
+        const float e[4] = {__shfl_sync(0xffffffffu, el.x, src), __shfl_sync(0xffffffffu, el.y, src),
+                            __shfl_sync(0xffffffffu, el.z, src), __shfl_sync(0xffffffffu, el.w, src)};
+        const float4 b = bf16x4_to_float4(bv[u]);
+        const float bb[4] = {b.x, b.y, b.z, b.w};
+        const bool live = u < cnt;
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) {
+          const float pv = a[cc] + bb[cc] + e[0] * wc[0][cc] + e[1] * wc[1][cc] + e[2] * wc[2][cc] + e[3] * wc[3][cc];
+          const float gg = (live && pv > 0.f) ? dm[cc] : 0.f;
+          sacc[cc] += gg;
+#pragma unroll
+          for (int f = 0; f < FE; f++) gw[f][cc] += e[f] * gg;
+          gw[4][cc] += gg;
+        }
+      }
     }
-    *reinterpret_cast<float2 *>(dA + i * H + c) = make_float2(s0, s1);
+    if (i < n) *reinterpret_cast<float4 *>(dA + i * H + c4) = make_float4(sacc[0], sacc[1], sacc[2], sacc[3]);
   }
 #pragma unroll
-  for (int f = 0; f < 5; f++) {
-    red[warp][f][c] = gw[f][0];
-    red[warp][f][c + 1] = gw[f][1];
-  }
+  for (int f = 0; f < 5; f++)
+#pragma unroll
+    for (int cc = 0; cc < 4; cc++) red[hw][f][c4 + cc] = gw[f][cc];
   __syncthreads();
   for (int q = threadIdx.x; q < 5 * H; q += blockDim.x) {
-    float s = 0.f;
-    for (int w8 = 0; w8 < 8; w8++) s += red[w8][q / H][q % H];
-    part[(int64_t)blockIdx.x * 5 * H + q] = s;
+    float t = 0.f;
+    for (int w = 0; w < 16; w++) t += red[w][q / H][q % H];
+    part[(int64_t)blockIdx.x * 5 * H + q] = t;
   }
 }
 
 // dB_j = sum over the rows i that receive from j of dM_i [P_ij > 0]: row j
 // of the symmetric graph lists those i; tr[k] is the position of (i, j)
-__global__ void edge_backward_b(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                                const int32_t *__restrict__ tr, const float *__restrict__ ef,
-                                const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B,
-                                const float *__restrict__ Wc, const float *__restrict__ bm,
-                                const float *__restrict__ dM, float *__restrict__ dB) {
-  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (j >= n) return;
-  const int c = lane * 2;
-  float w[FE][2];
+__global__ void __launch_bounds__(256) edge_backward_b(int64_t n, const int32_t *__restrict__ rp,
+                                                       const int32_t *__restrict__ ci, const int32_t *__restrict__ tr,
+                                                       const float4 *__restrict__ ef,
+                                                       const __nv_bfloat16 *__restrict__ A,
+                                                       const __nv_bfloat16 *__restrict__ B,
+                                                       const float *__restrict__ Wc, const float *__restrict__ bm,
+                                                       const float *__restrict__ dM, float *__restrict__ dB) {
+  const int lane = threadIdx.x & 31, hw = threadIdx.x >> 4, hl = lane & 15, half = lane >> 4, c4 = hl * 4;
+  float wc[FE][4], bmv[4];
 #pragma unroll
   for (int f = 0; f < FE; f++) {
-    w[f][0] = Wc[f * H + c];
-    w[f][1] = Wc[f * H + c + 1];
+    const float4 w = *reinterpret_cast<const float4 *>(Wc + f * H + c4);
+    wc[f][0] = w.x; wc[f][1] = w.y; wc[f][2] = w.z; wc[f][3] = w.w;
   }
-  const float2 bj = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(B + j * H + c));
-  const float c0 = bj.x + bm[c], c1 = bj.y + bm[c + 1];
-  float s0 = 0.f, s1 = 0.f;
-  for (int32_t k = rp[j]; k < rp[j + 1]; k++) {
-    const int32_t i = ci[k];
-    const float2 ai = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(A + (int64_t)i * H + c));
-    const float2 dm = *reinterpret_cast<const float2 *>(dM + (int64_t)i * H + c);
-    const float4 e = *reinterpret_cast<const float4 *>(ef + (int64_t)tr[k] * FE);
-    const float p0 = c0 + ai.x + e.x * w[0][0] + e.y * w[1][0] + e.z * w[2][0] + e.w * w[3][0];
-    const float p1 = c1 + ai.y + e.x * w[0][1] + e.y * w[1][1] + e.z * w[2][1] + e.w * w[3][1];
-    s0 += p0 > 0.f ? dm.x : 0.f;
-    s1 += p1 > 0.f ? dm.y : 0.f;
+  {
+    const float4 b = *reinterpret_cast<const float4 *>(bm + c4);
+    bmv[0] = b.x; bmv[1] = b.y; bmv[2] = b.z; bmv[3] = b.w;
   }
-  *reinterpret_cast<float2 *>(dB + j * H + c) = make_float2(s0, s1);
+  for (int rr = 0; rr < EB_ROWS / 16; rr++) {
+    const int64_t j = (int64_t)blockIdx.x * EB_ROWS + hw * (EB_ROWS / 16) + rr;
+    int32_t beg = 0, deg = 0;
+    float b[4] = {0.f, 0.f, 0.f, 0.f};
+    if (j < n) {
+      beg = rp[j];
+      deg = rp[j + 1] - beg;
+      const float4 bv = bf16x4_to_float4(*reinterpret_cast<const uint2 *>(B + j * H + c4));
+      b[0] = bv.x + bmv[0]; b[1] = bv.y + bmv[1]; b[2] = bv.z + bmv[2]; b[3] = bv.w + bmv[3];
+    }
+    float sacc[4] = {0.f, 0.f, 0.f, 0.f};
+    const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+    for (int k0 = 0; k0 < maxdeg; k0 += 16) {
+      const bool ok = k0 + hl < deg;
+      const int32_t il = ok ? ci[beg + k0 + hl] : 0;
+      const float4 el = ok ? ef[tr[beg + k0 + hl]] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const int cnt = deg - k0;
+      uint2 av[16];
+      float4 dv[16];
+#pragma unroll
+      for (int u = 0; u < 16; u++) {
+        const int32_t i = __shfl_sync(0xffffffffu, il, (half << 4) + u);
+        av[u] = *reinterpret_cast<const uint2 *>(A + (int64_t)i * H + c4);
+        dv[u] = *reinterpret_cast<const float4 *>(dM + (int64_t)i * H + c4);
+      }
+#pragma unroll
+      for (int u = 0; u < 16; u++) {
+        const int src = (half << 4) + u;
+        const float e[4] = {__shfl_sync(0xffffffffu, el.x, src), __shfl_sync(0xffffffffu, el.y, src),
+                            __shfl_sync(0xffffffffu, el.z, src), __shfl_sync(0xffffffffu, el.w, src)};
+        const float4 ai = bf16x4_to_float4(av[u]);
+        const float aa[4] = {ai.x, ai.y, ai.z, ai.w}, dd[4] = {dv[u].x, dv[u].y, dv[u].z, dv[u].w};
+        const bool live = u < cnt;
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) {
+          const float pv = aa[cc] + b[cc] + e[0] * wc[0][cc] + e[1] * wc[1][cc] + e[2] * wc[2][cc] + e[3] * wc[3][cc];
+          sacc[cc] += (live && pv > 0.f) ? dd[cc] : 0.f;
+        }
+      }
+    }
+    if (j < n) *reinterpret_cast<float4 *>(dB + j * H + c4) = make_float4(sacc[0], sacc[1], sacc[2], sacc[3]);
+  }
 }
 
-// ------------------------------------------------- weight gradients (FP32)
 // part[cta][k][c] = sum over the CTA's rows of in[r][k] * dout[r][c] (c <
 // 64) and, in row K, sum of dout[r][c] (bias gradient).  in = [in0 | in1].
-constexpr int WG_ROWS = 1024;
-__global__ void __launch_bounds__(256) wgrad_kernel(int64_t n, const float *__restrict__ in0, int K0,
-                                                    const float *__restrict__ in1, int K1,
-                                                    const float *__restrict__ dout, int ncol,
-                                                    float *__restrict__ part) {
-  __shared__ float sin_[32][129];
-  __shared__ float sd[32][65];
-  const int K = K0 + K1;
-  const int64_t rbeg = (int64_t)blockIdx.x * WG_ROWS, rend = min((int64_t)n, rbeg + WG_ROWS);
-  // each thread owns outputs q = tid + 256 * m over (K + 1) x ncol
-  const int nout = (K + 1) * ncol;
-  float acc[33];
-#pragma unroll
-  for (int m = 0; m < 33; m++) acc[m] = 0.f;
-  for (int64_t r0 = rbeg; r0 < rend; r0 += 32) {
-    __syncthreads();
-    for (int q = threadIdx.x; q < 32 * K; q += blockDim.x) {
-      const int rr = q / K, k = q % K;
+// part[cta][k][c] = sum over the CTA's rows of in[r][k] * dout[r][c]
+// (c < 64) and, in row K, the sum of dout[r][c] (bias gradient);
+// in = [in0 | in1], K = K0 + K1 <= 143.  Tensor cores: the reduction over
+// rows is the k dimension of m16n8k16 BF16 MMAs (FP32 accumulation), with
+// in^T and dout fragments loaded by ldmatrix.trans from row-major tiles of
+// 64 rows staged in shared memory; a ones column in the staged input makes
+// the bias row.  Each CTA (4 warps) owns a contiguous range of rows and the
+// whole (K+1) x 64 output, warps splitting it by 16-feature tiles.
+constexpr int WG_TILE = 64;
+constexpr int WG_MAXK = 144;
+constexpr int WG_LDI = WG_MAXK + 8;  // padded rows: conflict-free ldmatrix
+constexpr int WG_LDD = 64 + 8;
+constexpr int WG_PARTS = 3 * kNumSMs;
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const __nv_bfloat16 *p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_addr(p)));
+}
+
+// rows [r0, r0 + WG_TILE) of an n x width FP32 matrix -> BF16 shared-memory
+// columns [col0, col0 + width) (zeros past rend); float4 loads when width is
+// a multiple of 4, float2 otherwise (width is even)
+__device__ __forceinline__ void stage_rows(__nv_bfloat16 *dst, int ld, int col0, const float *__restrict__ src,
+                                           int width, int64_t r0, int64_t rend) {
+  if ((width & 3) == 0) {
+    const int per = width >> 2;
+    for (int q = threadIdx.x; q < WG_TILE * per; q += blockDim.x) {
+      const int rr = q / per, c = (q % per) * 4;
       const int64_t r = r0 + rr;
-      float v = 0.f;
-      if (r < rend) v = k < K0 ? in0[r * K0 + k] : in1[r * K1 + (k - K0)];
-      sin_[rr][k] = v;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < rend) v = *reinterpret_cast<const float4 *>(src + r * width + c);
+      __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(dst + rr * ld + col0 + c);
+      o[0] = __floats2bfloat162_rn(v.x, v.y);
+      o[1] = __floats2bfloat162_rn(v.z, v.w);
     }
-    for (int q = threadIdx.x; q < 32 * ncol; q += blockDim.x) {
-      const int rr = q / ncol, c = q % ncol;
+  } else {
+    const int per = width >> 1;
+    for (int q = threadIdx.x; q < WG_TILE * per; q += blockDim.x) {
+      const int rr = q / per, c = (q % per) * 2;
       const int64_t r = r0 + rr;
-      sd[rr][c] = r < rend ? dout[r * ncol + c] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int m = 0; m < 33; m++) {
-      const int q = threadIdx.x + 256 * m;
-      if (q >= nout) break;
-      const int k = q / ncol, c = q % ncol;
-      float s = 0.f;
-      if (k < K) {
-        for (int rr = 0; rr < 32; rr++) s += sin_[rr][k] * sd[rr][c];
-      } else {
-        for (int rr = 0; rr < 32; rr++) s += sd[rr][c];
-      }
-      acc[m] += s;
+      float2 v = make_float2(0.f, 0.f);
+      if (r < rend) v = *reinterpret_cast<const float2 *>(src + r * width + c);
+      *reinterpret_cast<__nv_bfloat162 *>(dst + rr * ld + col0 + c) = __floats2bfloat162_rn(v.x, v.y);
     }
   }
+}
+
+__global__ void __launch_bounds__(128, 3) wgrad_kernel(int64_t n, const float *__restrict__ in0, int K0,
+                                                    const float *__restrict__ in1, int K1,
+                                                    const float *__restrict__ dout, float *__restrict__ part) {
+  __shared__ __align__(16) __nv_bfloat16 sI[WG_TILE * WG_LDI];
+  __shared__ __align__(16) __nv_bfloat16 sD[WG_TILE * WG_LDD];
+  const int K = K0 + K1;
+  const int KP = (K + 1 + 15) & ~15;
+  const int MT = KP / 16;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q4 = lane & 3;
+  const int64_t rbeg = n * blockIdx.x / gridDim.x, rend = n * (blockIdx.x + 1) / gridDim.x;
+  float acc[3][8][4];
 #pragma unroll
-  for (int m = 0; m < 33; m++) {
-    const int q = threadIdx.x + 256 * m;
-    if (q >= nout) break;
-    part[(int64_t)blockIdx.x * nout + q] = acc[m];
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int t = 0; t < 8; t++) acc[i][t][0] = acc[i][t][1] = acc[i][t][2] = acc[i][t][3] = 0.f;
+  for (int64_t r0 = rbeg; r0 < rend; r0 += WG_TILE) {
+    __syncthreads();
+    stage_rows(sI, WG_LDI, 0, in0, K0, r0, rend);
+    if (K1 > 0) stage_rows(sI, WG_LDI, K0, in1, K1, r0, rend);
+    // the ones column (bias row) and the zero padding up to KP
+    for (int q = threadIdx.x; q < WG_TILE * (KP - K); q += blockDim.x) {
+      const int rr = q / (KP - K), k = K + q % (KP - K);
+      sI[rr * WG_LDI + k] = __float2bfloat16(k == K && r0 + rr < rend ? 1.f : 0.f);
+    }
+    stage_rows(sD, WG_LDD, 0, dout, 64, r0, rend);
+    __syncthreads();
+    const int mi = lane >> 3;
+#pragma unroll
+    for (int ks = 0; ks < WG_TILE / 16; ks++) {
+      uint32_t bfr[8][2];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        uint32_t t[4];
+        const int row = ks * 16 + (lane & 7) + (mi & 1) * 8, col = (2 * j + (mi >> 1)) * 8;
+        ldsm_x4_trans(t, sD + row * WG_LDD + col);
+        bfr[2 * j][0] = t[0];
+        bfr[2 * j][1] = t[1];
+        bfr[2 * j + 1][0] = t[2];
+        bfr[2 * j + 1][1] = t[3];
+      }
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const int mt = warp + 4 * i;
+        if (mt >= MT) break;
+        uint32_t a[4];
+        const int row = ks * 16 + (lane & 7) + (mi >> 1) * 8, col = mt * 16 + (mi & 1) * 8;
+        ldsm_x4_trans(a, sI + row * WG_LDI + col);
+#pragma unroll
+        for (int t = 0; t < 8; t++) mma_bf16(acc[i][t], a[0], a[1], a[2], a[3], bfr[t][0], bfr[t][1]);
+      }
+    }
+  }
+  // C fragment: feature rows mt*16 + g (+8), columns 8t + 2 q4 (+1)
+  float *out = part + (int64_t)blockIdx.x * (K + 1) * 64;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const int mt = warp + 4 * i;
+    if (mt >= MT) break;
+    const int f0 = mt * 16 + g, f1 = f0 + 8;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int c = t * 8 + q4 * 2;
+      if (f0 <= K) *reinterpret_cast<float2 *>(out + f0 * 64 + c) = make_float2(acc[i][t][0], acc[i][t][1]);
+      if (f1 <= K) *reinterpret_cast<float2 *>(out + f1 * 64 + c) = make_float2(acc[i][t][2], acc[i][t][3]);
+    }
   }
 }
 
 // grad[dst + q] (+)= sum_b part[b][q], fixed order; q < count.  The bias row
 // (q >= bias_from) goes to grad[bias_dst + q - bias_from] when bias_dst >= 0.
+// Blocks of 32 outputs x 8 partial groups; the groups are combined in a
+// fixed order (deterministic).
 __global__ void reduce_parts(int nparts, int count, const float *__restrict__ part, float *__restrict__ grad,
                              int64_t dst, int bias_from, int64_t bias_dst, int accumulate) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= count) return;
+  __shared__ float red[8][33];
+  const int q = blockIdx.x * 32 + threadIdx.x;
   float s = 0.f;
-  for (int b = 0; b < nparts; b++) s += part[(int64_t)b * count + q];
+  if (q < count)
+    for (int b = threadIdx.y; b < nparts; b += 8) s += part[(int64_t)b * count + q];
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y != 0 || q >= count) return;
+  s = ((red[0][threadIdx.x] + red[1][threadIdx.x]) + (red[2][threadIdx.x] + red[3][threadIdx.x])) +
+      ((red[4][threadIdx.x] + red[5][threadIdx.x]) + (red[6][threadIdx.x] + red[7][threadIdx.x]));
   int64_t o;
   if (q >= bias_from) {
     if (bias_dst < 0) return;
@@ -1000,7 +1142,7 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
   }
   for (DevBuf<float> *b : {&dH, &dR, &dM, &dA, &dB}) b->alloc(N * H);
   dz.alloc(H);
-  part.alloc(std::max<int64_t>(div_up(N, WG_ROWS) * (2 * H + 1) * H, div_up(N, 64) * 5 * H) + 64);
+  part.alloc(std::max<int64_t>((int64_t)WG_PARTS * (2 * H + 1) * H, div_up(N, 64) * 5 * H) + 64);
   const int64_t tiles = div_up(N, (int64_t)TILE);
   enc_grid = persistent_grid((const void *)encode_kernel, kEncSmem, tiles);
   layer_grid = persistent_grid((const void *)mp_layer_kernel<true, true>, kLayerSmem, tiles);
@@ -1081,10 +1223,12 @@ void Mpnn::Impl::forward(bool train) {
 void Mpnn::Impl::wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol,
                        int64_t dst, int64_t bias_dst) {
   cudaStream_t st = s.stream;
-  const int nb = div_up(N, WG_ROWS);
-  const int count = (K0 + K1 + 1) * ncol;
-  wgrad_kernel<<<nb, 256, 0, st>>>(N, in0, K0, in1, K1, dout, ncol, part.p);
-  reduce_parts<<<div_up(count, 256), 256, 0, st>>>(nb, count, part.p, grads.p, dst, (K0 + K1) * ncol, bias_dst, 0);
+  (void)ncol;  // always H
+  const int nb = (int)std::min<int64_t>(WG_PARTS, std::max<int64_t>(1, div_up(N, 4 * WG_TILE)));
+  const int count = (K0 + K1 + 1) * H;
+  wgrad_kernel<<<nb, 128, 0, st>>>(N, in0, K0, in1, K1, dout, part.p);
+  reduce_parts<<<div_up(count, 32), dim3(32, 8), 0, st>>>(nb, count, part.p, grads.p, dst, (K0 + K1) * H, bias_dst,
+                                                          0);
   s.launch_count += 2;
 }
 
@@ -1104,12 +1248,14 @@ double Mpnn::Impl::backward_and_step(float lr) {
     // dM = dR W_u[64:128]^T ; dh += dR W_u[0:64]^T (dh holds the residual path)
     gemm(EPI_LINEAR, dR.p, H, nullptr, 0, wtb_um[l], dM.p);
     gemm(EPI_ACCUM, dR.p, H, nullptr, 0, wtb_uh[l], dH.p);
-    const int nb = div_up(N, 64);
-    edge_backward_a<<<nb, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef.p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l],
+    const int nb = div_up(N, EB_ROWS);
+    const float4 *ef4 = reinterpret_cast<const float4 *>(ef.p);
+    edge_backward_a<<<nb, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef4, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l],
                                         dM.p, dA.p, part.p);
-    reduce_parts<<<div_up(5 * H, 256), 256, 0, st>>>(nb, 5 * H, part.p, grads.p, L.wc[l], 4 * H, L.bm[l], 0);
-    edge_backward_b<<<div_up(N * 32, 256), 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, tr.p, ef.p, A[l].p, B[l].p,
-                                                         P + L.wc[l], P + L.bm[l], dM.p, dB.p);
+    reduce_parts<<<div_up(5 * H, 32), dim3(32, 8), 0, st>>>(nb, 5 * H, part.p, grads.p, L.wc[l], 4 * H, L.bm[l],
+                                                             0);
+    edge_backward_b<<<nb, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, tr.p, ef4, A[l].p, B[l].p, P + L.wc[l],
+                                        P + L.bm[l], dM.p, dB.p);
     s.launch_count += 3;
     // A = h W_a, B = h W_b
     wgrad(Hs[l].p, H, nullptr, 0, dA.p, H, L.wa[l], -1);
