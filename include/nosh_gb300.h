@@ -122,14 +122,18 @@ int nosh_nls_param_name(nosh_nls nls, int index, char *buf, size_t len);
 /* Precision of J/K_reg applies and of the Krylov solver: NOSH_PREC_*. */
 int nosh_nls_set_precision(nosh_nls nls, int precision);
 /* Preconditioner options (the MueLu parameter list of
- * src/keo_regularized.cpp:296-315): maximum levels, coarsest size (nodes),
- * Chebyshev degree of pre- and post-smoothing, and the reuse period: the
- * numeric refreshes between two full Galerkin refreshes (1 = refresh every
- * level at every rebuild; the ones in between update the fine level only,
- * like MueLu "reuse: type full").  Defaults 10, 64, 2, 8.  Drops the current
+ * src/keo_regularized.cpp:296-315): maximum levels, coarsest size (nodes per
+ * system), Chebyshev degree of pre- and post-smoothing, the reuse period
+ * (numeric refreshes between two full Galerkin refreshes: 1 = every level
+ * at every rebuild; the ones in between update the fine level only, like
+ * MueLu "reuse: type full"), the strength threshold of the aggregation and
+ * the Chebyshev eigenvalue ratio (smoothing interval [lmax / ratio,
+ * 1.1 lmax]).  Defaults 10, 64, 2, 8 and, from sweeps, 0 and 15 on
+ * tetrahedral meshes, 0.05 and 30 on triangular ones.  Drops the current
  * hierarchy; the next rebuild builds a new one. */
 int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size,
-                             int smooth_degree, int reuse_period);
+                             int smooth_degree, int reuse_period,
+                             double strength_threshold, double cheb_ratio);
 /* Batched independent solves (many meshes in one handle): the handle's
  * mesh is the disjoint union of num_systems meshes, system s owning the
  * vertices [vertex_offsets[s], vertex_offsets[s+1]) (no edge may join two

@@ -95,7 +95,7 @@ _SIGS = {
     "nosh_nls_num_params": (_I, [_P, C.POINTER(_I)]),
     "nosh_nls_param_name": (_I, [_P, _I, C.c_char_p, C.c_size_t]),
     "nosh_nls_set_precision": (_I, [_P, _I]),
-    "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I]),
+    "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I, _D, _D]),
     "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_system_norms": (_I, [_P, _P]),
@@ -196,6 +196,7 @@ class mesh:
         n, e, t, z = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
         _check(_lib.nosh_mesh_sizes(h, C.byref(n), C.byref(e), C.byref(t), C.byref(z)))
         self.num_vertices, self.num_edges, self.num_cells, self.nnz_blocks = n.value, e.value, t.value, z.value
+        self.vertices_per_cell = c.shape[1]
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -351,10 +352,17 @@ class nls:
             return np.array([p["g"], p["mu"]], np.float64)
         return np.ascontiguousarray(params, np.float64)
 
-    def set_amg_options(self, max_levels=10, coarse_size=64, smooth_degree=2, reuse_period=8):
+    def set_amg_options(self, max_levels=10, coarse_size=64, smooth_degree=2, reuse_period=8,
+                        strength_threshold=None, cheb_ratio=None):
         """Preconditioner options (MueLu parameter list of the reference);
         the hierarchy is rebuilt at the next Newton step."""
-        _check(_lib.nosh_nls_set_amg_options(self._h, max_levels, coarse_size, smooth_degree, reuse_period))
+        tri = self.mesh.vertices_per_cell == 3
+        if strength_threshold is None:
+            strength_threshold = 0.05 if tri else 0.0
+        if cheb_ratio is None:
+            cheb_ratio = 30.0 if tri else 15.0
+        _check(_lib.nosh_nls_set_amg_options(self._h, max_levels, coarse_size, smooth_degree, reuse_period,
+                                             strength_threshold, cheb_ratio))
 
     def set_systems(self, vertex_offsets, mu):
         """Batched independent solves: the mesh is the disjoint union of

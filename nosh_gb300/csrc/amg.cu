@@ -30,8 +30,6 @@ using namespace dev;
 
 namespace {
 
-constexpr double kTheta = 0.05;  // strength-of-connection threshold
-constexpr double kChebRatio = 30.0;  // smoothing interval [lmax/ratio, 1.1 lmax]
 constexpr int64_t kTailMax = 1024;   // levels this small run in one CTA
 
 struct HostLevel {
@@ -59,13 +57,13 @@ int64_t max_block(const HostLevel &L) {
 // 1) a vertex whose strong neighbours are all free roots an aggregate with
 //    them; 2) every remaining vertex joins the aggregate it is most strongly
 //    connected to; 3) isolated leftovers become singletons.
-int64_t aggregate(const HostLevel &L, std::vector<int32_t> &agg) {
+int64_t aggregate(const HostLevel &L, std::vector<int32_t> &agg, double theta) {
   const int64_t n = L.n;
   std::vector<double> scale(n);
   for (int64_t i = 0; i < n; i++) scale[i] = std::max(0.5 * (L.dia[3 * i] + L.dia[3 * i + 1]), 1e-300);
   auto strong = [&](int64_t i, int64_t k) {
     const int64_t j = L.ci[k];
-    return std::abs(L.off[k]) >= kTheta * std::sqrt(scale[i] * scale[j]);
+    return std::abs(L.off[k]) >= theta * std::sqrt(scale[i] * scale[j]);
   };
   agg.assign(n, -1);
   int64_t na = 0;
@@ -101,9 +99,9 @@ int64_t aggregate(const HostLevel &L, std::vector<int32_t> &agg) {
 
 // Coarse graph + Galerkin plans for plain aggregation, and the coarse values
 // (host copy, used for the next level's strength test).
-void coarsen(HostLevel &F, HostLevel &C) {
+void coarsen(HostLevel &F, HostLevel &C, double theta) {
   const int64_t n = F.n;
-  const int64_t na = aggregate(F, F.agg);
+  const int64_t na = aggregate(F, F.agg, theta);
   C.n = na;
   // aggregates never cross systems (no edges between them); number them
   // system by system so every level keeps contiguous system ranges
@@ -285,9 +283,11 @@ __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
 // Chebyshev coefficients from lambda_max: c[0] = 1/theta, then per step
 // k >= 1 the pair (rho_k rho_{k-1}, 2 rho_k / delta).
 template <typename T>
-__global__ void cheb_coeffs(const unsigned long long *lmax_bits, int deg, T *coef, double *lmax_out) {
+__global__ void cheb_coeffs(const unsigned long long *lmax_bits, int deg, double ratio, T *coef,
+                            double *lmax_out) {
+  // smoothing interval [lmax / ratio, 1.1 lmax]
   const double lmax = 1.1 * __longlong_as_double((long long)*lmax_bits);
-  const double lmin = lmax / (1.1 * kChebRatio);
+  const double lmin = lmax / (1.1 * ratio);
   const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
   const double sigma = theta / delta;
   double rho = 1.0 / sigma;
@@ -851,7 +851,7 @@ Amg::Amg(NlsImpl &s, const AmgOptions &o) : impl(new Impl(s, o)) {
   // whole level)
   while ((int)H.size() < o.max_levels && max_block(H.back()) > o.coarse_size) {
     HostLevel C;
-    coarsen(H.back(), C);
+    coarsen(H.back(), C, o.strength_threshold);
     if (C.n >= H.back().n) {  // no coarsening progress: stop here
       H.back().agg.clear();
       break;
@@ -1030,7 +1030,8 @@ void Amg::refresh() {
     NOSH_CUDA(cudaMemsetAsync(I.lmax_bits.p, 0, sizeof(unsigned long long), st));
     dinv_gershgorin<T><<<div_up(I.lev[0].n, 256), 256, 0, st>>>(I.lev[0].n, I.lev[0].rp, I.off<T>(0), I.dia<T>(0),
                                                                 V.dinv[0].p, I.lmax_bits.p);
-    cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p, std::max(I.opt.smooth_degree, 1), V.coef[0].p, I.lmax.p);
+    cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p, std::max(I.opt.smooth_degree, 1), I.opt.cheb_ratio, V.coef[0].p,
+                                    I.lmax.p);
     I.nls.launch_count += 2;
     NOSH_CUDA(cudaGetLastError());
     return;
@@ -1052,7 +1053,7 @@ void Amg::refresh() {
       dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
                                                             V.dinv[l].p, I.lmax_bits.p + l);
       ++I.nls.launch_count;
-      cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1),
+      cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1), I.opt.cheb_ratio,
                                       V.coef[l].p, I.lmax.p + l);
       ++I.nls.launch_count;
     }

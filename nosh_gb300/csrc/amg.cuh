@@ -16,6 +16,8 @@ struct AmgOptions {
   // refreshes between full Galerkin refreshes; the ones in between update
   // the fine level only (hierarchy reuse)
   int reuse_period = 8;
+  double strength_threshold = 0.0;   // |a_ij| >= theta sqrt(d_i d_j) is strong
+  double cheb_ratio = 15.0;          // smoothing interval [lmax / ratio, 1.1 lmax]
 };
 
 struct Amg {

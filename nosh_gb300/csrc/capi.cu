@@ -296,16 +296,19 @@ int nosh_nls_set_precision(nosh_nls nls, int precision) {
 }
 
 int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size, int smooth_degree,
-                             int reuse_period) {
+                             int reuse_period, double strength_threshold, double cheb_ratio) {
   return guarded([&] {
     auto &s = N(nls);
     require(max_levels >= 1 && max_levels <= 16 && coarse_size >= 1 && coarse_size <= 512 &&
-                smooth_degree >= 1 && smooth_degree <= 8 && reuse_period >= 1,
+                smooth_degree >= 1 && smooth_degree <= 8 && reuse_period >= 1 && strength_threshold >= 0 &&
+                strength_threshold < 1 && cheb_ratio > 1,
             "AMG options out of range");
     s.amg_max_levels = max_levels;
     s.amg_coarse_size = coarse_size;
     s.amg_smooth_degree = smooth_degree;
     s.amg_reuse_period = reuse_period;
+    s.amg_theta = strength_threshold;
+    s.amg_cheb_ratio = cheb_ratio;
     nosh::reset_preconditioner(s);
   });
 }

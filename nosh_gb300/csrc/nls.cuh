@@ -137,6 +137,7 @@ struct NlsImpl {
   // preconditioner options (amg.cuh AmgOptions), applied when the hierarchy
   // is next built
   int amg_max_levels = 10, amg_coarse_size = 64, amg_smooth_degree = 2, amg_reuse_period = 8;
+  double amg_theta = 0.0, amg_cheb_ratio = 15.0;
   KernelTimer timers[2];  // NOSH_KERNEL_JACOBIAN, NOSH_KERNEL_SMOOTHER
   mutable int64_t launch_count = 0;  // kernels launched by this handle
   // algorithmic bytes of one fine-level SpMV launch: matrix + indices once,

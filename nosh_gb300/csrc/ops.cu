@@ -332,6 +332,13 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
              "deriv_parameter must be \"mu\" or \"g\"");
   NOSH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   cudaStream_t s = stream;
+  // aggregation defaults by mesh kind (sweeps of the 64^3 tetrahedral
+  // continuation and the batched triangular squares): tetrahedra aggregate
+  // every connection, triangles only strong ones
+  if (m->nvc == 3) {
+    amg_theta = 0.05;
+    amg_cheb_ratio = 30.0;
+  }
   h_V.assign(V, V + N);
   h_t.assign(t, t + N);
   d_A.upload(mvp, 3 * N, s);

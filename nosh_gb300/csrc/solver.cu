@@ -350,6 +350,8 @@ static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu
     o.coarse_size = s.amg_coarse_size;
     o.smooth_degree = s.amg_smooth_degree;
     o.reuse_period = s.amg_reuse_period;
+    o.strength_threshold = s.amg_theta;
+    o.cheb_ratio = s.amg_cheb_ratio;
     s.amg.reset(new Amg(s, o));
   }
   s.amg->refresh<T>();
