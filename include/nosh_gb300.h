@@ -149,6 +149,12 @@ int nosh_nls_set_systems(nosh_nls nls, int64_t num_systems,
                          const int64_t *vertex_offsets, const double *mu);
 /* Per-system ||F_s||_2 of the last residual a Newton solve evaluated. */
 int nosh_nls_system_norms(nosh_nls nls, double *norms);
+/* The preconditioner hierarchy (after the first rebuild): number of
+ * levels, their sizes (nodes; up to max_sizes entries) and the first level
+ * run by the single-CTA tail kernel.  num_levels is 0 before the first
+ * rebuild. */
+int nosh_nls_amg_levels(nosh_nls nls, int *num_levels, int64_t *sizes,
+                        int max_sizes, int *tail_level);
 /* SpMV schedule of the handle's operators: NOSH_SPMV_AUTO (default: each
  * matrix times both schedules once and keeps the faster), NOSH_SPMV_STAGED
  * (128-row blocks staged into shared memory by bulk copies) or

@@ -97,6 +97,7 @@ _SIGS = {
     "nosh_nls_set_precision": (_I, [_P, _I]),
     "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I, _D, _D]),
     "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
+    "nosh_nls_amg_levels": (_I, [_P, C.POINTER(_I), _P, _I, C.POINTER(_I)]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_system_norms": (_I, [_P, _P]),
     "nosh_nls_stream": (_I, [_P, C.POINTER(_P)]),
@@ -380,6 +381,14 @@ class nls:
         out = np.empty(self.num_systems)
         _check(_lib.nosh_nls_system_norms(self._h, _ptr(out)))
         return out
+
+    def amg_levels(self):
+        """(level sizes, first tail level) of the preconditioner hierarchy
+        (empty before the first Newton step)."""
+        n, tl = C.c_int(), C.c_int()
+        sizes = np.zeros(16, np.int64)
+        _check(_lib.nosh_nls_amg_levels(self._h, C.byref(n), _ptr(sizes), 16, C.byref(tl)))
+        return sizes[: n.value].tolist(), tl.value
 
     def set_spmv_schedule(self, schedule):
         """SPMV_AUTO, SPMV_STAGED or SPMV_WARP (see nosh_gb300.h)."""

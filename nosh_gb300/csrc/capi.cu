@@ -331,6 +331,21 @@ int nosh_nls_system_norms(nosh_nls nls, double *norms) {
   });
 }
 
+int nosh_nls_amg_levels(nosh_nls nls, int *num_levels, int64_t *sizes, int max_sizes, int *tail_level) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(num_levels != nullptr, "null argument");
+    if (!s.amg) {
+      *num_levels = 0;
+      if (tail_level) *tail_level = -1;
+      return;
+    }
+    *num_levels = s.amg->num_levels();
+    for (int l = 0; l < std::min(*num_levels, max_sizes) && sizes; l++) sizes[l] = s.amg->level_size(l);
+    if (tail_level) *tail_level = s.amg->tail_level();
+  });
+}
+
 int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule) {
   return guarded([&] {
     auto &s = N(nls);

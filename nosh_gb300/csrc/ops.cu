@@ -263,18 +263,25 @@ bool pick_warp_schedule(int N, const int32_t *rp, const int32_t *ci, const C2<T>
                         unsigned *counter, cudaStream_t st) {
   if (N <= 0) return false;
   DevBuf<C2<T>> xb, yb;
+  DevBuf<T> db;
+  DevBuf<double> rb;
   xb.alloc(N);
   yb.alloc(N);
+  db.alloc(3 * (int64_t)N);
+  rb.alloc(1);
   xb.zero(st);
-  PlainOp<T> op{yb.p};
+  db.zero(st);
+  // a representative epilogue: the diagonal block and a grid reduction, as
+  // the Jacobian and the last smoothing step have
+  BlockDiagOp<T, true> op{db.p, xb.p, yb.p};
   cudaEvent_t e0, e1;
   NOSH_CUDA(cudaEventCreate(&e0));
   NOSH_CUDA(cudaEventCreate(&e1));
   float ms[2] = {0.f, 0.f};
   for (int w = 0; w < 2; w++) {
-    for (int r = 0; r < 2; r++) launch_spmv<T>(w == 1, N, rp, ci, val, xb.p, cap, op, partials, counter, nullptr, st);
+    for (int r = 0; r < 2; r++) launch_spmv<T>(w == 1, N, rp, ci, val, xb.p, cap, op, partials, counter, rb.p, st);
     NOSH_CUDA(cudaEventRecord(e0, st));
-    for (int r = 0; r < 5; r++) launch_spmv<T>(w == 1, N, rp, ci, val, xb.p, cap, op, partials, counter, nullptr, st);
+    for (int r = 0; r < 5; r++) launch_spmv<T>(w == 1, N, rp, ci, val, xb.p, cap, op, partials, counter, rb.p, st);
     NOSH_CUDA(cudaEventRecord(e1, st));
     NOSH_CUDA(cudaEventSynchronize(e1));
     NOSH_CUDA(cudaEventElapsedTime(&ms[w], e0, e1));

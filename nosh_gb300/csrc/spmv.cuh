@@ -393,8 +393,9 @@ void launch_spmv(bool warp, int N, const int32_t *rp, const int32_t *ci, const C
   NOSH_CUDA(cudaGetLastError());
 }
 
-// The faster schedule for one matrix: both are timed on y = A x (CUDA
-// events, after a warm-up) once, when the matrix structure is set up.
+// The faster schedule for one matrix: both are timed once (CUDA events,
+// after a warm-up) on y = A x + D x with <x, y> reduced, when the matrix
+// structure is set up.
 template <typename T>
 bool pick_warp_schedule(int N, const int32_t *rp, const int32_t *ci, const C2<T> *val, int cap, double *partials,
                         unsigned *counter, cudaStream_t st);
