@@ -115,6 +115,11 @@ constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time)
 // that aligns x_k with x_0.  One launch of 32 threads: the FP64 square root
 // and divisions run once per factor, not once per vector element.
 __global__ void normalize_phases(int n, double *c);
+// out[2k], out[2k+1] = <x_k, x_0> (complex, sum conj(x_k) x_0) for the
+// count <= 4 vectors x_1..x_count, reading x_0 once; deterministic grid
+// reductions into counter slots 0 .. 2 count - 1.
+__global__ void history_dots(int64_t n, const double *x0, const double *x1, const double *x2, const double *x3,
+                             const double *x4, int count, double *partials, unsigned *counter, double *out);
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 }  // namespace nosh

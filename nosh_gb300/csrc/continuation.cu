@@ -14,20 +14,6 @@ using namespace dev;
 
 namespace {
 
-// c = sum conj(a_i) b_i, two deterministic reductions into out[0..1]
-__global__ void cdot2_kernel(int64_t n, const C2<double> *__restrict__ a, const C2<double> *__restrict__ b,
-                             double *partials, unsigned *counter, double *out) {
-  double re = 0.0, im = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const C2<double> x = a[i], y = b[i];
-    re += x.x * y.x + x.y * y.y;
-    im += x.x * y.y - x.y * y.x;
-  }
-  grid_reduce(re, partials, counter, out);
-  grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
-}
-
 // out = sum_k L_k e^{i phi_k} x_k (k <= order), the unit phase factors c
 // (normalize_phases) aligning x_k with x0 (solutions are defined up to a
 // global U(1) phase)
@@ -82,14 +68,12 @@ void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
     L[k] = v;
   }
   const int G = vgrid(s.N);
-  for (int k = 1; k <= order; k++) {
-    cdot2_kernel<<<G, 256, 0, st>>>(s.N, (const C2<double> *)slot(k), (const C2<double> *)slot(0),
-                                    s.red.partials.p, s.red.counter.p, dots.p + 2 * (k - 1));
-    ++s.launch_count;
-  }
   if (order >= 1) {
+    history_dots<<<G, 256, 0, st>>>(s.N, slot(0), slot(1), order >= 2 ? slot(2) : nullptr,
+                                    order >= 3 ? slot(3) : nullptr, nullptr, order, s.red.partials.p, s.red.counter.p,
+                                    dots.p);
     normalize_phases<<<1, 32, 0, st>>>(order, dots.p);
-    ++s.launch_count;
+    s.launch_count += 2;
   }
   const double *x1 = order >= 1 ? slot(1) : slot(0), *x2 = order >= 2 ? slot(2) : slot(0),
                *x3 = order >= 3 ? slot(3) : slot(0);

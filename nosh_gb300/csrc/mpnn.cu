@@ -987,17 +987,6 @@ __global__ void pool_backward(int64_t n, const float *__restrict__ dz, float *__
   if (q < n * H) dh[q] = dz[q % H] / (float)n;
 }
 
-__global__ void cdot_pair(int64_t n, const C2<double> *__restrict__ a, const C2<double> *__restrict__ b,
-                          double *partials, unsigned *counter, double *out) {
-  double re = 0.0, im = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const C2<double> x = a[i], y = b[i];
-    re += x.x * y.x + x.y * y.y;
-    im += x.x * y.y - x.y * y.x;
-  }
-  grid_reduce(re, partials, counter, out);
-  grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
-}
 
 // per-nonzero edge features and the transpose map of the symmetric graph
 __global__ void edge_setup(int64_t nnz, const int32_t *__restrict__ nz_edge, const int32_t *__restrict__ pf,
@@ -1303,16 +1292,10 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
     Lh[5 + k] = v;
   }
   Ls.upload(Lh, 9, st);
-  for (int k = 1; k < 4; k++) {
-    cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)x[k], (const C2<double> *)x[0], s.red.partials.p,
-                                 s.red.counter.p, dots.p + 2 * (k - 1));
-    ++s.launch_count;
-  }
-  if (target) {
-    cdot_pair<<<G, 256, 0, st>>>(N, (const C2<double> *)target, (const C2<double> *)x[0], s.red.partials.p,
-                                 s.red.counter.p, dots.p + 6);
-    ++s.launch_count;
-  }
+  // <x_k, x_0> for x_1..x_3 and the target, x_0 read once
+  history_dots<<<G, 256, 0, st>>>(N, x[0], x[1], x[2], x[3], target, target ? 4 : 3, s.red.partials.p,
+                                  s.red.counter.p, dots.p);
+  ++s.launch_count;
   normalize_phases<<<1, 32, 0, st>>>(target ? 4 : 3, dots.p);
   ++s.launch_count;
   features_a<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],

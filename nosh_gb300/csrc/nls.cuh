@@ -19,7 +19,7 @@ struct Reducer {
   DevBuf<double> out;        // result slots
   void init(int max_blocks, int nslots, cudaStream_t s) {
     partials.alloc(max_blocks * 4 + 64);
-    counter.alloc(8);
+    counter.alloc(16);
     counter.zero(s);
     out.alloc(nslots);
     out.zero(s);

@@ -62,6 +62,25 @@ __global__ void vertex_fields_kernel(int64_t N, const int32_t *__restrict__ rp,
 // a = mu p_e, complex coefficient -alpha e^{-ia} at (v0,v1) and its
 // conjugate at (v1,v0), written through the edge -> nonzero scatter map.
 // The diagonal (sum alpha) is mu-independent and kept separately.
+// sin and cos of an FP64 angle.  Magnetic phases on a mesh edge are small
+// (|mu A . e| <= 0.1 covers every mesh finer than about 10 cells per unit
+// field length): there the Maclaurin series of sin to x^11 and cos to x^12
+// (Horner form; truncation below 1e-21 relative at |x| = 0.1) costs a dozen
+// FP64 FMAs, well below a general sincos with argument reduction, which the
+// larger angles still use.
+__device__ __forceinline__ void edge_sincos(double x, double &s, double &c) {
+  if (fabs(x) <= 0.1) {
+    const double x2 = x * x;
+    // reciprocals folded at compile time: multiplications, no FP64 division
+    constexpr double r6 = 1.0 / 6, r20 = 1.0 / 20, r42 = 1.0 / 42, r72 = 1.0 / 72, r110 = 1.0 / 110;
+    constexpr double r2 = 1.0 / 2, r12 = 1.0 / 12, r30 = 1.0 / 30, r56 = 1.0 / 56, r90 = 1.0 / 90, r132 = 1.0 / 132;
+    s = x * (1.0 - x2 * r6 * (1.0 - x2 * r20 * (1.0 - x2 * r42 * (1.0 - x2 * r72 * (1.0 - x2 * r110)))));
+    c = 1.0 - x2 * r2 * (1.0 - x2 * r12 * (1.0 - x2 * r30 * (1.0 - x2 * r56 * (1.0 - x2 * r90 * (1.0 - x2 * r132)))));
+  } else {
+    sincos(x, &s, &c);
+  }
+}
+
 // mu_sys / esys (optional): the edge's system supplies its own mu
 __global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha,
                                const double *__restrict__ p, double mu,
@@ -72,7 +91,7 @@ __global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha,
   if (e >= E) return;
   const double m = mu_sys ? mu_sys[esys[e]] : mu;
   double s, c;
-  sincos(m * p[e], &s, &c);
+  edge_sincos(m * p[e], s, c);
   const double al = alpha[e];
   val[pf[e]] = C2<double>{-al * c, al * s};
   val[pb[e]] = C2<double>{-al * c, -al * s};
@@ -106,7 +125,7 @@ __global__ void dkeo_assemble64(int64_t E, const double *__restrict__ alpha,
   if (e >= E) return;
   const double m = mu_sys ? mu_sys[esys[e]] : mu;
   double s, c;
-  sincos(m * p[e], &s, &c);
+  edge_sincos(m * p[e], s, c);
   const double w = alpha[e] * p[e] * dscale;
   // complex v0 - i v1 at (v0,v1): w sin a + i w cos a; conjugate at (v1,v0)
   val[pf[e]] = C2<double>{w * s, w * c};
@@ -255,6 +274,29 @@ __global__ void normalize_phases(int n, double *c) {
   const double m = sqrt(re * re + im * im);
   c[2 * k] = m > 0 ? re / m : 1.0;
   c[2 * k + 1] = m > 0 ? im / m : 0.0;
+}
+
+__global__ void history_dots(int64_t n, const double *x0, const double *x1, const double *x2, const double *x3,
+                             const double *x4, int count, double *partials, unsigned *counter, double *out) {
+  const C2<double> *xs[4] = {(const C2<double> *)x1, (const C2<double> *)x2, (const C2<double> *)x3,
+                             (const C2<double> *)x4};
+  const C2<double> *a0 = (const C2<double> *)x0;
+  double re[4] = {0, 0, 0, 0}, im[4] = {0, 0, 0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const C2<double> y = a0[i];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (k < count) {
+        const C2<double> x = xs[k][i];
+        re[k] += x.x * y.x + x.y * y.y;
+        im[k] += x.x * y.y - x.y * y.x;
+      }
+    }
+  }
+  for (int k = 0; k < count; k++) {
+    dev::grid_reduce(re[k], partials + (2 * k) * gridDim.x, counter + 2 * k, out + 2 * k);
+    dev::grid_reduce(im[k], partials + (2 * k + 1) * gridDim.x, counter + 2 * k + 1, out + 2 * k + 1);
+  }
 }
 
 namespace dev {

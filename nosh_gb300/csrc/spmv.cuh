@@ -163,7 +163,7 @@ __host__ __device__ constexpr int stage_limit() {
 }
 // Slot of the per-stream reduction counters that records a staging copy
 // that never completed (checked by the host after each linear solve).
-constexpr int kStageErrorSlot = 7;
+constexpr int kStageErrorSlot = 15;
 
 template <typename T, class Op>
 __global__ void __launch_bounds__(kRows)

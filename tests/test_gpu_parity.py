@@ -76,6 +76,22 @@ def test_keo_values_fp64(case):
     assert np.abs(v - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("mu", [0.5, 7.0, 300.0])
+def test_keo_values_fp64_large_phases(case, mu):
+    # the FP64 assembly evaluates small edge phases by a series and larger
+    # ones by sincos: both branches against the oracle
+    name, m, P, gm, model, psi = case
+    model.keo.set_parameters({"mu": mu})
+    v = model.keo.values()
+    ref = P.keo_values(mu)
+    assert np.abs(v - ref).max() <= 1e-12 * np.abs(ref).max()
+    model.dkeo_dp.set_parameters({"mu": mu})
+    v = model.dkeo_dp.values()
+    ref = P.dkeo_values(mu)
+    assert np.abs(v - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1e-300)
+    model.keo.set_parameters({"mu": MU})
+
+
 def test_dkeo_values_fp64(case):
     name, m, P, gm, model, psi = case
     model.dkeo_dp.set_parameters({"mu": MU})
