@@ -631,15 +631,36 @@ struct LevelDesc {
   const int32_t *agg, *mem_ptr, *mem_idx;  // transfer to the next level
 };
 
-template <typename T>
-__device__ __forceinline__ void tail_row_sum(const LevelDesc<T> &A, int64_t i, const C2<T> *x, T &sr,
-                                             T &si) {
-  sr = 0;
-  si = 0;
-  for (int32_t k = A.rp[i]; k < A.rp[i + 1]; k++) {
-    const C2<T> v = A.off[k], xv = x[A.ci[k]];
-    sr += v.x * xv.x - v.y * xv.y;
-    si += v.x * xv.y + v.y * xv.x;
+
+// Threads per row for a tail level of n rows: the largest power of two
+// <= 32 that still leaves a thread group per row, so the short serial chains
+// of the coarse rows (and aggregates) are split across lanes.
+__device__ __forceinline__ int tail_tpr(int64_t n) {
+  int t = 1;
+  while (t < 32 && (int64_t)(blockDim.x / (2 * t)) >= n) t *= 2;
+  return t;
+}
+
+// For every row i < n: the row's off-diagonal sum over x, reduced across its
+// tpr lanes, then epi(i, sr, si) on the group's first lane.
+template <typename T, class F>
+__device__ __forceinline__ void tail_rows(const LevelDesc<T> &A, const C2<T> *x, F &&epi) {
+  const int tpr = tail_tpr(A.n);
+  const int groups = blockDim.x / tpr, g = threadIdx.x / tpr, li = threadIdx.x % tpr;
+  for (int64_t base = 0; base < A.n; base += groups) {
+    const int64_t i = base + g;
+    T sr = 0, si = 0;
+    if (i < A.n)
+      for (int32_t k = A.rp[i] + li; k < A.rp[i + 1]; k += tpr) {
+        const C2<T> v = A.off[k], xv = x[A.ci[k]];
+        sr += v.x * xv.x - v.y * xv.y;
+        si += v.x * xv.y + v.y * xv.x;
+      }
+    for (int off = tpr >> 1; off > 0; off >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, off);
+      si += __shfl_xor_sync(0xffffffffu, si, off);
+    }
+    if (i < A.n && li == 0) epi(i, sr, si);
   }
 }
 
@@ -653,33 +674,40 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
     for (int64_t i = tid; i < A.n; i += bs) cheb_first_elem<T>(i, A.dinv, A.coef[0], A.b[i], A.d, cur);
     __syncthreads();
     for (int k = 1; k < deg; k++) {
-      for (int64_t i = tid; i < A.n; i += bs) {
-        T sr, si;
-        tail_row_sum(A, i, cur, sr, si);
+      tail_rows<T>(A, cur, [&](int64_t i, T sr, T si) {
         cheb_elem<T>(i, k, sr, si, A.dia, A.dinv, A.coef, A.b, cur, A.d, oth);
-      }
+      });
       __syncthreads();
       C2<T> *t = cur;
       cur = oth;
       oth = t;
     }
-    for (int64_t i = tid; i < A.n; i += bs) {
-      T sr, si;
-      tail_row_sum(A, i, A.x, sr, si);
+    tail_rows<T>(A, A.x, [&](int64_t i, T sr, T si) {
       const C2<T> xi = A.x[i], bi = A.b[i];
       const T d0r = A.dia[3 * i], d0i = A.dia[3 * i + 1], d1b = A.dia[3 * i + 2];
       A.res[i] = C2<T>{bi.x - (sr + d0r * xi.x + d1b * xi.y), bi.y - (si + d1b * xi.x + d0i * xi.y)};
-    }
+    });
     __syncthreads();
+    // restriction: aggregate sums, split across lanes like the rows
     const LevelDesc<T> Cl = lv[l + 1];
-    for (int64_t a = tid; a < Cl.n; a += bs) {
-      T sr = 0, si = 0;
-      for (int32_t q = A.mem_ptr[a]; q < A.mem_ptr[a + 1]; q++) {
-        const C2<T> v = A.res[A.mem_idx[q]];
-        sr += v.x;
-        si += v.y;
+    {
+      const int tpr = tail_tpr(Cl.n);
+      const int groups = bs / tpr, g = tid / tpr, li = tid % tpr;
+      for (int64_t base = 0; base < Cl.n; base += groups) {
+        const int64_t a = base + g;
+        T sr = 0, si = 0;
+        if (a < Cl.n)
+          for (int32_t q = A.mem_ptr[a] + li; q < A.mem_ptr[a + 1]; q += tpr) {
+            const C2<T> v = A.res[A.mem_idx[q]];
+            sr += v.x;
+            si += v.y;
+          }
+        for (int off = tpr >> 1; off > 0; off >>= 1) {
+          sr += __shfl_xor_sync(0xffffffffu, sr, off);
+          si += __shfl_xor_sync(0xffffffffu, si, off);
+        }
+        if (a < Cl.n && li == 0) Cl.b[a] = C2<T>{sr, si};
       }
-      Cl.b[a] = C2<T>{sr, si};
     }
     __syncthreads();
   }
@@ -704,11 +732,9 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
     __syncthreads();
     C2<T> *cur = A.x, *oth = A.x2;
     for (int k = 0; k < deg; k++) {
-      for (int64_t i = tid; i < A.n; i += bs) {
-        T sr, si;
-        tail_row_sum(A, i, cur, sr, si);
+      tail_rows<T>(A, cur, [&](int64_t i, T sr, T si) {
         cheb_elem<T>(i, k, sr, si, A.dia, A.dinv, A.coef, A.b, cur, A.d, oth);
-      }
+      });
       __syncthreads();
       C2<T> *t = cur;
       cur = oth;
