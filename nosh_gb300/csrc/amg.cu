@@ -31,7 +31,6 @@ using namespace dev;
 namespace {
 
 constexpr int64_t kTailMax = 1024;   // levels this small run in one CTA
-constexpr int64_t kTailSmemMax = 200 * 1024;  // shared memory the staged tail may use
 
 struct HostLevel {
   int64_t n = 0;
@@ -755,111 +754,6 @@ __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restri
   tail_body(lv, lt, L, deg, Ainv, D);
 }
 
-// Shared-memory bytes of the tail levels [lt, L) of a hierarchy: matrix,
-// smoother data, transfer maps and work vectors, each array 16-byte aligned.
-template <typename T>
-__host__ __device__ inline int64_t tail_array_bytes(int64_t count, int64_t elem) {
-  return (count * elem + 15) / 16 * 16;
-}
-template <typename T>
-__host__ __device__ inline int64_t tail_level_bytes(int64_t n, int64_t nnz, int64_t nc, int deg, bool last) {
-  int64_t b = tail_array_bytes<T>(n + 1, 4) + tail_array_bytes<T>(nnz, 4) + tail_array_bytes<T>(nnz, sizeof(C2<T>)) +
-              2 * tail_array_bytes<T>(3 * n, sizeof(T)) + tail_array_bytes<T>(2 * deg + 2, sizeof(T)) +
-              5 * tail_array_bytes<T>(n, sizeof(C2<T>));
-  if (!last) b += 2 * tail_array_bytes<T>(n, 4) + tail_array_bytes<T>(nc + 1, 4);
-  return b;
-}
-
-// The same tail with every level's data staged into shared memory first
-// (one bulk pass), so the many dependent phases of the tail run at shared-
-// memory latency; level lt's solution is written back for the prolongation
-// above it.
-template <typename T>
-__global__ void __launch_bounds__(1024) tail_vcycle_smem(const LevelDesc<T> *__restrict__ lv, int lt, int L,
-                                                         int deg, const T *__restrict__ Ainv, DenseMap D,
-                                                         const int *halt) {
-  if (halt && *halt >= 2) return;
-  extern __shared__ __align__(16) unsigned char tsm[];
-  __shared__ LevelDesc<T> sd[16];
-  if (threadIdx.x == 0) {
-    int64_t o = 0;
-    auto take = [&](int64_t count, int64_t elem) {
-      unsigned char *p = tsm + o;
-      o += tail_array_bytes<T>(count, elem);
-      return p;
-    };
-    for (int l = lt; l < L; l++) {
-      const LevelDesc<T> &G = lv[l];
-      LevelDesc<T> S = G;
-      const int64_t n = G.n, nnz = G.rp[n];
-      S.rp = reinterpret_cast<const int32_t *>(take(n + 1, 4));
-      S.ci = reinterpret_cast<const int32_t *>(take(nnz, 4));
-      S.off = reinterpret_cast<const C2<T> *>(take(nnz, sizeof(C2<T>)));
-      S.dia = reinterpret_cast<const T *>(take(3 * n, sizeof(T)));
-      S.dinv = reinterpret_cast<const T *>(take(3 * n, sizeof(T)));
-      S.coef = reinterpret_cast<const T *>(take(2 * deg + 2, sizeof(T)));
-      S.b = reinterpret_cast<C2<T> *>(take(n, sizeof(C2<T>)));
-      S.x = reinterpret_cast<C2<T> *>(take(n, sizeof(C2<T>)));
-      S.x2 = reinterpret_cast<C2<T> *>(take(n, sizeof(C2<T>)));
-      S.d = reinterpret_cast<C2<T> *>(take(n, sizeof(C2<T>)));
-      S.res = reinterpret_cast<C2<T> *>(take(n, sizeof(C2<T>)));
-      if (l < L - 1) {
-        const int64_t nc = lv[l + 1].n;
-        S.agg = reinterpret_cast<const int32_t *>(take(n, 4));
-        S.mem_ptr = reinterpret_cast<const int32_t *>(take(nc + 1, 4));
-        S.mem_idx = reinterpret_cast<const int32_t *>(take(n, 4));
-      }
-      sd[l] = S;
-    }
-  }
-  __syncthreads();
-  const int tid = threadIdx.x, bs = blockDim.x;
-  auto copy = [&](const void *src, const void *dst, int64_t bytes) {
-    // 16-byte pieces where both ends are 16-byte aligned (device arrays and
-    // the staging layout are), the 4-byte tail after them; four loads in
-    // flight per thread
-    const uint32_t *s4 = reinterpret_cast<const uint32_t *>(src);
-    uint32_t *d4 = reinterpret_cast<uint32_t *>(const_cast<void *>(dst));
-    int64_t done = 0;
-    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-      const uint4 *s16 = reinterpret_cast<const uint4 *>(src);
-      uint4 *d16 = reinterpret_cast<uint4 *>(const_cast<void *>(dst));
-      const int64_t n16 = bytes / 16;
-      int64_t q = tid;
-      for (; q + 3 * bs < n16; q += 4 * bs) {
-        const uint4 a = s16[q], b = s16[q + bs], c = s16[q + 2 * bs], d = s16[q + 3 * bs];
-        d16[q] = a;
-        d16[q + bs] = b;
-        d16[q + 2 * bs] = c;
-        d16[q + 3 * bs] = d;
-      }
-      for (; q < n16; q += bs) d16[q] = s16[q];
-      done = n16 * 4;
-    }
-    for (int64_t q = done + tid; q < bytes / 4; q += bs) d4[q] = s4[q];
-  };
-  for (int l = lt; l < L; l++) {
-    const LevelDesc<T> &G = lv[l];
-    const LevelDesc<T> &S = sd[l];
-    const int64_t n = G.n, nnz = G.rp[n];
-    copy(G.rp, S.rp, (n + 1) * 4);
-    copy(G.ci, S.ci, nnz * 4);
-    copy(G.off, S.off, nnz * (int64_t)sizeof(C2<T>));
-    copy(G.dia, S.dia, 3 * n * (int64_t)sizeof(T));
-    copy(G.dinv, S.dinv, 3 * n * (int64_t)sizeof(T));
-    copy(G.coef, S.coef, (2 * deg + 2) * (int64_t)sizeof(T));
-    if (l < L - 1) {
-      copy(G.agg, S.agg, n * 4);
-      copy(G.mem_ptr, S.mem_ptr, (lv[l + 1].n + 1) * 4);
-      copy(G.mem_idx, S.mem_idx, n * 4);
-    }
-  }
-  copy(lv[lt].b, sd[lt].b, lv[lt].n * (int64_t)sizeof(C2<T>));
-  __syncthreads();
-  tail_body(sd, lt, L, deg, Ainv, D);
-  copy(sd[lt].x, lv[lt].x, lv[lt].n * (int64_t)sizeof(C2<T>));
-}
-
 // plain MINRES pieces for the single-level case
 template <typename T>
 __global__ void lanczos_only(int64_t n, const MinresScalars *__restrict__ s, const C2<T> *__restrict__ u,
@@ -910,7 +804,6 @@ struct AmgLevel {
 template <typename T>
 struct AmgVals {
   bool ready = false;
-  size_t tail_smem = 0;  // dynamic shared memory of the staged tail (0: global tail)
   int64_t refreshes = 0;  // numeric refreshes so far
   std::vector<DevBuf<C2<T>>> off;  // level >= 1
   std::vector<DevBuf<T>> dia;      // level >= 1
@@ -1144,17 +1037,6 @@ void Amg::Impl::ensure_vals() {
     D.mem_idx = lev[l].mem_idx.p;
   }
   V.desc.upload(desc, nls.stream);
-  {
-    // the tail levels stage into shared memory when they fit
-    int64_t bytes = 0;
-    const int deg = std::max(opt.smooth_degree, 1);
-    for (int l = lt; l < L; l++)
-      bytes += tail_level_bytes<T>(lev[l].n, lev[l].nnz, l + 1 < L ? lev[l + 1].n : 0, deg, l == L - 1);
-    V.tail_smem = (lt < L - 1 && bytes <= kTailSmemMax) ? (size_t)bytes : 0;
-    if (V.tail_smem)
-      NOSH_CUDA(cudaFuncSetAttribute(tail_vcycle_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)V.tail_smem));
-  }
   nls.sync();
   prime<T>();
   V.ready = true;
@@ -1299,10 +1181,7 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
                                                        V.b[l + 1].p, halt);
     ++nls.launch_count;
-    if (V.tail_smem > 0)
-      tail_vcycle_smem<T><<<1, 1024, V.tail_smem, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), halt);
-    else
-      tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), halt);
+    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), halt);
     ++nls.launch_count;
   }
   prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x, halt);

@@ -97,7 +97,6 @@ struct NlsImpl {
   // off-diagonal KEO values in adjacency-CSR order (2E + kPad)
   DevBuf<C2<double>> d_keo64, d_dkeo64;
   DevBuf<C2<float>> d_keo32;
-  DevBuf<C2<double>> d_keo_edge;  // per edge -alpha e^{-i mu p} (assembly scratch)
   double keo_mu = std::nan(""), dkeo_mu = std::nan("");
 
   // diagonal 2x2 blocks (Re-Re, Im-Im, Re-Im), K_ii included:

@@ -81,33 +81,35 @@ __device__ __forceinline__ void edge_sincos(double x, double &s, double &c) {
   }
 }
 
-// Two coalesced passes instead of scattered writes: the edge pass computes
-// c_e = -alpha_e e^{-i mu p_e} in edge order, the nonzero pass writes every
-// nonzero of the CSR in order -- c_e at (v0, v1), conj(c_e) at (v1, v0) --
-// in FP64 and FP32.  (Scattered 16-byte writes cost whole-sector read-
-// modify-writes.)  mu_sys / esys (optional): the edge's system supplies its
-// own mu.
-__global__ void keo_edge_values(int64_t E, const double *__restrict__ alpha, const double *__restrict__ p,
-                                double mu, const double *__restrict__ mu_sys, const int32_t *__restrict__ esys,
-                                C2<double> *__restrict__ ce) {
+// KEO assembly, edge-parallel through the scatter map (no atomics): c_e =
+// -alpha_e e^{-i mu p_e} at (v0, v1), conj(c_e) at (v1, v0).  mu_sys / esys
+// (optional): the edge's system supplies its own mu.
+__global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha, const double *__restrict__ p, double mu,
+                               const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
+                               C2<double> *__restrict__ val, const double *__restrict__ mu_sys,
+                               const int32_t *__restrict__ esys) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= E) return;
   const double m = mu_sys ? mu_sys[esys[e]] : mu;
   double s, c;
   edge_sincos(m * p[e], s, c);
   const double al = alpha[e];
-  ce[e] = C2<double>{-al * c, al * s};
+  val[pf[e]] = C2<double>{-al * c, al * s};
+  val[pb[e]] = C2<double>{-al * c, -al * s};
 }
-__global__ void keo_scatter_nonzeros(int64_t nnz, const int32_t *__restrict__ nz_edge,
-                                     const C2<double> *__restrict__ ce, C2<double> *__restrict__ v64,
-                                     C2<float> *__restrict__ v32) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= nnz) return;
-  const int32_t z = nz_edge[k];
-  C2<double> c = ce[z >= 0 ? z : ~z];
-  if (z < 0) c.y = -c.y;
-  v64[k] = c;
-  v32[k] = C2<float>{(float)c.x, (float)c.y};
+
+__global__ void keo_assemble32(int64_t E, const float *__restrict__ alpha, const float *__restrict__ p, float mu,
+                               const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
+                               C2<float> *__restrict__ val, const double *__restrict__ mu_sys,
+                               const int32_t *__restrict__ esys) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const float m = mu_sys ? (float)mu_sys[esys[e]] : mu;
+  float s, c;
+  sincosf(m * p[e], &s, &c);
+  const float al = alpha[e];
+  val[pf[e]] = C2<float>{-al * c, al * s};
+  val[pb[e]] = C2<float>{-al * c, -al * s};
 }
 
 // DkeoDP::refill_ (src/parameter_matrix_dkeo_dp.cpp:96-151): block entries
@@ -524,10 +526,10 @@ NlsImpl::~NlsImpl() {
 
 void NlsImpl::keo_refill(double mu) {
   const double *ms = sys_off.empty() ? nullptr : d_mu_sys.p;
-  d_keo_edge.alloc(E);
-  keo_edge_values<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, ms, d_esys.p, d_keo_edge.p);
-  keo_scatter_nonzeros<<<div_up(2 * E, 256), 256, 0, stream>>>(2 * E, mesh->d_nz_edge.p, d_keo_edge.p, d_keo64.p,
-                                                                d_keo32.p);
+  keo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, mesh->d_pos_fwd.p,
+                                                      mesh->d_pos_bwd.p, d_keo64.p, ms, d_esys.p);
+  keo_assemble32<<<div_up(E, 256), 256, 0, stream>>>(E, d_alphaf.p, d_pf.p, (float)mu, mesh->d_pos_fwd.p,
+                                                      mesh->d_pos_bwd.p, d_keo32.p, ms, d_esys.p);
   launch_count += 2;
   NOSH_CUDA(cudaGetLastError());
   keo_mu = mu;

@@ -34,10 +34,12 @@ __global__ void dot_kernel(int64_t n, const T *__restrict__ a, const T *__restri
   grid_reduce(v, partials, counter, out);
 }
 
-__global__ void minres_init(MinresScalars *s, double rtol, int maxit) {
+// params = {rtol, maxit} (device memory, written before each solve so the
+// captured prologue graph stays valid)
+__global__ void minres_init(MinresScalars *s, const double *params) {
   const double rz = s->rz;
-  s->rtol = rtol;
-  s->maxit = maxit;
+  s->rtol = params[0];
+  s->maxit = (int)params[1];
   s->itn = 0;
   s->flag = 0;
   s->done = 0;
@@ -155,6 +157,8 @@ Minres<T>::Minres(NlsImpl &nls) : s(nls), n2(2 * nls.N) {
   sc.alloc(1);
   NOSH_CUDA(cudaMallocHost(&h_sc, sizeof(MinresScalars)));
   NOSH_CUDA(cudaMallocHost(&h_err, 2 * sizeof(int)));
+  NOSH_CUDA(cudaMallocHost(&h_params, 2 * sizeof(double)));
+  params.alloc(2);
   NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, JacMinresOp<T>>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
 }
@@ -163,6 +167,8 @@ template <typename T>
 Minres<T>::~Minres() {
   for (cudaGraphExec_t &e : half_exec)
     if (e) cudaGraphExecDestroy(e);
+  if (pro_exec) cudaGraphExecDestroy(pro_exec);
+  if (h_params) cudaFreeHost(h_params);
   if (h_sc) cudaFreeHost(h_sc);
   if (h_err) cudaFreeHost(h_err);
 }
@@ -210,17 +216,42 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
   const int G = vec_grid(n2);
   const size_t bytes = n2 * sizeof(T);
   MinresScalars *d = sc.p;
-  // r_old = r_cur = b, x = w = 0, z = M b, beta1^2 = <b, z>
-  NOSH_CUDA(cudaMemcpyAsync(r[0].p, b, bytes, cudaMemcpyDeviceToDevice, st));
-  NOSH_CUDA(cudaMemcpyAsync(r[1].p, b, bytes, cudaMemcpyDeviceToDevice, st));
-  for (DevBuf<T> *q : {&x, &w[0], &w[1], &w[2]}) NOSH_CUDA(cudaMemsetAsync(q->p, 0, bytes, st));
-  s.amg->apply<T>(r[1].p, z[0].p);
-  dot_kernel<T><<<G, 256, 0, st>>>(n2, r[1].p, z[0].p, s.red.partials.p, s.red.counter.p, &d->rz);
-  minres_init<<<1, 1, 0, st>>>(d, rtol, maxit);
-  s.launch_count += 2;
-  NOSH_CUDA(cudaGetLastError());
   // graphs are used unless kernel timing is on (event pairs per launch)
   const bool graphs = !s.timers[NOSH_KERNEL_JACOBIAN].on;
+  h_params[0] = rtol;
+  h_params[1] = (double)maxit;
+  NOSH_CUDA(cudaMemcpyAsync(params.p, h_params, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  // prologue: r_old = r_cur = b, x = w = 0, z = M b, beta1^2 = <b, z>; one
+  // captured graph for a given right-hand-side buffer
+  auto prologue = [&] {
+    NOSH_CUDA(cudaMemcpyAsync(r[0].p, b, bytes, cudaMemcpyDeviceToDevice, st));
+    NOSH_CUDA(cudaMemcpyAsync(r[1].p, b, bytes, cudaMemcpyDeviceToDevice, st));
+    for (DevBuf<T> *q : {&x, &w[0], &w[1], &w[2]}) NOSH_CUDA(cudaMemsetAsync(q->p, 0, bytes, st));
+    s.amg->apply<T>(r[1].p, z[0].p);
+    dot_kernel<T><<<G, 256, 0, st>>>(n2, r[1].p, z[0].p, s.red.partials.p, s.red.counter.p, &d->rz);
+    minres_init<<<1, 1, 0, st>>>(d, params.p);
+    s.launch_count += 2;
+  };
+  if (graphs) {
+    if (!pro_exec || pro_b != b) {
+      if (pro_exec) NOSH_CUDA(cudaGraphExecDestroy(pro_exec));
+      cudaGraph_t g;
+      const int64_t before = s.launch_count;
+      NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      prologue();
+      NOSH_CUDA(cudaStreamEndCapture(st, &g));
+      pro_kernels = s.launch_count - before;
+      s.launch_count = before;
+      NOSH_CUDA(cudaGraphInstantiate(&pro_exec, g, 0));
+      NOSH_CUDA(cudaGraphDestroy(g));
+      pro_b = b;
+    }
+    NOSH_CUDA(cudaGraphLaunch(pro_exec, st));
+    s.launch_count += pro_kernels;
+  } else {
+    prologue();
+  }
+  NOSH_CUDA(cudaGetLastError());
   if (graphs && !half_exec[0]) {
     for (int h = 0; h < 2; h++) {
       cudaGraph_t g;

@@ -25,6 +25,13 @@ struct Minres {
   MinresScalars *h_sc = nullptr;  // pinned host mirror
   int *h_err = nullptr;
   cudaGraphExec_t half_exec[2] = {nullptr, nullptr};
+  // the captured prologue (initial V-cycle and recurrence set-up) for the
+  // right-hand side pro_b; rtol and maxit reach it through `params`
+  cudaGraphExec_t pro_exec = nullptr;
+  const T *pro_b = nullptr;
+  int64_t pro_kernels = 0;
+  DevBuf<double> params;
+  double *h_params = nullptr;
   int64_t half_kernels[2] = {0, 0};
   int last_its = 0;  // iterations of the previous solve
   explicit Minres(NlsImpl &nls);
