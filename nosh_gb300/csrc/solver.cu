@@ -430,11 +430,16 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     if (opt.forcing > 0) {
       eta = opt.forcing;
     } else {
-      // Eisenstat-Walker choice 2 (gamma 0.9, alpha 2), safeguarded, and no
-      // tighter than needed to reach the target (refine, else tol) in one step
+      // Eisenstat-Walker choice 2 (gamma 0.9, alpha 2), safeguarded, no
+      // tighter than needed to reach the target (refine, else tol) in one
+      // step, and at most 0.3 (a sweep of 0.1 against 0.3 at 64^3: 1.58
+      // against 1.41 ms per quadratic-predictor continuation step, same
+      // Newton steps)
       const double target = opt.refine > 0.0 ? opt.refine : opt.tol;
       const double ew = it == 0 ? 1e-2 : 0.9 * (fn / fn_prev) * (fn / fn_prev);
-      eta = std::min(0.1, std::max(ew, 0.5 * target / fn));
+      // (the 0.5 margin keeps a one-step target reachable when the cap is
+      // the binding term: the step's residual is about eta * fn)
+      eta = std::min(0.3, std::max(ew, 0.5 * target / fn));
     }
     eta = std::max(eta, eta_min);
     int status = 0;
