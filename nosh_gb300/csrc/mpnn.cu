@@ -22,10 +22,13 @@
 // squared error of the prediction relative to the quadratic's, exact from
 // three Gram scalars.
 // Node GEMMs run on the tensor cores with BF16 operands and FP32
-// accumulation (mma.sync m16n8k16); edge aggregation, weight gradients and
-// the optimiser are FP32.  Every reduction is deterministic (block partials
-// summed in a fixed order).
+// accumulation (mma.sync m16n8k16); the message operands A, B are stored in
+// FP16 and the forward messages are formed and summed in packed FP16
+// arithmetic (two channels per instruction); the backward pass, weight
+// gradients (tensor cores, FP32 accumulation) and the optimiser are FP32.
+// Every reduction is deterministic (block partials summed in a fixed order).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cmath>
 #include <vector>
@@ -212,10 +215,10 @@ __device__ __forceinline__ void stage_w(__nv_bfloat16 *dst, const __nv_bfloat16 
   }
 }
 
-// [A | B] = bf16(v) @ [W_a | W_b] for the warp's 16 rows; BF16 stores
+// [A | B] = bf16(v) @ [W_a | W_b] for the warp's 16 rows; FP16 stores (the
+// message operands, added in packed FP16 arithmetic by the aggregation)
 __device__ __forceinline__ void emit_ab(const float (&v)[8][4], const __nv_bfloat16 *sW, int64_t ra, int64_t rb,
-                                        int64_t n, __nv_bfloat16 *__restrict__ A, __nv_bfloat16 *__restrict__ B,
-                                        int g, int q) {
+                                        int64_t n, __half *__restrict__ A, __half *__restrict__ B, int g, int q) {
 #pragma unroll
   for (int part = 0; part < 2; part++) {
     float acc[8][4];
@@ -232,12 +235,12 @@ __device__ __forceinline__ void emit_ab(const float (&v)[8][4], const __nv_bfloa
                  *reinterpret_cast<const uint32_t *>(w + 8));
       }
     }
-    __nv_bfloat16 *dst = part ? B : A;
+    __half *dst = part ? B : A;
 #pragma unroll
     for (int t = 0; t < 8; t++) {
       const int c = t * 8 + q * 2;
-      if (ra < n) *reinterpret_cast<__nv_bfloat162 *>(dst + ra * H + c) = __floats2bfloat162_rn(acc[t][0], acc[t][1]);
-      if (rb < n) *reinterpret_cast<__nv_bfloat162 *>(dst + rb * H + c) = __floats2bfloat162_rn(acc[t][2], acc[t][3]);
+      if (ra < n) *reinterpret_cast<__half2 *>(dst + ra * H + c) = __floats2half2_rn(acc[t][0], acc[t][1]);
+      if (rb < n) *reinterpret_cast<__half2 *>(dst + rb * H + c) = __floats2half2_rn(acc[t][2], acc[t][3]);
     }
   }
 }
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(128) encode_kernel(int64_t n, const float *__r
                                                      const __nv_bfloat16 *__restrict__ We,
                                                      const float *__restrict__ be,
                                                      const __nv_bfloat16 *__restrict__ Wab, float *__restrict__ h,
-                                                     __nv_bfloat16 *__restrict__ A, __nv_bfloat16 *__restrict__ B) {
+                                                     __half *__restrict__ A, __half *__restrict__ B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *sWe = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
   __nv_bfloat16 *sWab = sWe + H * LDE;
@@ -311,10 +314,10 @@ __global__ void __launch_bounds__(128) encode_kernel(int64_t n, const float *__r
 template <bool TRAIN, bool LAST>
 __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
     int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const float4 *__restrict__ ef,
-    const float *__restrict__ h, const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B,
+    const float *__restrict__ h, const __half *__restrict__ A, const __half *__restrict__ B,
     const float *__restrict__ Wc, const float *__restrict__ bm, const __nv_bfloat16 *__restrict__ Wu,
     const float *__restrict__ bu, const __nv_bfloat16 *__restrict__ Wab, float *__restrict__ h_out,
-    __nv_bfloat16 *__restrict__ A_out, __nv_bfloat16 *__restrict__ B_out, float *__restrict__ M_out,
+    __half *__restrict__ A_out, __half *__restrict__ B_out, float *__restrict__ M_out,
     float *__restrict__ R_out, float *__restrict__ pool) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *sWu = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
@@ -328,15 +331,19 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
   __nv_bfloat16 *sMw = sM + warp * 16 * LDM;
   // aggregation: a half-warp per row, 4 channels per lane
   const int hl = lane & 15, half = lane >> 4, c4 = hl * 4;
-  float wc[FE][4], bmv[4];
+  __half2 w2[3][2];  // W_c rows 0..2 for this lane's channels, packed
+  float abias[4];    // b_m + W_c[3] (the constant edge feature)
+  const __half2 zero2 = __float2half2_rn(0.f);
 #pragma unroll
-  for (int f = 0; f < FE; f++) {
+  for (int f = 0; f < 3; f++) {
     const float4 w = *reinterpret_cast<const float4 *>(Wc + f * H + c4);
-    wc[f][0] = w.x; wc[f][1] = w.y; wc[f][2] = w.z; wc[f][3] = w.w;
+    w2[f][0] = __floats2half2_rn(w.x, w.y);
+    w2[f][1] = __floats2half2_rn(w.z, w.w);
   }
   {
     const float4 b = *reinterpret_cast<const float4 *>(bm + c4);
-    bmv[0] = b.x; bmv[1] = b.y; bmv[2] = b.z; bmv[3] = b.w;
+    const float4 w3 = *reinterpret_cast<const float4 *>(Wc + 3 * H + c4);
+    abias[0] = b.x + w3.x; abias[1] = b.y + w3.y; abias[2] = b.z + w3.z; abias[3] = b.w + w3.w;
   }
   float psum[8][2];
 #pragma unroll
@@ -350,14 +357,17 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
       const int rr = 2 * p + half;
       const int64_t r = r0 + rr;
       int32_t beg = 0, deg = 0;
-      float m[4] = {0.f, 0.f, 0.f, 0.f}, a[4] = {0.f, 0.f, 0.f, 0.f};
+      // packed FP16 message arithmetic: a = A_i + b_m + W_c[3] (the edge
+      // features' constant 1 folded in), two channels per instruction
+      __half2 a2[2] = {zero2, zero2}, m2[2] = {zero2, zero2};
       if (r < n) {
         beg = rp[r];
         deg = rp[r + 1] - beg;
         const uint2 av = *reinterpret_cast<const uint2 *>(A + r * H + c4);
-        const float2 a01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&av.x));
-        const float2 a23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&av.y));
-        a[0] = a01.x + bmv[0]; a[1] = a01.y + bmv[1]; a[2] = a23.x + bmv[2]; a[3] = a23.y + bmv[3];
+        const float2 a01 = __half22float2(*reinterpret_cast<const __half2 *>(&av.x));
+        const float2 a23 = __half22float2(*reinterpret_cast<const __half2 *>(&av.y));
+        a2[0] = __floats2half2_rn(a01.x + abias[0], a01.y + abias[1]);
+        a2[1] = __floats2half2_rn(a23.x + abias[2], a23.y + abias[3]);
       }
       const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
       for (int k0 = 0; k0 < maxdeg; k0 += 16) {
@@ -377,19 +387,23 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
 #pragma unroll
         for (int u = 0; u < 16; u++) {
           const int src = (half << 4) + u;
-          const float ex = __shfl_sync(0xffffffffu, el.x, src), ey = __shfl_sync(0xffffffffu, el.y, src);
-          const float ez = __shfl_sync(0xffffffffu, el.z, src), ew = __shfl_sync(0xffffffffu, el.w, src);
-          const float2 b01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&bv[u].x));
-          const float2 b23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&bv[u].y));
-          const float bb[4] = {b01.x, b01.y, b23.x, b23.y};
+          const __half2 ex = __float2half2_rn(__shfl_sync(0xffffffffu, el.x, src));
+          const __half2 ey = __float2half2_rn(__shfl_sync(0xffffffffu, el.y, src));
+          const __half2 ez = __float2half2_rn(__shfl_sync(0xffffffffu, el.z, src));
+          const __half2 *bb = reinterpret_cast<const __half2 *>(&bv[u]);
           const bool live = u < cnt;
 #pragma unroll
-          for (int cc = 0; cc < 4; cc++) {
-            const float pv = a[cc] + bb[cc] + ex * wc[0][cc] + ey * wc[1][cc] + ez * wc[2][cc] + ew * wc[3][cc];
-            m[cc] += live ? fmaxf(pv, 0.f) : 0.f;
+          for (int cc = 0; cc < 2; cc++) {
+            __half2 pv = __hadd2(a2[cc], bb[cc]);
+            pv = __hfma2(ex, w2[0][cc], pv);
+            pv = __hfma2(ey, w2[1][cc], pv);
+            pv = __hfma2(ez, w2[2][cc], pv);
+            if (live) m2[cc] = __hadd2(m2[cc], __hmax2(pv, zero2));
           }
         }
       }
+      const float2 m01 = __half22float2(m2[0]), m23 = __half22float2(m2[1]);
+      const float m[4] = {m01.x, m01.y, m23.x, m23.y};
       uint2 mv;
       *reinterpret_cast<__nv_bfloat162 *>(&mv.x) = __floats2bfloat162_rn(m[0], m[1]);
       *reinterpret_cast<__nv_bfloat162 *>(&mv.y) = __floats2bfloat162_rn(m[2], m[3]);
@@ -495,9 +509,9 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
 // the 16 neighbours of a batch before using any (as the forward layer does).
 constexpr int EB_ROWS = 64;  // rows per CTA (16 half-warps x 4)
 
-__device__ __forceinline__ float4 bf16x4_to_float4(uint2 u) {
-  const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.x));
-  const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.y));
+__device__ __forceinline__ float4 half4_to_float4(uint2 u) {
+  const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
   return make_float4(a.x, a.y, b.x, b.y);
 }
 
@@ -505,8 +519,8 @@ __device__ __forceinline__ float4 bf16x4_to_float4(uint2 u) {
 // CTA's partials of dW_c (4 x 64) and db_m (64): 5 x 64 floats per CTA
 __global__ void __launch_bounds__(256) edge_backward_a(int64_t n, const int32_t *__restrict__ rp,
                                                        const int32_t *__restrict__ ci, const float4 *__restrict__ ef,
-                                                       const __nv_bfloat16 *__restrict__ A,
-                                                       const __nv_bfloat16 *__restrict__ B,
+                                                       const __half *__restrict__ A,
+                                                       const __half *__restrict__ B,
                                                        const float *__restrict__ Wc, const float *__restrict__ bm,
                                                        const float *__restrict__ dM, float *__restrict__ dA,
                                                        float *__restrict__ part) {
@@ -532,7 +546,7 @@ __global__ void __launch_bounds__(256) edge_backward_a(int64_t n, const int32_t 
     if (i < n) {
       beg = rp[i];
       deg = rp[i + 1] - beg;
-      const float4 av = bf16x4_to_float4(*reinterpret_cast<const uint2 *>(A + i * H + c4));
+      const float4 av = half4_to_float4(*reinterpret_cast<const uint2 *>(A + i * H + c4));
       const float4 d = *reinterpret_cast<const float4 *>(dM + i * H + c4);
       a[0] = av.x + bmv[0]; a[1] = av.y + bmv[1]; a[2] = av.z + bmv[2]; a[3] = av.w + bmv[3];
       dm[0] = d.x; dm[1] = d.y; dm[2] = d.z; dm[3] = d.w;
@@ -555,7 +569,7 @@ __global__ void __launch_bounds__(256) edge_backward_a(int64_t n, const int32_t 
         const int src = (half << 4) + u;
         const float e[4] = {__shfl_sync(0xffffffffu, el.x, src), __shfl_sync(0xffffffffu, el.y, src),
                             __shfl_sync(0xffffffffu, el.z, src), __shfl_sync(0xffffffffu, el.w, src)};
-        const float4 b = bf16x4_to_float4(bv[u]);
+        const float4 b = half4_to_float4(bv[u]);
         const float bb[4] = {b.x, b.y, b.z, b.w};
         const bool live = u < cnt;
 #pragma unroll
@@ -588,8 +602,8 @@ __global__ void __launch_bounds__(256) edge_backward_a(int64_t n, const int32_t 
 __global__ void __launch_bounds__(256) edge_backward_b(int64_t n, const int32_t *__restrict__ rp,
                                                        const int32_t *__restrict__ ci, const int32_t *__restrict__ tr,
                                                        const float4 *__restrict__ ef,
-                                                       const __nv_bfloat16 *__restrict__ A,
-                                                       const __nv_bfloat16 *__restrict__ B,
+                                                       const __half *__restrict__ A,
+                                                       const __half *__restrict__ B,
                                                        const float *__restrict__ Wc, const float *__restrict__ bm,
                                                        const float *__restrict__ dM, float *__restrict__ dB) {
   const int lane = threadIdx.x & 31, hw = threadIdx.x >> 4, hl = lane & 15, half = lane >> 4, c4 = hl * 4;
@@ -610,7 +624,7 @@ __global__ void __launch_bounds__(256) edge_backward_b(int64_t n, const int32_t 
     if (j < n) {
       beg = rp[j];
       deg = rp[j + 1] - beg;
-      const float4 bv = bf16x4_to_float4(*reinterpret_cast<const uint2 *>(B + j * H + c4));
+      const float4 bv = half4_to_float4(*reinterpret_cast<const uint2 *>(B + j * H + c4));
       b[0] = bv.x + bmv[0]; b[1] = bv.y + bmv[1]; b[2] = bv.z + bmv[2]; b[3] = bv.w + bmv[3];
     }
     float sacc[4] = {0.f, 0.f, 0.f, 0.f};
@@ -633,7 +647,7 @@ __global__ void __launch_bounds__(256) edge_backward_b(int64_t n, const int32_t 
         const int src = (half << 4) + u;
         const float e[4] = {__shfl_sync(0xffffffffu, el.x, src), __shfl_sync(0xffffffffu, el.y, src),
                             __shfl_sync(0xffffffffu, el.z, src), __shfl_sync(0xffffffffu, el.w, src)};
-        const float4 ai = bf16x4_to_float4(av[u]);
+        const float4 ai = half4_to_float4(av[u]);
         const float aa[4] = {ai.x, ai.y, ai.z, ai.w}, dd[4] = {dv[u].x, dv[u].y, dv[u].z, dv[u].w};
         const bool live = u < cnt;
 #pragma unroll
@@ -1043,9 +1057,9 @@ struct Mpnn::Impl {
   DevBuf<__nv_bfloat16> wt;
   int64_t wt_enc, wt_a[LAYERS], wt_b[LAYERS], wt_u[LAYERS], wtb_a[LAYERS], wtb_b[LAYERS], wtb_uh[LAYERS],
       wtb_um[LAYERS];
-  // activations (A, B in BF16: the message operands) and gradients
+  // activations (A, B in FP16: the message operands) and gradients
   DevBuf<float> X, Hs[LAYERS], Mg[LAYERS], R[LAYERS];
-  DevBuf<__nv_bfloat16> A[LAYERS], B[LAYERS];
+  DevBuf<__half> A[LAYERS], B[LAYERS];
   DevBuf<float> dH, dR, dM, dA, dB, dz;
   DevBuf<float> part, pool;
   int enc_grid = 0, layer_grid = 0;

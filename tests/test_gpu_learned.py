@@ -4,9 +4,9 @@
   (exact-LU Newton, modulo the global phase);
 * the message-passing network's readout coefficient and parameter gradient
   match a torch FP32 CPU reference of the same network that rounds the node
-  GEMM operands and the stored message operands A, B to BF16 as the
-  tensor-core path does (gradient tolerance accounts for the BF16 operands
-  of the backward GEMMs);
+  GEMM operands to BF16 and the stored message operands A, B to FP16 as the
+  GPU path does (tolerances account for the GPU's FP16 message arithmetic
+  and the BF16 operands of the backward GEMMs);
 * trained online on the first steps of a continuation, the learned predictor
   starts Newton from a much smaller residual than the secant predictor (the
   plain method), and beats the quadratic extrapolation on the transitions it
@@ -68,9 +68,9 @@ def torch_reference(p, ef, rp, ci, X, gram):
     Xt = torch.tensor(X, dtype=torch.float32)
     h = torch.relu(bf(Xt) @ bf(w("enc_w", (FX, H))) + w("enc_b", (H,)))
     for l in range(LAYERS):
-        # A, B are stored in BF16
-        A = bf(bf(h) @ bf(w(f"wa{l}", (H, H))))
-        B = bf(bf(h) @ bf(w(f"wb{l}", (H, H))))
+        # A, B are stored in FP16 (the GPU also forms the messages in FP16)
+        A = (bf(h) @ bf(w(f"wa{l}", (H, H)))).half().float()
+        B = (bf(h) @ bf(w(f"wb{l}", (H, H)))).half().float()
         Pij = A[rows] + B[cols] + E @ w(f"wc{l}", (FE, H)) + w(f"bm{l}", (H,))
         M = torch.zeros(N, H).index_add_(0, rows, torch.relu(Pij))
         R = torch.relu(bf(torch.cat([h, M], dim=1)) @ bf(w(f"wu{l}", (2 * H, H))) + w(f"bu{l}", (H,)))
@@ -125,9 +125,9 @@ def test_mpnn_forward_and_gradient_match_torch(net):
     ef = mp.edge_features()
     w_ref, loss_ref, g_ref = torch_reference(p, ef, rp_od, ci_od, X, gram)
     w = mp.forward(X)
-    assert abs(w - w_ref) <= 2e-3 * abs(w_ref), (w, w_ref)
+    assert abs(w - w_ref) <= 3e-3 * abs(w_ref), (w, w_ref)
     loss, g = mp.loss_grad(X, gram)
-    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref, (loss, loss_ref)
     cos = float(g @ g_ref / (np.linalg.norm(g) * np.linalg.norm(g_ref)))
     rel = float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref))
     assert cos > 0.999 and rel < 3e-2, (cos, rel)
