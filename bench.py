@@ -14,9 +14,10 @@ The headline ("value") uses the learned predictor: a message-passing network
 trained online during the first --train-steps steps (untimed, part of the
 warm-up) that sets the weight of the cubic-minus-quadratic extrapolation
 field; it falls back to the secant whenever its prediction has the larger
-residual.  Under it the Newton steps aim at --refine (1e-12), so the stored
-states feed the 4-point extrapolants; a step whose prediction already meets
-||F|| <= 1e-10 takes no Newton iteration.  Also timed on the same workload:
+residual.  With --refine > 0 the Newton steps aim below the tolerance so
+the stored states feed the 4-point extrapolants exactly (a sweep at 64^3
+found refine = 0 fastest once the forcing cap is 0.3, so that is the
+default).  Also timed on the same workload:
 the plain predictor (the reference's secant, mixed precision:
 "plain_predictor"), the plain FP64 GPU path ("plain_fp64") and the
 polynomial predictors as ablations ("ablations").
@@ -58,8 +59,8 @@ def parse():
     ap.add_argument("--dmu", type=float, default=0.005)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--predictor", default="learned", choices=["learned", "secant", "quadratic", "cubic", "none"])
-    ap.add_argument("--refine", type=float, default=1e-12,
-                    help="residual the Newton steps aim at under the learned and cubic predictors")
+    ap.add_argument("--refine", type=float, default=0.0,
+                    help="residual the Newton steps aim at under the learned and cubic predictors (0: tol)")
     ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
     ap.add_argument("--train-iters", type=int, default=10, help="optimiser iterations per training step")
     ap.add_argument("--lr", type=float, default=2e-3)
