@@ -304,14 +304,32 @@ typedef struct nosh_continuation_s *nosh_continuation;
 int nosh_continuation_create(nosh_nls nls, const double *x0, double mu0,
                              nosh_continuation *out);
 int nosh_continuation_destroy(nosh_continuation c);
-/* One step to mu_new with the given predictor (NOSH_PREDICT_*); the
- * polynomial predictors fall back to lower order while the history is
+/* One natural step to mu_new with the given predictor (NOSH_PREDICT_*);
+ * the polynomial predictors fall back to lower order while the history is
  * short.  stats->f_norm0 is the residual of the prediction actually used. */
 int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
                               const nosh_newton_options *opt,
                               nosh_newton_stats *stats);
 /* The current state (2N doubles, host or device) and its mu. */
 int nosh_continuation_state(nosh_continuation c, double *x, double *mu);
+/* One pseudo-arclength step (LOCA "Arc Length", examples/conf.xml:43) of
+ * length ds in the norm ||(x, m)||^2 = x.x / (2N) + theta^2 m^2.  The unit
+ * tangent at the current state is the TANGENT one (-J^-1 dF/dmu, mu
+ * component 1, its U(1) gauge component removed) or the phase-aligned
+ * SECANT of the last two states; it is oriented along the last secant (the
+ * first step: towards larger mu for ds > 0).  The corrector is Newton on F
+ * and the arclength constraint, solved by bordering (two MINRES solves per
+ * Newton step with the same operators).  On success the new state becomes
+ * current (read mu with nosh_continuation_state); on failure the current
+ * state is unchanged and the return code is the Newton status. */
+int nosh_continuation_advance_arclength(nosh_continuation c, double ds,
+                                        int predictor, double theta,
+                                        const nosh_newton_options *opt,
+                                        nosh_newton_stats *stats);
+/* The mu component of the last unit arclength tangent (dmu/ds; its sign
+ * flips past a fold) and the theta it was normalised with. */
+int nosh_continuation_tangent(nosh_continuation c, double *tau_mu,
+                              double *theta);
 /* Learned predictor: creates the network (its readout starts at the cubic
  * extrapolation) and trains it online on the transitions of the next
  * `train_steps` steps, `iters_per_step` Adam iterations each, the step size

@@ -125,6 +125,9 @@ _SIGS = {
     "nosh_continuation_destroy": (_I, [_P]),
     "nosh_continuation_advance": (_I, [_P, _D, _I, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "nosh_continuation_state": (_I, [_P, _P, C.POINTER(_D)]),
+    "nosh_continuation_advance_arclength": (_I, [_P, _D, _I, _D, C.POINTER(NewtonOptions),
+                                                 C.POINTER(NewtonStats)]),
+    "nosh_continuation_tangent": (_I, [_P, C.POINTER(_D), C.POINTER(_D)]),
     "nosh_continuation_learning": (_I, [_P, _I, _I, _D]),
     "nosh_continuation_last_prediction": (_I, [_P, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), C.POINTER(_D),
                                                C.POINTER(_D)]),
@@ -487,8 +490,10 @@ class nls:
 
 # ---------------------------------------------------------------------------
 class continuation:
-    """Device-resident natural continuation run (LOCA stepper semantics): the
-    last converged states stay on the GPU between steps."""
+    """Device-resident continuation run (LOCA stepper semantics): natural
+    steps in mu (``advance``) and pseudo-arclength steps
+    (``advance_arclength``); the last converged states stay on the GPU
+    between steps."""
 
     def __init__(self, model: nls, x0, mu0: float):
         self.model = model
@@ -512,6 +517,34 @@ class continuation:
         rc = _lib.nosh_continuation_advance(self._h, mu_new, predictor, C.byref(o), C.byref(st))
         _check(rc, allow=(ERR_NOT_CONVERGED,))
         return nls._stats(st)
+
+    def advance_arclength(self, ds, predictor=PREDICT_TANGENT, theta=1.0, tol=1e-10, max_newton=20, forcing=0.0,
+                          max_krylov=1000, precision=None, verbose=0):
+        """One pseudo-arclength step of length ``ds`` (norm
+        ``x.x/(2N) + theta^2 mu^2``) with the TANGENT or SECANT predictor and
+        a bordered Newton corrector.  A failed step (no convergence, NaN or a
+        Krylov breakdown) leaves the current state unchanged and reports its
+        status; the new mu is ``stats["mu"]``."""
+        o = self.model._options(tol, max_newton, forcing, max_krylov, precision, verbose)
+        st = NewtonStats()
+        rc = _lib.nosh_continuation_advance_arclength(self._h, ds, predictor, theta, C.byref(o), C.byref(st))
+        _check(rc, allow=(ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN))
+        out = nls._stats(st)
+        out["status"] = rc
+        out["mu"] = self.mu
+        return out
+
+    @property
+    def mu(self):
+        mu = C.c_double()
+        _check(_lib.nosh_continuation_state(self._h, None, C.byref(mu)))
+        return mu.value
+
+    def tangent(self):
+        """(dmu/ds of the last unit arclength tangent, theta)."""
+        t, th = C.c_double(), C.c_double()
+        _check(_lib.nosh_continuation_tangent(self._h, C.byref(t), C.byref(th)))
+        return t.value, th.value
 
     def state(self, x=None):
         mu = C.c_double()

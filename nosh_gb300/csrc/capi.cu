@@ -658,6 +658,31 @@ int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
   return rc;
 }
 
+int nosh_continuation_advance_arclength(nosh_continuation c, double ds, int predictor, double theta,
+                                        const nosh_newton_options *opt, nosh_newton_stats *stats) {
+  nosh_newton_stats st{};
+  int rc = guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    nosh_newton_options o;
+    nosh_newton_default_options(&o);
+    if (opt) o = *opt;
+    require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0 && o.refine >= 0 && o.refine <= o.tol,
+            "bad solver options");
+    c->impl->advance_arclength(ds, predictor, theta, o, st);
+  });
+  if (rc == NOSH_OK) rc = st.status;
+  if (stats) *stats = st;
+  return rc;
+}
+
+int nosh_continuation_tangent(nosh_continuation c, double *tau_mu, double *theta) {
+  return guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    if (tau_mu) *tau_mu = c->impl->tau_mu;
+    if (theta) *theta = c->impl->theta;
+  });
+}
+
 int nosh_continuation_state(nosh_continuation c, double *x, double *mu) {
   return guarded([&] {
     require(c && c->impl, "null continuation handle");

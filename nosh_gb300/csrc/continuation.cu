@@ -1,8 +1,9 @@
-// Device-resident natural continuation (LOCA stepper semantics,
-// examples/conf.xml:35-75; the driver loop of
-// executables/nosh-cont/nosh-cont.cpp:226-345): the last converged states stay
-// in HBM, predictions are formed on the GPU and corrected by Newton.
+// Device-resident continuation (LOCA stepper semantics, examples/conf.xml:35-75;
+// the driver loop of executables/nosh-cont/nosh-cont.cpp:226-345): natural
+// steps in mu and pseudo-arclength steps.  The last converged states stay in
+// HBM, predictions are formed on the GPU and corrected by Newton.
 #include <cmath>
+#include <cstdio>
 
 #include "continuation.cuh"
 #include "mpnn.cuh"
@@ -42,6 +43,56 @@ __global__ void extrapolate_kernel(int64_t n, int order, const double *__restric
 }
 
 inline int vgrid(int64_t n) { return (int)std::min<int64_t>(div_up(n, 256), kNumSMs * 8); }
+
+// Up to six real inner products of complex vectors in one pass:
+// out[j] = sum_i Re(conj(a_j[i]) * b_j[i]), or with i*b_j[i] when rot[j]
+// (the U(1) gauge direction).
+struct DotSet {
+  const C2<double> *a[6] = {}, *b[6] = {};
+  bool rot[6] = {};
+  int k = 0;
+  void add(const double *x, const double *y, bool r = false) {
+    a[k] = (const C2<double> *)x;
+    b[k] = (const C2<double> *)y;
+    rot[k] = r;
+    k++;
+  }
+};
+
+__global__ void dot_set_kernel(int64_t n, DotSet d, double *partials, unsigned *counter, double *out) {
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      if (j < d.k) {
+        const C2<double> a = d.a[j][i], b = d.b[j][i];
+        v[j] += d.rot[j] ? a.y * b.x - a.x * b.y : a.x * b.x + a.y * b.y;
+      }
+    }
+  }
+  for (int j = 0; j < d.k; j++) dev::grid_reduce(v[j], partials + j * gridDim.x, counter + j, out + j);
+}
+
+// y = c0 x0 + c1 x1 + c2 (rot2 ? i x2 : x2); y may alias x0 or x1
+__global__ void lin3_kernel(int64_t n, C2<double> *y, double c0, const C2<double> *x0, double c1,
+                            const C2<double> *x1, double c2, const C2<double> *x2, bool rot2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    C2<double> r = x0[i];
+    r.x *= c0;
+    r.y *= c0;
+    if (x1) {
+      const C2<double> a = x1[i];
+      r.x += c1 * a.x;
+      r.y += c1 * a.y;
+    }
+    if (x2) {
+      const C2<double> a = x2[i];
+      r.x += c2 * (rot2 ? -a.y : a.x);
+      r.y += c2 * (rot2 ? a.x : a.y);
+    }
+    y[i] = r;
+  }
+}
 
 }  // namespace
 
@@ -84,15 +135,198 @@ void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
   NOSH_CUDA(cudaGetLastError());
 }
 
+namespace {
+double *dots_host(NlsImpl &s, const DotSet &d, int64_t n, double *dev_out, double *host) {
+  dot_set_kernel<<<vgrid(n), 256, 0, s.stream>>>(n, d, s.red.partials.p, s.red.counter.p, dev_out);
+  ++s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  NOSH_CUDA(cudaMemcpyAsync(host, dev_out, d.k * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  s.sync();
+  return host;
+}
+void lin3(NlsImpl &s, int64_t n, double *y, double c0, const double *x0, double c1 = 0.0,
+          const double *x1 = nullptr, double c2 = 0.0, const double *x2 = nullptr, bool rot2 = false) {
+  lin3_kernel<<<vgrid(n), 256, 0, s.stream>>>(n, (C2<double> *)y, c0, (const C2<double> *)x0, c1,
+                                              (const C2<double> *)x1, c2, (const C2<double> *)x2, rot2);
+  ++s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+}
+inline bool solve_failed(int status) { return status == NOSH_ERR_NAN || status == NOSH_ERR_BREAKDOWN; }
+}  // namespace
+
+int ContinuationImpl::tangent_direction(const nosh_newton_options &opt, double *out) {
+  // LOCA's tangent predictor: J dpsi/dmu = -dF/dmu at the converged state,
+  // dF/dmu = (dK/dmu) psi (src/model_evaluator_nls.cpp:632-695).  J is
+  // singular along the gauge direction i psi0 (J(i psi) = i F); the
+  // component of the solution along it is arbitrary and is removed, which
+  // makes the tangent, and the arclength norm built on it, unique.
+  NewtonState &ns = state_of(s);
+  const double g = s.g0, mu0 = mu_of(0);
+  NOSH_CUDA(cudaMemcpyAsync(ns.psi.p, slot(0), 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
+  s.dfdp64(ns.psi.p, g, mu0, 1, ns.tmp.p);
+  int status = 0;
+  const double rtol = opt.precision == NOSH_PREC_FP64 ? 1e-10 : 1e-5;
+  const int its = linear_solve(s, ns, ns.tmp.p, out, g, mu0, rtol, opt.max_krylov, opt.precision, true, status);
+  NOSH_CHECK(!solve_failed(status), status, "tangent solve failed");
+  DotSet d;
+  d.add(slot(0), out, true);  // <psi0, i v> = -<i psi0, v>
+  d.add(slot(0), slot(0));
+  double h[6];
+  dots_host(s, d, s.N, dots.p, h);
+  NOSH_CHECK(h[1] > 0.0, NOSH_ERR_BREAKDOWN, "tangent at a zero state");
+  const double kappa = -h[0] / h[1];
+  // out = -(v - kappa i psi0)
+  lin3(s, s.N, out, -1.0, out, 0.0, nullptr, kappa, slot(0), true);
+  return its;
+}
+
+void ContinuationImpl::advance_arclength(double ds, int predictor, double theta_in,
+                                         const nosh_newton_options &opt, nosh_newton_stats &st) {
+  // Pseudo-arclength continuation (Keller), LOCA "Arc Length" stepper
+  // (examples/conf.xml:38-46) with the bordering solve of the extended
+  // system.  With <a, b>_s = a.b / n (n = 2N reals) and
+  // ||(x, m)||^2 = <x, x>_s + theta^2 m^2, the unit tangent (tau, tau_mu)
+  // at (psi0, mu0) and the step length ds define the constraint
+  //   c(psi, mu) = <tau, psi - psi0>_s + theta^2 tau_mu (mu - mu0) - ds = 0.
+  // Predictor: (psi0, mu0) + ds (tau, tau_mu) (which satisfies c = 0).
+  // Corrector: Newton on (F, c); each step solves J a = F and J b = dF/dmu
+  // with the same operators and takes
+  //   dmu = <tau, a>_s / (theta^2 tau_mu - <tau, b>_s),  dpsi = -a - dmu b,
+  // which keeps c = 0 exactly, so convergence is ||F|| <= tol.
+  NOSH_CHECK(predictor == NOSH_PREDICT_TANGENT || predictor == NOSH_PREDICT_SECANT, NOSH_ERR_INVALID,
+             "arclength steps predict TANGENT or SECANT");
+  NOSH_CHECK(std::isfinite(ds) && ds != 0.0, NOSH_ERR_INVALID, "ds must be finite and nonzero");
+  NOSH_CHECK(std::isfinite(theta_in) && theta_in > 0.0, NOSH_ERR_INVALID, "theta must be positive");
+  theta = theta_in;
+  NewtonState &ns = state_of(s);
+  const double g = s.g0, mu0 = mu_of(0);
+  const int64_t N = s.N, n2 = 2 * N;
+  const double inv_n = 1.0 / (double)n2, th2 = theta * theta;
+  for (DevBuf<double> *b : {&tau, &va, &vb})
+    if (b->n < (size_t)n2) b->alloc(n2);
+  st = nosh_newton_stats{};
+  f_learned = f_secant = coef = std::nan("");
+  const bool have_secant = count >= 2;
+  const int G = vgrid(N);
+  if (have_secant) {
+    // phase-aligned secant psi0 - e^{i phi} psi1 into va
+    history_dots<<<G, 256, 0, s.stream>>>(N, slot(0), slot(1), nullptr, nullptr, nullptr, 1, s.red.partials.p,
+                                          s.red.counter.p, dots.p);
+    normalize_phases<<<1, 32, 0, s.stream>>>(1, dots.p);
+    extrapolate_kernel<<<G, 256, 0, s.stream>>>(N, 1, dots.p, 1.0, -1.0, 0.0, 0.0, (const C2<double> *)slot(0),
+                                                (const C2<double> *)slot(1), (const C2<double> *)slot(0),
+                                                (const C2<double> *)slot(0), (C2<double> *)va.p);
+    s.launch_count += 3;
+    NOSH_CUDA(cudaGetLastError());
+  }
+  double tmu;
+  if (predictor == NOSH_PREDICT_TANGENT || !have_secant) {
+    st.krylov_iters += tangent_direction(opt, tau.p);
+    tmu = 1.0;
+    last_used = NOSH_PREDICT_TANGENT;
+  } else {
+    NOSH_CUDA(cudaMemcpyAsync(tau.p, va.p, n2 * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
+    tmu = mu0 - mu_of(1);
+    last_used = NOSH_PREDICT_SECANT;
+  }
+  double h[6];
+  {
+    DotSet d;
+    d.add(tau.p, tau.p);
+    if (have_secant) d.add(tau.p, va.p);
+    dots_host(s, d, N, dots.p, h);
+  }
+  const double t2 = h[0] * inv_n + th2 * tmu * tmu;
+  NOSH_CHECK(t2 > 0.0 && std::isfinite(t2), NOSH_ERR_BREAKDOWN, "zero or non-finite tangent");
+  double sc = 1.0 / std::sqrt(t2);
+  // orientation: along the last secant (the direction of travel)
+  if (have_secant && h[1] * inv_n + th2 * tmu * (mu0 - mu_of(1)) < 0.0) sc = -sc;
+  lin3(s, N, tau.p, sc, tau.p);
+  tmu *= sc;
+  tau_mu = tmu;
+  // predictor
+  lin3(s, N, ns.psi.p, 1.0, slot(0), ds, tau.p);
+  double mc = mu0 + ds * tmu;
+  double fn = residual_norm(s, ns.psi.p, g, mc, ns.f.p);
+  st.f_norm0 = st.f_norm = fn;
+  NOSH_CHECK(!std::isnan(fn), NOSH_ERR_NAN, "predicted residual is NaN");
+  double fn_prev = fn;
+  const bool fp32 = opt.precision != NOSH_PREC_FP64;
+  for (int it = 0; it < opt.max_newton && fn > opt.tol; it++) {
+    const double eta = forcing_term(opt, it, fn, fn_prev, fp32);
+    int status = 0;
+    st.krylov_iters += linear_solve(s, ns, ns.f.p, va.p, g, mc, eta, opt.max_krylov, opt.precision, true, status);
+    if (solve_failed(status)) {
+      st.status = status;
+      return;
+    }
+    s.dfdp64(ns.psi.p, g, mc, 1, ns.tmp.p);
+    st.krylov_iters += linear_solve(s, ns, ns.tmp.p, vb.p, g, mc, eta, opt.max_krylov, opt.precision, false, status);
+    if (solve_failed(status)) {
+      st.status = status;
+      return;
+    }
+    DotSet d;
+    d.add(tau.p, va.p);
+    d.add(tau.p, vb.p);
+    dots_host(s, d, N, dots.p, h);
+    const double den = th2 * tmu - h[1] * inv_n;
+    if (!(std::isfinite(den) && den != 0.0)) {
+      st.status = NOSH_ERR_BREAKDOWN;  // singular bordered system
+      return;
+    }
+    const double dmu = h[0] * inv_n / den;
+    lin3(s, N, ns.psi.p, 1.0, ns.psi.p, -1.0, va.p, -dmu, vb.p);
+    mc += dmu;
+    fn_prev = fn;
+    fn = residual_norm(s, ns.psi.p, g, mc, ns.f.p);
+    st.newton_iters = it + 1;
+    st.f_norm = fn;
+    if (opt.verbose)
+      std::fprintf(stderr, "arclength newton %2d  mu = %.12f  ||F|| = %.3e  eta %.1e\n", it + 1, mc, fn, eta);
+    if (std::isnan(fn)) {
+      st.status = NOSH_ERR_NAN;
+      return;
+    }
+  }
+  if (!(fn <= opt.tol)) {
+    st.status = NOSH_ERR_NOT_CONVERGED;
+    return;
+  }
+  head = (head + 1) % kHist;
+  NOSH_CUDA(cudaMemcpyAsync(hist[head].p, ns.psi.p, n2 * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
+  mu[head] = mc;
+  count = std::min(count + 1, kHist);
+  s.sync();
+}
+
 void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_options &opt,
                                nosh_newton_stats &st) {
   NOSH_CHECK(predictor == NOSH_PREDICT_NONE || predictor == NOSH_PREDICT_SECANT ||
-                 predictor == NOSH_PREDICT_QUADRATIC || predictor == NOSH_PREDICT_CUBIC ||
-                 predictor == NOSH_PREDICT_LEARNED,
-             NOSH_ERR_INVALID, "continuation handles predict NONE, SECANT, QUADRATIC, CUBIC or LEARNED");
+                 predictor == NOSH_PREDICT_TANGENT || predictor == NOSH_PREDICT_QUADRATIC ||
+                 predictor == NOSH_PREDICT_CUBIC || predictor == NOSH_PREDICT_LEARNED,
+             NOSH_ERR_INVALID, "continuation handles predict NONE, SECANT, TANGENT, QUADRATIC, CUBIC or LEARNED");
   NOSH_CHECK(mu_new != mu_of(0), NOSH_ERR_INVALID, "mu_new equals the current mu");
   NewtonState &ns = state_of(s);
   const double g = s.g0;
+  if (predictor == NOSH_PREDICT_TANGENT) {
+    // psi0 + (mu_new - mu0) dpsi/dmu
+    if (tau.n < (size_t)(2 * s.N)) tau.alloc(2 * s.N);
+    const int its = tangent_direction(opt, tau.p);
+    lin3(s, s.N, ns.psi.p, 1.0, slot(0), mu_new - mu_of(0), tau.p);
+    last_used = NOSH_PREDICT_TANGENT;
+    f_learned = f_secant = coef = std::nan("");
+    newton_core(s, ns, g, mu_new, opt, st, -1.0);
+    st.krylov_iters += its;
+    if (st.status != NOSH_OK) return;
+    head = (head + 1) % kHist;
+    NOSH_CUDA(cudaMemcpyAsync(hist[head].p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice,
+                              s.stream));
+    mu[head] = mu_new;
+    count = std::min(count + 1, kHist);
+    s.sync();
+    return;
+  }
   int order = 0;
   if (predictor == NOSH_PREDICT_SECANT || predictor == NOSH_PREDICT_LEARNED) order = 1;
   if (predictor == NOSH_PREDICT_QUADRATIC) order = 2;

@@ -22,6 +22,10 @@ struct ContinuationImpl {
   double learning_rate = 0.0, train_loss = std::nan("");
   int last_used = NOSH_PREDICT_NONE;
   double f_learned = std::nan(""), f_secant = std::nan(""), coef = std::nan("");
+  // pseudo-arclength: the last normalised tangent (tau, tau_mu) and the
+  // parameter scale theta of the arclength norm
+  DevBuf<double> tau, va, vb;
+  double tau_mu = std::nan(""), theta = 1.0;
 
   ContinuationImpl(NlsImpl &nls, const double *x0, double mu0);
   ~ContinuationImpl();
@@ -30,6 +34,13 @@ struct ContinuationImpl {
   double mu_of(int k) const { return mu[(head - k + kHist) % kHist]; }
   void extrapolate(int order, double mu_new, double *out);
   void advance(double mu_new, int predictor, const nosh_newton_options &opt, nosh_newton_stats &st);
+  // one pseudo-arclength step of length ds (tangent or secant predictor,
+  // bordered Newton corrector); on success the new state is pushed
+  void advance_arclength(double ds, int predictor, double theta, const nosh_newton_options &opt,
+                         nosh_newton_stats &st);
+  // dpsi/dmu at the newest state (J^-1 of -dF/dmu, the U(1) gauge component
+  // removed) into out; returns the Krylov iterations
+  int tangent_direction(const nosh_newton_options &opt, double *out);
   void enable_learning(int train_steps, int iters, double lr);
 };
 

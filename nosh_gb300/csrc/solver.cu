@@ -334,6 +334,17 @@ __global__ void secant_kernel(int64_t n, const double *__restrict__ c, double r,
 }
 
 template <typename T>
+__global__ void cast_to(int64_t n, const double *__restrict__ a, T *__restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (T)a[i];
+}
+template <typename T>
+__global__ void cast_from(int64_t n, const T *__restrict__ a, double *__restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
+template <typename T>
 __global__ void axpy_to(int64_t n, double a, const T *__restrict__ t, const double *__restrict__ x,
                         double *__restrict__ y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -406,6 +417,27 @@ template <typename T> static DevBuf<T> &rhs_of(NewtonState &ns);
 template <> DevBuf<float> &rhs_of<float>(NewtonState &ns) { return ns.b32; }
 template <> DevBuf<double> &rhs_of<double>(NewtonState &ns) { return ns.b64; }
 
+double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn_prev, bool fp32) {
+  // FP32 Krylov cannot resolve relative residuals much below ~1e-6
+  const double eta_min = fp32 ? 1e-6 : 1e-12;
+  double eta;
+  if (opt.forcing > 0) {
+    eta = opt.forcing;
+  } else {
+    // Eisenstat-Walker choice 2 (gamma 0.9, alpha 2), safeguarded, no
+    // tighter than needed to reach the target (refine, else tol) in one
+    // step, and at most 0.3 (a sweep of 0.1 against 0.3 at 64^3: 1.58
+    // against 1.41 ms per quadratic-predictor continuation step, same
+    // Newton steps)
+    const double target = opt.refine > 0.0 ? opt.refine : opt.tol;
+    const double ew = it == 0 ? 1e-2 : 0.9 * (fn / fn_prev) * (fn / fn_prev);
+    // (the 0.5 margin keeps a one-step target reachable when the cap is
+    // the binding term: the step's residual is about eta * fn)
+    eta = std::min(0.3, std::max(ew, 0.5 * target / fn));
+  }
+  return std::max(eta, eta_min);
+}
+
 // Newton on ns.psi (device), residual already in ns.f with norm st.f_norm0.
 template <typename T>
 static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
@@ -414,8 +446,6 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
   DevBuf<T> &b = rhs_of<T>(ns);
   const int64_t n2 = 2 * s.N;
   const int G = vec_grid(n2);
-  // FP32 Krylov cannot resolve relative residuals much below ~1e-6
-  const double eta_min = sizeof(T) == 4 ? 1e-6 : 1e-12;
   double fn = st.f_norm0, fn_prev = fn;
   // with a refine target, a state above 4 refine gets at least one step
   const bool polish = opt.refine > 0.0 && fn > 4.0 * opt.refine;
@@ -426,22 +456,7 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     if (!s.sys_off.empty()) s.mask_converged(ns.f.p, opt.tol);
     neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.f.p, b.p);
     ++s.launch_count;
-    double eta;
-    if (opt.forcing > 0) {
-      eta = opt.forcing;
-    } else {
-      // Eisenstat-Walker choice 2 (gamma 0.9, alpha 2), safeguarded, no
-      // tighter than needed to reach the target (refine, else tol) in one
-      // step, and at most 0.3 (a sweep of 0.1 against 0.3 at 64^3: 1.58
-      // against 1.41 ms per quadratic-predictor continuation step, same
-      // Newton steps)
-      const double target = opt.refine > 0.0 ? opt.refine : opt.tol;
-      const double ew = it == 0 ? 1e-2 : 0.9 * (fn / fn_prev) * (fn / fn_prev);
-      // (the 0.5 margin keeps a one-step target reachable when the cap is
-      // the binding term: the step's residual is about eta * fn)
-      eta = std::min(0.3, std::max(ew, 0.5 * target / fn));
-    }
-    eta = std::max(eta, eta_min);
+    const double eta = forcing_term(opt, it, fn, fn_prev, sizeof(T) == 4);
     int status = 0;
     double rel = 0.0;
     const int its = mr.solve(b.p, eta, opt.max_krylov, status, rel);
@@ -509,6 +524,33 @@ static void tangent_predict(NlsImpl &s, NewtonState &ns, double g, double mu_cur
   NOSH_CHECK(status != NOSH_ERR_NAN && status != NOSH_ERR_BREAKDOWN, status, "tangent solve failed");
   axpy_to<T><<<G, 256, 0, s.stream>>>(n2, dmu, mr.x.p, ns.xc.p, ns.psi.p);
   ++s.launch_count;
+}
+
+// J(psi at ns.psi, g, mu) x = rhs (FP64 in and out, 2N reals), solved by the
+// preconditioned MINRES in the requested precision to relative tolerance
+// rtol; the operators are rebuilt at (ns.psi, mu) when `rebuild`.
+template <typename T>
+static int linear_solve_t(NlsImpl &s, NewtonState &ns, const double *rhs, double *x, double g, double mu,
+                          double rtol, int maxit, bool rebuild, int &status) {
+  Minres<T> &mr = minres_of<T>(s, ns);
+  DevBuf<T> &b = rhs_of<T>(ns);
+  const int64_t n2 = 2 * s.N;
+  const int G = vec_grid(n2);
+  if (rebuild) rebuild_operators<T>(s, ns.psi.p, g, mu);
+  cast_to<T><<<G, 256, 0, s.stream>>>(n2, rhs, b.p);
+  ++s.launch_count;
+  double rel = 0.0;
+  const int its = mr.solve(b.p, rtol, maxit, status, rel);
+  cast_from<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, x);
+  ++s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  return its;
+}
+
+int linear_solve(NlsImpl &s, NewtonState &ns, const double *rhs, double *x, double g, double mu, double rtol,
+                 int maxit, int precision, bool rebuild, int &status) {
+  return precision == NOSH_PREC_FP64 ? linear_solve_t<double>(s, ns, rhs, x, g, mu, rtol, maxit, rebuild, status)
+                                     : linear_solve_t<float>(s, ns, rhs, x, g, mu, rtol, maxit, rebuild, status);
 }
 
 void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double mu_new, double mu_cur,

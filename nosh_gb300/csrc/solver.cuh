@@ -64,6 +64,16 @@ double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double 
 void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
                  nosh_newton_stats &st, double f0 = -1.0);
 
+// Relative MINRES tolerance of Newton step `it` (fixed forcing, else
+// safeguarded Eisenstat-Walker), floored at what the Krylov precision resolves.
+double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn_prev, bool fp32);
+
+// J(ns.psi, g, mu) x = rhs (2N reals, FP64 in/out) by preconditioned MINRES
+// in `precision`; rebuilds the operators at (ns.psi, mu) when asked.
+// Returns the iterations; status as Minres::solve.
+int linear_solve(NlsImpl &s, NewtonState &ns, const double *rhs, double *x, double g, double mu, double rtol,
+                 int maxit, int precision, bool rebuild, int &status);
+
 void newton_solve(NlsImpl &s, double *x_user, double g, double mu,
                   const nosh_newton_options &opt, nosh_newton_stats &st);
 void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double mu_new,

@@ -381,6 +381,71 @@ def newton_exact(P: Problem, psi0, g, mu, tol=1e-12, max_it=30):
     return psi, hist
 
 
+def _exact_minres(P: Problem, psi, g, mu, rhs, rtol=1e-13):
+    import scipy.sparse.linalg as spla
+
+    J = P.jac_csr_real(psi, g, mu)
+    lu = spla.splu(P.kreg_csr_real(psi, g, mu).tocsc())
+    M = spla.LinearOperator(J.shape, matvec=lu.solve)
+    x, _ = spla.minres(J, rhs, M=M, rtol=rtol, maxiter=4000)
+    return x
+
+
+def _gauge(psi):
+    """i*psi in the interleaved real layout (the U(1) null direction of J)."""
+    out = np.empty_like(psi)
+    out[0::2], out[1::2] = -psi[1::2], psi[0::2]
+    return out
+
+
+def tangent(P: Problem, psi, g, mu):
+    """dpsi/dmu at a converged state: J v = -dF/dmu (LOCA "Tangent"
+    predictor; dF/dmu = (dK/dmu) psi, src/model_evaluator_nls.cpp:632-695),
+    with the component along the gauge direction i*psi removed."""
+    v = _exact_minres(P, psi, g, mu, -P.dfdp(psi, g, mu, "mu"))
+    ip = _gauge(psi)
+    return v - (ip @ v) / (ip @ ip) * ip
+
+
+def arclength_step(P: Problem, psi0, mu0, ds, g=1.0, prev=None, predictor="tangent", theta=1.0, tol=1e-12,
+                   max_it=20):
+    """One pseudo-arclength step (Keller; LOCA "Arc Length",
+    examples/conf.xml:43) with exact-LU-preconditioned MINRES solves.
+
+    Norm: ||(x, m)||^2 = x.x/n + theta^2 m^2 (n = 2N).  The unit tangent is
+    (tangent(psi0), 1) or the phase-aligned secant (psi0 - psi1, mu0 - mu1)
+    from ``prev = (psi1, mu1)``, oriented along that secant when given.
+    Corrector: Newton on F and the constraint
+    <tau, psi - psi0>/n + theta^2 tau_mu (mu - mu0) = ds by bordering.
+    Returns (psi, mu, tau_mu, newton_iters)."""
+    n = psi0.size
+    th2 = theta * theta
+    sec = None
+    if prev is not None:
+        sec = psi0 - align_phase(prev[0], psi0)
+        sec_mu = mu0 - prev[1]
+    if predictor == "tangent" or sec is None:
+        tx, tm = tangent(P, psi0, g, mu0), 1.0
+    else:
+        tx, tm = sec.copy(), sec_mu
+    sc = 1.0 / np.sqrt(tx @ tx / n + th2 * tm * tm)
+    if sec is not None and tx @ sec / n + th2 * tm * sec_mu < 0:
+        sc = -sc
+    tx, tm = tx * sc, tm * sc
+    psi, mu = psi0 + ds * tx, mu0 + ds * tm
+    its = 0
+    for its in range(max_it + 1):
+        F = P.compute_f(psi, g, mu)
+        if np.linalg.norm(F) <= tol or its == max_it:
+            break
+        a = _exact_minres(P, psi, g, mu, F)
+        b = _exact_minres(P, psi, g, mu, P.dfdp(psi, g, mu, "mu"))
+        dmu = (tx @ a / n) / (th2 * tm - tx @ b / n)
+        psi = psi - a - dmu * b
+        mu = mu + dmu
+    return psi, mu, tm, its
+
+
 def align_phase(psi, ref):
     """Rotate psi by the global phase that best matches ref (U(1) gauge)."""
     z = psi[0::2] + 1j * psi[1::2]
