@@ -319,7 +319,10 @@ int nosh_continuation_state(nosh_continuation c, double *x, double *mu);
  * SECANT of the last two states; it is oriented along the last secant (the
  * first step: towards larger mu for ds > 0).  The corrector is Newton on F
  * and the arclength constraint, solved by bordering (two MINRES solves per
- * Newton step with the same operators).  On success the new state becomes
+ * Newton step with the same operators) in FP64 whatever the handle's
+ * precision, at the relative tolerance opt->forcing, or 1e-8 when it is
+ * <= 0: near a fold only the combination of the two solutions is small,
+ * and looser or FP32 solves miss the fold.  On success the new state becomes
  * current (read mu with nosh_continuation_state); on failure the current
  * state is unchanged and the return code is the Newton status. */
 int nosh_continuation_advance_arclength(nosh_continuation c, double ds,

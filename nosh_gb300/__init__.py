@@ -522,7 +522,8 @@ class continuation:
                           max_krylov=1000, precision=None, verbose=0):
         """One pseudo-arclength step of length ``ds`` (norm
         ``x.x/(2N) + theta^2 mu^2``) with the TANGENT or SECANT predictor and
-        a bordered Newton corrector.  A failed step (no convergence, NaN or a
+        a bordered Newton corrector (FP64 solves at relative tolerance
+        ``forcing``, 1e-8 when 0).  A failed step (no convergence, NaN or a
         Krylov breakdown) leaves the current state unchanged and reports its
         status; the new mu is ``stats["mu"]``."""
         o = self.model._options(tol, max_newton, forcing, max_krylov, precision, verbose)

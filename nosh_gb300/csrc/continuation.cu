@@ -154,7 +154,7 @@ void lin3(NlsImpl &s, int64_t n, double *y, double c0, const double *x0, double 
 inline bool solve_failed(int status) { return status == NOSH_ERR_NAN || status == NOSH_ERR_BREAKDOWN; }
 }  // namespace
 
-int ContinuationImpl::tangent_direction(const nosh_newton_options &opt, double *out) {
+int ContinuationImpl::tangent_direction(const nosh_newton_options &opt, int precision, double rtol, double *out) {
   // LOCA's tangent predictor: J dpsi/dmu = -dF/dmu at the converged state,
   // dF/dmu = (dK/dmu) psi (src/model_evaluator_nls.cpp:632-695).  J is
   // singular along the gauge direction i psi0 (J(i psi) = i F); the
@@ -165,8 +165,7 @@ int ContinuationImpl::tangent_direction(const nosh_newton_options &opt, double *
   NOSH_CUDA(cudaMemcpyAsync(ns.psi.p, slot(0), 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
   s.dfdp64(ns.psi.p, g, mu0, 1, ns.tmp.p);
   int status = 0;
-  const double rtol = opt.precision == NOSH_PREC_FP64 ? 1e-10 : 1e-5;
-  const int its = linear_solve(s, ns, ns.tmp.p, out, g, mu0, rtol, opt.max_krylov, opt.precision, true, status);
+  const int its = linear_solve(s, ns, ns.tmp.p, out, g, mu0, rtol, opt.max_krylov, precision, true, status);
   NOSH_CHECK(!solve_failed(status), status, "tangent solve failed");
   DotSet d;
   d.add(slot(0), out, true);  // <psi0, i v> = -<i psi0, v>
@@ -221,7 +220,7 @@ void ContinuationImpl::advance_arclength(double ds, int predictor, double theta_
   }
   double tmu;
   if (predictor == NOSH_PREDICT_TANGENT || !have_secant) {
-    st.krylov_iters += tangent_direction(opt, tau.p);
+    st.krylov_iters += tangent_direction(opt, NOSH_PREC_FP64, 1e-10, tau.p);
     tmu = 1.0;
     last_used = NOSH_PREDICT_TANGENT;
   } else {
@@ -250,18 +249,23 @@ void ContinuationImpl::advance_arclength(double ds, int predictor, double theta_
   double fn = residual_norm(s, ns.psi.p, g, mc, ns.f.p);
   st.f_norm0 = st.f_norm = fn;
   NOSH_CHECK(!std::isnan(fn), NOSH_ERR_NAN, "predicted residual is NaN");
-  double fn_prev = fn;
-  const bool fp32 = opt.precision != NOSH_PREC_FP64;
+  // Constant forcing (the reference's NOX setting, "Forcing Term Method"
+  // Constant, examples/conf.xml:81) and FP64 Krylov whatever the handle's
+  // precision: near a fold J is nearly singular along the tangent, a and b
+  // are both large there and only their combination is small, so loose
+  // (Eisenstat-Walker) or FP32 solves stall the corrector or skip the fold
+  // (an 8x8 square, 97^2 vertices: both turned away from the fold at
+  // mu = 0.4097 that FP64 solves at 1e-8 follow).
+  const double eta = opt.forcing > 0.0 ? opt.forcing : kArclengthForcing;
   for (int it = 0; it < opt.max_newton && fn > opt.tol; it++) {
-    const double eta = forcing_term(opt, it, fn, fn_prev, fp32);
     int status = 0;
-    st.krylov_iters += linear_solve(s, ns, ns.f.p, va.p, g, mc, eta, opt.max_krylov, opt.precision, true, status);
+    st.krylov_iters += linear_solve(s, ns, ns.f.p, va.p, g, mc, eta, opt.max_krylov, NOSH_PREC_FP64, true, status);
     if (solve_failed(status)) {
       st.status = status;
       return;
     }
     s.dfdp64(ns.psi.p, g, mc, 1, ns.tmp.p);
-    st.krylov_iters += linear_solve(s, ns, ns.tmp.p, vb.p, g, mc, eta, opt.max_krylov, opt.precision, false, status);
+    st.krylov_iters += linear_solve(s, ns, ns.tmp.p, vb.p, g, mc, eta, opt.max_krylov, NOSH_PREC_FP64, false, status);
     if (solve_failed(status)) {
       st.status = status;
       return;
@@ -278,7 +282,6 @@ void ContinuationImpl::advance_arclength(double ds, int predictor, double theta_
     const double dmu = h[0] * inv_n / den;
     lin3(s, N, ns.psi.p, 1.0, ns.psi.p, -1.0, va.p, -dmu, vb.p);
     mc += dmu;
-    fn_prev = fn;
     fn = residual_norm(s, ns.psi.p, g, mc, ns.f.p);
     st.newton_iters = it + 1;
     st.f_norm = fn;
@@ -312,7 +315,9 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   if (predictor == NOSH_PREDICT_TANGENT) {
     // psi0 + (mu_new - mu0) dpsi/dmu
     if (tau.n < (size_t)(2 * s.N)) tau.alloc(2 * s.N);
-    const int its = tangent_direction(opt, tau.p);
+    // a predictor only: FP32 solves are accurate enough
+    const bool fp64 = opt.precision == NOSH_PREC_FP64;
+    const int its = tangent_direction(opt, opt.precision, fp64 ? 1e-10 : 1e-5, tau.p);
     lin3(s, s.N, ns.psi.p, 1.0, slot(0), mu_new - mu_of(0), tau.p);
     last_used = NOSH_PREDICT_TANGENT;
     f_learned = f_secant = coef = std::nan("");

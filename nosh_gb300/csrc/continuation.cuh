@@ -11,6 +11,8 @@ struct Mpnn;  // learned predictor (mpnn.cu)
 
 struct ContinuationImpl {
   static constexpr int kHist = 5;  // newest converged states kept in HBM
+  // relative MINRES tolerance of the arclength corrector's solves
+  static constexpr double kArclengthForcing = 1e-8;
   NlsImpl &s;
   DevBuf<double> hist[kHist];
   double mu[kHist] = {0, 0, 0, 0, 0};
@@ -39,8 +41,9 @@ struct ContinuationImpl {
   void advance_arclength(double ds, int predictor, double theta, const nosh_newton_options &opt,
                          nosh_newton_stats &st);
   // dpsi/dmu at the newest state (J^-1 of -dF/dmu, the U(1) gauge component
-  // removed) into out; returns the Krylov iterations
-  int tangent_direction(const nosh_newton_options &opt, double *out);
+  // removed) into out, solved in `precision` to relative tolerance rtol;
+  // returns the Krylov iterations
+  int tangent_direction(const nosh_newton_options &opt, int precision, double rtol, double *out);
   void enable_learning(int train_steps, int iters, double lr);
 };
 

@@ -1,9 +1,10 @@
 """Pseudo-arclength continuation on the GPU against the oracle's
 restatement: from the same two converged states, one arclength step with
 the tangent or the secant predictor reaches the oracle's (psi, mu) (modulo
-the global phase), in FP64 and mixed precision; the natural tangent
-predictor; and a stepper run with the adaptive step size and the observer's
-statistics file."""
+the global phase), from FP64 and mixed-precision handles (the arclength
+solves run in FP64 in both); the natural tangent predictor; a stepper run
+with the adaptive step size and the observer's statistics file; and an
+arclength run around the fold of the vortex-free branch on an 8 x 8 square."""
 import numpy as np
 import pytest
 
@@ -118,3 +119,29 @@ def test_stepper_run_with_observer(tmp_path):
     assert abs(obs.rows[-1]["(2) Gibbs energy"] - P.energy(x)) <= 1e-12 * abs(P.energy(x))
     assert abs(obs.rows[-1]["(2) ||x||_2 scaled"] - np.sqrt(P.inner_product(x, x))) <= 1e-12
     assert np.linalg.norm(P.compute_f(x, G, mu)) <= 1.5e-10
+
+
+def test_arclength_turns_around_a_fold():
+    # 8 x 8 square, 97^2 vertices: the vortex-free branch from mu = 0 has a
+    # fold near mu = 0.41; arclength steps follow the branch around it, back
+    # to smaller mu
+    import nosh_gb300 as ng
+    from nosh_gb300 import stepper
+
+    x, c, _ = O.gen_square(97, 5)
+    m = O.finish_mesh(x * 8.0, c)
+    A = O.mvp_constant_curl(m.x)
+    P = O.Problem(m, A)
+    model = ng.nls(ng.mesh(m.x, m.cells), A, -1.0, G, 1.0, mu=0.0)
+    psi = np.zeros(2 * m.N)
+    psi[0::2] = 1.0
+    run = ng.continuation(model, psi, 0.0)
+    out = stepper.Stepper(run, method="Arc Length", predictor="Tangent", initial_step=0.02, max_step=0.3,
+                          max_steps=12, max_value=1.5, min_value=-0.01, tol=1e-10).run()
+    mus = [r["mu"] for r in out["records"]]
+    top = int(np.argmax(mus))
+    assert 0.40 < mus[top] < 0.42 and 0 < top < len(mus) - 1
+    assert mus[-1] < mus[top] - 0.1  # came back down past the fold
+    assert run.tangent()[0] < 0
+    xs, mu = run.state()
+    assert np.linalg.norm(P.compute_f(xs, G, mu)) <= 1.5e-10

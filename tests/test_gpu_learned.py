@@ -81,7 +81,7 @@ def torch_reference(p, ef, rp, ci, X, gram):
     g = torch.tensor(gram, dtype=torch.float64)
     loss = (wc * wc * g[0] - 2 * wc * g[1] + g[2]) / g[2]
     loss.backward()
-    return float(wc.detach()), float(loss), P.grad.numpy()
+    return float(wc.detach()), float(loss.detach()), P.grad.numpy()
 
 
 @pytest.fixture(scope="module")
