@@ -106,7 +106,19 @@ ContinuationImpl::ContinuationImpl(NlsImpl &nls, const double *x0, double mu0) :
   s.sync();
 }
 
-ContinuationImpl::~ContinuationImpl() = default;
+ContinuationImpl::~ContinuationImpl() {
+  // the network's buffers outlive any inference still running on the side
+  if (side) cudaStreamSynchronize(side);
+  if (ev_main) cudaEventDestroy(ev_main);
+  if (ev_side) cudaEventDestroy(ev_side);
+  if (side) cudaStreamDestroy(side);
+  if (w_host) cudaFreeHost(w_host);
+}
+
+void ContinuationImpl::drain_side() {
+  if (w_pending) NOSH_CUDA(cudaStreamWaitEvent(s.stream, ev_side, 0));
+  w_pending = false;
+}
 
 // phase-aligned Lagrange extrapolation of the newest (order+1) states to mu_new
 void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
@@ -197,6 +209,7 @@ void ContinuationImpl::advance_arclength(double ds, int predictor, double theta_
   NOSH_CHECK(std::isfinite(ds) && ds != 0.0, NOSH_ERR_INVALID, "ds must be finite and nonzero");
   NOSH_CHECK(std::isfinite(theta_in) && theta_in > 0.0, NOSH_ERR_INVALID, "theta must be positive");
   theta = theta_in;
+  drain_side();  // a pending coefficient serves only the next learned step
   NewtonState &ns = state_of(s);
   const double g = s.g0, mu0 = mu_of(0);
   const int64_t N = s.N, n2 = 2 * N;
@@ -313,6 +326,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   NewtonState &ns = state_of(s);
   const double g = s.g0;
   if (predictor == NOSH_PREDICT_TANGENT) {
+    drain_side();  // a pending coefficient serves only the next learned step
     // psi0 + (mu_new - mu0) dpsi/dmu
     if (tau.n < (size_t)(2 * s.N)) tau.alloc(2 * s.N);
     // a predictor only: FP32 solves are accurate enough
@@ -344,17 +358,52 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   coef = std::nan("");
   extrapolate(order, mu_new, ns.psi.p);
   double f0 = -1.0;
-  if (predictor == NOSH_PREDICT_LEARNED && net && count >= 4) {
-    // learned correction of the secant prediction; a prediction that already
-    // meets the tolerance is taken as is, otherwise the one with the smaller
-    // residual starts Newton (the secant is the fallback)
+  const bool learned = predictor == NOSH_PREDICT_LEARNED && net && count >= 4;
+  // the weights change (training) or the network is not used: no inference
+  // may still be running
+  const bool overlap = learned && train_left == 0;
+  if (!overlap) drain_side();
+  if (learned) {
+    // learned correction of the secant prediction (built on it in ns.tmp)
     NOSH_CUDA(cudaMemcpyAsync(ns.tmp.p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
     const double *x[4] = {slot(0), slot(1), slot(2), slot(3)};
     const double m[4] = {mu_of(0), mu_of(1), mu_of(2), mu_of(3)};
-    coef = net->predict(x, m, mu_new, ns.tmp.p);
-    f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
-    if (!(f_learned <= opt.tol)) f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.xc.p);
-    if (f_learned <= opt.tol || f_learned < f_secant) {
+    bool compare;
+    if (overlap) {
+      if (!side) {
+        NOSH_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        NOSH_CUDA(cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming));
+        NOSH_CUDA(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
+        NOSH_CUDA(cudaMallocHost(&w_host, sizeof(double)));
+      }
+      // the coefficient inferred during the previous step (or now, on the
+      // first overlapped step)
+      const bool have_w = w_pending;
+      drain_side();
+      net->prepare(x, m, mu_new);
+      if (!have_w) net->infer(s.stream);
+      net->combine(ns.tmp.p, w_host);
+      // the next step's coefficient from these features, under this Newton
+      NOSH_CUDA(cudaEventRecord(ev_main, s.stream));
+      NOSH_CUDA(cudaStreamWaitEvent(side, ev_main, 0));
+      net->infer(side);
+      NOSH_CUDA(cudaEventRecord(ev_side, side));
+      w_pending = true;
+      f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);  // syncs: w_host is valid
+      coef = *w_host;
+      // the secant is evaluated only when the learned prediction looks
+      // broken: far worse than the last prediction taken
+      compare = !(f_learned <= opt.tol) && !(f_learned <= 4.0 * f0_prev);
+    } else {
+      coef = net->predict(x, m, mu_new, ns.tmp.p);
+      f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
+      compare = !(f_learned <= opt.tol);
+    }
+    // a prediction that meets the tolerance is taken as is, otherwise the
+    // one with the smaller residual starts Newton (the secant is the
+    // fallback)
+    if (compare) f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.xc.p);
+    if (!compare || f_learned < f_secant) {
       std::swap(ns.psi, ns.tmp);
       last_used = NOSH_PREDICT_LEARNED;
       f0 = f_learned;  // ns.f holds F of the learned prediction
@@ -362,6 +411,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
       std::swap(ns.f, ns.xc);
       f0 = f_secant;
     }
+    f0_prev = f0;
   }
   newton_core(s, ns, g, mu_new, opt, st, f0);
   if (st.status != NOSH_OK) return;
@@ -384,6 +434,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
 }
 
 void ContinuationImpl::enable_learning(int train_steps, int iters, double lr) {
+  drain_side();
   if (!net) net.reset(new Mpnn(s));
   train_left = train_steps;
   this->train_steps = train_steps;

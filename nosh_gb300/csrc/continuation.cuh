@@ -24,6 +24,18 @@ struct ContinuationImpl {
   double learning_rate = 0.0, train_loss = std::nan("");
   int last_used = NOSH_PREDICT_NONE;
   double f_learned = std::nan(""), f_secant = std::nan(""), coef = std::nan("");
+  // Overlapped inference: once the weights are fixed (after the training
+  // window) the network's coefficient for the next learned step runs on
+  // `side` while this step's Newton solve runs on the handle's stream, from
+  // this step's features (so the coefficient a step uses was inferred one
+  // step earlier).  w_host: pinned copy of the coefficient used.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_side = nullptr;
+  bool w_pending = false;
+  double *w_host = nullptr;
+  double f0_prev = std::nan("");  // residual of the last prediction taken
+  void drain_side();              // handle stream waits for the side stream
+
   // pseudo-arclength: the last normalised tangent (tau, tau_mu) and the
   // parameter scale theta of the arclength norm
   DevBuf<double> tau, va, vb;

@@ -1064,6 +1064,10 @@ struct Mpnn::Impl {
   DevBuf<float> part, pool;
   int enc_grid = 0, layer_grid = 0;
   DevBuf<double> sq, red, dots, Ls, gram, w, loss;
+  // launches go to `stream`: the handle's stream, or a side stream while an
+  // inference overlaps the solver; own reduction scratch for the features
+  cudaStream_t stream;
+  Reducer rd;
   explicit Impl(NlsImpl &nls);
   void refresh_bf16();
   void forward(bool train);               // X -> pooled embedding
@@ -1075,8 +1079,9 @@ struct Mpnn::Impl {
   void readout_launch(bool train);
 };
 
-Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
+Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E), stream(nls.stream) {
   cudaStream_t st = s.stream;
+  rd.init(2 * (vgrid(N) + 64), 4, st);  // history_dots: up to 8 slots of partials
   MeshImpl &m = *s.mesh;
   // normalisation of the edge features from the mesh and fields
   std::vector<double> alpha(s.E), p(s.E);
@@ -1166,7 +1171,7 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E) {
 }
 
 void Mpnn::Impl::refresh_bf16() {
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   const float *P = params.p;
   // encoder: K = 10 features padded to 16 (zero weights in the padding)
   enc_to_bf16<<<div_up(H * 16, 256), 256, 0, st>>>(P + L.enc_w, wt.p + wt_enc);
@@ -1186,7 +1191,7 @@ void Mpnn::Impl::refresh_bf16() {
 
 void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, float *out) {
   const int grid = div_up(N, 64);
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   const __nv_bfloat16 *W = wt.p + wt_off;
   switch (epi) {
     case EPI_LINEAR: gemm64_kernel<EPI_LINEAR><<<grid, 128, 0, st>>>(N, in0, K0, in1, K1, W, out); break;
@@ -1196,14 +1201,14 @@ void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K
 }
 
 void Mpnn::Impl::readout_launch(bool train) {
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   readout<<<1, 4 * H, 0, st>>>(layer_grid, N, pool.p, params.p, L.r1_w, L.r1_b, L.r2_w, L.r2_b, w.p,
                                train ? gram.p : nullptr, grads.p, dz.p, loss.p);
   ++s.launch_count;
 }
 
 void Mpnn::Impl::forward(bool train) {
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   const float *P = params.p;
   MeshImpl &m = *s.mesh;
   const float4 *ef4 = reinterpret_cast<const float4 *>(ef.p);
@@ -1225,7 +1230,7 @@ void Mpnn::Impl::forward(bool train) {
 
 void Mpnn::Impl::wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol,
                        int64_t dst, int64_t bias_dst) {
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   (void)ncol;  // always H
   const int nb = (int)std::min<int64_t>(WG_PARTS, std::max<int64_t>(1, div_up(N, 4 * WG_TILE)));
   const int count = (K0 + K1 + 1) * H;
@@ -1237,7 +1242,7 @@ void Mpnn::Impl::wgrad(const float *in0, int K0, const float *in1, int K1, const
 
 // forward must have run; gram holds the sample's Gram scalars
 double Mpnn::Impl::backward_and_step(float lr) {
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   const float *P = params.p;
   MeshImpl &m = *s.mesh;
   readout_launch(true);  // loss, readout gradients, dz
@@ -1281,14 +1286,14 @@ double Mpnn::Impl::backward_and_step(float lr) {
   }
   double hl = 0.0;
   loss.download(&hl, 1, st);
-  s.sync();
+  NOSH_CUDA(cudaStreamSynchronize(st));
   return hl;
 }
 
 // node features at mu_t from the newest states x[0..3] (mu[0..3]) and, with
 // a target (the converged state at mu_t), the sample's Gram scalars
 void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target) {
-  cudaStream_t st = s.stream;
+  cudaStream_t st = stream;
   const int G = vgrid(N);
   double Lh[9];
   Lh[0] = (t - mu[1]) / (mu[0] - mu[1]);
@@ -1307,20 +1312,20 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
   }
   Ls.upload(Lh, 9, st);
   // <x_k, x_0> for x_1..x_3 and the target, x_0 read once
-  history_dots<<<G, 256, 0, st>>>(N, x[0], x[1], x[2], x[3], target, target ? 4 : 3, s.red.partials.p,
-                                  s.red.counter.p, dots.p);
+  history_dots<<<G, 256, 0, st>>>(N, x[0], x[1], x[2], x[3], target, target ? 4 : 3, rd.partials.p,
+                                  rd.counter.p, dots.p);
   ++s.launch_count;
   normalize_phases<<<1, 32, 0, st>>>(target ? 4 : 3, dots.p);
   ++s.launch_count;
   features_a<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
-                                (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, s.red.partials.p,
-                                s.red.counter.p, red.p);
+                                (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, rd.partials.p,
+                                rd.counter.p, red.p);
   features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x[0], sq.p, X.p);
   s.launch_count += 2;
   if (target) {
     gram_kernel<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
-                                   (const C2<double> *)target, s.mesh->d_cv.p, sq.p, s.red.partials.p,
-                                   s.red.counter.p, gram.p);
+                                   (const C2<double> *)target, s.mesh->d_cv.p, sq.p, rd.partials.p,
+                                   rd.counter.p, gram.p);
     ++s.launch_count;
   }
   NOSH_CUDA(cudaGetLastError());
@@ -1341,6 +1346,26 @@ double Mpnn::predict(const double *const x[4], const double mu[4], double mu_new
   double w = 0.0;
   I.w.download(&w, 1, I.s.stream);  // pageable destination: returns once copied
   return w;
+}
+
+void Mpnn::prepare(const double *const x[4], const double mu[4], double mu_new) {
+  impl->features(x, mu, mu_new, nullptr);
+}
+
+void Mpnn::infer(cudaStream_t st) {
+  Impl &I = *impl;
+  I.stream = st;
+  I.forward(false);
+  I.readout_launch(false);
+  I.stream = I.s.stream;
+}
+
+void Mpnn::combine(double *out, double *w_host) {
+  Impl &I = *impl;
+  combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (C2<double> *)out);
+  ++I.s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  if (w_host) NOSH_CUDA(cudaMemcpyAsync(w_host, I.w.p, sizeof(double), cudaMemcpyDeviceToHost, I.s.stream));
 }
 
 double Mpnn::train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,

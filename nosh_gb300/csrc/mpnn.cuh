@@ -14,6 +14,14 @@ struct Mpnn {
   // x[0..3] at mu[0..3]
   // (returns w)
   double predict(const double *const x[4], const double mu[4], double mu_new, double *out);
+  // the same in parts, for an inference that overlaps the solver: node
+  // features and prediction fields for mu_new (handle stream), the network's
+  // coefficient w on stream `st` (it reads the features, writes w), and
+  // out += q + w c with the current w (handle stream; w copied to w_host, a
+  // pinned scalar, when given)
+  void prepare(const double *const x[4], const double mu[4], double mu_new);
+  void infer(cudaStream_t st);
+  void combine(double *out, double *w_host);
   // optimiser iterations on the transition x[0..3] -> target at mu_t;
   // returns the last relative loss
   double train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,

@@ -189,22 +189,25 @@ def test_learned_predictor_gains_over_secant():
     cont = ng.continuation(model, x0, mu0)
     cont.learning(train_steps=16, iters_per_step=20, learning_rate=2e-3)
     mu, gains = mu0, []
+    prev = (x0.copy(), mu0)
     for k in range(30):
         mu += 0.01
+        cur = cont.state()
         # converged states well below the tolerance serve the 4-point
         # extrapolants the network combines
         st = cont.advance(mu, predictor=ng.PREDICT_LEARNED, refine=1e-12)
         assert st["status"] == 0 and st["f_norm"] <= 1e-10
         lp = cont.last_prediction()
         if k >= 22:  # after the training window (+4 history steps)
-            assert lp["used"] == ng.PREDICT_LEARNED and np.isfinite(lp["f_learned"])
-            if np.isnan(lp["f_secant"]):
-                # the learned prediction met the tolerance: no comparison
-                # (Newton may still polish it towards the refine target)
-                assert lp["f_learned"] <= 1e-10
-                gains.append(np.inf)
-            else:
-                gains.append(lp["f_secant"] / lp["f_learned"])
+            # past the window the coefficient is inferred one step ahead,
+            # overlapping the previous step's Newton solve
+            assert lp["used"] == ng.PREDICT_LEARNED and np.isfinite(lp["f_learned"]) and np.isfinite(lp["coef"])
+            # the secant prediction from the same two states, by the oracle
+            xc, mc = cur
+            xp = O.align_phase(prev[0], xc)
+            sec = xc + (mu - mc) / (mc - prev[1]) * (xc - xp)
+            gains.append(np.linalg.norm(P.compute_f(sec, 1.0, mu)) / max(lp["f_learned"], 1e-16))
+        prev = cur
     # the trained network beats the quadratic extrapolation on its last
     # training transition, and starts Newton far closer than the secant
     assert 0.0 <= lp["train_loss"] < 1.0, lp
