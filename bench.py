@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--m", type=int, default=64, help="cubes per side")
+    ap.add_argument("--seed", type=int, default=2, help="mesh jitter / initial state seed")
+    ap.add_argument("--field", default="constant_curl", choices=["constant_curl", "stress"],
+                    help="magnetic vector potential: 1/2(-y,x,0), or that + 0.05 sin(2 pi z)(1,0,0)")
     ap.add_argument("--mu0", type=float, default=0.5)
     ap.add_argument("--dmu", type=float, default=0.005)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -70,10 +73,20 @@ def parse():
     return ap.parse_args()
 
 
+FIELDS = {"constant_curl": ("1/2(-y,x,0)", "mvp_constant_curl"),
+          "stress": ("1/2(-y,x,0)+0.05sin(2pi z)(1,0,0)", "mvp_stress")}
+
+
+def field_of(args, x):
+    from nosh_gb300 import meshgen
+
+    return getattr(meshgen, FIELDS[args.field][1])(x)
+
+
 def workload(args):
     return {
-        "workload": f"mu-continuation, {args.m}^3 Kuhn-tet unit cube (jittered 0.1h, seed 2), "
-        f"A=1/2(-y,x,0), V=-1, g=1, mu={args.mu0}+k*{args.dmu}, Newton to ||F||_2<=1e-10",
+        "workload": f"mu-continuation, {args.m}^3 Kuhn-tet unit cube (jittered 0.1h, seed {args.seed}), "
+        f"A={FIELDS[args.field][0]}, V=-1, g=1, mu={args.mu0}+k*{args.dmu}, Newton to ||F||_2<=1e-10",
         "mesh_cubes": args.m,
         "dmu": args.dmu,
         "mu0": args.mu0,
@@ -147,19 +160,29 @@ def measured_peak():
 
 
 def profiled_traffic():
-    """dram read+write bytes per launch of the timed kernel from the committed
-    ncu summary (profiles/traffic.txt: `<kernel> <bytes per launch>` lines)."""
+    """dram read+write bytes per launch of the timed kernels from the committed
+    ncu summary (profiles/traffic.txt: `<kernel> <bytes per launch>
+    <algorithmic bytes of the captured launch>` lines, captured at 64^3)."""
     p = os.path.join(ROOT, "profiles", "traffic.txt")
     out = {}
     try:
         with open(p) as f:
             for ln in f:
                 ln = ln.split("#")[0].split()
-                if len(ln) == 2:
-                    out[ln[0]] = float(ln[1])
+                if len(ln) == 3:
+                    out[ln[0]] = (float(ln[1]), float(ln[2]))
     except OSError:
         pass
     return out
+
+
+def scaled_traffic(traffic, name, alg_bytes):
+    """Captured traffic scaled to this workload's launch by the ratio of
+    algorithmic bytes (1 at the captured 64^3 workload)."""
+    if name not in traffic:
+        return None
+    t, alg = traffic[name]
+    return t * alg_bytes / alg
 
 
 def dist_env():
@@ -178,9 +201,9 @@ def cpu_run(args, steps, time_budget=None, x=None, cells=None, psi0=None):
     if x is None:
         from nosh_gb300 import meshgen
 
-        x, cells, psi0 = meshgen.cube(args.m, 2)
+        x, cells, psi0 = meshgen.cube(args.m, args.seed)
     m = O.finish_mesh(x, cells)
-    P = O.Problem(m, O.mvp_constant_curl(m.x))
+    P = O.Problem(m, field_of(args, m.x))
     S = O.CpuSolver(P)
     cur = psi0.copy()
     st = S.newton(cur, args.mu0)
@@ -250,8 +273,8 @@ def run_gb300(args):
     from nosh_gb300 import meshgen
 
     dev = torch.device("cuda", torch.cuda.current_device())
-    x, cells, psi0 = meshgen.cube(args.m, 2)
-    A = meshgen.mvp_constant_curl(x)
+    x, cells, psi0 = meshgen.cube(args.m, args.seed)
+    A = field_of(args, x)
     gm = ng.mesh(x, cells)
     prec = ng.PREC_MIXED if args.precision == "mixed" else ng.PREC_FP64
     model = ng.nls(gm, A, -1.0, 1.0, 1.0, mu=args.mu0, precision=prec)
@@ -385,7 +408,10 @@ def run_gb300(args):
         ach = (bytes_l / n_l) / (ms_l / n_l * 1e-3) / 1e9
         d = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
              "peak_kind": peak_kind, "kernel": name, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
-             "algorithmic_bytes_per_launch": bytes_l / n_l, "traffic": traffic.get(name),
+             "algorithmic_bytes_per_launch": bytes_l / n_l,
+             "traffic": scaled_traffic(traffic, name, bytes_l / n_l),
+             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 64^3 launch"
+                               + ("" if args.m == 64 else ", scaled to this launch by its algorithmic bytes"),
              "timing": "CUDA events around each launch on the library stream, during extra continuation "
                        "steps of the same workload run after the timed ones"}
         if name == dom:
