@@ -446,6 +446,22 @@ def arclength_step(P: Problem, psi0, mu0, ds, g=1.0, prev=None, predictor="tange
     return psi, mu, tm, its
 
 
+def lowest_eigenvalues(P: Problem, psi, g, mu, k, sigma=-0.1):
+    """The k eigenvalues of the real-symmetric Jacobian nearest ``sigma``
+    from below the spectrum (shift-invert Lanczos, scipy eigsh), without the
+    U(1) gauge mode i*psi (the eigenvector overlapping it most is dropped).
+    Stands in for the reference's Anasazi solve on the Jacobian
+    (executables/nosh-eig/nosh-eig.cpp)."""
+    import scipy.sparse.linalg as spla
+
+    J = P.jac_csr_real(psi, g, mu).tocsc()
+    vals, vecs = spla.eigsh(J, k=k + 1, sigma=sigma, which="LM")
+    u = _gauge(psi)
+    u = u / np.linalg.norm(u)
+    drop = int(np.argmax(np.abs(u @ vecs)))
+    return np.sort(np.delete(vals, drop))
+
+
 def align_phase(psi, ref):
     """Rotate psi by the global phase that best matches ref (U(1) gauge)."""
     z = psi[0::2] + 1j * psi[1::2]
