@@ -251,6 +251,14 @@ typedef struct {
                              States converged well below tol keep
                              high-order continuation predictors at their
                              truncation error                             */
+  int phase_fix;          /* 0 (default) or 1: every Newton update is made
+                             orthogonal to i psi, the U(1) gauge direction
+                             (J(i psi) = i F).  This is the solution the
+                             reference's bordered system gives,
+                             [J, i psi; (i psi)^T, 0]
+                             (src/bordering/ModelEvaluator_Bordered.cpp:
+                             187-283): F is orthogonal to i psi, so the
+                             border only removes the null direction     */
 } nosh_newton_options;
 
 typedef struct {

@@ -64,6 +64,7 @@ class NewtonOptions(C.Structure):
         ("precision", C.c_int),
         ("verbose", C.c_int),
         ("refine", C.c_double),
+        ("phase_fix", C.c_int),
     ]
 
 
@@ -444,11 +445,12 @@ class nls:
         return n.value, ms.value, b.value
 
     # -- solvers
-    def _options(self, tol, max_newton, forcing, max_krylov, precision, verbose, refine=0.0):
+    def _options(self, tol, max_newton, forcing, max_krylov, precision, verbose, refine=0.0, phase_fix=False):
         o = NewtonOptions()
         _lib.nosh_newton_default_options(C.byref(o))
         o.tol, o.max_newton, o.forcing, o.max_krylov = tol, max_newton, forcing, max_krylov
         o.refine = refine
+        o.phase_fix = 1 if phase_fix else 0
         o.precision = self.precision if precision is None else precision
         o.verbose = verbose
         return o
@@ -478,10 +480,12 @@ class nls:
         return self._stats(st)
 
     def newton(self, x, params, tol=1e-10, max_newton=20, forcing=0.0, max_krylov=1000, precision=None,
-               verbose=0, refine=0.0):
+               verbose=0, refine=0.0, phase_fix=False):
         """Full-step inexact Newton with AMG-preconditioned MINRES; ``x`` is
-        updated in place (numpy array or device tensor).  Returns stats."""
-        o = self._options(tol, max_newton, forcing, max_krylov, precision, verbose, refine)
+        updated in place (numpy array or device tensor).  ``phase_fix``
+        keeps every update orthogonal to the gauge direction i*psi (the
+        reference's bordered system).  Returns stats."""
+        o = self._options(tol, max_newton, forcing, max_krylov, precision, verbose, refine, phase_fix)
         st = NewtonStats()
         rc = _lib.nosh_newton_solve(self._h, _ptr(x), _ptr(self._pvec(params)), C.byref(o), C.byref(st))
         _check(rc, allow=(ERR_NOT_CONVERGED,))

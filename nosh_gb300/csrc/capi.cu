@@ -571,6 +571,7 @@ void nosh_newton_default_options(nosh_newton_options *opt) {
   opt->precision = NOSH_PREC_MIXED;
   opt->verbose = 0;
   opt->refine = 0.0;
+  opt->phase_fix = 0;
 }
 
 int nosh_newton_solve(nosh_nls nls, double *x, const double *p, const nosh_newton_options *opt,

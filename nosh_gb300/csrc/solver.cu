@@ -344,6 +344,31 @@ __global__ void cast_from(int64_t n, const T *__restrict__ a, double *__restrict
     b[i] = (double)a[i];
 }
 
+// <i psi, x> and |psi|^2 over complex entries (x in the Krylov precision)
+template <typename T>
+__global__ void gauge_dots(int64_t n, const T *__restrict__ x, const double *__restrict__ psi, double *partials,
+                           unsigned *counter, double *out) {
+  double a = 0.0, b = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pr = psi[2 * i], pi = psi[2 * i + 1];
+    a += pr * (double)x[2 * i + 1] - pi * (double)x[2 * i];
+    b += pr * pr + pi * pi;
+  }
+  grid_reduce(a, partials, counter, out);
+  grid_reduce(b, partials + gridDim.x, counter + 1, out + 1);
+}
+
+// x -= (<i psi, x> / |psi|^2) i psi, the coefficients from gauge_dots
+template <typename T>
+__global__ void gauge_remove(int64_t n, T *__restrict__ x, const double *__restrict__ psi,
+                             const double *__restrict__ d) {
+  const double k = d[1] > 0.0 ? d[0] / d[1] : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[2 * i] = (T)((double)x[2 * i] + k * psi[2 * i + 1]);
+    x[2 * i + 1] = (T)((double)x[2 * i + 1] - k * psi[2 * i]);
+  }
+}
+
 template <typename T>
 __global__ void axpy_to(int64_t n, double a, const T *__restrict__ t, const double *__restrict__ x,
                         double *__restrict__ y) {
@@ -464,6 +489,14 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     if (status == NOSH_ERR_NAN || status == NOSH_ERR_BREAKDOWN) {
       st.status = status;
       return;
+    }
+    if (opt.phase_fix) {
+      // the bordered system's update: no component along i psi
+      const int Gc = vec_grid(s.N);
+      gauge_dots<T><<<Gc, 256, 0, s.stream>>>(s.N, mr.x.p, ns.psi.p, s.red.partials.p, s.red.counter.p,
+                                               ns.red2.p);
+      gauge_remove<T><<<Gc, 256, 0, s.stream>>>(s.N, mr.x.p, ns.psi.p, ns.red2.p);
+      s.launch_count += 2;
     }
     axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, ns.psi.p);
     ++s.launch_count;

@@ -359,11 +359,14 @@ def real_graph_from_complex(row_ptr, cols):
 
 # --------------------------------------------------------------------------
 # Newton with exact linear algebra (small cases): the converged-state oracle.
-def newton_exact(P: Problem, psi0, g, mu, tol=1e-12, max_it=30):
+def newton_exact(P: Problem, psi0, g, mu, tol=1e-12, max_it=30, phase_fix=False):
     """Full-step Newton on F(psi) = 0 with MINRES preconditioned by an exact
     LU of the regularised KEO (scipy), FP64.  The Jacobian is singular along
     the gauge direction i*psi; MINRES handles the consistent singular system.
-    Returns (psi, [||F|| per step])."""
+    With ``phase_fix`` every update is made orthogonal to i*psi, the
+    solution of the reference's bordered system
+    (src/bordering/ModelEvaluator_Bordered.cpp).  Returns
+    (psi, [||F|| per step])."""
     import scipy.sparse.linalg as spla
 
     psi = np.array(psi0, dtype=np.float64, copy=True)
@@ -376,6 +379,9 @@ def newton_exact(P: Problem, psi0, g, mu, tol=1e-12, max_it=30):
         lu = spla.splu(P.kreg_csr_real(psi, g, mu).tocsc())
         M = spla.LinearOperator(J.shape, matvec=lu.solve)
         dx, _ = spla.minres(J, -F, M=M, rtol=1e-13, maxiter=2000)
+        if phase_fix:
+            ip = _gauge(psi)
+            dx = dx - (ip @ dx) / (ip @ ip) * ip
         psi = psi + dx
         hist.append(np.linalg.norm(P.compute_f(psi, g, mu)))
     return psi, hist
