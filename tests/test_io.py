@@ -1,0 +1,83 @@
+"""Mesh and state files (.vtu): bit-exact round trips of meshes, states and
+fields, ASCII arrays, the per-step data saver's file names and contents, and
+the reader's checks."""
+import os
+
+import numpy as np
+import pytest
+
+from nosh_gb300 import io as nio
+from nosh_gb300 import meshgen
+
+
+def test_round_trip_triangles_and_tets(tmp_path):
+    for x, c, _ in (meshgen.square(9, 3), meshgen.cube(3, 4)):
+        rng = np.random.default_rng(1)
+        psi = rng.standard_normal(2 * len(x))
+        A = meshgen.mvp_constant_curl(x)
+        V = rng.standard_normal(len(x))
+        p = str(tmp_path / "m.vtu")
+        nio.write_vtu(p, x, c, nio.state_point_data(psi, A, V), {"mu": 0.25, "step": 3})
+        x2, c2, pd, fd = nio.read_vtu(p)
+        np.testing.assert_array_equal(x2[:, : x.shape[1]], x)
+        np.testing.assert_array_equal(c2, c)
+        np.testing.assert_array_equal(pd["psi"].reshape(-1), psi)
+        np.testing.assert_array_equal(pd["A"], A.reshape(-1, 3))
+        np.testing.assert_array_equal(pd["V"], V)
+        assert fd["mu"][0] == 0.25 and fd["step"][0] == 3
+        xs, cs, psi2, fields, _ = nio.read_state(p)
+        np.testing.assert_array_equal(psi2, psi)
+        assert set(fields) == {"A", "V"}
+
+
+ASCII = """<?xml version="1.0"?>
+<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian">
+  <UnstructuredGrid>
+    <Piece NumberOfPoints="4" NumberOfCells="2">
+      <PointData>
+        <DataArray type="Float64" Name="psi" NumberOfComponents="2" format="ascii">1 0 1 0 0.5 0.5 1 -1</DataArray>
+      </PointData>
+      <Points>
+        <DataArray type="Float64" NumberOfComponents="3" format="ascii">0 0 0 1 0 0 0 1 0 1 1 0</DataArray>
+      </Points>
+      <Cells>
+        <DataArray type="Int32" Name="connectivity" format="ascii">0 1 2 1 3 2</DataArray>
+        <DataArray type="Int32" Name="offsets" format="ascii">3 6</DataArray>
+        <DataArray type="UInt8" Name="types" format="ascii">5 5</DataArray>
+      </Cells>
+    </Piece>
+  </UnstructuredGrid>
+</VTKFile>
+"""
+
+
+def test_ascii_arrays(tmp_path):
+    p = tmp_path / "a.vtu"
+    p.write_text(ASCII)
+    x, c, pd, fd = nio.read_vtu(str(p))
+    assert x.shape == (4, 3) and c.tolist() == [[0, 1, 2], [1, 3, 2]]
+    assert pd["psi"].reshape(-1).tolist() == [1, 0, 1, 0, 0.5, 0.5, 1, -1]
+    bad = ASCII.replace(">0 1 2 1 3 2<", ">0 1 2 1 3 7<")
+    p.write_text(bad)
+    with pytest.raises(ValueError):
+        nio.read_vtu(str(p))
+    p.write_text(ASCII.replace(">5 5<", ">5 10<"))
+    with pytest.raises(ValueError):
+        nio.read_vtu(str(p))
+
+
+def test_point_data_size_checked(tmp_path):
+    x, c, _ = meshgen.square(5, 1)
+    with pytest.raises(ValueError):
+        nio.write_vtu(str(tmp_path / "b.vtu"), x, c, {"V": np.zeros(len(x) + 1)})
+
+
+def test_data_saver_names_and_contents(tmp_path):
+    x, c, _ = meshgen.square(5, 1)
+    saver = nio.DataSaver(x, c, directory=str(tmp_path), A=meshgen.mvp_constant_curl(x))
+    for k in range(3):
+        saver(k, np.full(2 * len(x), k, np.float64), 0.1 * k)
+    saver.close()
+    assert [os.path.basename(p) for p in saver.paths] == ["out0000.vtu", "out0001.vtu", "out0002.vtu"]
+    _, _, psi, fields, fd = nio.read_state(saver.paths[2])
+    assert np.all(psi == 2.0) and fd["mu"][0] == pytest.approx(0.2) and "A" in fields and "V" not in fields
