@@ -356,16 +356,17 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   f_learned = std::nan("");
   f_secant = std::nan("");
   coef = std::nan("");
-  extrapolate(order, mu_new, ns.psi.p);
-  double f0 = -1.0;
   const bool learned = predictor == NOSH_PREDICT_LEARNED && net && count >= 4;
+  // (a learned step forms the secant with its features)
+  if (!learned) extrapolate(order, mu_new, ns.psi.p);
+  double f0 = -1.0;
   // the weights change (training) or the network is not used: no inference
   // may still be running
   const bool overlap = learned && train_left == 0;
   if (!overlap) drain_side();
   if (learned) {
-    // learned correction of the secant prediction (built on it in ns.tmp)
-    NOSH_CUDA(cudaMemcpyAsync(ns.tmp.p, ns.psi.p, 2 * s.N * sizeof(double), cudaMemcpyDeviceToDevice, s.stream));
+    // learned correction of the secant prediction: the secant into ns.psi
+    // (the fallback), the learned prediction into ns.tmp
     const double *x[4] = {slot(0), slot(1), slot(2), slot(3)};
     const double m[4] = {mu_of(0), mu_of(1), mu_of(2), mu_of(3)};
     bool compare;
@@ -380,9 +381,9 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
       // first overlapped step)
       const bool have_w = w_pending;
       drain_side();
-      net->prepare(x, m, mu_new);
+      net->prepare(x, m, mu_new, ns.psi.p);
       if (!have_w) net->infer(s.stream);
-      net->combine(ns.tmp.p, w_host);
+      net->combine(ns.psi.p, ns.tmp.p, w_host);
       // the next step's coefficient from these features, under this Newton
       NOSH_CUDA(cudaEventRecord(ev_main, s.stream));
       NOSH_CUDA(cudaStreamWaitEvent(side, ev_main, 0));
@@ -395,7 +396,7 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
       // broken: far worse than the last prediction taken
       compare = !(f_learned <= opt.tol) && !(f_learned <= 4.0 * f0_prev);
     } else {
-      coef = net->predict(x, m, mu_new, ns.tmp.p);
+      coef = net->predict(x, m, mu_new, ns.psi.p, ns.tmp.p);
       f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
       compare = !(f_learned <= opt.tol);
     }

@@ -196,6 +196,8 @@ constexpr int LDE = 16 + 8;
 constexpr size_t kLayerSmem = (size_t)(H * LDU + 2 * H * LDAB + 4 * 16 * LDM) * sizeof(__nv_bfloat16) +
                               4 * H * sizeof(float);
 constexpr size_t kEncSmem = (size_t)(H * LDE + 2 * H * LDAB) * sizeof(__nv_bfloat16);
+// the update-only layer (M from global memory): no M staging
+constexpr size_t kUpdateSmem = (size_t)(H * LDU + 2 * H * LDAB) * sizeof(__nv_bfloat16) + 4 * H * sizeof(float);
 
 __device__ __forceinline__ void frag_from_c(const float (&v)[8][4], int kk, uint32_t &a0, uint32_t &a1,
                                             uint32_t &a2, uint32_t &a3) {
@@ -305,25 +307,141 @@ __global__ void __launch_bounds__(128) encode_kernel(int64_t n, const float *__r
   }
 }
 
+// Per-lane message constants: W_c rows 0..2 for the lane's 4 channels
+// (packed FP16) and b_m + W_c[3] (the constant edge feature folded in).
+struct MsgConst {
+  __half2 w2[3][2];
+  float abias[4];
+};
+
+__device__ __forceinline__ void msg_const(const float *__restrict__ Wc, const float *__restrict__ bm, int c4,
+                                          MsgConst &k) {
+#pragma unroll
+  for (int f = 0; f < 3; f++) {
+    const float4 w = *reinterpret_cast<const float4 *>(Wc + f * H + c4);
+    k.w2[f][0] = __floats2half2_rn(w.x, w.y);
+    k.w2[f][1] = __floats2half2_rn(w.z, w.w);
+  }
+  const float4 b = *reinterpret_cast<const float4 *>(bm + c4);
+  const float4 w3 = *reinterpret_cast<const float4 *>(Wc + 3 * H + c4);
+  k.abias[0] = b.x + w3.x;
+  k.abias[1] = b.y + w3.y;
+  k.abias[2] = b.z + w3.z;
+  k.abias[3] = b.w + w3.w;
+}
+
+// M_r for the lane's 4 channels (c4 = 4 (lane % 16)); a half-warp per row,
+// both halves of the warp call together (the neighbour shuffles span the
+// warp); rows r >= n give zeros.  Packed FP16 message arithmetic: a = A_r +
+// b_m + W_c[3], two channels per instruction; the 16 neighbour gathers of a
+// batch are unconditional (row 0 stands in for missing neighbours, masked
+// out of the sum) so all are in flight at once.
+__device__ __forceinline__ void aggregate_row(int64_t r, int64_t n, const int32_t *__restrict__ rp,
+                                              const int32_t *__restrict__ ci, const float4 *__restrict__ ef,
+                                              const __half *__restrict__ A, const __half *__restrict__ B,
+                                              const MsgConst &k, int hl, int half, int c4, float (&m)[4]) {
+  const __half2 zero2 = __float2half2_rn(0.f);
+  int32_t beg = 0, deg = 0;
+  __half2 a2[2] = {zero2, zero2}, m2[2] = {zero2, zero2};
+  if (r < n) {
+    beg = rp[r];
+    deg = rp[r + 1] - beg;
+    const uint2 av = *reinterpret_cast<const uint2 *>(A + r * H + c4);
+    const float2 a01 = __half22float2(*reinterpret_cast<const __half2 *>(&av.x));
+    const float2 a23 = __half22float2(*reinterpret_cast<const __half2 *>(&av.y));
+    a2[0] = __floats2half2_rn(a01.x + k.abias[0], a01.y + k.abias[1]);
+    a2[1] = __floats2half2_rn(a23.x + k.abias[2], a23.y + k.abias[3]);
+  }
+  const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+  for (int k0 = 0; k0 < maxdeg; k0 += 16) {
+    // each lane fetches one neighbour index and its edge features
+    const bool ok = k0 + hl < deg;
+    const int32_t jl = ok ? ci[beg + k0 + hl] : 0;
+    const float4 el = ok ? ef[beg + k0 + hl] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int cnt = deg - k0;  // this half's remaining neighbours (may be <= 0)
+    uint2 bv[16];
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      const int32_t j = __shfl_sync(0xffffffffu, jl, (half << 4) + u);
+      bv[u] = *reinterpret_cast<const uint2 *>(B + (int64_t)j * H + c4);
+    }
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      const int src = (half << 4) + u;
+      const __half2 ex = __float2half2_rn(__shfl_sync(0xffffffffu, el.x, src));
+      const __half2 ey = __float2half2_rn(__shfl_sync(0xffffffffu, el.y, src));
+      const __half2 ez = __float2half2_rn(__shfl_sync(0xffffffffu, el.z, src));
+      const __half2 *bb = reinterpret_cast<const __half2 *>(&bv[u]);
+      const bool live = u < cnt;
+#pragma unroll
+      for (int cc = 0; cc < 2; cc++) {
+        __half2 pv = __hadd2(a2[cc], bb[cc]);
+        pv = __hfma2(ex, k.w2[0][cc], pv);
+        pv = __hfma2(ey, k.w2[1][cc], pv);
+        pv = __hfma2(ez, k.w2[2][cc], pv);
+        if (live) m2[cc] = __hadd2(m2[cc], __hmax2(pv, zero2));
+      }
+    }
+  }
+  const float2 m01 = __half22float2(m2[0]), m23 = __half22float2(m2[1]);
+  m[0] = m01.x;
+  m[1] = m01.y;
+  m[2] = m23.x;
+  m[3] = m23.y;
+}
+
+// Inference split of a layer: the aggregation alone, at high occupancy (the
+// fused layer holds 12 warps per SM and waits on the gathers), writing M in
+// BF16 (the update GEMM's operand, rounded as the fused layer rounds it).
+__global__ void __launch_bounds__(256, 4) mp_aggregate_kernel(int64_t n, const int32_t *__restrict__ rp,
+                                                           const int32_t *__restrict__ ci,
+                                                           const float4 *__restrict__ ef,
+                                                           const __half *__restrict__ A,
+                                                           const __half *__restrict__ B,
+                                                           const float *__restrict__ Wc,
+                                                           const float *__restrict__ bm,
+                                                           __nv_bfloat16 *__restrict__ Mb) {
+  const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4, c4 = hl * 4;
+  MsgConst k;
+  msg_const(Wc, bm, c4, k);
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  // warp-uniform loop over row pairs (a half-warp per row)
+  for (int64_t r0 = 2 * warp; r0 < n; r0 += 2 * nwarps) {
+    const int64_t r = r0 + half;
+    float m[4];
+    aggregate_row(r, n, rp, ci, ef, A, B, k, hl, half, c4, m);
+    if (r < n) {
+      uint2 mv;
+      *reinterpret_cast<__nv_bfloat162 *>(&mv.x) = __floats2bfloat162_rn(m[0], m[1]);
+      *reinterpret_cast<__nv_bfloat162 *>(&mv.y) = __floats2bfloat162_rn(m[2], m[3]);
+      *reinterpret_cast<uint2 *>(Mb + r * H + c4) = mv;
+    }
+  }
+}
+
 // One message-passing layer:
 //   M_i = sum_j relu(A_i + B_j + e_ij W_c + b_m)          (FP32 sums)
 //   R   = relu(bf16([h, M]) @ bf16(W_u) + b_u),  h' = h + R
 // then, for all but the last layer, the next layer's A, B from h'; the last
 // layer writes per-CTA column sums of h' (the mean-pool partials) instead of
-// h'.  TRAIN also stores M and R (FP32) for the backward pass.
-template <bool TRAIN, bool LAST>
+// h'.  TRAIN also stores M and R (FP32) for the backward pass.  PRE_M (the
+// inference split): M comes from mp_aggregate_kernel in BF16 (Mb) and the
+// kernel is the update GEMM alone.
+template <bool TRAIN, bool LAST, bool PRE_M>
 __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
     int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const float4 *__restrict__ ef,
     const float *__restrict__ h, const __half *__restrict__ A, const __half *__restrict__ B,
     const float *__restrict__ Wc, const float *__restrict__ bm, const __nv_bfloat16 *__restrict__ Wu,
     const float *__restrict__ bu, const __nv_bfloat16 *__restrict__ Wab, float *__restrict__ h_out,
     __half *__restrict__ A_out, __half *__restrict__ B_out, float *__restrict__ M_out,
-    float *__restrict__ R_out, float *__restrict__ pool) {
+    float *__restrict__ R_out, float *__restrict__ pool, const __nv_bfloat16 *__restrict__ Mb) {
+  static_assert(!(TRAIN && PRE_M), "training runs the fused layer");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *sWu = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
   __nv_bfloat16 *sWab = sWu + H * LDU;
   __nv_bfloat16 *sM = sWab + 2 * H * LDAB;
-  float *sPool = reinterpret_cast<float *>(sM + 4 * 16 * LDM);
+  float *sPool = reinterpret_cast<float *>(PRE_M ? sM : sM + 4 * 16 * LDM);
   stage_w(sWu, Wu, H, 2 * H, LDU);
   if (!LAST) stage_w(sWab, Wab, 2 * H, H, LDAB);
   __syncthreads();
@@ -331,20 +449,8 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
   __nv_bfloat16 *sMw = sM + warp * 16 * LDM;
   // aggregation: a half-warp per row, 4 channels per lane
   const int hl = lane & 15, half = lane >> 4, c4 = hl * 4;
-  __half2 w2[3][2];  // W_c rows 0..2 for this lane's channels, packed
-  float abias[4];    // b_m + W_c[3] (the constant edge feature)
-  const __half2 zero2 = __float2half2_rn(0.f);
-#pragma unroll
-  for (int f = 0; f < 3; f++) {
-    const float4 w = *reinterpret_cast<const float4 *>(Wc + f * H + c4);
-    w2[f][0] = __floats2half2_rn(w.x, w.y);
-    w2[f][1] = __floats2half2_rn(w.z, w.w);
-  }
-  {
-    const float4 b = *reinterpret_cast<const float4 *>(bm + c4);
-    const float4 w3 = *reinterpret_cast<const float4 *>(Wc + 3 * H + c4);
-    abias[0] = b.x + w3.x; abias[1] = b.y + w3.y; abias[2] = b.z + w3.z; abias[3] = b.w + w3.w;
-  }
+  MsgConst mk;
+  if (!PRE_M) msg_const(Wc, bm, c4, mk);
   float psum[8][2];
 #pragma unroll
   for (int t = 0; t < 8; t++) psum[t][0] = psum[t][1] = 0.f;
@@ -353,62 +459,18 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
   for (int64_t tile = t0; tile < t1; tile++) {
     const int64_t r0 = tile * TILE + warp * 16;
     if (r0 >= n) continue;
-    for (int p = 0; p < 8; p++) {
-      const int rr = 2 * p + half;
-      const int64_t r = r0 + rr;
-      int32_t beg = 0, deg = 0;
-      // packed FP16 message arithmetic: a = A_i + b_m + W_c[3] (the edge
-      // features' constant 1 folded in), two channels per instruction
-      __half2 a2[2] = {zero2, zero2}, m2[2] = {zero2, zero2};
-      if (r < n) {
-        beg = rp[r];
-        deg = rp[r + 1] - beg;
-        const uint2 av = *reinterpret_cast<const uint2 *>(A + r * H + c4);
-        const float2 a01 = __half22float2(*reinterpret_cast<const __half2 *>(&av.x));
-        const float2 a23 = __half22float2(*reinterpret_cast<const __half2 *>(&av.y));
-        a2[0] = __floats2half2_rn(a01.x + abias[0], a01.y + abias[1]);
-        a2[1] = __floats2half2_rn(a23.x + abias[2], a23.y + abias[3]);
+    if (!PRE_M) {
+      for (int p = 0; p < 8; p++) {
+        const int rr = 2 * p + half;
+        const int64_t r = r0 + rr;
+        float m[4];
+        aggregate_row(r, n, rp, ci, ef, A, B, mk, hl, half, c4, m);
+        uint2 mv;
+        *reinterpret_cast<__nv_bfloat162 *>(&mv.x) = __floats2bfloat162_rn(m[0], m[1]);
+        *reinterpret_cast<__nv_bfloat162 *>(&mv.y) = __floats2bfloat162_rn(m[2], m[3]);
+        *reinterpret_cast<uint2 *>(sMw + rr * LDM + c4) = mv;
+        if (TRAIN && r < n) *reinterpret_cast<float4 *>(M_out + r * H + c4) = make_float4(m[0], m[1], m[2], m[3]);
       }
-      const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
-      for (int k0 = 0; k0 < maxdeg; k0 += 16) {
-        // each lane fetches one neighbour index and its edge features; the
-        // gathers below are unconditional (row 0 stands in for missing
-        // neighbours, masked out of the sum) so all 16 are in flight at once
-        const bool ok = k0 + hl < deg;
-        const int32_t jl = ok ? ci[beg + k0 + hl] : 0;
-        const float4 el = ok ? ef[beg + k0 + hl] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const int cnt = deg - k0;  // this half's remaining neighbours (may be <= 0)
-        uint2 bv[16];
-#pragma unroll
-        for (int u = 0; u < 16; u++) {
-          const int32_t j = __shfl_sync(0xffffffffu, jl, (half << 4) + u);
-          bv[u] = *reinterpret_cast<const uint2 *>(B + (int64_t)j * H + c4);
-        }
-#pragma unroll
-        for (int u = 0; u < 16; u++) {
-          const int src = (half << 4) + u;
-          const __half2 ex = __float2half2_rn(__shfl_sync(0xffffffffu, el.x, src));
-          const __half2 ey = __float2half2_rn(__shfl_sync(0xffffffffu, el.y, src));
-          const __half2 ez = __float2half2_rn(__shfl_sync(0xffffffffu, el.z, src));
-          const __half2 *bb = reinterpret_cast<const __half2 *>(&bv[u]);
-          const bool live = u < cnt;
-#pragma unroll
-          for (int cc = 0; cc < 2; cc++) {
-            __half2 pv = __hadd2(a2[cc], bb[cc]);
-            pv = __hfma2(ex, w2[0][cc], pv);
-            pv = __hfma2(ey, w2[1][cc], pv);
-            pv = __hfma2(ez, w2[2][cc], pv);
-            if (live) m2[cc] = __hadd2(m2[cc], __hmax2(pv, zero2));
-          }
-        }
-      }
-      const float2 m01 = __half22float2(m2[0]), m23 = __half22float2(m2[1]);
-      const float m[4] = {m01.x, m01.y, m23.x, m23.y};
-      uint2 mv;
-      *reinterpret_cast<__nv_bfloat162 *>(&mv.x) = __floats2bfloat162_rn(m[0], m[1]);
-      *reinterpret_cast<__nv_bfloat162 *>(&mv.y) = __floats2bfloat162_rn(m[2], m[3]);
-      *reinterpret_cast<uint2 *>(sMw + rr * LDM + c4) = mv;
-      if (TRAIN && r < n) *reinterpret_cast<float4 *>(M_out + r * H + c4) = make_float4(m[0], m[1], m[2], m[3]);
     }
     __syncwarp();
     // update GEMM: K = 128 = [h (registers) | M (shared memory)]
@@ -437,11 +499,22 @@ __global__ void __launch_bounds__(128, 3) mp_layer_kernel(
     }
 #pragma unroll
     for (int kk = 0; kk < 4; kk++) {
-      const __nv_bfloat16 *mrow = sMw + kk * 16 + q * 2;
-      const uint32_t a0 = *reinterpret_cast<const uint32_t *>(mrow + g * LDM);
-      const uint32_t a1 = *reinterpret_cast<const uint32_t *>(mrow + (g + 8) * LDM);
-      const uint32_t a2 = *reinterpret_cast<const uint32_t *>(mrow + g * LDM + 8);
-      const uint32_t a3 = *reinterpret_cast<const uint32_t *>(mrow + (g + 8) * LDM + 8);
+      uint32_t a0, a1, a2, a3;
+      if (PRE_M) {
+        // the A-fragment straight from the BF16 rows (zeros past n, as the
+        // fused aggregation gives)
+        const __nv_bfloat16 *ma = Mb + ra * H + kk * 16 + q * 2, *mb = Mb + rb * H + kk * 16 + q * 2;
+        a0 = ra < n ? *reinterpret_cast<const uint32_t *>(ma) : 0u;
+        a1 = rb < n ? *reinterpret_cast<const uint32_t *>(mb) : 0u;
+        a2 = ra < n ? *reinterpret_cast<const uint32_t *>(ma + 8) : 0u;
+        a3 = rb < n ? *reinterpret_cast<const uint32_t *>(mb + 8) : 0u;
+      } else {
+        const __nv_bfloat16 *mrow = sMw + kk * 16 + q * 2;
+        a0 = *reinterpret_cast<const uint32_t *>(mrow + g * LDM);
+        a1 = *reinterpret_cast<const uint32_t *>(mrow + (g + 8) * LDM);
+        a2 = *reinterpret_cast<const uint32_t *>(mrow + g * LDM + 8);
+        a3 = *reinterpret_cast<const uint32_t *>(mrow + (g + 8) * LDM + 8);
+      }
 #pragma unroll
       for (int t = 0; t < 8; t++) {
         const __nv_bfloat16 *w = sWu + (t * 8 + g) * LDU + H + kk * 16 + q * 2;
@@ -833,11 +906,13 @@ __device__ __forceinline__ void phases(const double *c, int k, double &er, doubl
 }
 
 // per node: s = x0 - x1, q = quad - sec, c = cubic - quad at t (fields in
-// sq, 6 doubles per node), and the sums of |s|^2, |q|^2, |c|^2 into red[0..2]
+// sq, 6 doubles per node), the sums of |s|^2, |q|^2, |c|^2 into red[0..2],
+// and (when sec_out is given) the secant prediction itself
 __global__ void features_a(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
                            const C2<double> *__restrict__ x0, const C2<double> *__restrict__ x1,
                            const C2<double> *__restrict__ x2, const C2<double> *__restrict__ x3,
-                           double *__restrict__ sq, double *partials, unsigned *counter, double *red) {
+                           double *__restrict__ sq, C2<double> *__restrict__ sec_out, double *partials,
+                           unsigned *counter, double *red) {
   double er[3], ei[3];
   for (int k = 0; k < 3; k++) phases(dots, k, er[k], ei[k]);
   double as = 0.0, aq = 0.0, ac = 0.0;
@@ -857,6 +932,7 @@ __global__ void features_a(int64_t n, const double *__restrict__ dots, const dou
     const double qdi = Ls[2] * xi[0] + Ls[3] * xi[1] + Ls[4] * xi[2];
     const double cbr = Ls[5] * xr[0] + Ls[6] * xr[1] + Ls[7] * xr[2] + Ls[8] * xr[3];
     const double cbi = Ls[5] * xi[0] + Ls[6] * xi[1] + Ls[7] * xi[2] + Ls[8] * xi[3];
+    if (sec_out) sec_out[i] = C2<double>{secr, seci};
     double *o = sq + 6 * i;
     o[0] = xr[0] - xr[1];
     o[1] = xi[0] - xi[1];
@@ -877,8 +953,12 @@ __global__ void features_a(int64_t n, const double *__restrict__ dots, const dou
 __global__ void features_b(int64_t n, const double *__restrict__ red, double mu_new,
                            const C2<double> *__restrict__ x0, const double *__restrict__ sq,
                            float *__restrict__ X) {
-  const double rs = sqrt(red[0] / n), rq = sqrt(red[1] / n), rc = sqrt(red[2] / n);
-  const double is = rs > 0 ? 1.0 / rs : 0.0, iq = rq > 0 ? 1.0 / rq : 0.0, ic = rc > 0 ? 1.0 / rc : 0.0;
+  // the inverse RMS scales in FP32 (the features are FP32): an FP64 square
+  // root and division per thread cost more than the whole pass
+  const float fn = (float)n;
+  const float rs = sqrtf((float)red[0] / fn), rq = sqrtf((float)red[1] / fn), rc = sqrtf((float)red[2] / fn);
+  const double is = rs > 0.f ? (double)(1.f / rs) : 0.0, iq = rq > 0.f ? (double)(1.f / rq) : 0.0,
+               ic = rc > 0.f ? (double)(1.f / rc) : 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const C2<double> a = x0[i];
     const double *f = sq + 6 * i;
@@ -920,13 +1000,13 @@ __global__ void gram_kernel(int64_t n, const double *__restrict__ dots, const do
   for (int k = 0; k < 3; k++) grid_reduce(acc[k], partials + k * gridDim.x, counter + k, g + k);
 }
 
-// out (the secant prediction) += q + w c
+// out = sec + q + w c (sec: the secant prediction)
 __global__ void combine_kernel(int64_t n, const double *__restrict__ w, const double *__restrict__ sq,
-                               C2<double> *__restrict__ out) {
+                               const C2<double> *__restrict__ sec, C2<double> *__restrict__ out) {
   const double wc = w[0];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double *f = sq + 6 * i;
-    C2<double> o = out[i];
+    C2<double> o = sec[i];
     o.x += f[2] + wc * f[4];
     o.y += f[3] + wc * f[5];
     out[i] = o;
@@ -1062,7 +1142,9 @@ struct Mpnn::Impl {
   DevBuf<__half> A[LAYERS], B[LAYERS];
   DevBuf<float> dH, dR, dM, dA, dB, dz;
   DevBuf<float> part, pool;
-  int enc_grid = 0, layer_grid = 0;
+  DevBuf<__nv_bfloat16> Mb;  // inference split: one layer's M in BF16
+  int enc_grid = 0, layer_grid = 0, agg_grid = 0, upd_grid = 0;
+  int pool_parts = 0;  // pool partial rows written by the last forward
   DevBuf<double> sq, red, dots, Ls, gram, w, loss;
   // launches go to `stream`: the handle's stream, or a side stream while an
   // inference overlaps the solver; own reduction scratch for the features
@@ -1072,7 +1154,8 @@ struct Mpnn::Impl {
   void refresh_bf16();
   void forward(bool train);               // X -> pooled embedding
   double backward_and_step(float lr);     // needs gram
-  void features(const double *const x[4], const double mu[4], double mu_t, const double *target);
+  void features(const double *const x[4], const double mu[4], double mu_t, const double *target,
+                double *secant = nullptr);
   void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, float *out);
   void wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol, int64_t dst,
              int64_t bias_dst);
@@ -1153,11 +1236,23 @@ Mpnn::Impl::Impl(NlsImpl &nls) : s(nls), N(nls.N), nnz(2 * nls.E), stream(nls.st
   part.alloc(std::max<int64_t>((int64_t)WG_PARTS * (2 * H + 1) * H, div_up(N, 64) * 5 * H) + 64);
   const int64_t tiles = div_up(N, (int64_t)TILE);
   enc_grid = persistent_grid((const void *)encode_kernel, kEncSmem, tiles);
-  layer_grid = persistent_grid((const void *)mp_layer_kernel<true, true>, kLayerSmem, tiles);
-  for (const void *k : {(const void *)mp_layer_kernel<false, false>, (const void *)mp_layer_kernel<false, true>,
-                        (const void *)mp_layer_kernel<true, false>})
+  layer_grid = persistent_grid((const void *)mp_layer_kernel<true, true, false>, kLayerSmem, tiles);
+  for (const void *k : {(const void *)mp_layer_kernel<false, false, false>,
+                        (const void *)mp_layer_kernel<false, true, false>,
+                        (const void *)mp_layer_kernel<true, false, false>})
     layer_grid = std::min(layer_grid, persistent_grid(k, kLayerSmem, tiles));
-  pool.alloc((int64_t)layer_grid * H);
+  upd_grid = std::min(persistent_grid((const void *)mp_layer_kernel<false, false, true>, kUpdateSmem, tiles),
+                      persistent_grid((const void *)mp_layer_kernel<false, true, true>, kUpdateSmem, tiles));
+  {
+    int d = 0, sms = 0, per_sm = 0;
+    NOSH_CUDA(cudaGetDevice(&d));
+    NOSH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d));
+    NOSH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mp_aggregate_kernel, 256, 0));
+    // 16 rows per CTA pass (8 warps, a half-warp per row)
+    agg_grid = (int)std::max<int64_t>(1, std::min<int64_t>(div_up(N, 16), (int64_t)std::max(per_sm, 1) * sms));
+  }
+  Mb.alloc(N * H);
+  pool.alloc((int64_t)std::max(layer_grid, upd_grid) * H);
   sq.alloc(6 * N);
   red.alloc(8);
   dots.alloc(8);
@@ -1202,7 +1297,7 @@ void Mpnn::Impl::gemm(int epi, const float *in0, int K0, const float *in1, int K
 
 void Mpnn::Impl::readout_launch(bool train) {
   cudaStream_t st = stream;
-  readout<<<1, 4 * H, 0, st>>>(layer_grid, N, pool.p, params.p, L.r1_w, L.r1_b, L.r2_w, L.r2_b, w.p,
+  readout<<<1, 4 * H, 0, st>>>(pool_parts, N, pool.p, params.p, L.r1_w, L.r1_b, L.r2_w, L.r2_b, w.p,
                                train ? gram.p : nullptr, grads.p, dz.p, loss.p);
   ++s.launch_count;
 }
@@ -1217,12 +1312,28 @@ void Mpnn::Impl::forward(bool train) {
   ++s.launch_count;
   for (int l = 0; l < LAYERS; l++) {
     const bool last = l == LAYERS - 1;
-    auto kernel = train ? (last ? mp_layer_kernel<true, true> : mp_layer_kernel<true, false>)
-                        : (last ? mp_layer_kernel<false, true> : mp_layer_kernel<false, false>);
-    kernel<<<layer_grid, 128, kLayerSmem, st>>>(
-        N, m.d_rp.p, m.d_ci.p, ef4, Hs[l].p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l], wt.p + wt_u[l],
-        P + L.bu[l], last ? nullptr : wt.p + wt_a[l + 1], last ? nullptr : Hs[l + 1].p,
-        last ? nullptr : A[l + 1].p, last ? nullptr : B[l + 1].p, Mg[l].p, R[l].p, pool.p);
+    if (train) {
+      // fused layer (it also stores M and R for the backward pass)
+      auto kernel = last ? mp_layer_kernel<true, true, false> : mp_layer_kernel<true, false, false>;
+      kernel<<<layer_grid, 128, kLayerSmem, st>>>(
+          N, m.d_rp.p, m.d_ci.p, ef4, Hs[l].p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l], wt.p + wt_u[l],
+          P + L.bu[l], last ? nullptr : wt.p + wt_a[l + 1], last ? nullptr : Hs[l + 1].p,
+          last ? nullptr : A[l + 1].p, last ? nullptr : B[l + 1].p, Mg[l].p, R[l].p, pool.p, nullptr);
+      pool_parts = layer_grid;
+    } else {
+      // inference: the aggregation at high occupancy, then the update GEMM
+      // (bitwise the fused layer's result: the same arithmetic and the
+      // same BF16 rounding of M)
+      mp_aggregate_kernel<<<agg_grid, 256, 0, st>>>(N, m.d_rp.p, m.d_ci.p, ef4, A[l].p, B[l].p, P + L.wc[l],
+                                                    P + L.bm[l], Mb.p);
+      auto kernel = last ? mp_layer_kernel<false, true, true> : mp_layer_kernel<false, false, true>;
+      kernel<<<upd_grid, 128, kUpdateSmem, st>>>(
+          N, m.d_rp.p, m.d_ci.p, ef4, Hs[l].p, A[l].p, B[l].p, P + L.wc[l], P + L.bm[l], wt.p + wt_u[l],
+          P + L.bu[l], last ? nullptr : wt.p + wt_a[l + 1], last ? nullptr : Hs[l + 1].p,
+          last ? nullptr : A[l + 1].p, last ? nullptr : B[l + 1].p, nullptr, nullptr, pool.p, Mb.p);
+      pool_parts = upd_grid;
+      ++s.launch_count;
+    }
     ++s.launch_count;
   }
   NOSH_CUDA(cudaGetLastError());
@@ -1292,7 +1403,8 @@ double Mpnn::Impl::backward_and_step(float lr) {
 
 // node features at mu_t from the newest states x[0..3] (mu[0..3]) and, with
 // a target (the converged state at mu_t), the sample's Gram scalars
-void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target) {
+void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target,
+                          double *secant) {
   cudaStream_t st = stream;
   const int G = vgrid(N);
   double Lh[9];
@@ -1318,7 +1430,8 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
   normalize_phases<<<1, 32, 0, st>>>(target ? 4 : 3, dots.p);
   ++s.launch_count;
   features_a<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
-                                (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, rd.partials.p,
+                                (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, (C2<double> *)secant,
+                                rd.partials.p,
                                 rd.counter.p, red.p);
   features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x[0], sq.p, X.p);
   s.launch_count += 2;
@@ -1335,12 +1448,13 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
 Mpnn::Mpnn(NlsImpl &s) : impl(new Impl(s)) {}
 Mpnn::~Mpnn() = default;
 
-double Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, double *out) {
+double Mpnn::predict(const double *const x[4], const double mu[4], double mu_new, double *secant, double *out) {
   Impl &I = *impl;
-  I.features(x, mu, mu_new, nullptr);
+  I.features(x, mu, mu_new, nullptr, secant);
   I.forward(false);
   I.readout_launch(false);
-  combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (C2<double> *)out);
+  combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (const C2<double> *)secant,
+                                                     (C2<double> *)out);
   ++I.s.launch_count;
   NOSH_CUDA(cudaGetLastError());
   double w = 0.0;
@@ -1348,8 +1462,8 @@ double Mpnn::predict(const double *const x[4], const double mu[4], double mu_new
   return w;
 }
 
-void Mpnn::prepare(const double *const x[4], const double mu[4], double mu_new) {
-  impl->features(x, mu, mu_new, nullptr);
+void Mpnn::prepare(const double *const x[4], const double mu[4], double mu_new, double *secant) {
+  impl->features(x, mu, mu_new, nullptr, secant);
 }
 
 void Mpnn::infer(cudaStream_t st) {
@@ -1360,9 +1474,10 @@ void Mpnn::infer(cudaStream_t st) {
   I.stream = I.s.stream;
 }
 
-void Mpnn::combine(double *out, double *w_host) {
+void Mpnn::combine(const double *secant, double *out, double *w_host) {
   Impl &I = *impl;
-  combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (C2<double> *)out);
+  combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (const C2<double> *)secant,
+                                                     (C2<double> *)out);
   ++I.s.launch_count;
   NOSH_CUDA(cudaGetLastError());
   if (w_host) NOSH_CUDA(cudaMemcpyAsync(w_host, I.w.p, sizeof(double), cudaMemcpyDeviceToHost, I.s.stream));

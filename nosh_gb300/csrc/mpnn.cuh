@@ -9,19 +9,19 @@ namespace nosh {
 struct Mpnn {
   explicit Mpnn(NlsImpl &s);
   ~Mpnn();
-  // out (in: the secant prediction to mu_new) += q + w c, the learned
-  // multiple of the cubic-minus-quadratic field, from the newest states
-  // x[0..3] at mu[0..3]
-  // (returns w)
-  double predict(const double *const x[4], const double mu[4], double mu_new, double *out);
+  // From the newest states x[0..3] at mu[0..3]: the secant prediction to
+  // mu_new into `secant`, and out = secant + q + w c, the quadratic
+  // prediction plus the learned multiple w of the cubic-minus-quadratic
+  // field (returns w)
+  double predict(const double *const x[4], const double mu[4], double mu_new, double *secant, double *out);
   // the same in parts, for an inference that overlaps the solver: node
-  // features and prediction fields for mu_new (handle stream), the network's
-  // coefficient w on stream `st` (it reads the features, writes w), and
-  // out += q + w c with the current w (handle stream; w copied to w_host, a
-  // pinned scalar, when given)
-  void prepare(const double *const x[4], const double mu[4], double mu_new);
+  // features, prediction fields and the secant for mu_new (handle stream),
+  // the network's coefficient w on stream `st` (it reads the features,
+  // writes w), and out = secant + q + w c with the current w (handle stream;
+  // w copied to w_host, a pinned scalar, when given)
+  void prepare(const double *const x[4], const double mu[4], double mu_new, double *secant);
   void infer(cudaStream_t st);
-  void combine(double *out, double *w_host);
+  void combine(const double *secant, double *out, double *w_host);
   // optimiser iterations on the transition x[0..3] -> target at mu_t;
   // returns the last relative loss
   double train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,
