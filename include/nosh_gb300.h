@@ -376,9 +376,12 @@ int nosh_mpnn_params(nosh_mpnn net, float *get, const float *set);
 int nosh_mpnn_edge_features(nosh_mpnn net, float *ef);
 /* the readout coefficient *w for node features X (N x 10) */
 int nosh_mpnn_forward(nosh_mpnn net, const float *X, double *w);
-/* the training loss (w^2 cc - 2 w cd + dd) / dd for the cv-weighted Gram
- * scalars gram = [cc, cd, dd] of c and d = target - quadratic, and its
- * parameter gradient; the parameters are not changed */
+/* the training loss (w^2 cc - 2 w cd + dd) / dd for Gram scalars gram =
+ * [cc, cd, dd] (online training uses those of Jc and Jd: c = cubic -
+ * quadratic, d = target - quadratic, J the Jacobian at the target, so the
+ * loss is the linearised residual of the prediction relative to the
+ * quadratic's), and its parameter gradient; the parameters are not
+ * changed */
 int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const double *gram,
                         double *loss, float *grad);
 

@@ -609,7 +609,8 @@ class mpnn:
 
     def loss_grad(self, X, gram):
         """Training loss and parameter gradient for node features X and the
-        cv-weighted Gram scalars [cc, cd, dd]."""
+        Gram scalars [cc, cd, dd] of the two error fields (online
+        training uses those of Jc and Jd)."""
         X = np.ascontiguousarray(X, np.float32)
         gram = np.ascontiguousarray(gram, np.float64)
         g = np.empty(self.num_params, np.float32)

@@ -976,26 +976,38 @@ __global__ void features_b(int64_t n, const double *__restrict__ red, double mu_
   }
 }
 
-// cv-weighted Gram scalars of c and d = e_t x_t - quadratic (the quadratic
-// prediction's error): g = [<c,c>, <c,d>, <d,d>]
-__global__ void gram_kernel(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
-                            const C2<double> *__restrict__ x0, const C2<double> *__restrict__ x1,
-                            const C2<double> *__restrict__ xt, const double *__restrict__ cv,
-                            const double *__restrict__ sq, double *partials, unsigned *counter, double *g) {
+// The training sample's error fields: c (cubic - quadratic), d = e_t x_t -
+// quadratic (the quadratic prediction's error) and the phase-aligned target
+// e_t x_t, as complex vectors.
+__global__ void sample_fields(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
+                              const C2<double> *__restrict__ x0, const C2<double> *__restrict__ x1,
+                              const C2<double> *__restrict__ xt, const double *__restrict__ sq,
+                              C2<double> *__restrict__ c_out, C2<double> *__restrict__ d_out,
+                              C2<double> *__restrict__ t_out) {
   double e1r, e1i, etr, eti;
   phases(dots, 0, e1r, e1i);
   phases(dots, 3, etr, eti);
-  double acc[3] = {0, 0, 0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const C2<double> a = x0[i], p = x1[i], t = xt[i];
     const double pr = e1r * p.x - e1i * p.y, pi = e1r * p.y + e1i * p.x;
     const double *f = sq + 6 * i;
     const double qr = Ls[0] * a.x + Ls[1] * pr + f[2], qi = Ls[0] * a.y + Ls[1] * pi + f[3];
-    const double dr = etr * t.x - eti * t.y - qr, di = etr * t.y + eti * t.x - qi;
-    const double w = cv[i];
-    acc[0] += w * (f[4] * f[4] + f[5] * f[5]);
-    acc[1] += w * (f[4] * dr + f[5] * di);
-    acc[2] += w * (dr * dr + di * di);
+    const double tr = etr * t.x - eti * t.y, ti = etr * t.y + eti * t.x;
+    c_out[i] = C2<double>{f[4], f[5]};
+    d_out[i] = C2<double>{tr - qr, ti - qi};
+    t_out[i] = C2<double>{tr, ti};
+  }
+}
+
+// g = [<u,u>, <u,v>, <v,v>] over 2n reals
+__global__ void gram3_kernel(int64_t n2, const double *__restrict__ u, const double *__restrict__ v,
+                             double *partials, unsigned *counter, double *g) {
+  double acc[3] = {0, 0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x) {
+    const double a = u[i], b = v[i];
+    acc[0] += a * a;
+    acc[1] += a * b;
+    acc[2] += b * b;
   }
   for (int k = 0; k < 3; k++) grid_reduce(acc[k], partials + k * gridDim.x, counter + k, g + k);
 }
@@ -1146,6 +1158,7 @@ struct Mpnn::Impl {
   int enc_grid = 0, layer_grid = 0, agg_grid = 0, upd_grid = 0;
   int pool_parts = 0;  // pool partial rows written by the last forward
   DevBuf<double> sq, red, dots, Ls, gram, w, loss;
+  DevBuf<double> vc, vd, vt, jc, jd;  // training sample fields and their J applies
   // launches go to `stream`: the handle's stream, or a side stream while an
   // inference overlaps the solver; own reduction scratch for the features
   cudaStream_t stream;
@@ -1436,10 +1449,23 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
   features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x[0], sq.p, X.p);
   s.launch_count += 2;
   if (target) {
-    gram_kernel<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
-                                   (const C2<double> *)target, s.mesh->d_cv.p, sq.p, rd.partials.p,
-                                   rd.counter.p, gram.p);
+    // The loss is the linearised residual of the prediction, relative to
+    // the quadratic's: F(q + w c) ~ J (w c - d) with J at the aligned target
+    // (F there is ~0), so g = [|Jc|^2, <Jc, Jd>, |Jd|^2].  The residual is
+    // what Newton starts from; a state-space (cv-weighted) error favoured
+    // the cubic combination, whose amplified high-frequency noise the
+    // residual penalises.
+    if (vc.n < (size_t)(2 * N))
+      for (DevBuf<double> *b : {&vc, &vd, &vt, &jc, &jd}) b->alloc(2 * N);
+    sample_fields<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
+                                     (const C2<double> *)target, sq.p, (C2<double> *)vc.p, (C2<double> *)vd.p,
+                                     (C2<double> *)vt.p);
     ++s.launch_count;
+    s.jac_rebuild(vt.p, s.g0, t);
+    s.jac_apply<double>(vc.p, jc.p);
+    s.jac_apply<double>(vd.p, jd.p);
+    gram3_kernel<<<vgrid(2 * N), 256, 0, st>>>(2 * N, jc.p, jd.p, rd.partials.p, rd.counter.p, gram.p);
+    s.launch_count += 3;
   }
   NOSH_CUDA(cudaGetLastError());
 }
