@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 160^3 roofline of the fine-level SpMVs (the stress configuration)")
     return ap.parse_args()
 
 
@@ -183,6 +185,50 @@ def scaled_traffic(traffic, name, alg_bytes):
         return None
     t, alg = traffic[name]
     return t * alg_bytes / alg
+
+
+def large_roofline(peak, peak_kind, traffic, m=160, seed=5, mu0=0.8, dmu=0.01, steps=3):
+    """Fine-level smoother and Jacobian SpMV rooflines on the 160^3 stress
+    configuration (A = 1/2(-y,x,0) + 0.05 sin(2 pi z)(1,0,0), mu from 0.8 in
+    steps of 0.01): CUDA events around every launch during `steps` secant
+    continuation steps after two untimed ones."""
+    import torch
+
+    import nosh_gb300 as ng
+    from nosh_gb300 import meshgen
+
+    x, cells, psi0 = meshgen.cube(m, seed)
+    model = ng.nls(ng.mesh(x, cells), meshgen.mvp_stress(x), -1.0, 1.0, 1.0, mu=mu0)
+    x0 = torch.tensor(psi0, dtype=torch.float64, device="cuda")
+    assert model.newton(x0, {"mu": mu0})["status"] == 0
+    cont = ng.continuation(model, x0, mu0)
+    mu = mu0
+    for k in range(2 + steps):
+        if k == 2:
+            model.profile(True)
+            model.profile_read(ng.KERNEL_JACOBIAN)
+            model.profile_read(ng.KERNEL_SMOOTHER)
+        mu += dmu
+        st = cont.advance(mu, predictor=ng.PREDICT_SECANT)
+        assert st["status"] == 0 and st["f_norm"] <= 1e-10, st
+    out = {"workload": f"{m}^3 Kuhn-tet unit cube (seed {seed}), A=1/2(-y,x,0)+0.05sin(2pi z)(1,0,0), "
+                       f"mu={mu0}+k*{dmu}, secant continuation, mixed precision"}
+    for name, kk in (("smoother_spmv", ng.KERNEL_SMOOTHER), ("jacobian_spmv", ng.KERNEL_JACOBIAN)):
+        n_l, ms_l, bytes_l = model.profile_read(kk)
+        if n_l <= 0 or ms_l <= 0:
+            continue
+        ach = (bytes_l / n_l) / (ms_l / n_l * 1e-3) / 1e9
+        out[name] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "peak_kind": peak_kind, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
+                     "algorithmic_bytes_per_launch": bytes_l / n_l,
+                     "traffic": scaled_traffic(traffic, name, bytes_l / n_l),
+                     "traffic_source": "ncu capture of one 64^3 launch, scaled to this launch by its "
+                                       "algorithmic bytes"}
+    model.profile(False)
+    del cont, model, x0
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
 
 
 def dist_env():
@@ -419,6 +465,12 @@ def run_gb300(args):
         else:
             secondary = d
 
+    # the same two kernels on the 160^3 stress configuration, where a launch
+    # moves ~0.9 GB (the 64^3 launches above are latency-bound)
+    large = None
+    if rank == 0 and world == 1 and not args.no_large and args.m < 160:
+        large = large_roofline(peak, peak_kind, traffic)
+
     out = {
         "metric": METRIC,
         "value": value,
@@ -459,6 +511,7 @@ def run_gb300(args):
         "gpu_launches": int(head["launches"]),
         "roofline": roof,
         "roofline_secondary": secondary,
+        "roofline_160": large,
         "clocks": clk,
     }
     # -- CPU baseline: bounded sample of the same workload on the host cores
