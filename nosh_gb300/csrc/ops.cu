@@ -67,9 +67,18 @@ __global__ void vertex_fields_kernel(int64_t N, const int32_t *__restrict__ rp,
 // field length): there the Maclaurin series of sin to x^11 and cos to x^12
 // (Horner form; truncation below 1e-21 relative at |x| = 0.1) costs a dozen
 // FP64 FMAs, well below a general sincos with argument reduction, which the
-// larger angles still use.
+// larger angles still use.  Most phases are far smaller (|x| <= 0.02 on the
+// 64^3 cube at mu = 1): there sin to x^7 and cos to x^8 suffice (truncation
+// below 1e-18 relative), and the assembly is bound by FP64 arithmetic on
+// GB300.
 __device__ __forceinline__ void edge_sincos(double x, double &s, double &c) {
-  if (fabs(x) <= 0.1) {
+  if (fabs(x) <= 0.02) {
+    const double x2 = x * x;
+    constexpr double r6 = 1.0 / 6, r20 = 1.0 / 20, r42 = 1.0 / 42;
+    constexpr double r2 = 1.0 / 2, r12 = 1.0 / 12, r30 = 1.0 / 30, r56 = 1.0 / 56;
+    s = x * (1.0 - x2 * r6 * (1.0 - x2 * r20 * (1.0 - x2 * r42)));
+    c = 1.0 - x2 * r2 * (1.0 - x2 * r12 * (1.0 - x2 * r30 * (1.0 - x2 * r56)));
+  } else if (fabs(x) <= 0.1) {
     const double x2 = x * x;
     // reciprocals folded at compile time: multiplications, no FP64 division
     constexpr double r6 = 1.0 / 6, r20 = 1.0 / 20, r42 = 1.0 / 42, r72 = 1.0 / 72, r110 = 1.0 / 110;
