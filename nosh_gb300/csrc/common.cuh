@@ -109,6 +109,14 @@ void parallel_for(int64_t n, F &&f, int64_t grain = 1 << 14) {
 // ------------------------------------------------------------ launch math
 constexpr int kPad = 8;        // tail padding of nonzero arrays (elements)
 constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time)
+// Grid of a 256-thread FP64 reduction over n elements: about four elements
+// per thread, at most two CTAs per SM.  GB300 issues FP64 at a small
+// fraction of its FP32 rate, and with one element per thread the per-thread
+// shuffle tree of each reduction costs more FP64 adds than the element work.
+inline int reduce_grid(int64_t n) {
+  const int64_t g = (n + 1023) / 1024;
+  return (int)(g < 1 ? 1 : (g > 2 * kNumSMs ? 2 * kNumSMs : g));
+}
 
 // In place: each of the first n complex values c[2k], c[2k+1] (a dot
 // product <x_k, x_0>) becomes the unit phase factor c / |c| (1 when c = 0)

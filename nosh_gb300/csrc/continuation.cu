@@ -132,7 +132,7 @@ void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
   }
   const int G = vgrid(s.N);
   if (order >= 1) {
-    history_dots<<<G, 256, 0, st>>>(s.N, slot(0), slot(1), order >= 2 ? slot(2) : nullptr,
+    history_dots<<<reduce_grid(s.N), 256, 0, st>>>(s.N, slot(0), slot(1), order >= 2 ? slot(2) : nullptr,
                                     order >= 3 ? slot(3) : nullptr, nullptr, order, s.red.partials.p, s.red.counter.p,
                                     dots.p);
     normalize_phases<<<1, 32, 0, st>>>(order, dots.p);
@@ -149,7 +149,7 @@ void ContinuationImpl::extrapolate(int order, double mu_new, double *out) {
 
 namespace {
 double *dots_host(NlsImpl &s, const DotSet &d, int64_t n, double *dev_out, double *host) {
-  dot_set_kernel<<<vgrid(n), 256, 0, s.stream>>>(n, d, s.red.partials.p, s.red.counter.p, dev_out);
+  dot_set_kernel<<<reduce_grid(n), 256, 0, s.stream>>>(n, d, s.red.partials.p, s.red.counter.p, dev_out);
   ++s.launch_count;
   NOSH_CUDA(cudaGetLastError());
   NOSH_CUDA(cudaMemcpyAsync(host, dev_out, d.k * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
@@ -222,7 +222,8 @@ void ContinuationImpl::advance_arclength(double ds, int predictor, double theta_
   const int G = vgrid(N);
   if (have_secant) {
     // phase-aligned secant psi0 - e^{i phi} psi1 into va
-    history_dots<<<G, 256, 0, s.stream>>>(N, slot(0), slot(1), nullptr, nullptr, nullptr, 1, s.red.partials.p,
+    history_dots<<<reduce_grid(N), 256, 0, s.stream>>>(N, slot(0), slot(1), nullptr, nullptr, nullptr, 1,
+                                                        s.red.partials.p,
                                           s.red.counter.p, dots.p);
     normalize_phases<<<1, 32, 0, s.stream>>>(1, dots.p);
     extrapolate_kernel<<<G, 256, 0, s.stream>>>(N, 1, dots.p, 1.0, -1.0, 0.0, 0.0, (const C2<double> *)slot(0),

@@ -1437,12 +1437,12 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
   }
   Ls.upload(Lh, 9, st);
   // <x_k, x_0> for x_1..x_3 and the target, x_0 read once
-  history_dots<<<G, 256, 0, st>>>(N, x[0], x[1], x[2], x[3], target, target ? 4 : 3, rd.partials.p,
+  history_dots<<<reduce_grid(N), 256, 0, st>>>(N, x[0], x[1], x[2], x[3], target, target ? 4 : 3, rd.partials.p,
                                   rd.counter.p, dots.p);
   ++s.launch_count;
   normalize_phases<<<1, 32, 0, st>>>(target ? 4 : 3, dots.p);
   ++s.launch_count;
-  features_a<<<G, 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
+  features_a<<<reduce_grid(N), 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
                                 (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, (C2<double> *)secant,
                                 rd.partials.p,
                                 rd.counter.p, red.p);
@@ -1464,7 +1464,7 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
     s.jac_rebuild(vt.p, s.g0, t);
     s.jac_apply<double>(vc.p, jc.p);
     s.jac_apply<double>(vd.p, jd.p);
-    gram3_kernel<<<vgrid(2 * N), 256, 0, st>>>(2 * N, jc.p, jd.p, rd.partials.p, rd.counter.p, gram.p);
+    gram3_kernel<<<reduce_grid(2 * N), 256, 0, st>>>(2 * N, jc.p, jd.p, rd.partials.p, rd.counter.p, gram.p);
     s.launch_count += 3;
   }
   NOSH_CUDA(cudaGetLastError());

@@ -228,7 +228,8 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     NOSH_CUDA(cudaMemcpyAsync(r[1].p, b, bytes, cudaMemcpyDeviceToDevice, st));
     for (DevBuf<T> *q : {&x, &w[0], &w[1], &w[2]}) NOSH_CUDA(cudaMemsetAsync(q->p, 0, bytes, st));
     s.amg->apply<T>(r[1].p, z[0].p);
-    dot_kernel<T><<<G, 256, 0, st>>>(n2, r[1].p, z[0].p, s.red.partials.p, s.red.counter.p, &d->rz);
+    dot_kernel<T><<<reduce_grid(n2), 256, 0, st>>>(n2, r[1].p, z[0].p, s.red.partials.p, s.red.counter.p,
+                                                    &d->rz);
     minres_init<<<1, 1, 0, st>>>(d, params.p);
     s.launch_count += 2;
   };
@@ -493,7 +494,7 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     if (opt.phase_fix) {
       // the bordered system's update: no component along i psi
       const int Gc = vec_grid(s.N);
-      gauge_dots<T><<<Gc, 256, 0, s.stream>>>(s.N, mr.x.p, ns.psi.p, s.red.partials.p, s.red.counter.p,
+      gauge_dots<T><<<reduce_grid(s.N), 256, 0, s.stream>>>(s.N, mr.x.p, ns.psi.p, s.red.partials.p, s.red.counter.p,
                                                ns.red2.p);
       gauge_remove<T><<<Gc, 256, 0, s.stream>>>(s.N, mr.x.p, ns.psi.p, ns.red2.p);
       s.launch_count += 2;
@@ -598,7 +599,7 @@ void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double m
   nosh_newton_stats pst{};
   if (predictor == NOSH_PREDICT_SECANT && x_prev && mu_cur != mu_prev && !std::isnan(mu_prev)) {
     NOSH_CUDA(cudaMemcpyAsync(ns.xp.p, x_prev, bytes, cudaMemcpyDefault, st_));
-    cdot_kernel<<<G, 256, 0, st_>>>(s.N, (const C2<double> *)ns.xp.p, (const C2<double> *)ns.xc.p,
+    cdot_kernel<<<reduce_grid(s.N), 256, 0, st_>>>(s.N, (const C2<double> *)ns.xp.p, (const C2<double> *)ns.xc.p,
                                     s.red.partials.p, s.red.counter.p, ns.red2.p);
     normalize_phases<<<1, 32, 0, st_>>>(1, ns.red2.p);
     s.launch_count += 2;
