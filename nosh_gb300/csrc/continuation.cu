@@ -373,7 +373,9 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
     bool compare;
     if (overlap) {
       if (!side) {
-        NOSH_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        int lo = 0, hi = 0;
+        NOSH_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        NOSH_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, lo));  // below the solver
         NOSH_CUDA(cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming));
         NOSH_CUDA(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
         NOSH_CUDA(cudaMallocHost(&w_host, sizeof(double)));

@@ -393,7 +393,14 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
     : mesh(m), N(m->N), E(m->E), deriv_param(deriv ? deriv : "mu"), g0(g), mu0(mu) {
   NOSH_CHECK(deriv_param == "mu" || deriv_param == "g", NOSH_ERR_INVALID,
              "deriv_parameter must be \"mu\" or \"g\"");
-  NOSH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  // the solver's stream at the highest priority: work overlapped with it
+  // on other streams (the learned predictor's inference) yields SM slots to
+  // it as they free up
+  {
+    int lo = 0, hi = 0;
+    NOSH_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    NOSH_CUDA(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, hi));
+  }
   cudaStream_t s = stream;
   // aggregation defaults by mesh kind (sweeps of the 64^3 tetrahedral
   // continuation and the batched triangular squares): tetrahedra aggregate
