@@ -663,51 +663,10 @@ __device__ __forceinline__ void tail_rows(const LevelDesc<T> &A, const C2<T> *x,
   }
 }
 
-// Restriction from level l to l + 1 (aggregate sums of l's residual into
-// l + 1's right-hand side), split across lanes like the rows.
-template <typename T>
-__device__ __forceinline__ void tail_restrict(const LevelDesc<T> &A, const LevelDesc<T> &Cl) {
-  const int tid = threadIdx.x, bs = blockDim.x;
-  const int tpr = tail_tpr(Cl.n);
-  const int groups = bs / tpr, g = tid / tpr, li = tid % tpr;
-  for (int64_t base = 0; base < Cl.n; base += groups) {
-    const int64_t a = base + g;
-    T sr = 0, si = 0;
-    if (a < Cl.n) {
-      const int32_t q1 = A.mem_ptr[a + 1];
-      int32_t q = A.mem_ptr[a] + li;
-      // four members per round, their loads issued before any sum
-      for (; q + 3 * tpr < q1; q += 4 * tpr) {
-        const int32_t i0 = A.mem_idx[q], i1 = A.mem_idx[q + tpr], i2 = A.mem_idx[q + 2 * tpr],
-                      i3 = A.mem_idx[q + 3 * tpr];
-        const C2<T> v0 = A.res[i0], v1 = A.res[i1], v2 = A.res[i2], v3 = A.res[i3];
-        sr += (v0.x + v1.x) + (v2.x + v3.x);
-        si += (v0.y + v1.y) + (v2.y + v3.y);
-      }
-      for (; q < q1; q += tpr) {
-        const C2<T> v = A.res[A.mem_idx[q]];
-        sr += v.x;
-        si += v.y;
-      }
-    }
-    for (int off = tpr >> 1; off > 0; off >>= 1) {
-      sr += __shfl_xor_sync(0xffffffffu, sr, off);
-      si += __shfl_xor_sync(0xffffffffu, si, off);
-    }
-    if (a < Cl.n && li == 0) Cl.b[a] = C2<T>{sr, si};
-  }
-}
-
-// The tail also owns the transfers to and from the level above it (lt - 1):
-// it restricts that level's residual into its own right-hand side first and
-// prolongs its correction into xprev (that level's x) last, which saves the
-// two separate launches per V-cycle.
 template <typename T>
 __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L, int deg, const T *__restrict__ Ainv,
-                                          const DenseMap &D, C2<T> *__restrict__ xprev) {
+                                          const DenseMap &D) {
   const int tid = threadIdx.x, bs = blockDim.x;
-  tail_restrict<T>(lv[lt - 1], lv[lt]);
-  __syncthreads();
   for (int l = lt; l < L - 1; l++) {
     const LevelDesc<T> A = lv[l];
     C2<T> *cur = (deg % 2) ? A.x : A.x2, *oth = (deg % 2) ? A.x2 : A.x;
@@ -728,7 +687,27 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
       A.res[i] = C2<T>{bi.x - (sr + d0r * xi.x + d1b * xi.y), bi.y - (si + d1b * xi.x + d0i * xi.y)};
     });
     __syncthreads();
-    tail_restrict<T>(A, lv[l + 1]);
+    // restriction: aggregate sums, split across lanes like the rows
+    const LevelDesc<T> Cl = lv[l + 1];
+    {
+      const int tpr = tail_tpr(Cl.n);
+      const int groups = bs / tpr, g = tid / tpr, li = tid % tpr;
+      for (int64_t base = 0; base < Cl.n; base += groups) {
+        const int64_t a = base + g;
+        T sr = 0, si = 0;
+        if (a < Cl.n)
+          for (int32_t q = A.mem_ptr[a] + li; q < A.mem_ptr[a + 1]; q += tpr) {
+            const C2<T> v = A.res[A.mem_idx[q]];
+            sr += v.x;
+            si += v.y;
+          }
+        for (int off = tpr >> 1; off > 0; off >>= 1) {
+          sr += __shfl_xor_sync(0xffffffffu, sr, off);
+          si += __shfl_xor_sync(0xffffffffu, si, off);
+        }
+        if (a < Cl.n && li == 0) Cl.b[a] = C2<T>{sr, si};
+      }
+    }
     __syncthreads();
   }
   {
@@ -765,27 +744,14 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
       __syncthreads();
     }
   }
-  {
-    // prolongation of this level's correction into level lt - 1
-    const LevelDesc<T> P = lv[lt - 1];
-    const C2<T> *xc = lv[lt].x;
-#pragma unroll 4
-    for (int64_t i = tid; i < P.n; i += bs) {
-      const C2<T> c = xc[P.agg[i]];
-      C2<T> v = xprev[i];
-      v.x += c.x;
-      v.y += c.y;
-      xprev[i] = v;
-    }
-  }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restrict__ lv, int lt, int L,
                                                     int deg, const T *__restrict__ Ainv, DenseMap D,
-                                                    C2<T> *__restrict__ xprev, const int *halt) {
+                                                    const int *halt) {
   if (halt && *halt >= 2) return;
-  tail_body(lv, lt, L, deg, Ainv, D, xprev);
+  tail_body(lv, lt, L, deg, Ainv, D);
 }
 
 // plain MINRES pieces for the single-level case
@@ -1211,13 +1177,15 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
                                                       V.d[l + 1].p, first, halt);
     ++nls.launch_count;
     descend_ascend<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p, nullptr);
-    prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x, halt);
-    ++nls.launch_count;
   } else {
-    // the tail restricts this level's residual and prolongs into x itself
-    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), x, halt);
+    restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
+                                                       V.b[l + 1].p, halt);
+    ++nls.launch_count;
+    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), halt);
     ++nls.launch_count;
   }
+  prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x, halt);
+  ++nls.launch_count;
   cur = x;
   oth = V.x2[l].p;
   for (int k = 0; k < deg; k++) {
