@@ -9,6 +9,8 @@
 //   nosh::jacobian_operator             (src/jacobian_operator.hpp)
 //   nosh::keo_regularized               (src/keo_regularized.hpp)
 //   nosh::model_evaluator::nls          (src/model_evaluator_nls.hpp)
+//   nosh::continuation                  (the LOCA stepper of executables/
+//                                        nosh-cont and src/observer.cpp)
 //
 // Trilinos types are replaced by std::vector<double> (interleaved complex
 // vectors of length 2N, multivectors as a vector of columns) and parameter
@@ -18,7 +20,10 @@
 #ifndef NOSH_GB300_HPP
 #define NOSH_GB300_HPP
 
+#include <algorithm>
 #include <array>
+#include <cmath>
+#include <cstdio>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -328,6 +333,224 @@ class nls {
   std::shared_ptr<parameter_matrix::DkeoDP> dkeo_;
 };
 }  // namespace model_evaluator
+
+// ---------------------------------------------------------- continuation
+// The LOCA stepper loop of the reference's driver (executables/nosh-cont/
+// nosh-cont.cpp:226-345; parameters of examples/conf.xml:35-75) over the
+// device-resident continuation handle, and the continuation statistics
+// observer (src/observer.cpp:136-159, written in the layout of
+// src/csv_writer.cpp).  LOCA itself is a Trilinos package; the step-size
+// rule restated here: after a successful step of n nonlinear iterations
+// ds *= 1 + aggressiveness ((n_max - n) / (n_max - 1))^2, clipped to the
+// maximum step; after a failed one ds /= 2, and the run fails below the
+// minimum step.
+namespace continuation {
+
+// nosh_continuation: the last converged states stay on the GPU
+class run {
+ public:
+  run(const model_evaluator::nls &model, const vec &x0, double mu0) : n_(x0.size()) {
+    check(nosh_continuation_create(model.handle(), x0.data(), mu0, &h_));
+  }
+  ~run() { nosh_continuation_destroy(h_); }
+  run(const run &) = delete;
+  run &operator=(const run &) = delete;
+
+  double mu() const {
+    double m = 0.0;
+    check(nosh_continuation_state(h_, nullptr, &m));
+    return m;
+  }
+  void state(vec &x, double &m) const {
+    x.resize(n_);
+    check(nosh_continuation_state(h_, x.data(), &m));
+  }
+  // a natural step to mu_new; a step that did not converge (or hit NaN or a
+  // Krylov breakdown) reports it in status and leaves the state unchanged
+  nosh_newton_stats advance(double mu_new, int predictor, const nosh_newton_options &opt) {
+    nosh_newton_stats st{};
+    return finish(nosh_continuation_advance(h_, mu_new, predictor, &opt, &st), st);
+  }
+  nosh_newton_stats advance_arclength(double ds, int predictor, double theta, const nosh_newton_options &opt) {
+    nosh_newton_stats st{};
+    return finish(nosh_continuation_advance_arclength(h_, ds, predictor, theta, &opt, &st), st);
+  }
+  double tangent_mu() const {
+    double t = 0.0, th = 0.0;
+    check(nosh_continuation_tangent(h_, &t, &th));
+    return t;
+  }
+
+ private:
+  static nosh_newton_stats finish(int rc, nosh_newton_stats st) {
+    if (rc == NOSH_ERR_NOT_CONVERGED || rc == NOSH_ERR_NAN || rc == NOSH_ERR_BREAKDOWN) {
+      st.status = rc;
+      return st;
+    }
+    check(rc);
+    return st;
+  }
+  nosh_continuation h_ = nullptr;
+  size_t n_;
+};
+
+// The statistics table of the reference's csv_writer: "# " and the labels,
+// doubles in %.15e in columns 22 wide, integers in columns as wide as their
+// label (at least 5), three spaces between columns, rows indented by two.
+class csv_writer {
+ public:
+  explicit csv_writer(std::FILE *f) : f_(f) {}
+  struct cell {
+    std::string label;
+    bool integer;
+    double value;
+  };
+  void write_header(const std::vector<cell> &row) const {
+    std::fputs("# ", f_);
+    line(row, true);
+  }
+  void write_row(const std::vector<cell> &row) const {
+    std::fputs("  ", f_);
+    line(row, false);
+  }
+
+ private:
+  void line(const std::vector<cell> &row, bool header) const {
+    for (size_t k = 0; k < row.size(); k++) {
+      if (k) std::fputs("   ", f_);
+      const cell &c = row[k];
+      const int w = c.integer ? (int)std::max<size_t>(5, c.label.size()) : 22;
+      if (header)
+        std::fprintf(f_, "%-*s", w, c.label.c_str());
+      else if (c.integer)
+        std::fprintf(f_, "%-*lld", w, (long long)c.value);
+      else
+        std::fprintf(f_, "%-*.15e", w, c.value);
+    }
+    std::fputs("\n", f_);
+    std::fflush(f_);
+  }
+  std::FILE *f_;
+};
+
+// Per converged state: step, the parameter, the Gibbs energy and
+// sqrt(<psi, psi>) (src/model_evaluator_base.hpp norm).
+class statistics_observer {
+ public:
+  statistics_observer(const model_evaluator::nls &model, std::FILE *f, const std::string &param = "mu")
+      : model_(model), w_(f), param_(param) {}
+  void operator()(int index, const vec &x, double m) const {
+    const double ip = model_.inner_product(x, x);
+    const std::vector<csv_writer::cell> row = {{"(0) step", true, (double)index},
+                                               {"(1) " + param_, false, m},
+                                               {"(2) Gibbs energy", false, model_.gibbs_energy(x)},
+                                               {"(2) ||x||_2 scaled", false, std::sqrt(ip > 0 ? ip : 0.0)}};
+    if (index == 0) w_.write_header(row);
+    w_.write_row(row);
+  }
+
+ private:
+  const model_evaluator::nls &model_;
+  csv_writer w_;
+  std::string param_;
+};
+
+struct stepper_parameters {
+  bool arc_length = true;                 // "Continuation Method": Arc Length / Natural
+  int predictor = NOSH_PREDICT_TANGENT;   // "Predictor" Method
+  double initial_step = 1e-3, max_step = 1e-2, min_step = 1e-7;  // "Step Size"
+  double aggressiveness = 2.0;
+  bool adaptive = true;                   // "Adaptive" or "Constant"
+  int max_steps = 1000;                   // "Max Steps"
+  double max_value = 100.0, min_value = -100.0;
+  int max_nonlinear_iters = 15;
+  double theta = 1.0;                     // arclength parameter scale
+};
+
+struct step_record {
+  int step;
+  double mu, ds;
+  int newton_iters, krylov_iters;
+};
+
+struct stepper_result {
+  bool failed = false;  // the step size fell below the minimum
+  int steps = 0, failed_steps = 0;
+  std::vector<step_record> records;
+};
+
+// The stepper loop, generic over the run (any type with mu(), state(x, mu),
+// advance(mu, predictor, opt), advance_arclength(ds, predictor, theta, opt)
+// and tangent_mu()) and the observer (called as obs(index, x, mu)).
+template <class Run, class Observer>
+stepper_result step(Run &r, const stepper_parameters &p, nosh_newton_options opt, Observer &&obs) {
+  if (!(p.min_step > 0 && p.min_step <= std::fabs(p.initial_step) && std::fabs(p.initial_step) <= p.max_step))
+    throw error(NOSH_ERR_INVALID, "need 0 < min step <= |initial step| <= max step");
+  if (p.max_nonlinear_iters < 2) throw error(NOSH_ERR_INVALID, "max nonlinear iterations must be at least 2");
+  if (p.arc_length && p.predictor != NOSH_PREDICT_TANGENT && p.predictor != NOSH_PREDICT_SECANT)
+    throw error(NOSH_ERR_INVALID, "arclength steps predict TANGENT or SECANT");
+  opt.max_newton = p.max_nonlinear_iters;
+  stepper_result out;
+  vec x;
+  double m = 0.0;
+  r.state(x, m);
+  obs(0, x, m);
+  out.records.push_back({0, m, 0.0, 0, 0});
+  double ds = p.initial_step;
+  auto clip = [&](double d, double mu, double dmu_ds, bool &last) {
+    last = false;
+    if (!(std::isfinite(dmu_ds)) || dmu_ds == 0.0) return d;
+    const double target = mu + d * dmu_ds;
+    for (double bound : {p.max_value, p.min_value})
+      if ((target - bound) * (mu - bound) < 0.0 || target == bound) {
+        last = true;
+        return (bound - mu) / dmu_ds;
+      }
+    return d;
+  };
+  while (out.steps < p.max_steps) {
+    const double mu = r.mu();
+    if (mu >= p.max_value || mu <= p.min_value) break;
+    bool last = false;
+    double d;
+    nosh_newton_stats st;
+    if (!p.arc_length) {
+      d = clip(ds, mu, 1.0, last);
+      st = r.advance(mu + d, p.predictor, opt);
+    } else {
+      d = clip(ds, mu, out.steps > 0 ? r.tangent_mu() : std::nan(""), last);
+      st = r.advance_arclength(d, p.predictor, p.theta, opt);
+    }
+    if (st.status != NOSH_OK) {
+      out.failed_steps++;
+      ds = 0.5 * d;
+      if (std::fabs(ds) < p.min_step) {
+        out.failed = true;
+        break;
+      }
+      continue;
+    }
+    out.steps++;
+    r.state(x, m);
+    obs(out.steps, x, m);
+    out.records.push_back({out.steps, m, d, st.newton_iters, st.krylov_iters});
+    if (last) break;
+    if (p.adaptive) {
+      const double ratio = std::max(0.0, (double)(p.max_nonlinear_iters - st.newton_iters) /
+                                              (double)(p.max_nonlinear_iters - 1));
+      ds = d * (1.0 + p.aggressiveness * ratio * ratio);
+      ds = std::copysign(std::min(std::fabs(ds), p.max_step), ds);
+    } else {
+      ds = d;
+    }
+    // from the second arclength step on the tangent follows the last secant
+    if (p.arc_length) ds = std::fabs(ds);
+    if (std::fabs(ds) < p.min_step) ds = std::copysign(p.min_step, ds);
+  }
+  return out;
+}
+
+}  // namespace continuation
 }  // namespace nosh
 
 #endif  // NOSH_GB300_HPP

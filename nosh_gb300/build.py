@@ -75,7 +75,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
-CPP_TESTS = {"test_reference_api": os.path.join(ROOT, "tests", "cpp", "test_reference_api.cpp")}
+CPP_TESTS = {"test_reference_api": os.path.join(ROOT, "tests", "cpp", "test_reference_api.cpp"),
+             "test_stepper": os.path.join(ROOT, "tests", "cpp", "test_stepper.cpp")}
 
 
 def build_cpp_tests(force: bool = False) -> dict:
