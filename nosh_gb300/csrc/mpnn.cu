@@ -404,14 +404,18 @@ __global__ void __launch_bounds__(256, 4) mp_aggregate_kernel(int64_t n, const i
   const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4, c4 = hl * 4;
   MsgConst k;
   msg_const(Wc, bm, c4, k);
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  // warp-uniform loop over row pairs (a half-warp per row)
-  for (int64_t r0 = 2 * warp; r0 < n; r0 += 2 * nwarps) {
+  // each CTA walks one contiguous range of rows, 16 at a time (a half-warp
+  // per row): the neighbours of nearby rows (mesh-ordered graphs: bands at
+  // fixed index offsets) are then largely in this SM's L1
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5;
+  const int64_t per = ((n + gridDim.x - 1) / gridDim.x + 1) & ~(int64_t)1;
+  const int64_t beg = blockIdx.x * per, end = beg + per < n ? beg + per : n;
+  // warp-uniform loop over row pairs
+  for (int64_t r0 = beg + 2 * w; r0 < end; r0 += 2 * wpc) {
     const int64_t r = r0 + half;
     float m[4];
-    aggregate_row(r, n, rp, ci, ef, A, B, k, hl, half, c4, m);
-    if (r < n) {
+    aggregate_row(r, end, rp, ci, ef, A, B, k, hl, half, c4, m);
+    if (r < end) {
       uint2 mv;
       *reinterpret_cast<__nv_bfloat162 *>(&mv.x) = __floats2bfloat162_rn(m[0], m[1]);
       *reinterpret_cast<__nv_bfloat162 *>(&mv.y) = __floats2bfloat162_rn(m[2], m[3]);
