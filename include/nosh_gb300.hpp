@@ -11,6 +11,7 @@
 //   nosh::model_evaluator::nls          (src/model_evaluator_nls.hpp)
 //   nosh::continuation                  (the LOCA stepper of executables/
 //                                        nosh-cont and src/observer.cpp)
+//   nosh::io                            (mesh / state files, .vtu for .h5m)
 //
 // Trilinos types are replaced by std::vector<double> (interleaved complex
 // vectors of length 2N, multivectors as a vector of columns) and parameter
@@ -24,6 +25,8 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -551,6 +554,264 @@ stepper_result step(Run &r, const stepper_parameters &p, nosh_newton_options opt
 }
 
 }  // namespace continuation
+
+// ------------------------------------------------------------------ files
+// Mesh and state files as VTK XML unstructured grids (.vtu), the format of
+// nosh_gb300/io.py: the reference reads psi, A and V vertex tags through
+// MOAB (src/mesh_reader.cpp:20-162) and writes one state per continuation
+// step (src/continuation_data_saver.hpp:26-50); MOAB's .h5m needs HDF5,
+// which this build does not have.  Arrays are base64 with UInt64 size
+// headers, little endian, and round-trip bit for bit; the reader also takes
+// ASCII arrays.
+namespace io {
+
+struct array {
+  std::string name;
+  int components = 1;
+  std::vector<double> values;  // tuples of `components`
+};
+
+struct grid {
+  std::vector<double> coords;  // 3 per point
+  std::vector<int32_t> cells;  // nvc per cell
+  int nvc = 0;                 // 3: triangles, 4: tetrahedra
+  std::vector<array> point_data;
+  std::vector<std::pair<std::string, double>> field_data;
+  const array *find(const std::string &name) const {
+    for (const array &a : point_data)
+      if (a.name == name) return &a;
+    return nullptr;
+  }
+};
+
+namespace detail {
+inline std::string b64(const unsigned char *p, size_t n) {
+  static const char *t = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
+  std::string o;
+  o.reserve((n + 2) / 3 * 4);
+  for (size_t i = 0; i < n; i += 3) {
+    const unsigned v = (unsigned)p[i] << 16 | (i + 1 < n ? (unsigned)p[i + 1] << 8 : 0u) | (i + 2 < n ? p[i + 2] : 0u);
+    o += t[v >> 18 & 63];
+    o += t[v >> 12 & 63];
+    o += i + 1 < n ? t[v >> 6 & 63] : '=';
+    o += i + 2 < n ? t[v & 63] : '=';
+  }
+  return o;
+}
+inline std::vector<unsigned char> unb64(const std::string &s) {
+  std::vector<unsigned char> o;
+  unsigned v = 0;
+  int bits = 0;
+  for (char ch : s) {
+    int d;
+    if (ch >= 'A' && ch <= 'Z') d = ch - 'A';
+    else if (ch >= 'a' && ch <= 'z') d = ch - 'a' + 26;
+    else if (ch >= '0' && ch <= '9') d = ch - '0' + 52;
+    else if (ch == '+') d = 62;
+    else if (ch == '/') d = 63;
+    else continue;  // padding and whitespace
+    v = v << 6 | (unsigned)d;
+    bits += 6;
+    if (bits >= 8) {
+      bits -= 8;
+      o.push_back((unsigned char)(v >> bits & 255u));
+    }
+  }
+  return o;
+}
+// host byte order is little endian on every machine this builds for
+template <class T>
+inline std::string encode(const std::vector<T> &v) {
+  const uint64_t n = v.size() * sizeof(T);
+  std::vector<unsigned char> raw(8 + n);
+  std::memcpy(raw.data(), &n, 8);
+  if (n) std::memcpy(raw.data() + 8, v.data(), n);
+  return b64(raw.data(), raw.size());
+}
+inline std::string attr(const std::string &tag, const std::string &key) {
+  const std::string k = " " + key + "=\"";
+  const size_t a = tag.find(k);
+  if (a == std::string::npos) return "";
+  const size_t b = tag.find('"', a + k.size());
+  return tag.substr(a + k.size(), b - a - k.size());
+}
+inline size_t type_size(const std::string &t) {
+  if (t == "Float64" || t == "Int64" || t == "UInt64") return 8;
+  if (t == "Float32" || t == "Int32" || t == "UInt32") return 4;
+  if (t == "UInt8" || t == "Int8") return 1;
+  throw error(NOSH_ERR_INVALID, "unsupported DataArray type " + t);
+}
+inline double element(const unsigned char *p, const std::string &t) {
+  if (t == "Float64") { double v; std::memcpy(&v, p, 8); return v; }
+  if (t == "Float32") { float v; std::memcpy(&v, p, 4); return v; }
+  if (t == "Int64") { int64_t v; std::memcpy(&v, p, 8); return (double)v; }
+  if (t == "UInt64") { uint64_t v; std::memcpy(&v, p, 8); return (double)v; }
+  if (t == "Int32") { int32_t v; std::memcpy(&v, p, 4); return v; }
+  if (t == "UInt32") { uint32_t v; std::memcpy(&v, p, 4); return v; }
+  if (t == "Int8") return (double)(int8_t)*p;
+  return (double)*p;
+}
+inline std::vector<double> values(const std::string &tag, const std::string &body) {
+  const std::string type = attr(tag, "type"), fmt = attr(tag, "format");
+  std::vector<double> out;
+  if (fmt == "binary") {
+    const std::vector<unsigned char> raw = unb64(body);
+    if (raw.size() < 8) throw error(NOSH_ERR_INVALID, "truncated binary DataArray");
+    uint64_t n = 0;
+    std::memcpy(&n, raw.data(), 8);
+    const size_t es = type_size(type);
+    if (raw.size() < 8 + n || n % es) throw error(NOSH_ERR_INVALID, "binary DataArray size mismatch");
+    for (uint64_t i = 0; i < n / es; i++) out.push_back(element(raw.data() + 8 + i * es, type));
+  } else if (fmt == "ascii" || fmt.empty()) {
+    type_size(type);
+    const char *c = body.c_str();
+    char *end = nullptr;
+    for (;;) {
+      const double v = std::strtod(c, &end);
+      if (end == c) break;
+      out.push_back(v);
+      c = end;
+    }
+  } else {
+    throw error(NOSH_ERR_INVALID, "unsupported DataArray format " + fmt);
+  }
+  return out;
+}
+}  // namespace detail
+
+inline void write_vtu(const std::string &path, const grid &g) {
+  if (g.nvc != 3 && g.nvc != 4) throw error(NOSH_ERR_INVALID, "cells must be triangles (3) or tetrahedra (4)");
+  const size_t n = g.coords.size() / 3, t = g.cells.size() / (size_t)g.nvc;
+  std::FILE *f = std::fopen(path.c_str(), "w");
+  if (!f) throw error(NOSH_ERR_INVALID, "cannot write " + path);
+  std::fprintf(f, "<?xml version='1.0' encoding='utf-8'?>\n<VTKFile type=\"UnstructuredGrid\" version=\"1.0\" "
+                  "byte_order=\"LittleEndian\" header_type=\"UInt64\"><UnstructuredGrid>");
+  auto arr = [&](const char *type, const std::string &name, int nc, const std::string &data, long ntuples) {
+    std::fprintf(f, "<DataArray type=\"%s\" Name=\"%s\" format=\"binary\"", type, name.c_str());
+    if (nc > 1) std::fprintf(f, " NumberOfComponents=\"%d\"", nc);
+    if (ntuples >= 0) std::fprintf(f, " NumberOfTuples=\"%ld\"", ntuples);
+    std::fprintf(f, ">%s</DataArray>", data.c_str());
+  };
+  if (!g.field_data.empty()) {
+    std::fprintf(f, "<FieldData>");
+    for (const auto &kv : g.field_data) arr("Float64", kv.first, 1, detail::encode(std::vector<double>{kv.second}), 1);
+    std::fprintf(f, "</FieldData>");
+  }
+  std::fprintf(f, "<Piece NumberOfPoints=\"%zu\" NumberOfCells=\"%zu\">", n, t);
+  if (!g.point_data.empty()) {
+    std::fprintf(f, "<PointData>");
+    for (const array &a : g.point_data) {
+      if (a.values.size() != n * (size_t)a.components) {
+        std::fclose(f);
+        throw error(NOSH_ERR_INVALID, "point data " + a.name + " does not match the points");
+      }
+      arr("Float64", a.name, a.components, detail::encode(a.values), -1);
+    }
+    std::fprintf(f, "</PointData>");
+  }
+  std::fprintf(f, "<Points>");
+  arr("Float64", "Points", 3, detail::encode(g.coords), -1);
+  std::fprintf(f, "</Points><Cells>");
+  std::vector<int64_t> conn(g.cells.begin(), g.cells.end()), off(t);
+  for (size_t k = 0; k < t; k++) off[k] = (int64_t)((k + 1) * (size_t)g.nvc);
+  arr("Int64", "connectivity", 1, detail::encode(conn), -1);
+  arr("Int64", "offsets", 1, detail::encode(off), -1);
+  arr("UInt8", "types", 1, detail::encode(std::vector<uint8_t>(t, g.nvc == 3 ? 5 : 10)), -1);
+  std::fprintf(f, "</Cells></Piece></UnstructuredGrid></VTKFile>\n");
+  std::fclose(f);
+}
+
+inline grid read_vtu(const std::string &path) {
+  std::FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) throw error(NOSH_ERR_INVALID, "cannot read " + path);
+  std::string doc;
+  char buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) doc.append(buf, got);
+  std::fclose(f);
+  if (doc.find("type=\"UnstructuredGrid\"") == std::string::npos)
+    throw error(NOSH_ERR_INVALID, "not a VTK unstructured grid");
+  grid g;
+  std::vector<double> conn, off, types;
+  std::string section;
+  for (size_t pos = 0;;) {
+    const size_t lt = doc.find('<', pos);
+    if (lt == std::string::npos) break;
+    const size_t gt = doc.find('>', lt);
+    if (gt == std::string::npos) break;
+    const std::string tag = doc.substr(lt, gt - lt + 1);
+    pos = gt + 1;
+    for (const char *sec : {"PointData", "Points", "Cells", "FieldData"}) {
+      const std::string s = sec;
+      if (tag.compare(0, s.size() + 1, "<" + s) == 0 && (tag[s.size() + 1] == '>' || tag[s.size() + 1] == ' '))
+        section = s;
+      if (tag == "</" + s + ">") section.clear();
+    }
+    if (tag.compare(0, 10, "<DataArray") != 0) continue;
+    const size_t close = doc.find("</DataArray>", pos);
+    if (close == std::string::npos) throw error(NOSH_ERR_INVALID, "unterminated DataArray");
+    const std::vector<double> v = detail::values(tag, doc.substr(pos, close - pos));
+    pos = close + 12;
+    const std::string name = detail::attr(tag, "Name");
+    const std::string ncs = detail::attr(tag, "NumberOfComponents");
+    const int nc = ncs.empty() ? 1 : std::stoi(ncs);
+    if (section == "Points") g.coords = v;
+    else if (section == "Cells" && name == "connectivity") conn = v;
+    else if (section == "Cells" && name == "offsets") off = v;
+    else if (section == "Cells" && name == "types") types = v;
+    else if (section == "PointData") g.point_data.push_back({name, nc, v});
+    else if (section == "FieldData" && !v.empty()) g.field_data.push_back({name, v[0]});
+  }
+  if (types.empty()) throw error(NOSH_ERR_INVALID, "no cells");
+  for (double ty : types)
+    if (ty != types[0]) throw error(NOSH_ERR_INVALID, "cells must all be triangles or all tetrahedra");
+  g.nvc = types[0] == 5 ? 3 : types[0] == 10 ? 4 : 0;
+  if (!g.nvc) throw error(NOSH_ERR_INVALID, "cells must be triangles or tetrahedra");
+  const size_t n = g.coords.size() / 3;
+  for (size_t k = 0; k < off.size(); k++)
+    if (off[k] != (double)((k + 1) * (size_t)g.nvc)) throw error(NOSH_ERR_INVALID, "cell offsets do not match the type");
+  g.cells.resize(conn.size());
+  for (size_t k = 0; k < conn.size(); k++) {
+    if (conn[k] < 0 || conn[k] >= (double)n) throw error(NOSH_ERR_INVALID, "cell connectivity out of range");
+    g.cells[k] = (int32_t)conn[k];
+  }
+  return g;
+}
+
+// One state file per converged continuation state, <prefix>0000.vtu, ...,
+// as the reference's continuation data saver names them; usable as the
+// stepper's observer.
+class data_saver {
+ public:
+  data_saver(const std::vector<double> &coords, const std::vector<int32_t> &cells, int nvc,
+             const std::string &prefix = "out", const std::vector<double> *A = nullptr)
+      : coords_(coords), cells_(cells), nvc_(nvc), prefix_(prefix), A_(A) {}
+  void operator()(int index, const vec &psi, double mu) {
+    grid g;
+    g.coords = coords_;
+    g.cells = cells_;
+    g.nvc = nvc_;
+    g.point_data.push_back({"psi", 2, psi});
+    if (A_) g.point_data.push_back({"A", 3, *A_});
+    g.field_data = {{"mu", mu}, {"step", (double)index}};
+    char name[32];
+    std::snprintf(name, sizeof name, "%04d.vtu", count_++);
+    paths_.push_back(prefix_ + name);
+    write_vtu(paths_.back(), g);
+  }
+  const std::vector<std::string> &paths() const { return paths_; }
+
+ private:
+  std::vector<double> coords_;
+  std::vector<int32_t> cells_;
+  int nvc_;
+  std::string prefix_;
+  const std::vector<double> *A_;
+  int count_ = 0;
+  std::vector<std::string> paths_;
+};
+
+}  // namespace io
 }  // namespace nosh
 
 #endif  // NOSH_GB300_HPP

@@ -81,3 +81,57 @@ def test_data_saver_names_and_contents(tmp_path):
     assert [os.path.basename(p) for p in saver.paths] == ["out0000.vtu", "out0001.vtu", "out0002.vtu"]
     _, _, psi, fields, fd = nio.read_state(saver.paths[2])
     assert np.all(psi == 2.0) and fd["mu"][0] == pytest.approx(0.2) and "A" in fields and "V" not in fields
+
+
+def _cpp_io():
+    import importlib.util
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("nosh_gb300_build", os.path.join(root, "nosh_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build()
+    return b.build_cpp_tests()["test_io"]
+
+
+def test_cpp_io_self_checks(tmp_path):
+    import subprocess
+
+    r = subprocess.run([_cpp_io()], capture_output=True, text=True, timeout=120, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all io checks passed" in r.stdout
+
+
+def test_cpp_and_python_files_interchange(tmp_path):
+    import subprocess
+
+    exe = _cpp_io()
+    # C++ writes, Python reads (bit-exact against the same formulas)
+    p = str(tmp_path / "cpp.vtu")
+    assert subprocess.run([exe, "write", p], timeout=60).returncode == 0
+    x, c, pd, fd = nio.read_vtu(p)
+    i = np.arange(10)
+    np.testing.assert_array_equal(pd["psi"].reshape(-1), np.sin(0.7 * i + 0.1) / 3.0)
+    np.testing.assert_array_equal(pd["V"], -1.0 + np.arange(5) / 7.0)
+    assert c.tolist() == [[0, 1, 2, 3], [1, 2, 3, 4]] and fd["mu"][0] == 0.25
+    # Python writes, C++ reads
+    xs, cs, _ = meshgen.cube(2, 1)
+    psi = np.random.default_rng(2).standard_normal(2 * len(xs))
+    q = str(tmp_path / "py.vtu")
+    nio.write_vtu(q, xs, cs, nio.state_point_data(psi, meshgen.mvp_constant_curl(xs)), {"mu": 0.5})
+    r = subprocess.run([exe, "read", q], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout
+    got = {ln.split()[0] + ("" if len(ln.split()) == 2 else ln.split()[1]): float(ln.split()[-1])
+           for ln in r.stdout.splitlines()}
+    # plain left-to-right sums, in the reader's order (bit-exact values;
+    # Python's sum() compensates, numpy's sums pairwise)
+    def seq(a):
+        t = 0.0
+        for v in np.asarray(a, np.float64).reshape(-1).tolist():
+            t += v
+        return t
+
+    assert got["points"] == seq(xs)
+    assert got["cells"] == seq(cs)
+    assert got["psi2"] == seq(psi)
+    assert got["fieldmu"] == 0.5 and got["nvc"] == 4
