@@ -121,6 +121,7 @@ int nosh_nls_num_params(nosh_nls nls, int *num);
 int nosh_nls_param_name(nosh_nls nls, int index, char *buf, size_t len);
 /* Precision of J/K_reg applies and of the Krylov solver: NOSH_PREC_*. */
 int nosh_nls_set_precision(nosh_nls nls, int precision);
+int nosh_nls_get_precision(nosh_nls nls, int *precision);
 /* Preconditioner options (the MueLu parameter list of
  * src/keo_regularized.cpp:296-315): maximum levels, coarsest size (nodes per
  * system), Chebyshev degree of pre- and post-smoothing, the reuse period

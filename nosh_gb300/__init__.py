@@ -126,6 +126,7 @@ _SIGS = {
     "nosh_continuation_destroy": (_I, [_P]),
     "nosh_continuation_advance": (_I, [_P, _D, _I, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "nosh_continuation_state": (_I, [_P, _P, C.POINTER(_D)]),
+    "nosh_nls_get_precision": (_I, [_P, C.POINTER(_I)]),
     "nosh_continuation_advance_arclength": (_I, [_P, _D, _I, _D, C.POINTER(NewtonOptions),
                                                  C.POINTER(NewtonStats)]),
     "nosh_continuation_tangent": (_I, [_P, C.POINTER(_D), C.POINTER(_D)]),

@@ -77,7 +77,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
 CPP_TESTS = {"test_reference_api": os.path.join(ROOT, "tests", "cpp", "test_reference_api.cpp"),
              "test_stepper": os.path.join(ROOT, "tests", "cpp", "test_stepper.cpp"),
-             "test_io": os.path.join(ROOT, "tests", "cpp", "test_io.cpp")}
+             "test_io": os.path.join(ROOT, "tests", "cpp", "test_io.cpp"),
+             "test_eig": os.path.join(ROOT, "tests", "cpp", "test_eig.cpp")}
 
 
 def build_cpp_tests(force: bool = False) -> dict:

@@ -295,6 +295,13 @@ int nosh_nls_set_precision(nosh_nls nls, int precision) {
   });
 }
 
+int nosh_nls_get_precision(nosh_nls nls, int *precision) {
+  return guarded([&] {
+    require(precision != nullptr, "null argument");
+    *precision = N(nls).precision;
+  });
+}
+
 int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size, int smooth_degree,
                              int reuse_period, double strength_threshold, double cheb_ratio) {
   return guarded([&] {

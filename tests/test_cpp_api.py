@@ -46,3 +46,27 @@ def test_cpp_stepper_on_the_gpu():
     r = subprocess.run([exe, "--gpu"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "all stepper checks passed" in r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_eigensolver_matches_oracle(tmp_path):
+    # the C++ LOBPCG's four lowest eigenvalues of J at its converged state
+    # against the oracle's shift-invert Lanczos on the same state
+    import numpy as np
+
+    from nosh_gb300 import io as nio
+    from oracle import oracle as O
+
+    exe = _build("test_eig")
+    path = str(tmp_path / "state.vtu")
+    r = subprocess.run([exe, path], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all eig checks passed" in r.stdout
+    lam = np.array([float(ln.split()[1]) for ln in r.stdout.splitlines() if ln.startswith("eigenvalue")])
+    x, cells, psi, fields, fd = nio.read_state(path)
+    m = O.finish_mesh(x, cells)
+    P = O.Problem(m, fields["A"])
+    mu = float(fd["mu"][0])
+    assert np.linalg.norm(P.compute_f(psi, 1.0, mu)) <= 1e-11
+    ref = O.lowest_eigenvalues(P, psi, 1.0, mu, 4)
+    assert np.abs(lam - ref).max() <= 1e-7 * max(1.0, np.abs(ref).max()), (lam, ref)
