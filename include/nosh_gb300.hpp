@@ -774,7 +774,7 @@ inline result lowest_eigenpairs(model_evaluator::nls &model, const vec &psi,
 // nosh_gb300/io.py: the reference reads psi, A and V vertex tags through
 // MOAB (src/mesh_reader.cpp:20-162) and writes one state per continuation
 // step (src/continuation_data_saver.hpp:26-50); MOAB's .h5m needs HDF5,
-// which this build does not have.  Arrays are base64 with UInt64 size
+// which the library does not depend on.  Arrays are base64 with UInt64 size
 // headers, little endian, and round-trip bit for bit; the reader also takes
 // ASCII arrays.
 namespace io {
@@ -833,7 +833,8 @@ inline std::vector<unsigned char> unb64(const std::string &s) {
   }
   return o;
 }
-// host byte order is little endian on every machine this builds for
+// host byte order is little endian on every supported platform (x86-64,
+// aarch64)
 template <class T>
 inline std::string encode(const std::vector<T> &v) {
   const uint64_t n = v.size() * sizeof(T);

@@ -1,7 +1,7 @@
 /*
  * nosh_oracle.c -- CPU FP64 restatement of nosh's NLS hot path.
  *
- * TEST INFRASTRUCTURE ONLY (parity checker + timed CPU baseline); never part
+ * TEST INFRASTRUCTURE ONLY (parity oracle + timed CPU baseline); never part
  * of the product.  Each function names the reference file:line it restates.
  * Parity pins: tests/test_oracle_kat.py reproduces the constants of the
  * reference's own (disabled) rectangle / cube test cases.

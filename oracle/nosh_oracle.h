@@ -2,7 +2,7 @@
  * nosh_oracle.h -- CPU FP64 restatement of nosh's Ginzburg-Landau /
  * nonlinear-Schroedinger hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the parity checker and the
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity oracle and the
  * timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's
  * CPU-baseline / reference arm may load it.  The product library
  * (nosh_gb300) never links, loads or calls it.

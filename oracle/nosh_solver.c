@@ -3,7 +3,7 @@
  * continuation for the NLS problem, OpenMP over the host cores.
  *
  * TEST INFRASTRUCTURE ONLY: the timed CPU baseline (bench.py's reference arm
- * and cpu_baseline) and a checker for the unpinned solver parts.  The
+ * and cpu_baseline) and the oracle for the unpinned solver parts.  The
  * reference's own path (Belos MINRES + MueLu SA-AMG + NOX/LOCA, Trilinos)
  * cannot be built here; this restates the same algorithmic roles:
  *   - operators: KEO (src/parameter_matrix_keo.cpp:106-180), F
