@@ -165,7 +165,7 @@ Minres<T>::Minres(NlsImpl &nls) : s(nls), n2(2 * nls.N) {
 
 template <typename T>
 Minres<T>::~Minres() {
-  for (cudaGraphExec_t &e : half_exec)
+  for (cudaGraphExec_t &e : part_exec)
     if (e) cudaGraphExecDestroy(e);
   if (pro_exec) cudaGraphExecDestroy(pro_exec);
   if (h_params) cudaFreeHost(h_params);
@@ -253,32 +253,33 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     prologue();
   }
   NOSH_CUDA(cudaGetLastError());
-  if (graphs && !half_exec[0]) {
-    for (int h = 0; h < 2; h++) {
+  if (graphs && !part_exec[0]) {
+    for (int h = 0; h < kParts; h++) {
       cudaGraph_t g;
       const int64_t before = s.launch_count;
       NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int j = h * kHalf; j < (h + 1) * kHalf; j++) iteration(j);
+      for (int j = h * kPart; j < (h + 1) * kPart; j++) iteration(j);
       NOSH_CUDA(cudaStreamEndCapture(st, &g));
-      half_kernels[h] = s.launch_count - before;
+      part_kernels[h] = s.launch_count - before;
       s.launch_count = before;
-      NOSH_CUDA(cudaGraphInstantiate(&half_exec[h], g, 0));
+      NOSH_CUDA(cudaGraphInstantiate(&part_exec[h], g, 0));
       NOSH_CUDA(cudaGraphDestroy(g));
     }
   }
-  auto launch_half = [&](int h) {
+  auto launch_part = [&](int h) {
     if (graphs) {
-      NOSH_CUDA(cudaGraphLaunch(half_exec[h], st));
-      s.launch_count += half_kernels[h];
+      NOSH_CUDA(cudaGraphLaunch(part_exec[h], st));
+      s.launch_count += part_kernels[h];
     } else {
-      for (int j = h * kHalf; j < (h + 1) * kHalf; j++) iteration(j);
+      for (int j = h * kPart; j < (h + 1) * kPart; j++) iteration(j);
     }
   };
-  // first batch: as many half-chunks as the previous solve used (two at first)
-  int batch = last_its > 0 ? (last_its + kHalf - 1) / kHalf : 2;
+  // first batch: as many parts as the previous solve used (one chunk at
+  // first)
+  int batch = last_its > 0 ? (last_its + kPart - 1) / kPart : kParts;
   int it = 0, h = 0;
   for (;;) {
-    for (int q = 0; q < batch; q++, h ^= 1, it += kHalf) launch_half(h);
+    for (int q = 0; q < batch; q++, h = (h + 1) % kParts, it += kPart) launch_part(h);
     batch = 1;
     NOSH_CUDA(cudaGetLastError());
     NOSH_CUDA(cudaMemcpyAsync(h_sc, d, sizeof(MinresScalars), cudaMemcpyDeviceToHost, st));
@@ -289,7 +290,8 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     if (h_sc->done || it >= maxit + kChunk) break;
   }
   // converged on the last issued iteration: its w/x update is still due
-  if (h_sc->wx_pending) wx_final(h == 1 ? kHalf - 1 : kChunk - 1);
+  // (h is the next part; the last issued iteration ends the part before it)
+  if (h_sc->wx_pending) wx_final(((h + kParts - 1) % kParts + 1) * kPart - 1);
   NOSH_CHECK(h_err[1] == 0, NOSH_ERR_CUDA, "an SpMV staging copy did not complete");
   NOSH_CHECK(h_err[0] == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
   status = h_sc->flag;

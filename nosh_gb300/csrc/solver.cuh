@@ -10,21 +10,23 @@ namespace nosh {
 // Preconditioned MINRES (Paige-Saunders) on J dx = b with the AMG V-cycle as
 // the SPD preconditioner, vectors in T, scalars in FP64 (minres_state.cuh).
 // Buffer roles repeat every kChunk iterations; the chunk is captured once as
-// two CUDA graphs of kChunk / 2 iterations (half-chunks, replayed
-// alternately).  A solve launches as many half-chunks as the previous solve
-// needed before the host first polls the convergence flag, then one at a
-// time; launches after convergence return at once.
+// kParts CUDA graphs of kPart iterations (replayed in turn).  A solve
+// launches as many parts as the previous solve needed before the host first
+// polls the convergence flag, then one at a time; launches after
+// convergence return at once (each such iteration still costs its kernels'
+// launches, so parts are kept short).
 template <typename T>
 struct Minres {
   static constexpr int kChunk = 6;  // multiple of the 2- and 3-buffer rotations
-  static constexpr int kHalf = kChunk / 2;
+  static constexpr int kParts = 3;
+  static constexpr int kPart = kChunk / kParts;
   NlsImpl &s;
   int64_t n2;  // real length (2N)
   DevBuf<T> r[2], z[2], w[3], u, x;
   DevBuf<MinresScalars> sc;
   MinresScalars *h_sc = nullptr;  // pinned host mirror
   int *h_err = nullptr;
-  cudaGraphExec_t half_exec[2] = {nullptr, nullptr};
+  cudaGraphExec_t part_exec[kParts] = {};
   // the captured prologue (initial V-cycle and recurrence set-up) for the
   // right-hand side pro_b; rtol and maxit reach it through `params`
   cudaGraphExec_t pro_exec = nullptr;
@@ -32,7 +34,7 @@ struct Minres {
   int64_t pro_kernels = 0;
   DevBuf<double> params;
   double *h_params = nullptr;
-  int64_t half_kernels[2] = {0, 0};
+  int64_t part_kernels[kParts] = {};
   int last_its = 0;  // iterations of the previous solve
   explicit Minres(NlsImpl &nls);
   ~Minres();
