@@ -135,3 +135,21 @@ def test_cpp_and_python_files_interchange(tmp_path):
     assert got["cells"] == seq(cs)
     assert got["psi2"] == seq(psi)
     assert got["fieldmu"] == 0.5 and got["nvc"] == 4
+
+
+def test_reference_io_case_rectanglesmall(tmp_path):
+    # the reference's io test (test/io.cpp:30-44 with the constants of
+    # :52-58): the "rectanglesmall" state psi = 1 and A = 1/2(-y, x, 0),
+    # written and read back, has ||psi||_1 = 4, ||psi||_inf = 1 and the
+    # per-component max norms {0.25, 2.5, 0} of A
+    from oracle import oracle as O
+
+    m = O.rectanglesmall()
+    psi = np.zeros(2 * m.N)
+    psi[0::2] = 1.0
+    A = O.mvp_constant_curl(m.x)
+    p = str(tmp_path / "rectanglesmall.vtu")
+    nio.write_vtu(p, m.x, m.cells, nio.state_point_data(psi, A))
+    _, _, psi_r, fields, _ = nio.read_state(p)
+    assert np.abs(psi_r).sum() == 4.0 and np.abs(psi_r).max() == 1.0
+    np.testing.assert_allclose(np.abs(fields["A"]).max(axis=0), [0.25, 2.5, 0.0], rtol=0, atol=1e-15)
