@@ -11,3 +11,17 @@ if ROOT not in sys.path:
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: larger CPU cases")
+
+
+def pytest_sessionstart(session):
+    # the package refuses to import without its compiled library; on a fresh
+    # checkout build it first (nvcc cross-compiles for sm_103a without a GPU)
+    if os.path.exists(os.path.join(ROOT, "nosh_gb300", "libnosh_gb300.so")):
+        return
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location(
+        "nosh_gb300_build", os.path.join(ROOT, "nosh_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build()
