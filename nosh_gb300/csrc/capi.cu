@@ -169,6 +169,8 @@ int nosh_mesh_create(const double *coords, int64_t num_vertices, const int32_t *
   return guarded([&] {
     require(out != nullptr && coords != nullptr && cells != nullptr, "null argument");
     *out = nullptr;
+    // a malformed mesh is reported as such with or without a GPU
+    nosh::MeshImpl::validate(num_vertices, cells, num_cells, verts_per_cell);
     require_gpu();
     auto *h = new nosh_mesh_s{nullptr};
     try {

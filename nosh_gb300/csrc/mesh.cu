@@ -224,28 +224,34 @@ __global__ void edge_length_kernel(int64_t E, const int32_t *__restrict__ edges,
 }  // namespace
 
 // ------------------------------------------------------------------------
-MeshImpl::MeshImpl(const double *coords, int64_t n_vertices, const int32_t *cells_in,
-                   int64_t n_cells, int verts_per_cell) {
+void MeshImpl::validate(int64_t n_vertices, const int32_t *cells, int64_t n_cells,
+                        int verts_per_cell) {
   NOSH_CHECK(verts_per_cell == 3 || verts_per_cell == 4, NOSH_ERR_INVALID,
              "verts_per_cell must be 3 (triangles) or 4 (tetrahedra)");
   NOSH_CHECK(n_vertices > 0 && n_cells > 0, NOSH_ERR_INVALID, "empty mesh");
   NOSH_CHECK(n_cells * verts_per_cell < (int64_t)1 << 31 && n_vertices < (int64_t)1 << 30,
              NOSH_ERR_INVALID, "mesh too large for 32-bit indices");
+  const int nvc = verts_per_cell;
+  // bounds of every index before anything is uploaded
+  for (int64_t k = 0; k < nvc * n_cells; k++)
+    NOSH_CHECK(cells[k] >= 0 && cells[k] < n_vertices, NOSH_ERR_INVALID,
+               "cell vertex index out of range at entry " + std::to_string(k));
+  for (int64_t c = 0; c < n_cells; c++)
+    for (int a = 0; a < nvc; a++)
+      for (int b = a + 1; b < nvc; b++)
+        NOSH_CHECK(cells[nvc * c + a] != cells[nvc * c + b], NOSH_ERR_MESH,
+                   "cell " + std::to_string(c) + " repeats a vertex");
+}
+
+MeshImpl::MeshImpl(const double *coords, int64_t n_vertices, const int32_t *cells_in,
+                   int64_t n_cells, int verts_per_cell) {
+  validate(n_vertices, cells_in, n_cells, verts_per_cell);
   nvc = verts_per_cell;
   ne = nvc == 3 ? 3 : 6;
   N = n_vertices;
   T = n_cells;
   x.assign(coords, coords + 3 * N);
   cells.assign(cells_in, cells_in + nvc * T);
-  // host-side bounds validation of every index before anything is uploaded
-  for (int64_t k = 0; k < nvc * T; k++)
-    NOSH_CHECK(cells[k] >= 0 && cells[k] < N, NOSH_ERR_INVALID,
-               "cell vertex index out of range at entry " + std::to_string(k));
-  for (int64_t c = 0; c < T; c++)
-    for (int a = 0; a < nvc; a++)
-      for (int b = a + 1; b < nvc; b++)
-        NOSH_CHECK(cells[nvc * c + a] != cells[nvc * c + b], NOSH_ERR_MESH,
-                   "cell " + std::to_string(c) + " repeats a vertex");
   NOSH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   build_topology();
   build_geometry();

@@ -36,6 +36,10 @@ struct MeshImpl {
   MeshImpl(const double *coords, int64_t n_vertices, const int32_t *cells,
            int64_t n_cells, int verts_per_cell);
   ~MeshImpl();
+  // host-only checks of a mesh description (sizes, cell type, every vertex
+  // index in range, no cell repeating a vertex); throws nosh::Error
+  static void validate(int64_t n_vertices, const int32_t *cells, int64_t n_cells,
+                       int verts_per_cell);
   MeshImpl(const MeshImpl &) = delete;
   MeshImpl &operator=(const MeshImpl &) = delete;
 
