@@ -1038,7 +1038,7 @@ __global__ void readout(int nparts, int64_t n, const float *__restrict__ part, c
                         const double *__restrict__ gram, float *__restrict__ grad, float *__restrict__ dz,
                         double *__restrict__ loss) {
   __shared__ float z[H], zs[4][H], h1[RH], dh1[RH];
-  __shared__ double w, dw;
+  __shared__ double dw;
   const int t = threadIdx.x;
   {
     const int c = t & (H - 1), grp = t / H;  // 4 groups of 64 channels
@@ -1063,7 +1063,6 @@ __global__ void readout(int nparts, int64_t n, const float *__restrict__ part, c
   if (t == 0) {
     double a = P[o_b2];
     for (int k = 0; k < RH; k++) a += (double)h1[k] * P[o_w2 + k];
-    w = a;
     *wout = a;
     if (gram) {
       const double dd = gram[2] > 0 ? gram[2] : 1.0;
