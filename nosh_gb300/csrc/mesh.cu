@@ -253,8 +253,17 @@ MeshImpl::MeshImpl(const double *coords, int64_t n_vertices, const int32_t *cell
   x.assign(coords, coords + 3 * N);
   cells.assign(cells_in, cells_in + nvc * T);
   NOSH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-  build_topology();
-  build_geometry();
+  try {
+    build_topology();
+    build_geometry();
+  } catch (...) {
+    // a throwing constructor runs no destructor: release the stream here
+    // (the device buffers free themselves)
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+    stream = nullptr;
+    throw;
+  }
 }
 
 MeshImpl::~MeshImpl() {
