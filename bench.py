@@ -50,26 +50,29 @@ FALLBACK_HBM_GBS = 6800.0
 
 def parse():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--gpus", type=int, default=1, help="GPUs of the job (N > 1: one rank per GPU under torchrun)")
+    ap.add_argument("--steps", type=int, default=30, help="timed continuation steps")
+    ap.add_argument("--warmup", type=int, default=5, help="untimed continuation steps before them")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"],
+                    help="reference: the FP64 CPU restatement on the host cores")
     ap.add_argument("--m", type=int, default=64, help="cubes per side")
     ap.add_argument("--seed", type=int, default=2, help="mesh jitter / initial state seed")
     ap.add_argument("--field", default="constant_curl", choices=["constant_curl", "stress"],
                     help="magnetic vector potential: 1/2(-y,x,0), or that + 0.05 sin(2 pi z)(1,0,0)")
-    ap.add_argument("--mu0", type=float, default=0.5)
-    ap.add_argument("--dmu", type=float, default=0.005)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--predictor", default="learned", choices=["learned", "secant", "quadratic", "cubic", "none"])
+    ap.add_argument("--mu0", type=float, default=0.5, help="first continuation parameter (a Newton solve, untimed)")
+    ap.add_argument("--dmu", type=float, default=0.005, help="continuation step in mu")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="headline precision: FP32 operators with FP64 residual and scalars, or all FP64")
+    ap.add_argument("--predictor", default="learned", choices=["learned", "secant", "quadratic", "cubic", "none"],
+                    help="headline predictor (the plain secant, the plain FP64 and the other polynomial predictors are timed too)")
     ap.add_argument("--refine", type=float, default=0.0,
                     help="residual the Newton steps aim at under the learned and cubic predictors (0: tol)")
     ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
     ap.add_argument("--train-iters", type=int, default=10, help="optimiser iterations per training step")
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=2e-3, help="learning rate of the online training")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end line through the C ABI")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the 160^3 roofline of the fine-level SpMVs (the stress configuration)")
     return ap.parse_args()
