@@ -245,7 +245,8 @@ void MeshImpl::validate(int64_t n_vertices, const int32_t *cells, int64_t n_cell
 
 MeshImpl::MeshImpl(const double *coords, int64_t n_vertices, const int32_t *cells_in,
                    int64_t n_cells, int verts_per_cell) {
-  validate(n_vertices, cells_in, n_cells, verts_per_cell);
+  // the description has passed validate() (nosh_mesh_create runs it before
+  // it looks for a device): one pass over the cells, not two
   nvc = verts_per_cell;
   ne = nvc == 3 ? 3 : 6;
   N = n_vertices;

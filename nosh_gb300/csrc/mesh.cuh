@@ -33,6 +33,7 @@ struct MeshImpl {
   DevBuf<int64_t> d_rp64;
   DevBuf<int32_t> d_rp, d_ci, d_nz_edge, d_pos_fwd, d_pos_bwd;
 
+  // expects a description that validate() accepted
   MeshImpl(const double *coords, int64_t n_vertices, const int32_t *cells,
            int64_t n_cells, int verts_per_cell);
   ~MeshImpl();
