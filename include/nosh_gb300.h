@@ -165,6 +165,14 @@ int nosh_nls_amg_levels(nosh_nls nls, int *num_levels, int64_t *sizes,
 #define NOSH_SPMV_STAGED 1
 #define NOSH_SPMV_WARP 2
 int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule);
+/* Diagnostics (no counterpart in the reference, whose Tpetra SpMV has no
+ * bounded wait): the bound, in mbarrier polls, of the waits of the staged
+ * SpMV schedule for the copies of its matrix rows into shared memory; the
+ * default is 2^20, and polls < 0 restores it.  A wait that runs out leaves
+ * its launch early and flags it; the call that ran that launch returns
+ * NOSH_ERR_CUDA at its next synchronisation, and the handle stays usable.
+ * polls = 0 makes every staged wait give up at once (tests of that path). */
+int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls);
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int nosh_nls_stream(nosh_nls nls, void **stream);
 
@@ -229,6 +237,15 @@ int nosh_keo_regularized_rebuild(nosh_nls nls, const double *p,
 int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y,
                                int num_vectors, int mode, double alpha,
                                double beta);
+/* y = the fine level's Chebyshev smoothing sweep of the preconditioner,
+ * from a zero initial guess on right-hand side x: y = p(D^-1 K_reg) D^-1 x,
+ * D the 2x2 diagonal blocks of K_reg and p the Chebyshev polynomial of the
+ * smoothing degree on [lmax / ratio, 1.1 lmax] (lmax a Gershgorin bound of
+ * D^-1 K_reg).  In the handle's precision.  For checking: MueLu's smoother
+ * inside the reference's V-cycle (src/keo_regularized.cpp:296-315) has no
+ * call of its own.  Needs a hierarchy of two levels or more. */
+int nosh_keo_regularized_smoother_apply(nosh_nls nls, const double *x,
+                                        double *y);
 /* Y = K_reg X (the regularised operator itself, for checking). */
 int nosh_keo_regularized_operator_apply(nosh_nls nls, const double *x,
                                         double *y);
@@ -418,6 +435,13 @@ int nosh_nls_profile_read(nosh_nls nls, int kernel, int64_t *launches,
  *   cv_thickness[N], scalar_potential[N], g
  *   psi[2N] (in), f[2N] (out)  interleaved complex, 16-byte aligned
  *   norm[1] (out)           ||F||_2
+ * Memory of another GPU, or host memory, is rejected with NOSH_ERR_INVALID;
+ * managed memory is accepted.
+ * The call cannot read the graph arrays on the host, so they must already be
+ * a valid CSR: row_ptr non-decreasing with row_ptr[0] = 0 and row_ptr[N] =
+ * the number of entries, and every cols[k] in [0, N).  Any other graph reads
+ * out of bounds (undefined behaviour).  nosh_mesh_complex_graph with its
+ * diagonal entries removed gives one that meets this.
  * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream)
  * and the call returns without waiting for it.
  *

@@ -18,8 +18,10 @@ reference (src/...)                        here
 Vectors are numpy float64 arrays (host) or anything exposing a CUDA device
 pointer via ``data_ptr()`` (e.g. a torch tensor); complex states are
 interleaved ``[Re0, Im0, Re1, Im1, ...]``.  There is no CPU fallback: the
-package refuses to import without its compiled library, and every compute
-call fails with :class:`NoshError` when no GPU is present.
+compiled library is mapped on the first call that needs it (so the numpy-only
+modules :mod:`nosh_gb300.meshgen` and :mod:`nosh_gb300.batch` import without
+it), that call raises ImportError when the library is missing, and every
+compute call fails with :class:`NoshError` when no GPU is present.
 """
 from __future__ import annotations
 
@@ -31,13 +33,34 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libnosh_gb300.so")
 
-if not os.path.exists(LIB_PATH):
-    raise ImportError(
-        f"nosh_gb300: compiled library {LIB_PATH} is missing; build it with "
-        "`python nosh_gb300/build.py` (nvcc, sm_103a)"
-    )
 
-_lib = C.CDLL(LIB_PATH)
+class _Library:
+    """The ctypes view of ``libnosh_gb300.so``, mapped on first attribute
+    access with every entry point's signature set."""
+
+    def __init__(self):
+        self._cdll = None
+
+    def load(self):
+        if self._cdll is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(
+                    f"nosh_gb300: compiled library {LIB_PATH} is missing; build it with "
+                    "`python nosh_gb300/build.py` (nvcc, sm_103a)"
+                )
+            cdll = C.CDLL(LIB_PATH)
+            for name, (res, args) in _SIGS.items():
+                fn = getattr(cdll, name)
+                fn.restype = res
+                fn.argtypes = args
+            self._cdll = cdll
+        return self._cdll
+
+    def __getattr__(self, name):
+        return getattr(self.load(), name)
+
+
+_lib = _Library()
 
 OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_BREAKDOWN = 1, 2, 3, 4, 5
@@ -98,6 +121,7 @@ _SIGS = {
     "nosh_nls_set_precision": (_I, [_P, _I]),
     "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I, _D, _D]),
     "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
+    "nosh_nls_set_stage_wait_limit": (_I, [_P, _I64]),
     "nosh_nls_amg_levels": (_I, [_P, C.POINTER(_I), _P, _I, C.POINTER(_I)]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_system_norms": (_I, [_P, _P]),
@@ -118,6 +142,7 @@ _SIGS = {
     "nosh_keo_regularized_rebuild": (_I, [_P, _P, _P]),
     "nosh_keo_regularized_apply": (_I, [_P, _P, _P, _I, _I, _D, _D]),
     "nosh_keo_regularized_operator_apply": (_I, [_P, _P, _P]),
+    "nosh_keo_regularized_smoother_apply": (_I, [_P, _P, _P]),
     "nosh_newton_default_options": (None, [C.POINTER(NewtonOptions)]),
     "nosh_newton_solve": (_I, [_P, _P, _P, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "nosh_continuation_step": (_I, [_P, _P, _P, _P, _D, _D, _I, C.POINTER(NewtonOptions),
@@ -143,15 +168,12 @@ _SIGS = {
     "nosh_nls_profile_enable": (_I, [_P, _I]),
     "nosh_nls_profile_read": (_I, [_P, _I, C.POINTER(_I64), C.POINTER(_D), C.POINTER(_D)]),
 }
-for _name, (_res, _args) in _SIGS.items():
-    _fn = getattr(_lib, _name)
-    _fn.restype = _res
-    _fn.argtypes = _args
 
 
 def lib():
-    """The loaded ctypes library (for low-level use and tests)."""
-    return _lib
+    """The loaded ctypes library (for low-level use and tests); maps it on
+    first use."""
+    return _lib.load()
 
 
 def _check(rc, allow=()):
@@ -300,6 +322,14 @@ class keo_regularized:
         _check(_lib.nosh_keo_regularized_apply(self._o._h, _ptr(X), _ptr(Y), nvec, mode, alpha, beta))
         return Y
 
+    def smoother_apply(self, x, y=None):
+        """The fine level's Chebyshev smoothing sweep from zero on right-hand
+        side x (the V-cycle's pre-smoother alone), in the handle's precision."""
+        x = _f64(x)
+        y = np.empty(2 * self._o.n) if y is None else y
+        _check(_lib.nosh_keo_regularized_smoother_apply(self._o._h, _ptr(x), _ptr(y)))
+        return y
+
     def operator_apply(self, x, y=None):
         x = _f64(x)
         y = np.empty(2 * self._o.n) if y is None else y
@@ -398,6 +428,12 @@ class nls:
     def set_spmv_schedule(self, schedule):
         """SPMV_AUTO, SPMV_STAGED or SPMV_WARP (see nosh_gb300.h)."""
         _check(_lib.nosh_nls_set_spmv_schedule(self._h, schedule))
+
+    def set_stage_wait_limit(self, polls):
+        """Diagnostics: bound (mbarrier polls) of the staged SpMV's waits for
+        its row copies; < 0 restores the default, 0 makes them give up at
+        once (see nosh_nls_set_stage_wait_limit)."""
+        _check(_lib.nosh_nls_set_stage_wait_limit(self._h, int(polls)))
 
     def stream(self) -> int:
         s = C.c_void_p()

@@ -247,7 +247,7 @@ __global__ void rap_diag(int64_t na, const int32_t *__restrict__ mptr,
 template <typename T>
 __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
                                 const C2<T> *__restrict__ off, const T *__restrict__ dia,
-                                T *__restrict__ dinv, unsigned long long *lmax_bits) {
+                                T *__restrict__ dinv, unsigned long long *lmax_bits, int *err) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double bound = 0.0;
   if (i < n) {
@@ -263,6 +263,9 @@ __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
       s += sqrt(v.x * v.x + v.y * v.y);
     }
     bound = (lmin > 0 && det > 0) ? 1.0 + (double)(s / lmin) : 1e300;
+    // a diagonal block that is not positive definite: the operator is not
+    // SPD (a g < 0 regularisation), so neither is the V-cycle
+    if (!(lmin > 0 && det > 0)) atomicOr(err, 32);
   }
   // max over the block, then one atomic per block (non-negative doubles
   // order like their bit patterns)
@@ -981,6 +984,14 @@ int Amg::tail_level() const { return impl->lt; }
 
 const int *Amg::error_flag_ptr() const { return impl->err.p; }
 
+void Amg::clear_error() {
+  // the coarse operators that failed the pivot check are replaced by the
+  // next refresh, which is made a full Galerkin one
+  NOSH_CUDA(cudaMemsetAsync(impl->err.p, 0, sizeof(int), impl->nls.stream));
+  impl->vf.refreshes = 0;
+  impl->vd.refreshes = 0;
+}
+
 int Amg::error_flag() {
   int herr = 0;
   impl->err.download(&herr, 1, impl->nls.stream);
@@ -1061,7 +1072,7 @@ void Amg::refresh() {
     // an SPD preconditioner)
     NOSH_CUDA(cudaMemsetAsync(I.lmax_bits.p, 0, sizeof(unsigned long long), st));
     dinv_gershgorin<T><<<div_up(I.lev[0].n, 256), 256, 0, st>>>(I.lev[0].n, I.lev[0].rp, I.off<T>(0), I.dia<T>(0),
-                                                                V.dinv[0].p, I.lmax_bits.p);
+                                                                V.dinv[0].p, I.lmax_bits.p, I.err.p);
     cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p, std::max(I.opt.smooth_degree, 1), I.opt.cheb_ratio, V.coef[0].p,
                                     I.lmax.p);
     I.nls.launch_count += 2;
@@ -1083,7 +1094,7 @@ void Amg::refresh() {
     }
     if (l < L - 1) {  // the coarsest level is solved directly
       dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
-                                                            V.dinv[l].p, I.lmax_bits.p + l);
+                                                            V.dinv[l].p, I.lmax_bits.p + l, I.err.p);
       ++I.nls.launch_count;
       cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1), I.opt.cheb_ratio,
                                       V.coef[l].p, I.lmax.p + l);
@@ -1229,6 +1240,29 @@ void Amg::apply(const T *r, T *z) {
   NOSH_CUDA(cudaGetLastError());
 }
 
+// The fine level's pre-smoothing sweep alone, from x = 0: the first
+// Chebyshev step, then degree - 1 SpMV steps (as in descend_ascend).
+template <typename T>
+void Amg::presmooth(const T *b, T *x) {
+  Impl &I = *impl;
+  NOSH_CHECK(I.lev.size() >= 2, NOSH_ERR_INVALID, "the hierarchy has one level: no smoother");
+  AmgVals<T> &V = I.vals<T>();
+  cudaStream_t st = I.nls.stream;
+  const AmgLevel &A = I.lev[0];
+  const int deg = std::max(I.opt.smooth_degree, 1);
+  C2<T> *cur = (deg % 2 == 1) ? (C2<T> *)x : V.x2[0].p;
+  C2<T> *oth = (deg % 2 == 1) ? V.x2[0].p : (C2<T> *)x;
+  cheb_first<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, V.dinv[0].p, V.coef[0].p, (const C2<T> *)b, V.d[0].p,
+                                                  cur);
+  ++I.nls.launch_count;
+  for (int k = 1; k < deg; k++) {
+    ChebOp<T> op{I.dia<T>(0), V.dinv[0].p, V.coef[0].p, k, (const C2<T> *)b, cur, V.d[0].p, oth, nullptr};
+    I.rows<T>(0, cur, op);
+    std::swap(cur, oth);
+  }
+  NOSH_CUDA(cudaGetLastError());
+}
+
 // One MINRES Lanczos step around the V-cycle:
 //   r_old <- J z / beta - (beta/oldb) r_old - (alfa/beta) r_cur  (= r_new)
 //   z_out <- V-cycle(r_new),  <r_new, z_out> and the Givens recurrence.
@@ -1266,6 +1300,8 @@ template void Amg::refresh<float>();
 template void Amg::refresh<double>();
 template void Amg::apply<float>(const float *, float *);
 template void Amg::apply<double>(const double *, double *);
+template void Amg::presmooth<float>(const float *, float *);
+template void Amg::presmooth<double>(const double *, double *);
 template void Amg::apply_minres<float>(MinresScalars *, const float *, float *, const float *, float *);
 template void Amg::apply_minres<double>(MinresScalars *, const double *, double *, const double *, double *);
 

@@ -29,6 +29,10 @@ struct Amg {
   // z = V-cycle(r); r, z device vectors of 2N (interleaved complex)
   template <typename T>
   void apply(const T *r, T *z);
+  // x = the fine level's Chebyshev smoothing sweep from x = 0 on right-hand
+  // side b (the V-cycle's pre-smoother alone); needs two levels or more
+  template <typename T>
+  void presmooth(const T *b, T *x);
   // One MINRES Lanczos step fused around the V-cycle (see amg.cu)
   template <typename T>
   void apply_minres(MinresScalars *ms, const T *u, T *r_old, const T *r_cur, T *z_out);
@@ -38,6 +42,9 @@ struct Amg {
   // pivot-failure flags of the coarsest factorisation (synchronises)
   int error_flag();
   const int *error_flag_ptr() const;  // device address of the same flags
+  // clears the flags and makes the next refresh a full one (after a failed
+  // pivot check, so the handle can go on with other parameters)
+  void clear_error();
 
   struct Impl;
   std::unique_ptr<Impl> impl;

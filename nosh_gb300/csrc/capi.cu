@@ -365,6 +365,10 @@ int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule) {
   });
 }
 
+int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls) {
+  return guarded([&] { N(nls).set_stage_wait_limit(polls); });
+}
+
 int nosh_nls_stream(nosh_nls nls, void **stream) {
   return guarded([&] {
     require(stream != nullptr, "null output");
@@ -531,9 +535,9 @@ int nosh_keo_regularized_rebuild(nosh_nls nls, const double *p, const double *x)
     double g, mu;
     read_params(p, g, mu);
     s.reg_rebuild(stage_in(s, x, s.d_in, 2 * s.N), g, mu);
-    if (!s.amg) s.amg.reset(new nosh::Amg(s));
-    if (s.precision == NOSH_PREC_FP64) s.amg->refresh<double>();
-    else s.amg->refresh<float>();
+    nosh::Amg &amg = nosh::ensure_preconditioner(s);
+    if (s.precision == NOSH_PREC_FP64) amg.refresh<double>();
+    else amg.refresh<float>();
     s.sync();
   });
 }
@@ -556,6 +560,23 @@ int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y, int nve
       }
       o.finish(s);
     }
+  });
+}
+
+int nosh_keo_regularized_smoother_apply(nosh_nls nls, const double *x, double *y) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(s.reg_ready && s.amg, "preconditioner not built: call nosh_keo_regularized_rebuild");
+    const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
+    OutVec o(s, y, s.d_out, 2 * s.N);
+    if (s.precision == NOSH_PREC_FP64) {
+      s.amg->presmooth<double>(dx, o.dev);
+    } else {
+      nosh::launch_f64_to_f32(dx, s.d_inf.p, 2 * s.N, s.stream);
+      s.amg->presmooth<float>(s.d_inf.p, s.d_outf.p);
+      nosh::launch_f32_to_f64(s.d_outf.p, o.dev, 2 * s.N, s.stream);
+    }
+    o.finish(s);
   });
 }
 

@@ -18,9 +18,11 @@
 // The readout is global: the correction is a multiple of a smooth
 // history-difference field, so node-level rounding noise (which the KEO
 // amplifies) never enters the predicted state, and an error in w is scaled
-// by |c|, the difference of two extrapolants.  The loss is the cv-weighted
-// squared error of the prediction relative to the quadratic's, exact from
-// three Gram scalars.
+// by |c|, the difference of two extrapolants.  The loss is the linearised
+// residual of the prediction relative to the quadratic's: with d = target -
+// quadratic and J the Jacobian at the phase-aligned target,
+// F(quadratic + w c) ~ J (w c - d), and the loss ||J(w c - d)||^2 / ||J d||^2
+// is exact from the three Gram scalars of (J c, J d).
 // Node GEMMs run on the tensor cores with BF16 operands and FP32
 // accumulation (mma.sync m16n8k16); the message operands A, B are stored in
 // FP16 and the forward messages are formed and summed in packed FP16

@@ -170,7 +170,14 @@ struct NlsImpl {
   // full-graph values (with diagonal) in complex_graph order, complex
   void export_values(const C2<double> *offdiag, const double *diag, double *out);
 
-  void sync() { NOSH_CUDA(cudaStreamSynchronize(stream)); }
+  // Waits for the handle's stream.  A staged SpMV that gave up waiting for
+  // its copies (kStageErrorSlot set) makes it throw NOSH_ERR_CUDA after
+  // clearing the flag and the reduction counters, so the handle stays usable.
+  void sync();
+  [[noreturn]] void stage_failure();
+  unsigned *h_stage_err = nullptr;  // pinned, one word
+  // diagnostics: bound of the staging waits (polls; < 0 restores the default)
+  void set_stage_wait_limit(int64_t polls);
 };
 
 // launch helpers shared with the solver

@@ -45,16 +45,26 @@ double *scratch_on_current_device() {
   return g_scratch_ptr[dev];
 }
 
-__global__ void sqrt_in_place(double *v) { *v = sqrt(*v); }
+// The residual epilogue whose finishing thread also takes the square root:
+// grid_reduce stores ||F||^2 into *norm, then the hook overwrites it with
+// ||F||, so the call is one launch.
+struct ResidualNormOp : ResidualOp<true> {
+  static constexpr bool kHook = true;
+  double *norm;
+  __device__ void hook(double total) const { *norm = sqrt(total); }
+};
 
-bool device_resident(const void *p, size_t align) {
+// Device memory of `device` (or managed memory, reachable from every
+// device), aligned to `align` bytes.
+bool device_resident(const void *p, size_t align, int device) {
   if (p == nullptr || reinterpret_cast<uintptr_t>(p) % align != 0) return false;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 }  // namespace
@@ -73,30 +83,38 @@ extern "C" int nosh_residual_norm_noalloc(int64_t num_vertices, const int32_t *r
                "nosh_residual_norm_noalloc: " + std::to_string(num_vertices) +
                    " vertices exceed the fixed scratch limit of " +
                    std::to_string(kNoallocMaxVertices) + "; use nosh_nls_compute_f_norm");
-    NOSH_CHECK(device_resident(row_ptr, 4) && device_resident(cols, 4) && device_resident(keo_diag, 8) &&
-                   device_resident(cv_thickness, 8) && device_resident(scalar_potential, 8) &&
-                   device_resident(norm, 8),
-               NOSH_ERR_INVALID, "nosh_residual_norm_noalloc: every array must be device memory");
-    NOSH_CHECK(device_resident(keo_offdiag, 16) && device_resident(psi, 16) && device_resident(f, 16),
+    int device = 0;
+    NOSH_CUDA(cudaGetDevice(&device));
+    NOSH_CHECK(device_resident(row_ptr, 4, device) && device_resident(cols, 4, device) &&
+                   device_resident(keo_diag, 8, device) && device_resident(cv_thickness, 8, device) &&
+                   device_resident(scalar_potential, 8, device) && device_resident(norm, 8, device),
+               NOSH_ERR_INVALID,
+               "nosh_residual_norm_noalloc: every array must be device memory of the current device (" +
+                   std::to_string(device) + ")");
+    NOSH_CHECK(device_resident(keo_offdiag, 16, device) && device_resident(psi, 16, device) &&
+                   device_resident(f, 16, device),
                NOSH_ERR_INVALID,
                "nosh_residual_norm_noalloc: complex arrays (keo_offdiag, psi, f) must be "
-               "16-byte aligned device memory");
+               "16-byte aligned device memory of the current device (" + std::to_string(device) + ")");
     double *scratch = scratch_on_current_device();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the arrival counter must start at zero; the partials are overwritten
     NOSH_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double), s));
-    dev::ResidualOp<true> op{keo_diag, cv_thickness, scalar_potential, g,
-                             reinterpret_cast<const dev::C2<double> *>(psi),
-                             reinterpret_cast<dev::C2<double> *>(f)};
+    ResidualNormOp op;
+    op.kdiag = keo_diag;
+    op.cvt = cv_thickness;
+    op.V = scalar_potential;
+    op.g = g;
+    op.x = reinterpret_cast<const dev::C2<double> *>(psi);
+    op.y = reinterpret_cast<dev::C2<double> *>(f);
+    op.norm = norm;
     const int grid = div_up(num_vertices, dev::kRows);
     // cap = 0: nonzeros are read directly (no shared-memory staging), so the
     // launch needs no host-side knowledge of the row pointers
-    dev::row_block_apply<double, dev::ResidualOp<true>><<<grid, dev::kRows, 0, s>>>(
+    dev::row_block_apply<double, ResidualNormOp><<<grid, dev::kRows, 0, s>>>(
         (int)num_vertices, row_ptr, cols, reinterpret_cast<const dev::C2<double> *>(keo_offdiag),
         reinterpret_cast<const dev::C2<double> *>(psi), 0, op, scratch + 1,
         reinterpret_cast<unsigned *>(scratch), norm);
-    NOSH_CUDA(cudaGetLastError());
-    sqrt_in_place<<<1, 1, 0, s>>>(norm);
     NOSH_CUDA(cudaGetLastError());
     set_last_error("");
     return NOSH_OK;

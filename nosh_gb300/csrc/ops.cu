@@ -447,6 +447,8 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
   d_inf.alloc(2 * N);
   d_outf.alloc(2 * N);
   red.init(div_up(N, kRows) + div_up(N, 256) + 1024, 64, s);
+  NOSH_CUDA(cudaMallocHost(&h_stage_err, sizeof(unsigned)));
+  *h_stage_err = 0u;
   cap32 = staging_cap<float>(*m);
   cap64 = staging_cap<double>(*m);
   tune_schedules();
@@ -538,6 +540,38 @@ NlsImpl::~NlsImpl() {
   solver_state.reset();
   amg.reset();
   if (stream) cudaStreamDestroy(stream);
+  if (h_stage_err) cudaFreeHost(h_stage_err);
+}
+
+void NlsImpl::sync() {
+  if (!h_stage_err || !red.counter.p) {
+    NOSH_CUDA(cudaStreamSynchronize(stream));
+    return;
+  }
+  NOSH_CUDA(cudaMemcpyAsync(h_stage_err, red.counter.p + kStageErrorSlot, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            stream));
+  NOSH_CUDA(cudaStreamSynchronize(stream));
+  if (*h_stage_err) stage_failure();
+}
+
+void NlsImpl::stage_failure() {
+  // the CTAs that left early never reached their grid reductions: reset the
+  // arrival counters they left behind along with the flag (the wait-bound
+  // override in kStageWaitSlot stays)
+  NOSH_CUDA(cudaMemsetAsync(red.counter.p, 0, kStageWaitSlot * sizeof(unsigned), stream));
+  NOSH_CUDA(cudaMemsetAsync(red.counter.p + kStageErrorSlot, 0, sizeof(unsigned), stream));
+  NOSH_CUDA(cudaStreamSynchronize(stream));
+  if (h_stage_err) *h_stage_err = 0;
+  throw Error(NOSH_ERR_CUDA,
+              "an SpMV staging copy did not complete within its wait bound: the results of this call are "
+              "invalid (the handle stays usable)");
+}
+
+void NlsImpl::set_stage_wait_limit(int64_t polls) {
+  NOSH_CHECK(polls < (int64_t)0xffffffffLL, NOSH_ERR_INVALID, "stage wait limit out of range");
+  const unsigned v = polls < 0 ? 0u : (unsigned)(polls + 1);
+  NOSH_CUDA(cudaMemcpyAsync(red.counter.p + kStageWaitSlot, &v, sizeof(unsigned), cudaMemcpyHostToDevice, stream));
+  NOSH_CUDA(cudaStreamSynchronize(stream));
 }
 
 void NlsImpl::keo_refill(double mu) {

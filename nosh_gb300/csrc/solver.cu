@@ -287,13 +287,18 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     NOSH_CUDA(cudaMemcpyAsync(h_err + 1, s.red.counter.p + kStageErrorSlot, sizeof(int), cudaMemcpyDeviceToHost,
                               st));
     NOSH_CUDA(cudaStreamSynchronize(st));
-    if (h_sc->done || it >= maxit + kChunk) break;
+    if (h_sc->done || h_err[1] != 0 || it >= maxit + kChunk) break;
   }
   // converged on the last issued iteration: its w/x update is still due
   // (h is the next part; the last issued iteration ends the part before it)
   if (h_sc->wx_pending) wx_final(((h + kParts - 1) % kParts + 1) * kPart - 1);
-  NOSH_CHECK(h_err[1] == 0, NOSH_ERR_CUDA, "an SpMV staging copy did not complete");
-  NOSH_CHECK(h_err[0] == 0, NOSH_ERR_BREAKDOWN, "AMG coarsest matrix is not positive definite");
+  if (h_err[1] != 0) s.stage_failure();
+  if (h_err[0] != 0) {
+    s.amg->clear_error();
+    throw Error(NOSH_ERR_BREAKDOWN,
+                "the regularised KEO or a level of its AMG hierarchy is not positive definite "
+                "(a diagonal block or a coarsest pivot)");
+  }
   status = h_sc->flag;
   rel_res = h_sc->beta1 > 0 ? h_sc->phibar / h_sc->beta1 : 0.0;
   last_its = h_sc->itn;
@@ -409,11 +414,7 @@ double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double 
   return std::sqrt(n2);
 }
 
-// Refresh the Jacobian and the preconditioner at (psi, g, mu) in precision T.
-template <typename T>
-static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu) {
-  s.jac_rebuild(psi, g, mu);
-  s.reg_rebuild(psi, g, mu);
+Amg &ensure_preconditioner(NlsImpl &s) {
   if (!s.amg) {
     AmgOptions o;
     o.max_levels = s.amg_max_levels;
@@ -424,7 +425,15 @@ static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu
     o.cheb_ratio = s.amg_cheb_ratio;
     s.amg.reset(new Amg(s, o));
   }
-  s.amg->refresh<T>();
+  return *s.amg;
+}
+
+// Refresh the Jacobian and the preconditioner at (psi, g, mu) in precision T.
+template <typename T>
+static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu) {
+  s.jac_rebuild(psi, g, mu);
+  s.reg_rebuild(psi, g, mu);
+  ensure_preconditioner(s).refresh<T>();
 }
 
 template <typename T>
@@ -490,6 +499,9 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     const int its = mr.solve(b.p, eta, opt.max_krylov, status, rel);
     st.krylov_iters += its;
     if (status == NOSH_ERR_NAN || status == NOSH_ERR_BREAKDOWN) {
+      // the hierarchy's coarse operators are rebuilt in full next time, so
+      // a later solve does not inherit the failed ones
+      s.amg->clear_error();
       st.status = status;
       return;
     }

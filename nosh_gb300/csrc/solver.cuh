@@ -59,6 +59,8 @@ NewtonState &state_of(NlsImpl &s);
 // drop the AMG hierarchy (and the MINRES graphs that reference it); the next
 // rebuild constructs it from the current options
 void reset_preconditioner(NlsImpl &s);
+// the AMG hierarchy with the handle's options, created when missing
+Amg &ensure_preconditioner(NlsImpl &s);
 // ||F(psi)||_2 (writes F into f; synchronises)
 double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f);
 // Newton on state_of(s).psi in place.  With f0 >= 0, ns.f already holds

@@ -135,10 +135,13 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
-// Bounded wait for the phase with the given parity; false after the limit.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Default bound of a staging wait, in polls of mbarrier.try_wait.
+constexpr uint32_t kStageWaitPolls = 1u << 20;
+// Bounded wait for the phase with the given parity; false after `limit`
+// polls (at once for a limit of 0).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit = kStageWaitPolls) {
   const uint32_t a = smem_addr(bar);
-  for (int it = 0; it < (1 << 20); it++) {
+  for (uint32_t it = 0; it < limit; it++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -162,8 +165,12 @@ __host__ __device__ constexpr int stage_limit() {
   return (int)((48 * 1024) / (sizeof(int32_t) + sizeof(C2<T>))) & ~3;
 }
 // Slot of the per-stream reduction counters that records a staging copy
-// that never completed (checked by the host after each linear solve).
+// that never completed (checked by the host at its next synchronisation).
 constexpr int kStageErrorSlot = 15;
+// Slot holding a diagnostic override of the staging-wait bound: 0 = the
+// default kStageWaitPolls, v > 0 = v - 1 polls.  Read only by launches that
+// stage (cap > 0).
+constexpr int kStageWaitSlot = 14;
 
 template <typename T, class Op>
 __global__ void __launch_bounds__(kRows)
@@ -205,6 +212,13 @@ __global__ void __launch_bounds__(kRows)
   A part = 0;
   uint32_t parity[2] = {0u, 0u};
   bool ok = true;
+  // copies issued and not yet waited for: the current and the next row block
+  bool cur_staged = false, next_staged = false;
+  uint32_t limit = kStageWaitPolls;
+  if (cap > 0) {
+    const unsigned o = __ldcg(counter + kStageWaitSlot);
+    if (o != 0u) limit = o - 1u;
+  }
   if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue(blockIdx.x, 0);
   int stage = 0;
   for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, stage ^= 1) {
@@ -217,7 +231,14 @@ __global__ void __launch_bounds__(kRows)
     typename Op::Pre pre{};
     if (row < N) pre = op.load(row);
     const bool staged = n > 0 && n <= cap;
-    const bool arrived = staged ? mbar_wait(&bar[stage], parity[stage]) : true;
+    cur_staged = staged;
+    next_staged = false;
+    if (rb + (int)gridDim.x < nblocks) {
+      int ks2, n2;
+      range(rb + gridDim.x, ks2, n2);
+      next_staged = n2 > 0 && n2 <= cap;
+    }
+    const bool arrived = staged ? mbar_wait(&bar[stage], parity[stage], limit) : true;
     if (__syncthreads_or(!arrived)) {  // the CTA leaves together
       ok = false;
       break;
@@ -263,11 +284,13 @@ __global__ void __launch_bounds__(kRows)
     __syncthreads();  // this buffer is refilled two row blocks later
   }
   if (!ok) {
-    // a copy never completed: record it, give the copies in flight a last
-    // bounded wait, and leave (the results of this launch are invalid)
-    atomicOr(counter + kStageErrorSlot, 1u);
-    mbar_wait(&bar[0], parity[0]);
-    mbar_wait(&bar[1], parity[1]);
+    // a wait gave up: record it, give the copies still in flight (this row
+    // block's and the next one's) a last wait at the default bound, so no
+    // copy lands in shared memory after the CTA has left, and leave (the
+    // results of this launch are invalid)
+    if (threadIdx.x == 0) atomicOr(counter + kStageErrorSlot, 1u);
+    if (cur_staged) mbar_wait(&bar[stage], parity[stage]);
+    if (next_staged) mbar_wait(&bar[stage ^ 1], parity[stage ^ 1]);
     return;
   }
   if (Op::kReduce) {

@@ -281,6 +281,73 @@ class Problem:
         )
         return y
 
+    def kreg_blocks(self, psi, g, mu):
+        """K_reg in compact form: the off-diagonal complex values as (rows,
+        cols, values) and the real 2x2 diagonal blocks (d0r, d0i, d1b) per
+        vertex, K_ii included (src/keo_regularized.cpp:233-258)."""
+        vals = self.keo_values(mu)
+        N = self.m.N
+        rows = np.repeat(np.arange(N), np.diff(self.row_ptr))
+        diag = self.cols == rows
+        kii = np.zeros(N)
+        kii[rows[diag]] = vals[diag].real
+        psi = _f(psi)
+        re, im = psi[0::2], psi[1::2]
+        w = g * self.m.cv * self.t
+        al = w * 2.0 * (re * re + im * im)
+        be = w * 2.0 * re * im
+        ga = w * (re * re - im * im)
+        return rows[~diag], self.cols[~diag], vals[~diag], (kii + al + ga, kii + al - ga, be)
+
+    def cheb_presmooth(self, psi, g, mu, b, degree=2, ratio=15.0):
+        """One block-Jacobi Chebyshev smoothing sweep of K_reg from x = 0 on
+        right-hand side b: the pre-smoother of the GPU preconditioner's fine
+        level, restated in FP64.  The reference only configures its MueLu
+        smoother (src/keo_regularized.cpp:296-315), so this restates the
+        smoother the GPU build defines: D the 2x2 diagonal blocks, lmax =
+        1.1 max_i (1 + sum_j |K_ij| / lambda_min(D_i)) (Gershgorin), the
+        Chebyshev polynomial of `degree` on [lmax / (1.1 ratio), lmax]."""
+        import scipy.sparse as sp
+
+        N = self.m.N
+        r_, c_, v_, (a, d, bb) = self.kreg_blocks(psi, g, mu)
+        Koff = sp.csr_matrix((v_, (r_, c_)), shape=(N, N))
+        det = a * d - bb * bb
+        ia, ie, if_ = d / det, a / det, -bb / det
+        lmin_b = 0.5 * (a + d) - np.sqrt(0.25 * (a - d) ** 2 + bb * bb)
+        rs = np.asarray(abs(Koff).sum(axis=1)).ravel()
+        with np.errstate(divide="ignore"):
+            bound = np.where((lmin_b > 0) & (det > 0), 1.0 + rs / lmin_b, 1e300)
+        lmax = 1.1 * bound.max()
+        lmin = lmax / (1.1 * ratio)
+        theta, delta = 0.5 * (lmax + lmin), 0.5 * (lmax - lmin)
+        sigma = theta / delta
+        rho = 1.0 / sigma
+        coef = [(None, None)]
+        for _ in range(1, degree):
+            rn = 1.0 / (2.0 * sigma - rho)
+            coef.append((rn * rho, 2.0 * rn / delta))
+            rho = rn
+        b = _f(b)
+        bz = b[0::2] + 1j * b[1::2]
+
+        def dinv(z):
+            return (ia * z.real + if_ * z.imag) + 1j * (if_ * z.real + ie * z.imag)
+
+        def apply(z):
+            y = Koff @ z
+            return y + (a * z.real + bb * z.imag) + 1j * (bb * z.real + d * z.imag)
+
+        dd = dinv(bz) / theta
+        x = dd.copy()
+        for k in range(1, degree):
+            c1, c2 = coef[k]
+            dd = c1 * dd + c2 * dinv(bz - apply(x))
+            x = x + dd
+        out = np.empty(2 * N)
+        out[0::2], out[1::2] = x.real, x.imag
+        return out
+
     def energy(self, psi):
         return lib().nor_energy(self.m.N, self.m.cv, _f(psi))
 

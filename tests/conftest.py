@@ -14,7 +14,7 @@ def pytest_configure(config):
 
 
 def pytest_sessionstart(session):
-    # the package refuses to import without its compiled library; on a fresh
+    # the package's compute calls need its compiled library; on a fresh
     # checkout build it first (nvcc cross-compiles for sm_103a without a GPU)
     if os.path.exists(os.path.join(ROOT, "nosh_gb300", "libnosh_gb300.so")):
         return

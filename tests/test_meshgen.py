@@ -36,3 +36,22 @@ def test_edges_count_formula():
     x, c, _ = meshgen.cube(m, 1)
     mesh = O.finish_mesh(x, c)
     assert mesh.E == 3 * m * (m + 1) ** 2 + 3 * m * m * (m + 1) + m**3
+
+
+def test_numpy_modules_do_not_map_the_cuda_library():
+    """The CPU arm of the benchmark builds its meshes with meshgen; importing
+    it (and batch) must not map libnosh_gb300.so into the process."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, sys.argv[1]); "
+            "from nosh_gb300 import meshgen, batch; meshgen.cube(2, 1); "
+            "print(open('/proc/self/maps').read())")
+    out = subprocess.run([sys.executable, "-c", code, root], capture_output=True, text=True, check=True).stdout
+    assert "libnosh_gb300" not in out
+    code_lib = ("import sys; sys.path.insert(0, sys.argv[1]); import nosh_gb300 as ng; ng.lib(); "
+                "print(open('/proc/self/maps').read())")
+    out = subprocess.run([sys.executable, "-c", code_lib, root], capture_output=True, text=True, check=True).stdout
+    assert "libnosh_gb300" in out

@@ -38,7 +38,10 @@ def _split_graph(rp, ci, vals):
     return rp_od, ci[keep].astype(np.int32), np.ascontiguousarray(vals[keep]), kdiag
 
 
-def test_noalloc_residual_matches_handle_path():
+@pytest.mark.parametrize("m", [12, 41])
+def test_noalloc_residual_matches_handle_path(m):
+    """m = 12: 2,197 vertices, 18 CTAs; m = 41: 74,088 vertices, 579 CTAs, so
+    the finishing CTA sums the partials with its four-accumulator loop."""
     import torch
 
     import nosh_gb300 as ng
@@ -46,7 +49,7 @@ def test_noalloc_residual_matches_handle_path():
 
     fn = _bind(ng.lib())
     dev = torch.device("cuda", 0)
-    x, cells, psi0 = meshgen.cube(12, 5)
+    x, cells, psi0 = meshgen.cube(m, 5)
     A = meshgen.mvp_constant_curl(x)
     gm = ng.mesh(x, cells)
     g, mu = 1.0, 0.37
@@ -67,17 +70,39 @@ def test_noalloc_residual_matches_handle_path():
     d_f = torch.empty(2 * N, dtype=torch.float64, device=dev)
     d_norm = torch.empty(1, dtype=torch.float64, device=dev)
     rng = np.random.default_rng(17)
+    # both states are on the device before the calls, so nothing else
+    # allocates between the free-memory readings below
+    states = [psi0, psi0 + 0.3 * rng.standard_normal(psi0.size)]
+    d_psi = [d(p) for p in states]
+    torch.cuda.synchronize()
     for call in range(2):  # two calls in a row share the scratch array
-        psi = psi0 + (0.3 if call else 0.0) * rng.standard_normal(psi0.size)
-        d_psi = d(psi)
+        free_before = torch.cuda.mem_get_info(dev)[0]
         rc = fn(N, d_rp.data_ptr(), d_ci.data_ptr(), d_off.data_ptr(), d_kd.data_ptr(), d_cvt.data_ptr(),
-                d_V.data_ptr(), g, d_psi.data_ptr(), d_f.data_ptr(), d_norm.data_ptr(), None)
+                d_V.data_ptr(), g, d_psi[call].data_ptr(), d_f.data_ptr(), d_norm.data_ptr(), None)
         assert rc == 0, ng.lib().nosh_last_error()
         torch.cuda.synchronize()
-        f_ref, n_ref = model.compute_f(psi, {"g": g, "mu": mu}, with_norm=True)
+        if call == 1:
+            # the first call on a device may load the library's module (and
+            # with it the fixed scratch array); later calls allocate nothing
+            assert torch.cuda.mem_get_info(dev)[0] == free_before
+        f_ref, n_ref = model.compute_f(states[call], {"g": g, "mu": mu}, with_norm=True)
         f = d_f.cpu().numpy()
         assert np.abs(f - f_ref).max() <= 1e-12 * np.abs(f_ref).max()
         assert abs(d_norm.item() - n_ref) <= 1e-12 * n_ref
+
+
+def test_noalloc_rejects_host_memory():
+    import torch
+
+    import nosh_gb300 as ng
+
+    fn = _bind(ng.lib())
+    t = torch.zeros(16, dtype=torch.float64, device="cuda")
+    h = np.zeros(16)
+    p = t.data_ptr()
+    rc = fn(2, p, p, p, p, p, p, 1.0, h.ctypes.data, p, p, None)
+    assert rc == ng.ERR_INVALID
+    assert "current device" in ng.lib().nosh_last_error().decode()
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
