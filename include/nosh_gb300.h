@@ -246,6 +246,22 @@ int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y,
  * call of its own.  Needs a hierarchy of two levels or more. */
 int nosh_keo_regularized_smoother_apply(nosh_nls nls, const double *x,
                                         double *y);
+/* The k smallest eigenvalues of the FP64 Jacobian J(psi, p) and their unit
+ * eigenvectors: the stability test of a state, the role of Anasazi in the
+ * reference's eigen tool (executables/nosh-eig/nosh-eig.cpp:57-) and of the
+ * continuation's eigen analysis (examples/conf.xml:50-66).  LOBPCG on the
+ * GPU with one AMG V-cycle of the regularised KEO as preconditioner; with
+ * deflate_gauge the U(1) gauge mode i psi is projected out, so the values
+ * are the physical ones.  guard: extra block vectors (< 0: max(2, k));
+ * 3 (k + guard) <= 64.  Convergence: ||J x - lambda x|| <= tol * ||J||_est
+ * for each of the k pairs, within maxit iterations (the estimates reached
+ * are returned either way; compare *iterations with maxit).
+ *   eigenvalues[k] (host, ascending); eigenvectors[k * 2N] (host or device,
+ *   NULL to skip); seed: the random start block (splitmix64). */
+int nosh_eig_lowest(nosh_nls nls, const double *psi, const double *p, int k,
+                    double tol, int maxit, int guard, int deflate_gauge,
+                    uint64_t seed, double *eigenvalues, double *eigenvectors,
+                    int *iterations);
 /* Y = K_reg X (the regularised operator itself, for checking). */
 int nosh_keo_regularized_operator_apply(nosh_nls nls, const double *x,
                                         double *y);
@@ -366,11 +382,25 @@ int nosh_continuation_tangent(nosh_continuation c, double *tau_mu,
  * LEARNED predicts with it once four states are known. */
 int nosh_continuation_learning(nosh_continuation c, int train_steps,
                                int iters_per_step, double learning_rate);
+/* After the training window the network's coefficient for the next learned
+ * step is inferred on a second stream while the current step's Newton solve
+ * runs.  With period p > 1 it is re-inferred on every p-th learned step
+ * only and reused in between (default 1).  No counterpart in the reference
+ * (its LOCA predictors have no network). */
+int nosh_continuation_inference_period(nosh_continuation c, int period);
+/* Diagnostics: ||F||_2 at mu_new of the secant, quadratic, cubic and learned
+ * predictions (residuals[0..3]) formed from the handle's current history,
+ * without advancing it (NaN where a predictor lacks history or the network
+ * is not enabled).  The learned one uses a coefficient inferred from these
+ * very features. */
+int nosh_continuation_predictor_residuals(nosh_continuation c, double mu_new,
+                                          double *residuals);
 /* Predictor telemetry: which predictor the last advance used
  * (NOSH_PREDICT_*), the learned prediction's residual and the secant one's
- * (NaN when not evaluated: the secant is only evaluated when the learned
- * prediction misses the tolerance), the last training loss, and the
- * learned coefficient w of the last learned prediction (NaN if none). */
+ * (NaN when not evaluated: the secant is evaluated whenever the learned
+ * prediction misses the tolerance, and the one with the smaller residual
+ * starts Newton), the last training loss, and the learned coefficient w of
+ * the last learned prediction (NaN if none). */
 int nosh_continuation_last_prediction(nosh_continuation c, int *used,
                                       double *f_learned, double *f_secant,
                                       double *train_loss, double *coef);

@@ -573,197 +573,35 @@ stepper_result step(Run &r, const stepper_parameters &p, nosh_newton_options opt
 // host; the projected problem by cyclic Jacobi rotations.
 namespace eig {
 
-namespace detail {
-inline double dot(const vec &a, const vec &b) {
-  double s = 0.0;
-  for (size_t i = 0; i < a.size(); i++) s += a[i] * b[i];
-  return s;
-}
-// symmetric A (m x m, row major) -> ascending eigenvalues w and
-// eigenvectors as the columns of V (cyclic Jacobi)
-inline void jacobi_eig(std::vector<double> A, int m, std::vector<double> &w, std::vector<double> &V) {
-  V.assign((size_t)m * m, 0.0);
-  for (int i = 0; i < m; i++) V[(size_t)i * m + i] = 1.0;
-  for (int sweep = 0; sweep < 100; sweep++) {
-    double off = 0.0, tot = 0.0;
-    for (int i = 0; i < m; i++)
-      for (int j = 0; j < m; j++) (i == j ? tot : off) += A[(size_t)i * m + j] * A[(size_t)i * m + j];
-    if (off <= 1e-30 * (tot + off)) break;
-    for (int p = 0; p < m; p++)
-      for (int q = p + 1; q < m; q++) {
-        const double apq = A[(size_t)p * m + q];
-        if (apq == 0.0) continue;
-        const double th = (A[(size_t)q * m + q] - A[(size_t)p * m + p]) / (2.0 * apq);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int r = 0; r < m; r++) {  // A <- A G (columns p, q)
-          const double a = A[(size_t)r * m + p], b = A[(size_t)r * m + q];
-          A[(size_t)r * m + p] = c * a - s * b;
-          A[(size_t)r * m + q] = s * a + c * b;
-        }
-        for (int r = 0; r < m; r++) {  // A <- G^T A (rows p, q)
-          const double a = A[(size_t)p * m + r], b = A[(size_t)q * m + r];
-          A[(size_t)p * m + r] = c * a - s * b;
-          A[(size_t)q * m + r] = s * a + c * b;
-        }
-        for (int r = 0; r < m; r++) {
-          const double a = V[(size_t)r * m + p], b = V[(size_t)r * m + q];
-          V[(size_t)r * m + p] = c * a - s * b;
-          V[(size_t)r * m + q] = s * a + c * b;
-        }
-      }
-  }
-  std::vector<int> order(m);
-  for (int i = 0; i < m; i++) order[i] = i;
-  std::sort(order.begin(), order.end(),
-            [&](int a, int b) { return A[(size_t)a * m + a] < A[(size_t)b * m + b]; });
-  w.resize(m);
-  std::vector<double> Vs((size_t)m * m);
-  for (int j = 0; j < m; j++) {
-    w[j] = A[(size_t)order[j] * m + order[j]];
-    for (int r = 0; r < m; r++) Vs[(size_t)r * m + j] = V[(size_t)r * m + order[j]];
-  }
-  V.swap(Vs);
-}
-}  // namespace detail
-
 struct result {
   std::vector<double> values;  // ascending
   std::vector<vec> vectors;    // unit, orthogonal to i psi
   int iterations = 0;
 };
 
+// The k smallest eigenvalues of the FP64 Jacobian J(psi, params) and their
+// eigenvectors, the stability test of a state (the reference's nosh-eig,
+// executables/nosh-eig/nosh-eig.cpp:57-, hands J to Anasazi).  LOBPCG runs
+// inside the library on the GPU (nosh_eig_lowest): the block algebra is the
+// library's own kernels, the preconditioner one AMG V-cycle of the
+// regularised KEO, and the gauge mode i psi is deflated.
 inline result lowest_eigenpairs(model_evaluator::nls &model, const vec &psi,
                                 const std::map<std::string, double> &params, int k, double tol = 1e-8,
                                 int maxit = 500, unsigned seed = 1) {
   const size_t n = psi.size();
   const int guard = std::max(2, k), mb = k + guard;
-  if (k < 1 || (size_t)(3 * mb + 1) >= n) throw error(NOSH_ERR_INVALID, "need 1 <= k and 3 (2k) + 1 < 2N");
-  const int prec0 = model.precision();
-  model.set_precision(NOSH_PREC_FP64);
-  auto J = model.create_W_op();
-  auto T = model.create_W_prec();
-  J->rebuild(params, psi);
-  T->rebuild(params, psi);
-  vec u(n);
-  for (size_t i = 0; i < n / 2; i++) {
-    u[2 * i] = -psi[2 * i + 1];
-    u[2 * i + 1] = psi[2 * i];
-  }
-  const double nu = std::sqrt(detail::dot(u, u));
-  for (double &v : u) v /= nu;
-  auto proj = [&](vec &v) {
-    const double c = detail::dot(u, v);
-    for (size_t i = 0; i < n; i++) v[i] -= c * u[i];
-  };
-  // orthonormalise rows in place (two Gram-Schmidt passes), dropping
-  // directions that are numerically dependent
-  auto orth = [&](std::vector<vec> &S) {
-    std::vector<vec> out;
-    for (vec &v : S) {
-      proj(v);
-      const double n0 = std::sqrt(detail::dot(v, v));
-      for (int pass = 0; pass < 2; pass++)
-        for (const vec &q : out) {
-          const double c = detail::dot(q, v);
-          for (size_t i = 0; i < n; i++) v[i] -= c * q[i];
-        }
-      const double n1 = std::sqrt(detail::dot(v, v));
-      if (!(n1 > 1e-10 * n0) || n1 == 0.0) continue;
-      for (double &x : v) x /= n1;
-      out.push_back(std::move(v));
-    }
-    S.swap(out);
-  };
-  auto unit = [&](std::vector<vec> &S) {
-    for (vec &v : S) {
-      const double nv = std::sqrt(detail::dot(v, v));
-      if (nv > 0) for (double &x : v) x /= nv;
-    }
-  };
-  // Ritz pairs of span(S): returns the combination coefficients (columns)
-  auto ritz = [&](const std::vector<vec> &S, const std::vector<vec> &AS, std::vector<double> &w,
-                  std::vector<double> &C) {
-    const int m = (int)S.size();
-    std::vector<double> Hm((size_t)m * m);
-    for (int a = 0; a < m; a++)
-      for (int b = 0; b < m; b++) Hm[(size_t)a * m + b] = detail::dot(S[a], AS[b]);
-    for (int a = 0; a < m; a++)
-      for (int b = a + 1; b < m; b++) {
-        const double s = 0.5 * (Hm[(size_t)a * m + b] + Hm[(size_t)b * m + a]);
-        Hm[(size_t)a * m + b] = Hm[(size_t)b * m + a] = s;
-      }
-    detail::jacobi_eig(Hm, m, w, C);
-  };
-  auto combine = [&](const std::vector<vec> &S, const std::vector<double> &C, int m, int cols) {
-    std::vector<vec> out(cols, vec(n, 0.0));
-    for (int j = 0; j < cols; j++)
-      for (int a = 0; a < m; a++) {
-        const double c = C[(size_t)a * m + j];
-        for (size_t i = 0; i < n; i++) out[j][i] += c * S[a][i];
-      }
-    return out;
-  };
-  // random start (splitmix64), projected and orthonormalised
-  std::vector<vec> X(mb, vec(n));
-  uint64_t st = seed;
-  for (vec &v : X)
-    for (double &x : v) {
-      uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
-      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-      x = (double)((z ^ (z >> 31)) >> 11) * 0x1.0p-53 - 0.5;
-    }
-  orth(X);
-  std::vector<vec> AX, P;
-  J->apply(X, AX);
-  std::vector<double> lam, C;
-  ritz(X, AX, lam, C);
-  X = combine(X, C, (int)X.size(), (int)X.size());
-  AX = combine(AX, C, (int)AX.size(), (int)AX.size());
-  double jnorm = 0.0;
-  for (const vec &v : AX) jnorm = std::max(jnorm, std::sqrt(detail::dot(v, v)));
+  if (k < 1 || 3 * mb > 64 || (size_t)(3 * mb + 1) >= n)
+    throw error(NOSH_ERR_INVALID, "need 1 <= k, 3 (k + guard) <= 64 and 3 (k + guard) + 1 < 2N");
+  const vec p = params_vector(params, model.nominal_parameters());
   result out;
-  for (out.iterations = 1; out.iterations <= maxit; out.iterations++) {
-    const int nx = (int)X.size();
-    std::vector<vec> R(nx, vec(n));
-    bool done = true;
-    for (int j = 0; j < nx; j++) {
-      jnorm = std::max(jnorm, std::fabs(lam[j]));
-      for (size_t i = 0; i < n; i++) R[j][i] = AX[j][i] - lam[j] * X[j][i];
-    }
-    for (int j = 0; j < std::min(k, nx); j++)
-      if (!(std::sqrt(detail::dot(R[j], R[j])) <= tol * jnorm)) done = false;
-    if (done) break;
-    std::vector<vec> W;
-    T->apply(R, W);
-    for (vec &v : W) proj(v);
-    unit(W);
-    unit(P);
-    std::vector<vec> S = X;
-    for (vec &v : W) S.push_back(v);
-    for (vec &v : P) S.push_back(v);
-    orth(S);
-    std::vector<vec> AS;
-    J->apply(S, AS);
-    std::vector<double> th, Cs;
-    ritz(S, AS, th, Cs);
-    const int m = (int)S.size(), keep = std::min(mb, m);
-    std::vector<vec> Xn = combine(S, Cs, m, keep), AXn = combine(AS, Cs, m, keep);
-    // the new search directions: the part of the update outside span(X)
-    P = Xn;
-    for (vec &p : P)
-      for (const vec &x : X) {
-        const double c = detail::dot(x, p);
-        for (size_t i = 0; i < n; i++) p[i] -= c * x[i];
-      }
-    X.swap(Xn);
-    AX.swap(AXn);
-    lam.assign(th.begin(), th.begin() + keep);
-  }
-  model.set_precision(prec0);
-  out.values.assign(lam.begin(), lam.begin() + std::min<size_t>(k, lam.size()));
-  out.vectors.assign(X.begin(), X.begin() + std::min<size_t>(k, X.size()));
+  out.values.resize(k);
+  std::vector<double> flat((size_t)k * n);
+  int its = 0;
+  check(nosh_eig_lowest(model.handle(), psi.data(), p.data(), k, tol, maxit, guard, 1, seed, out.values.data(),
+                        flat.data(), &its));
+  out.iterations = its;
+  out.vectors.resize(k);
+  for (int j = 0; j < k; j++) out.vectors[j].assign(flat.begin() + (size_t)j * n, flat.begin() + (size_t)(j + 1) * n);
   return out;
 }
 

@@ -143,6 +143,7 @@ _SIGS = {
     "nosh_keo_regularized_apply": (_I, [_P, _P, _P, _I, _I, _D, _D]),
     "nosh_keo_regularized_operator_apply": (_I, [_P, _P, _P]),
     "nosh_keo_regularized_smoother_apply": (_I, [_P, _P, _P]),
+    "nosh_eig_lowest": (_I, [_P, _P, _P, _I, _D, _I, _I, _I, C.c_uint64, _P, _P, C.POINTER(_I)]),
     "nosh_newton_default_options": (None, [C.POINTER(NewtonOptions)]),
     "nosh_newton_solve": (_I, [_P, _P, _P, C.POINTER(NewtonOptions), C.POINTER(NewtonStats)]),
     "nosh_continuation_step": (_I, [_P, _P, _P, _P, _D, _D, _I, C.POINTER(NewtonOptions),
@@ -156,6 +157,8 @@ _SIGS = {
                                                  C.POINTER(NewtonStats)]),
     "nosh_continuation_tangent": (_I, [_P, C.POINTER(_D), C.POINTER(_D)]),
     "nosh_continuation_learning": (_I, [_P, _I, _I, _D]),
+    "nosh_continuation_inference_period": (_I, [_P, _I]),
+    "nosh_continuation_predictor_residuals": (_I, [_P, _D, _P]),
     "nosh_continuation_last_prediction": (_I, [_P, C.POINTER(_I), C.POINTER(_D), C.POINTER(_D), C.POINTER(_D),
                                                C.POINTER(_D)]),
     "nosh_mpnn_create": (_I, [_P, C.POINTER(_P)]),
@@ -596,6 +599,18 @@ class continuation:
 
     def learning(self, train_steps, iters_per_step=20, learning_rate=1e-3):
         _check(_lib.nosh_continuation_learning(self._h, train_steps, iters_per_step, learning_rate))
+
+    def inference_period(self, period):
+        """Re-infer the learned coefficient every ``period``-th learned step
+        after training (reused in between)."""
+        _check(_lib.nosh_continuation_inference_period(self._h, int(period)))
+
+    def predictor_residuals(self, mu_new):
+        """||F|| at mu_new of the secant, quadratic, cubic and learned
+        predictions from the current history, without advancing."""
+        out = np.empty(4)
+        _check(_lib.nosh_continuation_predictor_residuals(self._h, mu_new, _ptr(out)))
+        return dict(zip(("secant", "quadratic", "cubic", "learned"), out.tolist()))
 
     def last_prediction(self):
         u, fl, fs, tl, w = C.c_int(), C.c_double(), C.c_double(), C.c_double(), C.c_double()

@@ -26,12 +26,15 @@ def union(meshes):
     return np.concatenate(xs), np.concatenate(cs).astype(np.int32), np.asarray(off, np.int64)
 
 
-def squares(sides, mus, seed0=1000):
+def squares(sides, mus, seed0=1000, seeds=None):
     """The batch of jittered unit squares with ``sides[k]`` vertices per side
-    (seed ``seed0 + k``): (x, cells, offsets, psi0, A, mu)."""
+    (seed ``seeds[k]``, default ``seed0 + k``): (x, cells, offsets, psi0, A,
+    mu)."""
     meshes, psis = [], []
+    if seeds is None:
+        seeds = [seed0 + k for k in range(len(sides))]
     for k, s in enumerate(sides):
-        x, c, p = meshgen.square(int(s), seed0 + k)
+        x, c, p = meshgen.square(int(s), int(seeds[k]))
         meshes.append((x, c))
         psis.append(p)
     x, c, off = union(meshes)
@@ -64,3 +67,64 @@ def partition(weights, world):
 def split_state(x, offsets):
     """Per-system slices of a union state (2N interleaved)."""
     return [x[2 * offsets[k] : 2 * offsets[k + 1]] for k in range(len(offsets) - 1)]
+
+
+def solve_union(sides, mus, seeds, tol=1e-10, precision=None, repeats=1, timer=None):
+    """Solve the squares ``sides`` (seeds ``seeds``, parameters ``mus``) as one
+    batched handle on the GPU, from their initial states, to ``||F_s|| <=
+    tol`` in every system.  The solve runs ``repeats`` times from the same
+    initial states (the set-up is not repeated); ``timer``, when given, is
+    called as ``timer(phase)`` with phase "start" / "stop" around each.
+    Returns (per-system norms, the last solve's stats, the states)."""
+    import nosh_gb300 as ng
+
+    x, c, off, psi0, A, mu = squares(sides, mus, seeds=seeds)
+    model = ng.nls(ng.mesh(x, c), A, -1.0, 1.0, 1.0, mu=0.0,
+                   precision=ng.PREC_MIXED if precision is None else precision)
+    model.set_systems(off, mu)
+    st, psi = None, None
+    for _ in range(repeats):
+        psi = psi0.copy()
+        if timer:
+            timer("start")
+        st = model.newton(psi, {"mu": 0.0}, tol=tol)
+        if timer:
+            timer("stop")
+        if st["status"] != 0:
+            raise RuntimeError(f"batched solve failed: {st}")
+    return model.system_norms(), st, split_state(psi, off)
+
+
+def sharded_solve(sides, mus, rank, world, seed0=1000, solve=None, gather=None):
+    """The batched-solve workload sharded over ranks: rank ``rank`` of
+    ``world`` takes ``partition(sides^2, world)[rank]`` (longest processing
+    time by vertex count), solves those systems with ``solve(sides, mus,
+    seeds)`` -- by default :func:`solve_union` on this rank's GPU -- and the
+    per-system norms of every rank are gathered (``gather(obj) -> list`` of
+    every rank's obj, by default ``torch.distributed.all_gather_object``).
+    No collective touches the data path: the only exchange is that gather.
+    Returns {system index: norm} over all systems on every rank."""
+    sides = np.asarray(sides)
+    parts = partition(sides.astype(np.float64) ** 2, world)
+    mine = parts[rank]
+    if solve is None:
+        def solve(s, m, sd):
+            return solve_union(s, m, sd)[0]
+    norms = solve([int(sides[k]) for k in mine], [float(mus[k]) for k in mine], [seed0 + k for k in mine]) \
+        if mine else []
+    local = {int(k): float(v) for k, v in zip(mine, norms)}
+    if world == 1:
+        return local
+    if gather is None:
+        import torch.distributed as dist
+
+        def gather(obj):
+            out = [None] * world
+            dist.all_gather_object(out, obj)
+            return out
+    merged = {}
+    for g in gather(local):
+        if set(g) & set(merged):
+            raise RuntimeError("a system was solved by two ranks")
+        merged.update(g)
+    return merged

@@ -19,7 +19,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnosh_gb300.so")
-SOURCES = ["mesh.cu", "ops.cu", "amg.cu", "solver.cu", "continuation.cu", "mpnn.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["mesh.cu", "ops.cu", "amg.cu", "solver.cu", "continuation.cu", "mpnn.cu", "capi.cu", "eig.cu",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -563,6 +563,21 @@ int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y, int nve
   });
 }
 
+int nosh_eig_lowest(nosh_nls nls, const double *psi, const double *p, int k, double tol, int maxit, int guard,
+                    int deflate_gauge, uint64_t seed, double *eigenvalues, double *eigenvectors, int *iterations) {
+  return guarded([&] {
+    auto &s = N(nls);
+    double g, mu;
+    read_params(p, g, mu);
+    require(eigenvalues != nullptr, "null eigenvalue output");
+    require(k >= 1 && tol > 0 && maxit >= 1, "bad eigensolver options");
+    const double *dpsi = stage_in(s, psi, s.d_tmp, 2 * s.N);
+    const int its = nosh::lowest_eigenpairs(s, dpsi, g, mu, k, tol, maxit, guard, deflate_gauge != 0, seed,
+                                            eigenvalues, eigenvectors);
+    if (iterations) *iterations = its;
+  });
+}
+
 int nosh_keo_regularized_smoother_apply(nosh_nls nls, const double *x, double *y) {
   return guarded([&] {
     auto &s = N(nls);
@@ -731,6 +746,23 @@ int nosh_continuation_learning(nosh_continuation c, int train_steps, int iters_p
     require(c && c->impl, "null continuation handle");
     require(train_steps >= 0 && iters_per_step >= 0 && learning_rate >= 0, "bad learning settings");
     c->impl->enable_learning(train_steps, iters_per_step, learning_rate);
+  });
+}
+
+int nosh_continuation_inference_period(nosh_continuation c, int period) {
+  return guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    require(period >= 1, "the inference period must be >= 1");
+    c->impl->infer_period = period;
+    c->impl->infer_count = 0;
+  });
+}
+
+int nosh_continuation_predictor_residuals(nosh_continuation c, double mu_new, double *residuals) {
+  return guarded([&] {
+    require(c && c->impl, "null continuation handle");
+    require(residuals != nullptr, "null output");
+    c->impl->predictor_residuals(mu_new, residuals);
   });
 }
 

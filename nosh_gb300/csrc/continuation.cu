@@ -380,32 +380,35 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
         NOSH_CUDA(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
         NOSH_CUDA(cudaMallocHost(&w_host, sizeof(double)));
       }
-      // the coefficient inferred during the previous step (or now, on the
+      // the coefficient inferred during an earlier step (or now, on the
       // first overlapped step)
-      const bool have_w = w_pending;
+      const bool have_w = w_pending || w_valid;
       drain_side();
       net->prepare(x, m, mu_new, ns.psi.p);
       if (!have_w) net->infer(s.stream);
+      w_valid = true;
       net->combine(ns.psi.p, ns.tmp.p, w_host);
-      // the next step's coefficient from these features, under this Newton
-      NOSH_CUDA(cudaEventRecord(ev_main, s.stream));
-      NOSH_CUDA(cudaStreamWaitEvent(side, ev_main, 0));
-      net->infer(side);
-      NOSH_CUDA(cudaEventRecord(ev_side, side));
-      w_pending = true;
+      // the next coefficient from these features, under this Newton
+      if (++infer_count >= infer_period) {
+        infer_count = 0;
+        NOSH_CUDA(cudaEventRecord(ev_main, s.stream));
+        NOSH_CUDA(cudaStreamWaitEvent(side, ev_main, 0));
+        net->infer(side);
+        NOSH_CUDA(cudaEventRecord(ev_side, side));
+        w_pending = true;
+      }
       f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);  // syncs: w_host is valid
       coef = *w_host;
-      // the secant is evaluated only when the learned prediction looks
-      // broken: far worse than the last prediction taken
-      compare = !(f_learned <= opt.tol) && !(f_learned <= 4.0 * f0_prev);
+      compare = !(f_learned <= opt.tol);
     } else {
       coef = net->predict(x, m, mu_new, ns.psi.p, ns.tmp.p);
+      w_valid = false;  // the weights may change before the next step
       f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
       compare = !(f_learned <= opt.tol);
     }
     // a prediction that meets the tolerance is taken as is, otherwise the
-    // one with the smaller residual starts Newton (the secant is the
-    // fallback)
+    // one with the smaller residual starts Newton: the plain secant is the
+    // fallback whenever the network's starting residual is worse
     if (compare) f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.xc.p);
     if (!compare || f_learned < f_secant) {
       std::swap(ns.psi, ns.tmp);
@@ -415,7 +418,6 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
       std::swap(ns.f, ns.xc);
       f0 = f_secant;
     }
-    f0_prev = f0;
   }
   newton_core(s, ns, g, mu_new, opt, st, f0);
   if (st.status != NOSH_OK) return;
@@ -437,8 +439,29 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
   s.sync();
 }
 
+void ContinuationImpl::predictor_residuals(double mu_new, double out[4]) {
+  NOSH_CHECK(mu_new != mu_of(0), NOSH_ERR_INVALID, "mu_new equals the current mu");
+  drain_side();
+  NewtonState &ns = state_of(s);
+  const double g = s.g0;
+  for (int q = 0; q < 4; q++) out[q] = std::nan("");
+  for (int order = 1; order <= 3; order++)
+    if (count > order) {
+      extrapolate(order, mu_new, ns.tmp.p);
+      out[order - 1] = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
+    }
+  if (net && count >= 4) {
+    const double *x[4] = {slot(0), slot(1), slot(2), slot(3)};
+    const double m[4] = {mu_of(0), mu_of(1), mu_of(2), mu_of(3)};
+    net->predict(x, m, mu_new, ns.xc.p, ns.tmp.p);
+    w_valid = false;  // the device coefficient now belongs to these features
+    out[3] = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
+  }
+}
+
 void ContinuationImpl::enable_learning(int train_steps, int iters, double lr) {
   drain_side();
+  w_valid = false;
   if (!net) net.reset(new Mpnn(s));
   train_left = train_steps;
   this->train_steps = train_steps;

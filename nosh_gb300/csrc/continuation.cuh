@@ -33,7 +33,11 @@ struct ContinuationImpl {
   cudaEvent_t ev_main = nullptr, ev_side = nullptr;
   bool w_pending = false;
   double *w_host = nullptr;
-  double f0_prev = std::nan("");  // residual of the last prediction taken
+  // the network's coefficient is re-inferred on every infer_period-th
+  // overlapped step and reused in between; w_valid: the device coefficient
+  // belongs to the current weights
+  int infer_period = 1, infer_count = 0;
+  bool w_valid = false;
   void drain_side();              // handle stream waits for the side stream
 
   // pseudo-arclength: the last normalised tangent (tau, tau_mu) and the
@@ -57,6 +61,11 @@ struct ContinuationImpl {
   // returns the Krylov iterations
   int tangent_direction(const nosh_newton_options &opt, int precision, double rtol, double *out);
   void enable_learning(int train_steps, int iters, double lr);
+  // diagnostics: ||F|| at mu_new of the secant, quadratic, cubic and learned
+  // predictions from the current history (NaN where unavailable), without
+  // advancing; the learned one uses a coefficient inferred from these
+  // features
+  void predictor_residuals(double mu_new, double out[4]);
 };
 
 }  // namespace nosh

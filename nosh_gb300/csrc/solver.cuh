@@ -78,6 +78,13 @@ double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn
 int linear_solve(NlsImpl &s, NewtonState &ns, const double *rhs, double *x, double g, double mu, double rtol,
                  int maxit, int precision, bool rebuild, int &status);
 
+// The k smallest eigenvalues of the FP64 Jacobian at psi (device, 2N) by
+// LOBPCG with the AMG preconditioner, the gauge mode deflated (eig.cu);
+// values[k] on the host, vectors (k x 2N, host or device) when non-null.
+// guard < 0: max(2, k) extra block vectors.  Returns the iterations.
+int lowest_eigenpairs(NlsImpl &s, const double *psi_dev, double g, double mu, int k, double tol, int maxit,
+                      int guard, bool deflate_gauge, uint64_t seed, double *values, double *vectors);
+
 void newton_solve(NlsImpl &s, double *x_user, double g, double mu,
                   const nosh_newton_options &opt, nosh_newton_stats &st);
 void continuation_step(NlsImpl &s, double *x, double *x_prev, double g, double mu_new,

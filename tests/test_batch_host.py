@@ -43,6 +43,23 @@ def test_partition_balances_and_covers():
         assert max(loads) <= min(loads) + w.max()
 
 
+def _cpu_solve(sides, mus, seeds):
+    """Rank-local solve injected in place of the GPU one: the oracle's FP64
+    CPU Newton-MINRES on each square, returning each system's ||F||."""
+    from nosh_gb300 import meshgen
+    from oracle import oracle as O
+
+    norms = []
+    for s, mu, seed in zip(sides, mus, seeds):
+        x, c, psi = meshgen.square(int(s), int(seed))
+        m = O.finish_mesh(x, c)
+        P = O.Problem(m, O.mvp_constant_curl(m.x))
+        st = O.CpuSolver(P).newton(psi, mu, tol=1e-10)
+        assert st["status"] == 0, st
+        norms.append(float(np.linalg.norm(P.compute_f(psi, 1.0, mu))))
+    return norms
+
+
 def _rank_main(rank, world, port, out):
     import torch.distributed as dist
 
@@ -50,18 +67,9 @@ def _rank_main(rank, world, port, out):
 
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    sides, mus = batch.config_squares(32)
-    parts = batch.partition(sides.astype(float) ** 2, world)
-    mine = parts[rank]
-    # stand-in for the rank's solve: a per-system result computed locally
-    res = {int(k): float(sides[k]) * 2.0 + mus[k] for k in mine}
-    gathered = [None] * world
-    dist.all_gather_object(gathered, res)
+    sides, mus = batch.config_squares(12, lo=5, hi=17)
+    merged = batch.sharded_solve(sides, mus, rank, world, solve=_cpu_solve)
     if rank == 0:
-        merged = {}
-        for g in gathered:
-            assert not (set(g) & set(merged))  # disjoint shards
-            merged.update(g)
         out.put(sorted(merged.items()))
     dist.destroy_process_group()
 
@@ -81,10 +89,28 @@ def test_two_rank_sharding_gathers_every_system():
     procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
-    merged = q.get(timeout=120)
+    merged = q.get(timeout=300)
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    sides, mus = batch.config_squares(32)
-    assert [k for k, _ in merged] == list(range(32))
-    assert all(abs(v - (sides[k] * 2.0 + mus[k])) < 1e-12 for k, v in merged)
+    assert [k for k, _ in merged] == list(range(12))
+    assert all(v <= 1e-10 for _, v in merged)
+    # the same function on one rank solves the same systems to the same norms
+    sides, mus = batch.config_squares(12, lo=5, hi=17)
+    single = batch.sharded_solve(sides, mus, 0, 1, solve=_cpu_solve)
+    assert sorted(single) == list(range(12))
+    for k, v in merged:
+        assert abs(v - single[k]) <= 1e-14
+
+
+def test_sharded_solve_rejects_overlapping_shards():
+    from nosh_gb300 import batch
+
+    sides, mus = batch.config_squares(4, lo=5, hi=9)
+
+    def fake_solve(s, m, sd):
+        return [0.0] * len(s)
+
+    # a gather that returns this rank's shard twice: every system twice
+    with pytest.raises(RuntimeError):
+        batch.sharded_solve(sides, mus, 0, 2, solve=fake_solve, gather=lambda obj: [obj, obj])

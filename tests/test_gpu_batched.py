@@ -45,3 +45,22 @@ def test_batched_rejects_cross_system_edges():
     model = ng.nls(gm, A, -1.0, 1.0, 1.0)
     with pytest.raises(ng.NoshError):
         model.set_systems([0, 20, off[-1]], mu)  # splits the first square
+
+
+def test_thirty_two_uneven_systems_pass_the_oracle_residual():
+    """32 squares with sides drawn from {9..65} and mu from [0, 1] (the
+    batched workload's sampling at smaller sides), solved as one batch
+    through batch.solve_union: every system's FP64 residual, evaluated by the
+    oracle on that system alone, is at most 1.5e-10."""
+    from nosh_gb300 import batch
+
+    sides, mus = batch.config_squares(32, lo=9, hi=65, seed=77)
+    seeds = [500 + k for k in range(32)]
+    norms, st, states = batch.solve_union(sides, mus, seeds)
+    assert len(set(int(s) for s in sides)) >= 16  # uneven sizes
+    assert np.all(norms <= 1e-10)
+    for k in range(32):
+        xs, cs, _ = O.gen_square(int(sides[k]), seeds[k])
+        mk = O.finish_mesh(xs, cs)
+        P = O.Problem(mk, O.mvp_constant_curl(mk.x))
+        assert np.linalg.norm(P.compute_f(states[k], 1.0, mus[k])) <= 1.5e-10

@@ -9,10 +9,10 @@ residual tolerance:
 
 * a NaN in the host state          -> NOSH_ERR_NAN
 * one Newton step / one MINRES step -> NOSH_ERR_NOT_CONVERGED
-* an indefinite regularised KEO    -> NOSH_ERR_BREAKDOWN
-  (g = -1e4 makes the diagonal blocks of K + g cv t [[2|psi|^2 + gamma, beta],
-  [beta, 2|psi|^2 - gamma]] negative definite; the preconditioner's refresh
-  finds the non-positive-definite blocks)
+* a singular regularised KEO       -> NOSH_ERR_BREAKDOWN
+  (zero thickness on a patch zeroes the patch's rows of K_reg; the
+  preconditioner's refresh finds the diagonal blocks that are not positive
+  definite)
 * a staged-SpMV wait that runs out -> NOSH_ERR_CUDA (the wait bound is set to
   0 polls, so every staged wait gives up at once and its launch leaves after
   its copies land)
@@ -72,18 +72,29 @@ def test_iteration_caps_give_not_converged(prec):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-def test_indefinite_preconditioner_gives_breakdown(prec):
+def test_singular_preconditioner_gives_breakdown(prec):
     import nosh_gb300 as ng
+    from oracle import oracle as O
 
-    model, P, psi0 = _case(prec)
-    # the hierarchy's aggregation is set up by the first solve, from a good
-    # operator; the failing solve then refreshes its numeric values only
-    _solves_afterwards(model, P, psi0)
-    psi = psi0.copy()
+    # zero thickness on the corner patch x, y < 0.3: the edge coefficients
+    # alpha = covolume / length * mean thickness vanish inside it, and so
+    # does the regularisation cv t g (...), so the patch's interior rows of
+    # K_reg are zero.  The reference's MueLu would divide by those zero
+    # diagonals and Belos would fail its Converged assertion
+    # (src/keo_regularized.cpp:161).
+    x, c, psi0 = O.gen_square(17, 3)
+    m = O.finish_mesh(x, c)
+    A = O.mvp_constant_curl(m.x)
+    t = np.where((m.x[:, 0] < 0.3) & (m.x[:, 1] < 0.3), 0.0, 1.0)
+    P = O.Problem(m, A, thickness=t)
+    model = ng.nls(ng.mesh(m.x, m.cells), A, -1.0, 1.0, t, mu=0.5, precision=prec)
     with pytest.raises(ng.NoshError) as e:
-        model.newton(psi, {"g": -1.0e4, "mu": 0.5})
-    assert e.value.code == ng.ERR_BREAKDOWN
-    _solves_afterwards(model, P, psi0)
+        model.newton(psi0.copy(), {"g": 1.0, "mu": 0.5})
+    assert e.value.code == ng.ERR_BREAKDOWN and "positive definite" in str(e.value)
+    # the handle still evaluates the model
+    f = model.compute_f(psi0, {"g": 1.0, "mu": 0.5})
+    fr = P.compute_f(psi0, 1.0, 0.5)
+    assert np.abs(f - fr).max() <= 1e-12 * np.abs(fr).max()
 
 
 @pytest.mark.parametrize("prec", [0, 1])
