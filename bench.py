@@ -74,8 +74,9 @@ def parse():
     ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
     ap.add_argument("--train-iters", type=int, default=10, help="optimiser iterations per training step")
     ap.add_argument("--lr", type=float, default=2e-3, help="learning rate of the online training")
-    ap.add_argument("--infer-period", type=int, default=1,
-                    help="after training, re-infer the learned coefficient every this many steps")
+    ap.add_argument("--infer-period", type=int, default=8,
+                    help="after training, re-infer the learned coefficient every this many steps (a sweep at "
+                         "64^3: 1, 2, 4, 8 gave 509, 559, 588, 603 steps/s at the same 6.4 MINRES iterations)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end line through the C ABI")
@@ -479,6 +480,41 @@ def run_gb300(args):
         else:
             secondary = d
 
+    # calibration: the library's streaming-read probe over the dominant
+    # launch's algorithmic bytes, timed the same way (CUDA events around one
+    # launch): the bandwidth a single launch of this size reaches at all,
+    # from a flushed L2 and from a warm one
+    if roof is not None:
+        nb = int(roof["algorithmic_bytes_per_launch"]) // 16 * 16
+        buf = torch.ones(nb // 4, dtype=torch.float32, device=dev)
+        word = torch.zeros(1, dtype=torch.int32, device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cur = torch.cuda.current_stream().cuda_stream
+
+        def timed(cold):
+            ts = []
+            for _ in range(10):
+                if cold:
+                    flush_l2()
+                else:
+                    ng.stream_read(buf, nb, word, cur)
+                e0.record()
+                ng.stream_read(buf, nb, word, cur)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return 1000.0 * float(np.median(ts))
+
+        cold_us, warm_us = timed(True), timed(False)
+        roof["control_read"] = {"bytes": nb, "cold_us": cold_us, "warm_us": warm_us,
+                                "cold_gbs": nb / cold_us / 1e3, "warm_gbs": nb / warm_us / 1e3,
+                                "frac_of_peak_cold": nb / cold_us / 1e3 / peak,
+                                "kernel_over_cold_read": roof["achieved"] / (nb / cold_us / 1e3),
+                                "note": "nosh_diag_stream_read (16-byte streaming loads, 8 CTAs/SM) over the same "
+                                        "bytes, CUDA events around one launch: cold = after a 256 MB L2 flush, "
+                                        "warm = L2-resident"}
+        del buf
+
     # the same two kernels on the 160^3 stress configuration, where a launch
     # moves ~0.9 GB (the 64^3 launches above are latency-bound)
     large = None
@@ -635,6 +671,7 @@ def run_batched(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
+    nw_sys, kr_sys = model.system_iterations()
     ms_all, e2e_all = maxrank(ms), maxrank(e2e_ms)
     gathered = batch.sharded_solve(sides, mus, rank, world, solve=lambda s_, m_, sd_: norms) if world > 1 else {
         int(k): float(v) for k, v in zip(mine, norms)}
@@ -648,6 +685,8 @@ def run_batched(args):
                                             "parallelism": f"systems sharded over {world} rank(s), LPT by vertices"},
         "vertices": int(sum(int(sides[k]) ** 2 for k in range(256))),
         "rank0_systems": len(mine), "newton_krylov": [stats[-1]["newton_iters"], stats[-1]["krylov_iters"]],
+        "per_system_newton_min_median_max": [int(nw_sys.min()), float(np.median(nw_sys)), int(nw_sys.max())],
+        "per_system_krylov_min_median_max": [int(kr_sys.min()), float(np.median(kr_sys)), int(kr_sys.max())],
         "max_system_norm": float(max(gathered.values())),
         "e2e": {"value": 256 * 1000.0 / e2e_all, "unit": "systems/s", "ms_per_step": e2e_all,
                 "h2d_bytes_per_step": int(psi0.size * 8 * world), "d2h_bytes_per_step": int(psi0.size * 8 * world),

@@ -148,6 +148,11 @@ int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size,
  * each system is its own. */
 int nosh_nls_set_systems(nosh_nls nls, int64_t num_systems,
                          const int64_t *vertex_offsets, const double *mu);
+/* Per-system Newton steps and MINRES iterations of the last Newton solve
+ * (num_systems entries each; either pointer may be NULL).  Every system
+ * runs its own MINRES recurrence; the batch's Krylov test is the union's
+ * residual.  No counterpart in the reference (one nls per system there). */
+int nosh_nls_system_iterations(nosh_nls nls, int *newton_iters, int *krylov_iters);
 /* Per-system ||F_s||_2 of the last residual a Newton solve evaluated. */
 int nosh_nls_system_norms(nosh_nls nls, double *norms);
 /* The preconditioner hierarchy (after the first rebuild): number of
@@ -173,6 +178,13 @@ int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule);
  * NOSH_ERR_CUDA at its next synchronisation, and the handle stays usable.
  * polls = 0 makes every staged wait give up at once (tests of that path). */
 int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls);
+/* Diagnostics (no counterpart in the reference): the achievable-bandwidth
+ * probe.  Enqueues on `stream` one launch that streams `bytes` (a multiple
+ * of 16) of the 16-byte aligned device buffer `buf` with 16-byte loads and
+ * XOR-folds them into the 32-bit device word *out_word.  Timing it beside a
+ * kernel that moves the same bytes shows what a single launch of that size
+ * reaches at all on this GPU. */
+int nosh_diag_stream_read(const void *buf, int64_t bytes, void *out_word, void *stream);
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int nosh_nls_stream(nosh_nls nls, void **stream);
 

@@ -122,9 +122,11 @@ _SIGS = {
     "nosh_nls_set_amg_options": (_I, [_P, _I, _I, _I, _I, _D, _D]),
     "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
     "nosh_nls_set_stage_wait_limit": (_I, [_P, _I64]),
+    "nosh_diag_stream_read": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_amg_levels": (_I, [_P, C.POINTER(_I), _P, _I, C.POINTER(_I)]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_system_norms": (_I, [_P, _P]),
+    "nosh_nls_system_iterations": (_I, [_P, _P, _P]),
     "nosh_nls_stream": (_I, [_P, C.POINTER(_P)]),
     "nosh_nls_compute_f": (_I, [_P, _P, _P, _P]),
     "nosh_nls_compute_f_norm": (_I, [_P, _P, _P, _P, C.POINTER(_D)]),
@@ -202,6 +204,13 @@ def _f64(a):
     if hasattr(a, "data_ptr"):
         return a
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def stream_read(buf, nbytes, out_word, stream=None):
+    """Diagnostics: one launch streaming ``nbytes`` of the device buffer
+    ``buf`` (XOR-folded into the 32-bit device word ``out_word``), enqueued
+    on ``stream`` (a cudaStream_t handle, default stream when None)."""
+    _check(_lib.nosh_diag_stream_read(_ptr(buf), int(nbytes), _ptr(out_word), C.c_void_p(stream or 0)))
 
 
 def device_count() -> int:
@@ -419,6 +428,14 @@ class nls:
         out = np.empty(self.num_systems)
         _check(_lib.nosh_nls_system_norms(self._h, _ptr(out)))
         return out
+
+    def system_iterations(self):
+        """(Newton steps, MINRES iterations) per system of the last Newton
+        solve (each system has its own MINRES recurrence)."""
+        nw = np.zeros(self.num_systems, np.int32)
+        kr = np.zeros(self.num_systems, np.int32)
+        _check(_lib.nosh_nls_system_iterations(self._h, _ptr(nw), _ptr(kr)))
+        return nw, kr
 
     def amg_levels(self):
         """(level sizes, first tail level) of the preconditioner hierarchy

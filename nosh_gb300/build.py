@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnosh_gb300.so")
 SOURCES = ["mesh.cu", "ops.cu", "amg.cu", "solver.cu", "continuation.cu", "mpnn.cu", "capi.cu", "eig.cu",
-           "noalloc.cu"]
+           "minres_sys.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -331,6 +331,19 @@ int nosh_nls_set_systems(nosh_nls nls, int64_t num_systems, const int64_t *verte
   });
 }
 
+int nosh_nls_system_iterations(nosh_nls nls, int *newton_iters, int *krylov_iters) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(!s.sys_off.empty(), "no systems set");
+    nosh::NewtonState &ns = nosh::state_of(s);
+    const int64_t S = s.nsys();
+    for (int64_t q = 0; q < S; q++) {
+      if (newton_iters) newton_iters[q] = q < (int64_t)ns.sys_newton.size() ? ns.sys_newton[q] : 0;
+      if (krylov_iters) krylov_iters[q] = q < (int64_t)ns.sys_krylov.size() ? ns.sys_krylov[q] : 0;
+    }
+  });
+}
+
 int nosh_nls_system_norms(nosh_nls nls, double *norms) {
   return guarded([&] {
     auto &s = N(nls);
@@ -362,6 +375,17 @@ int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule) {
     s.spmv_schedule = schedule;
     s.tune_schedules();
     nosh::reset_preconditioner(s);
+  });
+}
+
+int nosh_diag_stream_read(const void *buf, int64_t bytes, void *out_word, void *stream) {
+  return guarded([&] {
+    require(buf != nullptr && out_word != nullptr, "null argument");
+    require(bytes >= 16 && bytes % 16 == 0, "bytes must be a positive multiple of 16");
+    require(reinterpret_cast<uintptr_t>(buf) % 16 == 0 && reinterpret_cast<uintptr_t>(out_word) % 4 == 0,
+            "misaligned buffer");
+    require(nosh::is_device_pointer(buf) && nosh::is_device_pointer(out_word), "device memory expected");
+    nosh::stream_read(buf, bytes, static_cast<unsigned *>(out_word), static_cast<cudaStream_t>(stream));
   });
 }
 

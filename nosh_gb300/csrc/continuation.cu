@@ -384,7 +384,8 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
       // first overlapped step)
       const bool have_w = w_pending || w_valid;
       drain_side();
-      net->prepare(x, m, mu_new, ns.psi.p);
+      // the node features only when an inference reads them
+      net->prepare(x, m, mu_new, ns.psi.p, !have_w || infer_count + 1 >= infer_period);
       if (!have_w) net->infer(s.stream);
       w_valid = true;
       net->combine(ns.psi.p, ns.tmp.p, w_host);
@@ -397,19 +398,21 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
         NOSH_CUDA(cudaEventRecord(ev_side, side));
         w_pending = true;
       }
-      f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);  // syncs: w_host is valid
-      coef = *w_host;
-      compare = !(f_learned <= opt.tol);
     } else {
       coef = net->predict(x, m, mu_new, ns.psi.p, ns.tmp.p);
       w_valid = false;  // the weights may change before the next step
-      f_learned = residual_norm(s, ns.tmp.p, g, mu_new, ns.f.p);
-      compare = !(f_learned <= opt.tol);
     }
-    // a prediction that meets the tolerance is taken as is, otherwise the
-    // one with the smaller residual starts Newton: the plain secant is the
-    // fallback whenever the network's starting residual is worse
-    if (compare) f_secant = residual_norm(s, ns.psi.p, g, mu_new, ns.xc.p);
+    // F of the learned prediction and of the secant in one pass over the
+    // KEO (syncs: w_host is valid after it); a prediction that meets the
+    // tolerance is taken as is, otherwise the one with the smaller residual
+    // starts Newton: the plain secant is the fallback whenever the
+    // network's starting residual is worse
+    double nrm[2];
+    s.residual_pair(ns.tmp.p, ns.psi.p, g, mu_new, ns.f.p, ns.xc.p, nrm);
+    if (overlap) coef = *w_host;
+    f_learned = nrm[0];
+    f_secant = nrm[1];
+    compare = !(f_learned <= opt.tol);
     if (!compare || f_learned < f_secant) {
       std::swap(ns.psi, ns.tmp);
       last_used = NOSH_PREDICT_LEARNED;

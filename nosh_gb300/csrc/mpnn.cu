@@ -1173,7 +1173,7 @@ struct Mpnn::Impl {
   void forward(bool train);               // X -> pooled embedding
   double backward_and_step(float lr);     // needs gram
   void features(const double *const x[4], const double mu[4], double mu_t, const double *target,
-                double *secant = nullptr);
+                double *secant = nullptr, bool node_features = true);
   void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, float *out);
   void wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol, int64_t dst,
              int64_t bias_dst);
@@ -1422,7 +1422,7 @@ double Mpnn::Impl::backward_and_step(float lr) {
 // node features at mu_t from the newest states x[0..3] (mu[0..3]) and, with
 // a target (the converged state at mu_t), the sample's Gram scalars
 void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target,
-                          double *secant) {
+                          double *secant, bool node_features) {
   cudaStream_t st = stream;
   const int G = vgrid(N);
   double Lh[9];
@@ -1451,8 +1451,11 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
                                 (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, (C2<double> *)secant,
                                 rd.partials.p,
                                 rd.counter.p, red.p);
-  features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x[0], sq.p, X.p);
-  s.launch_count += 2;
+  ++s.launch_count;
+  if (node_features || target) {  // the network's input (not needed by combine alone)
+    features_b<<<G, 256, 0, st>>>(N, red.p, t, (const C2<double> *)x[0], sq.p, X.p);
+    ++s.launch_count;
+  }
   if (target) {
     // The loss is the linearised residual of the prediction, relative to
     // the quadratic's: F(q + w c) ~ J (w c - d) with J at the aligned target
@@ -1493,8 +1496,9 @@ double Mpnn::predict(const double *const x[4], const double mu[4], double mu_new
   return w;
 }
 
-void Mpnn::prepare(const double *const x[4], const double mu[4], double mu_new, double *secant) {
-  impl->features(x, mu, mu_new, nullptr, secant);
+void Mpnn::prepare(const double *const x[4], const double mu[4], double mu_new, double *secant,
+                   bool node_features) {
+  impl->features(x, mu, mu_new, nullptr, secant, node_features);
 }
 
 void Mpnn::infer(cudaStream_t st) {

@@ -19,7 +19,10 @@ struct Mpnn {
   // the network's coefficient w on stream `st` (it reads the features,
   // writes w), and out = secant + q + w c with the current w (handle stream;
   // w copied to w_host, a pinned scalar, when given)
-  void prepare(const double *const x[4], const double mu[4], double mu_new, double *secant);
+  // (node_features = false: only the prediction fields and the secant, for
+  // a step whose features feed no inference)
+  void prepare(const double *const x[4], const double mu[4], double mu_new, double *secant,
+               bool node_features = true);
   void infer(cudaStream_t st);
   void combine(const double *secant, double *out, double *w_host);
   // optimiser iterations on the transition x[0..3] -> target at mu_t;

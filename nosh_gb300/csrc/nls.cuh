@@ -159,6 +159,10 @@ struct NlsImpl {
   // y = F(x); optional ||F||^2 into red.out[slot]
   void compute_f64(const double *x, double g, double mu, double *f, int norm_slot);
   void dfdp64(const double *x, double g, double mu, int param, double *out);
+  // F(xa) into fa and F(xb) into fb in one pass, norms[0..1] = their norms
+  // (synchronises)
+  void residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
+                     double norms[2]);
   void jac_rebuild(const double *x, double g, double mu);
   void reg_rebuild(const double *x, double g, double mu);
   template <typename T>
@@ -179,6 +183,10 @@ struct NlsImpl {
   // diagnostics: bound of the staging waits (polls; < 0 restores the default)
   void set_stage_wait_limit(int64_t polls);
 };
+
+// streaming read of `bytes` (a multiple of 16) at 16-byte aligned device
+// memory, XOR-reduced into *out (the achievable-bandwidth probe)
+void stream_read(const void *buf, int64_t bytes, unsigned *out, cudaStream_t st);
 
 // launch helpers shared with the solver
 void launch_f64_to_f32(const double *a, float *b, int64_t n, cudaStream_t s);

@@ -380,6 +380,83 @@ int row_grid(const void *kernel, size_t smem, int64_t n_rows) {
 }
 }  // namespace dev
 
+// F(a) and F(b) (FP64, compute_f_) in one pass over the KEO graph, their
+// squared norms into out[0], out[1]: thread per row, the nonzeros read once
+// for both states, gathers in batches of four.  Per row the same summation
+// order as the row-block kernel's ResidualOp.
+__global__ void __launch_bounds__(128) residual_pair_kernel(
+    int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const C2<double> *__restrict__ val,
+    const double *__restrict__ kdiag, const double *__restrict__ cvt, const double *__restrict__ V, double g,
+    const C2<double> *__restrict__ xa, const C2<double> *__restrict__ xb, C2<double> *__restrict__ fa,
+    C2<double> *__restrict__ fb, double *partials, unsigned *counter, double *out) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  double na = 0.0, nb = 0.0;
+  if (row < N) {
+    double ar = 0.0, ai = 0.0, br = 0.0, bi = 0.0;
+    const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+    for (int k0 = b; k0 < e; k0 += 4) {
+      C2<double> v[4], p[4], q[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (k0 + u < e) {
+          const int c = __ldg(ci + k0 + u);
+          v[u] = ldg(val + k0 + u);
+          p[u] = ldg(xa + c);
+          q[u] = ldg(xb + c);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (k0 + u < e) {
+          ar += v[u].x * p[u].x - v[u].y * p[u].y;
+          ai += v[u].x * p[u].y + v[u].y * p[u].x;
+          br += v[u].x * q[u].x - v[u].y * q[u].y;
+          bi += v[u].x * q[u].y + v[u].y * q[u].x;
+        }
+      }
+    }
+    const double kd = kdiag[row], ct = cvt[row], vv = V[row];
+    const C2<double> pa = xa[row], pb = xb[row];
+    const double ca = kd + ct * (vv + g * (pa.x * pa.x + pa.y * pa.y));
+    const double cb = kd + ct * (vv + g * (pb.x * pb.x + pb.y * pb.y));
+    const double far = ar + ca * pa.x, fai = ai + ca * pa.y, fbr = br + cb * pb.x, fbi = bi + cb * pb.y;
+    fa[row] = C2<double>{far, fai};
+    fb[row] = C2<double>{fbr, fbi};
+    na = far * far + fai * fai;
+    nb = fbr * fbr + fbi * fbi;
+  }
+  grid_reduce(na, partials, counter, out);
+  grid_reduce(nb, partials + gridDim.x, counter + 1, out + 1);
+}
+
+// Achievable-bandwidth probe: a streaming read of n16 16-byte words with a
+// cheap integer reduction (XOR), four independent loads in flight per
+// thread, eight CTAs per SM.
+__global__ void __launch_bounds__(256) stream_read_kernel(int64_t n16, const uint4 *__restrict__ a,
+                                                          unsigned *out) {
+  unsigned acc = 0u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 v0 = __ldcs(a + i), v1 = __ldcs(a + i + stride), v2 = __ldcs(a + i + 2 * stride),
+                v3 = __ldcs(a + i + 3 * stride);
+    acc ^= v0.x ^ v0.y ^ v0.z ^ v0.w ^ v1.x ^ v1.y ^ v1.z ^ v1.w ^ v2.x ^ v2.y ^ v2.z ^ v2.w ^ v3.x ^ v3.y ^ v3.z ^
+           v3.w;
+  }
+  for (; i < n16; i += stride) {
+    const uint4 v = __ldcs(a + i);
+    acc ^= v.x ^ v.y ^ v.z ^ v.w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicXor(out, acc);
+}
+
+void stream_read(const void *buf, int64_t bytes, unsigned *out, cudaStream_t st) {
+  stream_read_kernel<<<8 * kNumSMs, 256, 0, st>>>(bytes / 16, reinterpret_cast<const uint4 *>(buf), out);
+  NOSH_CUDA(cudaGetLastError());
+}
+
 void launch_f64_to_f32(const double *a, float *b, int64_t n, cudaStream_t s) {
   if (n) d2f_kernel<<<div_up(n, 256), 256, 0, s>>>(a, b, n);
 }
@@ -615,6 +692,20 @@ void NlsImpl::compute_f64(const double *x, double g, double mu, double *f, int n
     ResidualOp<false> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f};
     launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, nullptr);
   }
+}
+
+void NlsImpl::residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
+                            double norms[2]) {
+  if (!(keo_mu == mu)) keo_refill(mu);
+  residual_pair_kernel<<<div_up(N, 128), 128, 0, stream>>>(
+      (int)N, mesh->d_rp.p, mesh->d_ci.p, d_keo64.p, d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)xa,
+      (const C2<double> *)xb, (C2<double> *)fa, (C2<double> *)fb, red.partials.p, red.counter.p, red.out.p);
+  ++launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  red.out.download(norms, 2, stream);
+  sync();
+  norms[0] = std::sqrt(norms[0]);
+  norms[1] = std::sqrt(norms[1]);
 }
 
 void NlsImpl::dfdp64(const double *x, double g, double mu, int param, double *out) {

@@ -12,6 +12,7 @@
 // Newton: full step (NOX "Line Search Based" / "Full Step",
 // examples/conf.xml:168-174), NormF two-norm test (conf.xml:178-189) on the
 // FP64 residual, Eisenstat-Walker style forcing.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -392,6 +393,8 @@ void reset_preconditioner(NlsImpl &s) {
     NewtonState &ns = *(NewtonState *)s.solver_state.get();
     ns.m32.reset();
     ns.m64.reset();
+    ns.s32.reset();
+    ns.s64.reset();
   }
   s.amg.reset();
 }
@@ -475,10 +478,86 @@ double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn
   return std::max(eta, eta_min);
 }
 
+template <typename T>
+static MinresSys<T> &minres_sys_of(NlsImpl &s, NewtonState &ns);
+template <>
+MinresSys<float> &minres_sys_of<float>(NlsImpl &s, NewtonState &ns) {
+  if (!ns.s32 || ns.s32->S != s.nsys()) ns.s32.reset(new MinresSys<float>(s));
+  if (ns.b32.n < (size_t)(2 * s.N)) ns.b32.alloc(2 * s.N);
+  return *ns.s32;
+}
+template <>
+MinresSys<double> &minres_sys_of<double>(NlsImpl &s, NewtonState &ns) {
+  if (!ns.s64 || ns.s64->S != s.nsys()) ns.s64.reset(new MinresSys<double>(s));
+  if (ns.b64.n < (size_t)(2 * s.N)) ns.b64.alloc(2 * s.N);
+  return *ns.s64;
+}
+
+// Newton for batched independent systems: one MINRES recurrence per system;
+// a converged system gets a zero right-hand side (its update is zero: the
+// Jacobian is block diagonal).
+template <typename T>
+static void newton_loop_systems(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
+                                nosh_newton_stats &st) {
+  MinresSys<T> &mr = minres_sys_of<T>(s, ns);
+  DevBuf<T> &b = rhs_of<T>(ns);
+  const int64_t n2 = 2 * s.N, S = s.nsys();
+  const int G = vec_grid(n2);
+  ns.sys_newton.assign(S, 0);
+  ns.sys_krylov.assign(S, 0);
+  std::vector<double> fcur = s.h_sys_norm, rtol(S, sizeof(T) == 4 ? 1e-6 : 1e-12);
+  std::vector<int> its;
+  double fn = st.f_norm0, fn_prev = fn;
+  for (int it = 0; it < opt.max_newton && fn > opt.tol; it++) {
+    rebuild_operators<T>(s, ns.psi.p, g, mu);
+    s.mask_converged(ns.f.p, opt.tol);
+    neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.f.p, b.p);
+    ++s.launch_count;
+    // one Eisenstat-Walker forcing term from the largest residual is the
+    // batch's test (the union's residual relative to its right-hand side);
+    // a system that reaches the Krylov precision's floor on its own stops
+    // early.  (The same term as each system's own test made the slowest
+    // system of the 256-square workload take 7 Newton steps and the batch
+    // 704 MINRES iterations; per-system terms, 11 Newton steps.)
+    const double eta = forcing_term(opt, it, fn, fn_prev, sizeof(T) == 4);
+    int status = 0;
+    st.krylov_iters += mr.solve(b.p, eta, rtol, opt.max_krylov, its, status);
+    for (int64_t q = 0; q < S; q++)
+      if (fcur[q] > opt.tol) {
+        ns.sys_newton[q]++;
+        ns.sys_krylov[q] += its[q];
+      }
+    if (status == NOSH_ERR_NAN || status == NOSH_ERR_BREAKDOWN) {
+      s.amg->clear_error();
+      st.status = status;
+      return;
+    }
+    axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, ns.psi.p);
+    ++s.launch_count;
+    residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+    fn_prev = fn;
+    fn = s.system_norms(ns.f.p);
+    fcur = s.h_sys_norm;
+    st.newton_iters = it + 1;
+    st.f_norm = fn;
+    if (opt.verbose)
+      std::fprintf(stderr, "newton %2d  max ||F_s|| = %.3e  minres its (largest over systems) %4d\n", it + 1, fn,
+                   *std::max_element(its.begin(), its.end()));
+    if (std::isnan(fn)) {
+      st.status = NOSH_ERR_NAN;
+      return;
+    }
+  }
+}
+
 // Newton on ns.psi (device), residual already in ns.f with norm st.f_norm0.
 template <typename T>
 static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
                         const nosh_newton_options &opt, nosh_newton_stats &st) {
+  if (!s.sys_off.empty() && !opt.phase_fix) {
+    newton_loop_systems<T>(s, ns, g, mu, opt, st);
+    return;
+  }
   Minres<T> &mr = minres_of<T>(s, ns);
   DevBuf<T> &b = rhs_of<T>(ns);
   const int64_t n2 = 2 * s.N;

@@ -46,6 +46,35 @@ struct Minres {
   void wx_final(int j);    // deferred w/x update of iteration j, the last issued
 };
 
+// Batched independent solves: one Paige-Saunders recurrence per system
+// over the shared vectors (minres_sys.cu).
+template <typename T>
+struct MinresSys {
+  NlsImpl &s;
+  int64_t N, S;
+  DevBuf<T> r[2], z[2], w[3], u, x;
+  DevBuf<double> rowdot, cpart, rtol;
+  DevBuf<MinresScalars> sc;
+  DevBuf<int32_t> vsys, csys, schunk;
+  DevBuf<int64_t> cstart;
+  DevBuf<unsigned> counter;
+  DevBuf<int> active;
+  int nchunks = 0;
+  std::vector<MinresScalars> h_sc;
+  int *h_active = nullptr, *h_err = nullptr;
+  explicit MinresSys(NlsImpl &nls);
+  ~MinresSys();
+  // b: device vector of T (2N); eta: the batch's relative tolerance (the
+  // union's preconditioned residual); rtol: per system (a system stops early
+  // at its own); its: iterations per system; returns the largest; x holds
+  // the solution
+  int solve(const T *b, double eta, const std::vector<double> &rtol, int maxit, std::vector<int> &its,
+            int &status);
+
+ private:
+  void reduce(int mode, int maxit);
+};
+
 // Newton work space of an nls handle (solver.cu)
 struct NewtonState {
   DevBuf<double> psi, f, xc, xp, tmp;  // working state, residual, staged inputs
@@ -54,6 +83,11 @@ struct NewtonState {
   DevBuf<double> red2;  // complex reduction (phase alignment)
   std::unique_ptr<Minres<float>> m32;
   std::unique_ptr<Minres<double>> m64;
+  std::unique_ptr<MinresSys<float>> s32;
+  std::unique_ptr<MinresSys<double>> s64;
+  // batched solves: per-system Newton steps and MINRES iterations of the
+  // last Newton solve
+  std::vector<int> sys_newton, sys_krylov;
 };
 NewtonState &state_of(NlsImpl &s);
 // drop the AMG hierarchy (and the MINRES graphs that reference it); the next

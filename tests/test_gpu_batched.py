@@ -26,6 +26,10 @@ def test_batched_squares_match_oracle():
     assert st["status"] == 0 and st["f_norm"] <= 1e-10
     norms = model.system_norms()
     assert norms.shape == (len(sides),) and np.all(norms <= 1e-10)
+    # every system ran its own MINRES recurrences and Newton steps
+    nw, kr = model.system_iterations()
+    assert nw.shape == kr.shape == (len(sides),)
+    assert np.all(nw >= 1) and np.all(kr >= nw) and st["newton_iters"] == nw.max()
     for k, (s, m) in enumerate(zip(sides, mus)):
         xs, cs, p0 = O.gen_square(s, 40 + k)
         mk = O.finish_mesh(xs, cs)

@@ -206,9 +206,53 @@ def test_learned_predictor_gains_over_secant():
             xc, mc = cur
             xp = O.align_phase(prev[0], xc)
             sec = xc + (mu - mc) / (mc - prev[1]) * (xc - xp)
-            gains.append(np.linalg.norm(P.compute_f(sec, 1.0, mu)) / max(lp["f_learned"], 1e-16))
+            f_sec = np.linalg.norm(P.compute_f(sec, 1.0, mu))
+            gains.append(f_sec / max(lp["f_learned"], 1e-16))
+            # the fallback's residual, evaluated in the same pass as the
+            # learned one, is the oracle's
+            assert abs(lp["f_secant"] - f_sec) <= 1e-6 * f_sec, (lp["f_secant"], f_sec)
         prev = cur
     # the trained network beats the quadratic extrapolation on its last
     # training transition, and starts Newton far closer than the secant
     assert 0.0 <= lp["train_loss"] < 1.0, lp
     assert np.median(gains) > 10.0, gains
+
+
+@pytest.mark.parametrize("name", ["cube64", "square65"])
+def test_learned_adapts_to_the_better_extrapolation(name):
+    """On held-out steps after the training window, the trained network's
+    prediction starts Newton within 10 % of the better of the two fixed
+    extrapolations it blends (quadratic, cubic) and at least 20 % below the
+    worse one.  Which one is better depends on the problem: the quadratic on
+    the 64^3 cube (mu 0.5 + k 0.005, where the cubic amplifies the stored
+    states' solver noise), the cubic on the 65 x 65 square (mu 0.1 + k
+    0.005); a fixed choice loses on one of them.  The residuals come from
+    one history per step (nosh_continuation_predictor_residuals)."""
+    import torch
+
+    import nosh_gb300 as ng
+    from nosh_gb300 import meshgen
+
+    if name == "cube64":
+        x, cells, psi0 = meshgen.cube(64, 2)
+        mu0 = 0.5
+    else:
+        x, cells, psi0 = meshgen.square(65, 5)
+        mu0 = 0.1
+    model = ng.nls(ng.mesh(x, cells), meshgen.mvp_constant_curl(x), -1.0, 1.0, 1.0, mu=mu0)
+    x0 = torch.tensor(psi0, dtype=torch.float64, device="cuda")
+    assert model.newton(x0, {"mu": mu0})["status"] == 0
+    cont = ng.continuation(model, x0, mu0)
+    cont.learning(12, 10, 2e-3)
+    mu, rows = mu0, []
+    for k in range(32):
+        mu += 0.005
+        if k >= 16:  # past the 12 training steps and the 4 history steps
+            rows.append(cont.predictor_residuals(mu))
+        st = cont.advance(mu, predictor=ng.PREDICT_LEARNED)
+        assert st["status"] == 0 and st["f_norm"] <= 1e-10
+    q = np.mean([r["quadratic"] for r in rows])
+    c = np.mean([r["cubic"] for r in rows])
+    l = np.mean([r["learned"] for r in rows])
+    assert l <= 1.10 * min(q, c), (l, q, c)
+    assert l <= 0.80 * max(q, c), (l, q, c)
