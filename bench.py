@@ -232,8 +232,9 @@ def large_roofline(peak, peak_kind, traffic, m=160, seed=5, mu0=0.8, dmu=0.01, s
         out[name] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                      "peak_kind": peak_kind, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
                      "algorithmic_bytes_per_launch": bytes_l / n_l,
-                     "traffic": scaled_traffic(traffic, name, bytes_l / n_l),
-                     "traffic_source": "ncu capture of one 64^3 launch, scaled to this launch by its "
+                     "traffic": scaled_traffic(traffic, name + "_cold", bytes_l / n_l),
+                     "traffic_source": "ncu capture of one 64^3 launch after a cache flush (nothing "
+                                       "resident, as at this size), scaled to this launch by its "
                                        "algorithmic bytes"}
     model.profile(False)
     del cont, model, x0
@@ -471,8 +472,10 @@ def run_gb300(args):
              "peak_kind": peak_kind, "kernel": name, "launches": n_l, "avg_launch_us": 1000.0 * ms_l / n_l,
              "algorithmic_bytes_per_launch": bytes_l / n_l,
              "traffic": scaled_traffic(traffic, name, bytes_l / n_l),
-             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 64^3 launch"
-                               + ("" if args.m == 64 else ", scaled to this launch by its algorithmic bytes"),
+             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 64^3 launch inside "
+                               "the step (--cache-control none): the working set stays in L2 between "
+                               "launches, so DRAM moves far fewer bytes than the algorithmic count"
+                               + ("" if args.m == 64 else "; scaled to this launch by its algorithmic bytes"),
              "timing": "CUDA events around each launch on the library stream, during extra continuation "
                        "steps of the same workload run after the timed ones"}
         if name == dom:
@@ -571,6 +574,13 @@ def run_gb300(args):
         out["cpu_baseline"] = {"value": cv, "unit": "steps/s", "cores": threads, "kind": "port",
                                "sample": f"{len(times)} secant continuation steps of the same workload "
                                          f"(FP64 CPU restatement, {threads} OpenMP threads)"}
+        out["same_precision"] = {"plain_fp64_gpu": out["plain_fp64"]["value"], "cpu_fp64": cv,
+                                 "ratio": out["plain_fp64"]["value"] / cv,
+                                 "note": "the FP64 GPU path with the plain predictor against the FP64 CPU "
+                                         "restatement: the speed-up at the same precision and predictor"}
+    # the comparison lines last, where a truncated tail of the output keeps them
+    for k in ("plain_predictor", "plain_fp64", "ablations", "learned_vs_plain", "learned_mixed_vs_plain_fp64"):
+        out[k] = out.pop(k)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -749,7 +759,7 @@ def run_batched_reference(args):
 
 
 # ------------------------------------------------------ 48^3 continuation run
-CONT48_METRIC = "continuation steps/s, 48³ tet GL mesh, mu 0→1 in 200 steps, learned predictor trained on 40"
+CONT48_METRIC = "continuation steps/s, 48³ tet GL mesh, mu 0→1 in 200 steps, learned predictor trained on the first 40"
 
 
 def cont48_workload(args):
@@ -788,7 +798,9 @@ def run_cont48(args):
     def run(name):
         cont = ng.continuation(model, x0, 0.0)
         if name == "learned":
-            cont.learning(40, args.train_iters, args.lr)
+            # a training step needs four stored states before it: 36 training
+            # steps end with the 40th continuation step
+            cont.learning(36, args.train_iters, args.lr)
             cont.inference_period(args.infer_period)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(200)]
         its, used = [], []
