@@ -72,7 +72,9 @@ def parse():
     ap.add_argument("--refine", type=float, default=0.0,
                     help="residual the Newton steps aim at under the learned and cubic predictors (0: tol)")
     ap.add_argument("--train-steps", type=int, default=12, help="online-training window of the learned predictor")
-    ap.add_argument("--train-iters", type=int, default=10, help="optimiser iterations per training step")
+    ap.add_argument("--train-iters", type=int, default=None,
+                    help="optimiser iterations per training step (default 10; 2 for cont48, whose timed "
+                         "amortized line includes the training: 500 against 191 steps/s at 10)")
     ap.add_argument("--lr", type=float, default=2e-3, help="learning rate of the online training")
     ap.add_argument("--infer-period", type=int, default=8,
                     help="after training, re-infer the learned coefficient every this many steps (a sweep at "
@@ -881,6 +883,8 @@ def run_cont48_reference(args):
 
 def main():
     args = parse()
+    if args.train_iters is None:
+        args.train_iters = 2 if args.workload == "cont48" else 10
     if args.workload == "batched256":
         run_batched_reference(args) if args.impl == "reference" else run_batched(args)
     elif args.workload == "cont48":

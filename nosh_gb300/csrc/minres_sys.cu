@@ -171,7 +171,8 @@ __global__ void wx_sys(int64_t N, const int32_t *__restrict__ vsys, const Minres
 // the running systems into *active, and applies the batch's stopping test
 // sum_s phibar_s^2 <= eta^2 sum_s beta1_s^2; when it holds every running
 // system stops (done = 1: frozen at its next Lanczos step).
-__global__ void batch_check(int S, MinresScalars *sc, double eta, int *active) {
+__global__ void batch_check(int S, MinresScalars *sc, const double *eta_p, int *active) {
+  const double eta = *eta_p;
   __shared__ double s32[32];
   __shared__ bool stop;
   double num = 0.0, den = 0.0, run = 0.0;
@@ -230,6 +231,8 @@ MinresSys<T>::MinresSys(NlsImpl &nls) : s(nls), N(nls.N), S(nls.nsys()) {
   h_sc.resize(S);
   NOSH_CUDA(cudaMallocHost(&h_active, sizeof(int)));
   NOSH_CUDA(cudaMallocHost(&h_err, sizeof(int)));
+  NOSH_CUDA(cudaMallocHost(&h_eta, sizeof(double)));
+  eta.alloc(1);
   NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, JacRowDotOp<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  100 * 1024));
   s.sync();
@@ -237,8 +240,40 @@ MinresSys<T>::MinresSys(NlsImpl &nls) : s(nls), N(nls.N), S(nls.nsys()) {
 
 template <typename T>
 MinresSys<T>::~MinresSys() {
+  if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
   if (h_active) cudaFreeHost(h_active);
   if (h_err) cudaFreeHost(h_err);
+  if (h_eta) cudaFreeHost(h_eta);
+}
+
+// Iteration j (0..5) of a chunk: buffer roles rotate with periods 2 (z, r)
+// and 3 (w), so six iterations always start from the same assignment.
+template <typename T>
+void MinresSys<T>::iteration(int j, int maxit) {
+  cudaStream_t st = s.stream;
+  const int G = egrid(N);
+  const int cap = sizeof(T) == 4 ? s.cap32 : s.cap64;
+  const C2<T> *val = sizeof(T) == 4 ? (const C2<T> *)s.d_keo32.p : (const C2<T> *)s.d_keo64.p;
+  const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
+  const bool warp = sizeof(T) == 4 ? s.warp32 : s.warp64;
+  T *zc = z[j % 2].p, *zn = z[(j + 1) % 2].p;
+  T *r_old = r[j % 2].p, *r_cur = r[(j + 1) % 2].p;
+  JacRowDotOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, rowdot.p};
+  launch_spmv<T>(warp, (int)N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, (const C2<T> *)zc, cap, op, s.red.partials.p,
+                 s.red.counter.p, nullptr, st);
+  ++s.launch_count;
+  reduce(kLanczos, maxit);
+  lanczos_sys<T><<<G, 256, 0, st>>>(N, vsys.p, sc.p, (const C2<T> *)u.p, (C2<T> *)r_old, (const C2<T> *)r_cur);
+  ++s.launch_count;
+  s.amg->apply<T>(r_old, zn);
+  rowdot_kernel<T><<<G, 256, 0, st>>>(N, (const C2<T> *)r_old, (const C2<T> *)zn, rowdot.p);
+  ++s.launch_count;
+  reduce(kAdvance, maxit);
+  // the Givens step's w/x update: v = z of this iteration / beta
+  wx_sys<T><<<G, 256, 0, st>>>(N, vsys.p, sc.p, zc, w[j % 3].p, w[(j + 1) % 3].p, w[(j + 2) % 3].p, x.p);
+  batch_check<<<1, 1024, 0, st>>>((int)S, sc.p, eta.p, active.p);
+  s.launch_count += 2;
+  NOSH_CUDA(cudaGetLastError());
 }
 
 template <typename T>
@@ -264,6 +299,8 @@ int MinresSys<T>::solve(const T *b, double eta, const std::vector<double> &rtol_
   const size_t bytes = n2 * sizeof(T);
   const int G = egrid(N);
   rtol.upload(rtol_host.data(), S, st);
+  *h_eta = eta;
+  NOSH_CUDA(cudaMemcpyAsync(this->eta.p, h_eta, sizeof(double), cudaMemcpyHostToDevice, st));
   // prologue: r_old = r_cur = b, x = w = 0, z = M b, <b, z>_s
   NOSH_CUDA(cudaMemcpyAsync(r[0].p, b, bytes, cudaMemcpyDeviceToDevice, st));
   NOSH_CUDA(cudaMemcpyAsync(r[1].p, b, bytes, cudaMemcpyDeviceToDevice, st));
@@ -273,36 +310,34 @@ int MinresSys<T>::solve(const T *b, double eta, const std::vector<double> &rtol_
   ++s.launch_count;
   reduce(kInit, maxit);
   NOSH_CUDA(cudaGetLastError());
-  const int cap = sizeof(T) == 4 ? s.cap32 : s.cap64;
-  const C2<T> *val = sizeof(T) == 4 ? (const C2<T> *)s.d_keo32.p : (const C2<T> *)s.d_keo64.p;
-  const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
-  const bool warp = sizeof(T) == 4 ? s.warp32 : s.warp64;
+  // the six iterations of a chunk are captured once as a CUDA graph (the
+  // tolerance and iteration limit reach it through device memory), unless
+  // kernel timing is on
+  const bool graphs = !s.timers[NOSH_KERNEL_JACOBIAN].on;
+  if (graphs && (!chunk_exec || chunk_maxit != maxit)) {
+    if (chunk_exec) NOSH_CUDA(cudaGraphExecDestroy(chunk_exec));
+    chunk_exec = nullptr;
+    cudaGraph_t g;
+    const int64_t before = s.launch_count;
+    NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int q = 0; q < 6; q++) iteration(q, maxit);
+    NOSH_CUDA(cudaStreamEndCapture(st, &g));
+    chunk_kernels = s.launch_count - before;
+    s.launch_count = before;
+    NOSH_CUDA(cudaGraphInstantiate(&chunk_exec, g, 0));
+    NOSH_CUDA(cudaGraphDestroy(g));
+    chunk_maxit = maxit;
+  }
   int it = 0;
   for (;;) {
-    // a batch of iterations between two polls of the running count; buffer
-    // roles rotate with periods 2 (z, r) and 3 (w)
-    for (int q = 0; q < 6; q++, it++) {
-      const int j = it % 6;
-      T *zc = z[j % 2].p, *zn = z[(j + 1) % 2].p;
-      T *r_old = r[j % 2].p, *r_cur = r[(j + 1) % 2].p;
-      JacRowDotOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, rowdot.p};
-      launch_spmv<T>(warp, (int)N, s.mesh->d_rp.p, s.mesh->d_ci.p, val, (const C2<T> *)zc, cap, op,
-                     s.red.partials.p, s.red.counter.p, nullptr, st);
-      ++s.launch_count;
-      reduce(kLanczos, maxit);
-      lanczos_sys<T><<<G, 256, 0, st>>>(N, vsys.p, sc.p, (const C2<T> *)u.p, (C2<T> *)r_old,
-                                        (const C2<T> *)r_cur);
-      ++s.launch_count;
-      s.amg->apply<T>(r_old, zn);
-      rowdot_kernel<T><<<G, 256, 0, st>>>(N, (const C2<T> *)r_old, (const C2<T> *)zn, rowdot.p);
-      ++s.launch_count;
-      reduce(kAdvance, maxit);
-      // the Givens step's w/x update: v = z of this iteration / beta
-      wx_sys<T><<<G, 256, 0, st>>>(N, vsys.p, sc.p, zc, w[j % 3].p, w[(j + 1) % 3].p, w[(j + 2) % 3].p, x.p);
-      batch_check<<<1, 1024, 0, st>>>((int)S, sc.p, eta, active.p);
-      s.launch_count += 2;
-      NOSH_CUDA(cudaGetLastError());
+    // a chunk of iterations between two polls of the running count
+    if (graphs) {
+      NOSH_CUDA(cudaGraphLaunch(chunk_exec, st));
+      s.launch_count += chunk_kernels;
+    } else {
+      for (int q = 0; q < 6; q++) iteration(q, maxit);
     }
+    it += 6;
     NOSH_CUDA(cudaMemcpyAsync(h_active, active.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     s.sync();
     if (*h_active <= 0 || it >= maxit + 6) break;

@@ -62,6 +62,11 @@ struct MinresSys {
   int nchunks = 0;
   std::vector<MinresScalars> h_sc;
   int *h_active = nullptr, *h_err = nullptr;
+  double *h_eta = nullptr;
+  DevBuf<double> eta;  // the batch's tolerance (read by the captured chunk)
+  cudaGraphExec_t chunk_exec = nullptr;
+  int64_t chunk_kernels = 0;
+  int chunk_maxit = -1;
   explicit MinresSys(NlsImpl &nls);
   ~MinresSys();
   // b: device vector of T (2N); eta: the batch's relative tolerance (the
@@ -73,6 +78,7 @@ struct MinresSys {
 
  private:
   void reduce(int mode, int maxit);
+  void iteration(int j, int maxit);
 };
 
 // Newton work space of an nls handle (solver.cu)
