@@ -178,6 +178,23 @@ int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule);
  * NOSH_ERR_CUDA at its next synchronisation, and the handle stays usable.
  * polls = 0 makes every staged wait give up at once (tests of that path). */
 int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls);
+/* Index-check mode (the reference's debug builds assert sizes on the host,
+ * e.g. src/jacobian_operator.cpp:68-86; there is no device counterpart).
+ * With enable != 0 the handle validates its KEO graph on the device before
+ * every Newton solve, continuation step and operator apply of this ABI (and
+ * once now): row ranges in order and within the entry count, column ids in
+ * [0, N), off the diagonal and increasing along each row.  The first
+ * offence is recorded in a device word (no trap, no out-of-range access)
+ * and the call returns NOSH_ERR_INVALID naming its position.  Costs one
+ * pass over the index arrays per call. */
+int nosh_nls_set_index_checks(nosh_nls nls, int enable);
+/* The same validation for a caller's off-diagonal CSR graph in device
+ * memory (row_ptr[N+1], cols[nnz]), e.g. the one passed to
+ * nosh_residual_norm_noalloc, which cannot read it on the host.  NOSH_OK or
+ * NOSH_ERR_INVALID with the position of the first offence; work on
+ * `stream`, waited for. */
+int nosh_graph_check(int64_t num_vertices, int64_t nnz, const int32_t *row_ptr,
+                     const int32_t *cols, void *stream);
 /* Diagnostics (no counterpart in the reference): the achievable-bandwidth
  * probe.  Enqueues on `stream` one launch that streams `bytes` (a multiple
  * of 16) of the 16-byte aligned device buffer `buf` with 16-byte loads and

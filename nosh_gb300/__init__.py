@@ -123,6 +123,8 @@ _SIGS = {
     "nosh_nls_set_spmv_schedule": (_I, [_P, _I]),
     "nosh_nls_set_stage_wait_limit": (_I, [_P, _I64]),
     "nosh_diag_stream_read": (_I, [_P, _I64, _P, _P]),
+    "nosh_nls_set_index_checks": (_I, [_P, _I]),
+    "nosh_graph_check": (_I, [_I64, _I64, _P, _P, _P]),
     "nosh_nls_amg_levels": (_I, [_P, C.POINTER(_I), _P, _I, C.POINTER(_I)]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_system_norms": (_I, [_P, _P]),
@@ -211,6 +213,13 @@ def stream_read(buf, nbytes, out_word, stream=None):
     ``buf`` (XOR-folded into the 32-bit device word ``out_word``), enqueued
     on ``stream`` (a cudaStream_t handle, default stream when None)."""
     _check(_lib.nosh_diag_stream_read(_ptr(buf), int(nbytes), _ptr(out_word), C.c_void_p(stream or 0)))
+
+
+def graph_check(row_ptr, cols, stream=None):
+    """Validate an off-diagonal CSR graph held in device memory (tensors with
+    data_ptr); raises NoshError naming the first offending position."""
+    n = int(row_ptr.numel()) - 1
+    _check(_lib.nosh_graph_check(n, int(cols.numel()), _ptr(row_ptr), _ptr(cols), C.c_void_p(stream or 0)))
 
 
 def device_count() -> int:
@@ -448,6 +457,11 @@ class nls:
     def set_spmv_schedule(self, schedule):
         """SPMV_AUTO, SPMV_STAGED or SPMV_WARP (see nosh_gb300.h)."""
         _check(_lib.nosh_nls_set_spmv_schedule(self._h, schedule))
+
+    def set_index_checks(self, enable=True):
+        """Index-check mode: the KEO graph is validated on the device before
+        every compute call (see nosh_nls_set_index_checks)."""
+        _check(_lib.nosh_nls_set_index_checks(self._h, 1 if enable else 0))
 
     def set_stage_wait_limit(self, polls):
         """Diagnostics: bound (mbarrier polls) of the staged SpMV's waits for

@@ -63,6 +63,13 @@ nosh::NlsImpl &N(nosh_nls h) {
   require(h && h->impl, "null nls handle");
   return *h->impl;
 }
+// N() for the entry points that run kernels over the KEO graph: in
+// index-check mode the graph is validated on the device first
+nosh::NlsImpl &NC(nosh_nls h) {
+  nosh::NlsImpl &s = N(h);
+  if (s.index_checks) s.check_indices();
+  return s;
+}
 nosh::MeshImpl &M(nosh_mesh h) {
   require(h && h->impl, "null mesh handle");
   return *h->impl;
@@ -389,6 +396,30 @@ int nosh_diag_stream_read(const void *buf, int64_t bytes, void *out_word, void *
   });
 }
 
+int nosh_nls_set_index_checks(nosh_nls nls, int enable) {
+  return guarded([&] {
+    auto &s = N(nls);
+    s.index_checks = enable != 0;
+    if (s.index_checks) s.check_indices();
+  });
+}
+
+int nosh_graph_check(int64_t num_vertices, int64_t nnz, const int32_t *row_ptr, const int32_t *cols,
+                     void *stream) {
+  return guarded([&] {
+    require(num_vertices >= 1 && nnz >= 0, "bad sizes");
+    require(nosh::is_device_pointer(row_ptr) && (nnz == 0 || nosh::is_device_pointer(cols)),
+            "row_ptr and cols must be device memory");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    nosh::DevBuf<unsigned long long> err(1);
+    nosh::check_graph(num_vertices, nnz, row_ptr, cols, err.p, st);
+    unsigned long long w = 0;
+    NOSH_CUDA(cudaMemcpyAsync(&w, err.p, sizeof(w), cudaMemcpyDeviceToHost, st));
+    NOSH_CUDA(cudaStreamSynchronize(st));
+    nosh::report_graph_error(w);
+  });
+}
+
 int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls) {
   return guarded([&] { N(nls).set_stage_wait_limit(polls); });
 }
@@ -403,7 +434,7 @@ int nosh_nls_stream(nosh_nls nls, void **stream) {
 int nosh_nls_compute_f_norm(nosh_nls nls, const double *x, const double *p, double *f,
                             double *norm) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     double g, mu;
     read_params(p, g, mu);
     const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
@@ -422,7 +453,7 @@ int nosh_nls_compute_f(nosh_nls nls, const double *x, const double *p, double *f
 
 int nosh_nls_compute_dfdp(nosh_nls nls, const double *x, const double *p, double *dfdp) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     double g, mu;
     read_params(p, g, mu);
     const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
@@ -478,7 +509,7 @@ int nosh_keo_values(nosh_nls nls, double *vals) {
 
 int nosh_keo_apply(nosh_nls nls, const double *x, double *y) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     require(!std::isnan(s.keo_mu), "KEO not filled: call nosh_keo_set_parameters first");
     const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
     OutVec o(s, y, s.d_out, 2 * s.N);
@@ -511,7 +542,7 @@ int nosh_dkeo_values(nosh_nls nls, double *vals) {
 
 int nosh_dkeo_apply(nosh_nls nls, const double *x, double *y) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     require(!std::isnan(s.dkeo_mu), "DkeoDP not filled: call nosh_dkeo_set_parameters first");
     const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
     OutVec o(s, y, s.d_out, 2 * s.N);
@@ -534,7 +565,7 @@ int nosh_jacobian_rebuild(nosh_nls nls, const double *p, const double *x) {
 int nosh_jacobian_apply(nosh_nls nls, const double *X, double *Y, int nvec, int mode,
                         double alpha, double beta) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     check_apply_args(mode, alpha, beta, nvec);
     require(s.jac_ready, "Jacobian not built: call nosh_jacobian_rebuild first");
     for (int k = 0; k < nvec; k++) {
@@ -569,7 +600,7 @@ int nosh_keo_regularized_rebuild(nosh_nls nls, const double *p, const double *x)
 int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y, int nvec, int mode,
                                double alpha, double beta) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     check_apply_args(mode, alpha, beta, nvec);
     require(s.reg_ready && s.amg, "preconditioner not built: call nosh_keo_regularized_rebuild");
     for (int k = 0; k < nvec; k++) {
@@ -590,7 +621,7 @@ int nosh_keo_regularized_apply(nosh_nls nls, const double *X, double *Y, int nve
 int nosh_eig_lowest(nosh_nls nls, const double *psi, const double *p, int k, double tol, int maxit, int guard,
                     int deflate_gauge, uint64_t seed, double *eigenvalues, double *eigenvectors, int *iterations) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     double g, mu;
     read_params(p, g, mu);
     require(eigenvalues != nullptr, "null eigenvalue output");
@@ -604,7 +635,7 @@ int nosh_eig_lowest(nosh_nls nls, const double *psi, const double *p, int k, dou
 
 int nosh_keo_regularized_smoother_apply(nosh_nls nls, const double *x, double *y) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     require(s.reg_ready && s.amg, "preconditioner not built: call nosh_keo_regularized_rebuild");
     const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
     OutVec o(s, y, s.d_out, 2 * s.N);
@@ -621,7 +652,7 @@ int nosh_keo_regularized_smoother_apply(nosh_nls nls, const double *x, double *y
 
 int nosh_keo_regularized_operator_apply(nosh_nls nls, const double *x, double *y) {
   return guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     require(s.reg_ready, "preconditioner not built: call nosh_keo_regularized_rebuild");
     const double *dx = stage_in(s, x, s.d_in, 2 * s.N);
     OutVec o(s, y, s.d_out, 2 * s.N);
@@ -647,7 +678,7 @@ int nosh_newton_solve(nosh_nls nls, double *x, const double *p, const nosh_newto
                       nosh_newton_stats *stats) {
   nosh_newton_stats st{};
   int rc = guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     double g, mu;
     read_params(p, g, mu);
     nosh_newton_options o;
@@ -668,7 +699,7 @@ int nosh_continuation_step(nosh_nls nls, double *x, double *x_prev, const double
                            const nosh_newton_options *opt, nosh_newton_stats *stats) {
   nosh_newton_stats st{};
   int rc = guarded([&] {
-    auto &s = N(nls);
+    auto &s = NC(nls);
     double g, mu;
     read_params(p_new, g, mu);
     require(predictor >= NOSH_PREDICT_NONE && predictor <= NOSH_PREDICT_TANGENT, "unknown predictor");
@@ -721,6 +752,7 @@ int nosh_continuation_advance(nosh_continuation c, double mu_new, int predictor,
     if (opt) o = *opt;
     require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0 && o.refine >= 0 && o.refine <= o.tol,
             "bad solver options");
+    if (c->impl->s.index_checks) c->impl->s.check_indices();
     c->impl->advance(mu_new, predictor, o, st);
   });
   if (rc == NOSH_OK) rc = st.status;
@@ -738,6 +770,7 @@ int nosh_continuation_advance_arclength(nosh_continuation c, double ds, int pred
     if (opt) o = *opt;
     require(o.tol > 0 && o.max_newton >= 0 && o.max_krylov > 0 && o.refine >= 0 && o.refine <= o.tol,
             "bad solver options");
+    if (c->impl->s.index_checks) c->impl->s.check_indices();
     c->impl->advance_arclength(ds, predictor, theta, o, st);
   });
   if (rc == NOSH_OK) rc = st.status;

@@ -182,7 +182,19 @@ struct NlsImpl {
   unsigned *h_stage_err = nullptr;  // pinned, one word
   // diagnostics: bound of the staging waits (polls; < 0 restores the default)
   void set_stage_wait_limit(int64_t polls);
+  // index-check mode: the KEO graph is validated on the device before every
+  // Newton solve, continuation step and operator apply of the C ABI
+  bool index_checks = false;
+  DevBuf<unsigned long long> d_check;
+  void check_indices();
 };
+
+// index-check mode: validates an off-diagonal CSR graph on the device into
+// *err_dev (all ones: valid; else the first offence, see ops.cu), and turns
+// a host copy of that word into NOSH_ERR_INVALID with the position
+void check_graph(int64_t N, int64_t nnz, const int32_t *rp, const int32_t *ci, unsigned long long *err_dev,
+                 cudaStream_t st);
+void report_graph_error(unsigned long long w);
 
 // streaming read of `bytes` (a multiple of 16) at 16-byte aligned device
 // memory, XOR-reduced into *out (the achievable-bandwidth probe)

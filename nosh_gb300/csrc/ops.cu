@@ -429,6 +429,52 @@ __global__ void __launch_bounds__(128) residual_pair_kernel(
   grid_reduce(nb, partials + gridDim.x, counter + 1, out + 1);
 }
 
+// Device-side validation of an off-diagonal CSR graph (index-check mode):
+// every row's range must be non-decreasing within [0, nnz], every column id
+// in [0, N), different from the row and increasing along the row.  The
+// first offending position is recorded as (kind << 56 | position) with an
+// atomicMin, so the report is the same on every run; nothing is trapped and
+// no out-of-range entry is dereferenced.
+__global__ void graph_check_kernel(int64_t N, int64_t nnz, const int32_t *__restrict__ rp,
+                                   const int32_t *__restrict__ ci, unsigned long long *err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = rp[i], e = rp[i + 1];
+    if (i == 0 && b != 0) atomicMin(err, (1ull << 56) | 0ull);
+    if (i == N - 1 && e != nnz) atomicMin(err, (1ull << 56) | (unsigned long long)N);
+    if (b > e || b < 0 || e > nnz) {
+      atomicMin(err, (1ull << 56) | (unsigned long long)i);
+      continue;
+    }
+    int64_t prev = -1;
+    for (int64_t k = b; k < e; k++) {
+      const int64_t c = ci[k];
+      if (c < 0 || c >= N || c == i || c <= prev) {
+        atomicMin(err, (2ull << 56) | (unsigned long long)k);
+        break;
+      }
+      prev = c;
+    }
+  }
+}
+
+void check_graph(int64_t N, int64_t nnz, const int32_t *rp, const int32_t *ci, unsigned long long *err_dev,
+                 cudaStream_t st) {
+  NOSH_CUDA(cudaMemsetAsync(err_dev, 0xff, sizeof(unsigned long long), st));
+  graph_check_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>(div_up(N, 256), 8 * kNumSMs)), 256, 0, st>>>(
+      N, nnz, rp, ci, err_dev);
+  NOSH_CUDA(cudaGetLastError());
+}
+
+void report_graph_error(unsigned long long w) {
+  if (w == ~0ull) return;
+  const unsigned long long kind = w >> 56, pos = w & ((1ull << 56) - 1);
+  if (kind == 1)
+    throw Error(NOSH_ERR_INVALID, "index check: row pointer out of order or out of range at row " +
+                                      std::to_string(pos));
+  throw Error(NOSH_ERR_INVALID, "index check: column id out of range, on the diagonal or not increasing at "
+                                "entry " + std::to_string(pos));
+}
+
 // Achievable-bandwidth probe: a streaming read of n16 16-byte words with a
 // cheap integer reduction (XOR), four independent loads in flight per
 // thread, eight CTAs per SM.
@@ -642,6 +688,15 @@ void NlsImpl::stage_failure() {
   throw Error(NOSH_ERR_CUDA,
               "an SpMV staging copy did not complete within its wait bound: the results of this call are "
               "invalid (the handle stays usable)");
+}
+
+void NlsImpl::check_indices() {
+  if (d_check.n == 0) d_check.alloc(1);
+  check_graph(N, 2 * E, mesh->d_rp.p, mesh->d_ci.p, d_check.p, stream);
+  unsigned long long w = 0;
+  d_check.download(&w, 1, stream);
+  sync();
+  report_graph_error(w);
 }
 
 void NlsImpl::set_stage_wait_limit(int64_t polls) {
