@@ -311,8 +311,8 @@ def run_reference(args):
         "data": "synthetic",
         # what this arm runs: the plain (secant) predictor in FP64, as the
         # reference's LOCA "Secant" predictor with Belos MINRES does
-        "config": workload(args) | {"precision": "fp64", "predictor": "secant",
-                                    "solver": "CPU restatement (oracle/nosh_solver.c)"},
+        "config": {k: v for k, v in workload(args).items() if k != "infer_period"}
+        | {"precision": "fp64", "predictor": "secant", "solver": "CPU restatement (oracle/nosh_solver.c)"},
         "cpu_baseline": {"value": val, "unit": "steps/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))],
