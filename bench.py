@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--infer-period", type=int, default=8,
                     help="after training, re-infer the learned coefficient every this many steps (a sweep at "
                          "64^3: 1, 2, 4, 8 gave 509, 559, 588, 603 steps/s at the same 6.4 MINRES iterations)")
+    ap.add_argument("--forcing-aim", type=float, default=0.5,
+                    help="fraction of the tolerance a Newton step's forcing term aims at")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end line through the C ABI")
@@ -107,6 +109,7 @@ def workload(args):
         "precision": args.precision,
         "predictor": args.predictor,
         "infer_period": args.infer_period,
+        "forcing_aim": args.forcing_aim,
     }
 
 
@@ -311,7 +314,7 @@ def run_reference(args):
         "data": "synthetic",
         # what this arm runs: the plain (secant) predictor in FP64, as the
         # reference's LOCA "Secant" predictor with Belos MINRES does
-        "config": {k: v for k, v in workload(args).items() if k != "infer_period"}
+        "config": {k: v for k, v in workload(args).items() if k not in ("infer_period", "forcing_aim")}
         | {"precision": "fp64", "predictor": "secant", "solver": "CPU restatement (oracle/nosh_solver.c)"},
         "cpu_baseline": {"value": val, "unit": "steps/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -341,6 +344,7 @@ def run_gb300(args):
     gm = ng.mesh(x, cells)
     prec = ng.PREC_MIXED if args.precision == "mixed" else ng.PREC_FP64
     model = ng.nls(gm, A, -1.0, 1.0, 1.0, mu=args.mu0, precision=prec)
+    model.set_forcing_aim(args.forcing_aim)
     stream = torch.cuda.ExternalStream(model.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
 

@@ -170,6 +170,13 @@ int nosh_nls_amg_levels(nosh_nls nls, int *num_levels, int64_t *sizes,
 #define NOSH_SPMV_STAGED 1
 #define NOSH_SPMV_WARP 2
 int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule);
+/* Newton's forcing (no counterpart in the reference, whose NOX forcing is
+ * constant, examples/conf.xml:81): the Eisenstat-Walker term is never tighter
+ * than what reaches the target in one step, eta >= aim * target / ||F||;
+ * `aim` in (0, 1] is the fraction of the target a step aims at (default
+ * 0.5; a larger aim takes fewer Krylov iterations per step and risks a
+ * second Newton step). */
+int nosh_nls_set_forcing_aim(nosh_nls nls, double aim);
 /* Diagnostics (no counterpart in the reference, whose Tpetra SpMV has no
  * bounded wait): the bound, in mbarrier polls, of the waits of the staged
  * SpMV schedule for the copies of its matrix rows into shared memory; the

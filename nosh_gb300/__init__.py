@@ -124,6 +124,7 @@ _SIGS = {
     "nosh_nls_set_stage_wait_limit": (_I, [_P, _I64]),
     "nosh_diag_stream_read": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_set_index_checks": (_I, [_P, _I]),
+    "nosh_nls_set_forcing_aim": (_I, [_P, _D]),
     "nosh_graph_check": (_I, [_I64, _I64, _P, _P, _P]),
     "nosh_nls_amg_levels": (_I, [_P, C.POINTER(_I), _P, _I, C.POINTER(_I)]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
@@ -457,6 +458,11 @@ class nls:
     def set_spmv_schedule(self, schedule):
         """SPMV_AUTO, SPMV_STAGED or SPMV_WARP (see nosh_gb300.h)."""
         _check(_lib.nosh_nls_set_spmv_schedule(self._h, schedule))
+
+    def set_forcing_aim(self, aim):
+        """Fraction of the Newton target a step's forcing term aims at
+        (default 0.5; see nosh_nls_set_forcing_aim)."""
+        _check(_lib.nosh_nls_set_forcing_aim(self._h, float(aim)))
 
     def set_index_checks(self, enable=True):
         """Index-check mode: the KEO graph is validated on the device before

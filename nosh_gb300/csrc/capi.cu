@@ -420,6 +420,13 @@ int nosh_graph_check(int64_t num_vertices, int64_t nnz, const int32_t *row_ptr, 
   });
 }
 
+int nosh_nls_set_forcing_aim(nosh_nls nls, double aim) {
+  return guarded([&] {
+    require(aim > 0.0 && aim <= 1.0, "the forcing aim must lie in (0, 1]");
+    N(nls).forcing_aim = aim;
+  });
+}
+
 int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls) {
   return guarded([&] { N(nls).set_stage_wait_limit(polls); });
 }

@@ -137,6 +137,9 @@ struct NlsImpl {
   // preconditioner options (amg.cuh AmgOptions), applied when the hierarchy
   // is next built
   int amg_max_levels = 10, amg_coarse_size = 64, amg_smooth_degree = 2, amg_reuse_period = 8;
+  // the fraction of the Newton target a step's forcing term aims at when the
+  // target bounds it (eta >= forcing_aim * target / ||F||)
+  double forcing_aim = 0.5;
   double amg_theta = 0.0, amg_cheb_ratio = 15.0;
   KernelTimer timers[2];  // NOSH_KERNEL_JACOBIAN, NOSH_KERNEL_SMOOTHER
   mutable int64_t launch_count = 0;  // kernels launched by this handle

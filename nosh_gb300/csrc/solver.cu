@@ -457,7 +457,7 @@ template <typename T> static DevBuf<T> &rhs_of(NewtonState &ns);
 template <> DevBuf<float> &rhs_of<float>(NewtonState &ns) { return ns.b32; }
 template <> DevBuf<double> &rhs_of<double>(NewtonState &ns) { return ns.b64; }
 
-double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn_prev, bool fp32) {
+double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn_prev, bool fp32, double aim) {
   // FP32 Krylov cannot resolve relative residuals much below ~1e-6
   const double eta_min = fp32 ? 1e-6 : 1e-12;
   double eta;
@@ -471,9 +471,9 @@ double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn
     // Newton steps)
     const double target = opt.refine > 0.0 ? opt.refine : opt.tol;
     const double ew = it == 0 ? 1e-2 : 0.9 * (fn / fn_prev) * (fn / fn_prev);
-    // (the 0.5 margin keeps a one-step target reachable when the cap is
-    // the binding term: the step's residual is about eta * fn)
-    eta = std::min(0.3, std::max(ew, 0.5 * target / fn));
+    // (the margin `aim` < 1 keeps a one-step target reachable when the cap
+    // is the binding term: the step's residual is about eta * fn)
+    eta = std::min(0.3, std::max(ew, aim * target / fn));
   }
   return std::max(eta, eta_min);
 }
@@ -519,7 +519,7 @@ static void newton_loop_systems(NlsImpl &s, NewtonState &ns, double g, double mu
     // early.  (The same term as each system's own test made the slowest
     // system of the 256-square workload take 7 Newton steps and the batch
     // 704 MINRES iterations; per-system terms, 11 Newton steps.)
-    const double eta = forcing_term(opt, it, fn, fn_prev, sizeof(T) == 4);
+    const double eta = forcing_term(opt, it, fn, fn_prev, sizeof(T) == 4, s.forcing_aim);
     int status = 0;
     st.krylov_iters += mr.solve(b.p, eta, rtol, opt.max_krylov, its, status);
     for (int64_t q = 0; q < S; q++)
@@ -572,7 +572,7 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
     if (!s.sys_off.empty()) s.mask_converged(ns.f.p, opt.tol);
     neg_cast<T><<<G, 256, 0, s.stream>>>(n2, ns.f.p, b.p);
     ++s.launch_count;
-    const double eta = forcing_term(opt, it, fn, fn_prev, sizeof(T) == 4);
+    const double eta = forcing_term(opt, it, fn, fn_prev, sizeof(T) == 4, s.forcing_aim);
     int status = 0;
     double rel = 0.0;
     const int its = mr.solve(b.p, eta, opt.max_krylov, status, rel);

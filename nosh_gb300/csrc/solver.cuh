@@ -110,7 +110,8 @@ void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_ne
 
 // Relative MINRES tolerance of Newton step `it` (fixed forcing, else
 // safeguarded Eisenstat-Walker), floored at what the Krylov precision resolves.
-double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn_prev, bool fp32);
+double forcing_term(const nosh_newton_options &opt, int it, double fn, double fn_prev, bool fp32,
+                    double aim = 0.5);
 
 // J(ns.psi, g, mu) x = rhs (2N reals, FP64 in/out) by preconditioned MINRES
 // in `precision`; rebuilds the operators at (ns.psi, mu) when asked.
