@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5, help="untimed continuation steps before them")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"],
                     help="reference: the FP64 CPU restatement on the host cores")
-    ap.add_argument("--workload", default="cont64", choices=["cont64", "batched256", "cont48"],
+    ap.add_argument("--workload", default="cont64", choices=["cont64", "batched256", "cont48", "solve65", "solve64"],
                     help="cont64: the headline (64^3 continuation); batched256: 256 independent squares "
                          "(systems/s, sharded over ranks); cont48: 48^3 continuation, mu 0 -> 1 in 200 steps "
                          "with the learned predictor trained on the first 40")
@@ -885,11 +885,150 @@ def run_cont48_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# ----------------------------------------------------- single Newton solves
+SOLVE_METRIC = "Newton solves/s from psi0 to ||F||<=1e-10"
+SOLVES = {"solve65": ("jittered 65x65 unit square (seed 1), mu=0.1", 0.1),
+          "solve64": ("jittered 64^3 Kuhn-tet unit cube (seed 2), mu=0.5", 0.5)}
+
+
+def solve_mesh(args):
+    from nosh_gb300 import meshgen
+
+    return meshgen.square(65, 1) if args.workload == "solve65" else meshgen.cube(64, 2)
+
+
+def solve_workload(args):
+    desc, mu = SOLVES[args.workload]
+    return {"workload": f"one Newton solve on the {desc}, A=1/2(-y,x,0), V=-1, g=1, psi0=1+noise, "
+                        "AMG-preconditioned MINRES, to ||F||_2<=1e-10", "mu": mu}
+
+
+def run_solve(args):
+    """Configurations 1 and 2: one step = one full Newton solve from the
+    initial state (mixed precision headline; the plain FP64 path beside it)."""
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    import nosh_gb300 as ng
+    from nosh_gb300 import meshgen
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    _, mu = SOLVES[args.workload]
+    x, cells, psi0 = solve_mesh(args)
+    model = ng.nls(ng.mesh(x, cells), meshgen.mvp_constant_curl(x), -1.0, 1.0, 1.0, mu=mu)
+    stream = torch.cuda.ExternalStream(model.stream(), device=dev)
+    x0 = torch.tensor(psi0, dtype=torch.float64, device=dev)
+    xd = torch.empty_like(x0)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+
+    launches = [0]
+
+    def timed(precision, host):
+        ts, its = [], None
+        h = np.empty(psi0.size)
+        for k in range(args.warmup + args.steps):
+            if k == args.warmup:
+                model.profile_read(ng.KERNEL_ALL)
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            if host:
+                h[:] = psi0
+                st = model.newton(h, {"mu": mu}, precision=precision)
+                dt = time.perf_counter() - t0
+            else:
+                xd.copy_(x0)
+                e0.record(stream)
+                st = model.newton(xd, {"mu": mu}, precision=precision)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                dt = e0.elapsed_time(e1) / 1000.0
+            assert st["status"] == 0 and st["f_norm"] <= 1e-10, st
+            if k >= args.warmup:
+                ts.append(dt)
+                its = [st["newton_iters"], st["krylov_iters"]]
+        launches[0] = model.profile_read(ng.KERNEL_ALL)[0]
+        return float(np.mean(ts)), its
+
+    t_mixed, it_mixed = timed(ng.PREC_MIXED, False)
+    launches_mixed = launches[0]
+    t_fp64, it_fp64 = timed(ng.PREC_FP64, False)
+    t_e2e, _ = timed(ng.PREC_MIXED, True)
+    clk = clocks.stop()
+    out = {"metric": SOLVE_METRIC, "value": world / t_mixed, "unit": "solves/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_mixed, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "config": solve_workload(args) | {"l2": "flushed (256 MB write) before every timed solve",
+                                             "parallelism": f"replicas x{world}"},
+           "newton_krylov": it_mixed,
+           "plain_fp64": {"value": world / t_fp64, "ms_per_step": 1000.0 * t_fp64, "newton_krylov": it_fp64},
+           "e2e": {"value": world / t_e2e, "unit": "solves/s", "ms_per_step": 1000.0 * t_e2e,
+                   "h2d_bytes_per_step": int(psi0.size * 8), "d2h_bytes_per_step": int(psi0.size * 8),
+                   "note": "nosh_newton_solve on a host state: the library copies it in and out"},
+           "gpu_launches": int(launches_mixed), "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, thr, cits = cpu_solve(args)
+        out["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": thr, "kind": "port",
+                               "sample": f"the same solve, FP64 CPU restatement, {thr} OpenMP threads "
+                                         f"(Newton / MINRES {cits})"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_solve(args, reps=None):
+    from nosh_gb300 import meshgen
+    from oracle import oracle as O
+
+    _, mu = SOLVES[args.workload]
+    x, cells, psi0 = solve_mesh(args)
+    m = O.finish_mesh(x, cells)
+    S = O.CpuSolver(O.Problem(m, meshgen.mvp_constant_curl(m.x)))
+    ts, its = [], None
+    t_start = time.perf_counter()
+    while len(ts) < (reps or 1000) and (not ts or time.perf_counter() - t_start < args.cpu_seconds):
+        psi = psi0.copy()
+        t0 = time.perf_counter()
+        st = S.newton(psi, mu, tol=1e-10)
+        ts.append(time.perf_counter() - t0)
+        assert st["status"] == 0, st
+        its = [st["newton_iters"], st["krylov_iters"]]
+    return 1.0 / float(np.mean(ts)), S.threads(), its
+
+
+def run_solve_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    v, thr, its = cpu_solve(args)
+    out = {"impl": "reference", "metric": SOLVE_METRIC, "value": v, "unit": "solves/s", "n_gpus": world,
+           "steps": 1, "warmup": 0, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": solve_workload(args) | {"precision": "fp64", "solver": "CPU restatement (oracle/nosh_solver.c)"},
+           "cpu_baseline": {"value": v, "unit": "solves/s", "cores": thr, "kind": "port",
+                            "sample": f"the same solve, bounded to {args.cpu_seconds} s (Newton / MINRES {its})"},
+           "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.train_iters is None:
         args.train_iters = 2 if args.workload == "cont48" else 10
-    if args.workload == "batched256":
+    if args.workload in SOLVES:
+        run_solve_reference(args) if args.impl == "reference" else run_solve(args)
+    elif args.workload == "batched256":
         run_batched_reference(args) if args.impl == "reference" else run_batched(args)
     elif args.workload == "cont48":
         run_cont48_reference(args) if args.impl == "reference" else run_cont48(args)
