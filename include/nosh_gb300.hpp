@@ -271,6 +271,10 @@ class nls {
 
   nosh_nls handle() const { return h_; }
   void set_precision(int p) { check(nosh_nls_set_precision(h_, p)); }
+  // device-side validation of every graph index before each launch
+  void set_index_checks(bool on) { check(nosh_nls_set_index_checks(h_, on ? 1 : 0)); }
+  // the fraction of the tolerance a Newton step's forcing term aims at
+  void set_forcing_aim(double aim) { check(nosh_nls_set_forcing_aim(h_, aim)); }
   int precision() const {
     int p = 0;
     check(nosh_nls_get_precision(h_, &p));
@@ -388,6 +392,19 @@ class run {
     double t = 0.0, th = 0.0;
     check(nosh_continuation_tangent(h_, &t, &th));
     return t;
+  }
+  // the learned predictor (NOSH_PREDICT_LEARNED): online training window,
+  // then overlapped inference every `period`-th learned step
+  void learning(int train_steps, int iters_per_step, double learning_rate) {
+    check(nosh_continuation_learning(h_, train_steps, iters_per_step, learning_rate));
+  }
+  void inference_period(int period) { check(nosh_continuation_inference_period(h_, period)); }
+  // ||F|| at mu_new of the secant, quadratic, cubic and learned predictions
+  // from the current history (NaN where one is not available)
+  std::array<double, 4> predictor_residuals(double mu_new) const {
+    std::array<double, 4> r{};
+    check(nosh_continuation_predictor_residuals(h_, mu_new, r.data()));
+    return r;
   }
 
  private:

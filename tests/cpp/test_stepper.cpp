@@ -231,6 +231,20 @@ static void gpu_checks() {
     CHECK(std::fgets(l0, sizeof l0, f) && std::strncmp(l0, "# (0) step", 10) == 0);
     std::fclose(f);
   }
+  // the predictors' residuals from a four-state history: every one finite,
+  // the extrapolations below the secant on this smooth branch
+  {
+    cont::run r(model, x, 0.0);
+    r.learning(4, 2, 1e-3);
+    r.inference_period(2);
+    model.set_forcing_aim(0.5);
+    nosh_newton_options o;
+    nosh_newton_default_options(&o);
+    for (int k = 1; k <= 4; k++) CHECK(r.advance(0.01 * k, NOSH_PREDICT_SECANT, o).status == NOSH_OK);
+    const auto res = r.predictor_residuals(0.05);
+    for (double v : res) CHECK(std::isfinite(v) && v > 0.0);
+    CHECK(res[1] < res[0] && res[2] < res[0]);
+  }
 }
 
 int main(int argc, char **argv) {
