@@ -81,6 +81,8 @@ def parse():
                          "64^3: 1, 2, 4, 8 gave 509, 559, 588, 603 steps/s at the same 6.4 MINRES iterations)")
     ap.add_argument("--forcing-aim", type=float, default=0.5,
                     help="fraction of the tolerance a Newton step's forcing term aims at")
+    ap.add_argument("--launch-overlap", type=int, default=1, choices=[0, 1],
+                    help="programmatic dependent launch of the MINRES/V-cycle kernels (1, the library default)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end line through the C ABI")
@@ -110,6 +112,7 @@ def workload(args):
         "predictor": args.predictor,
         "infer_period": args.infer_period,
         "forcing_aim": args.forcing_aim,
+        "launch_overlap": bool(args.launch_overlap),
     }
 
 
@@ -314,7 +317,7 @@ def run_reference(args):
         "data": "synthetic",
         # what this arm runs: the plain (secant) predictor in FP64, as the
         # reference's LOCA "Secant" predictor with Belos MINRES does
-        "config": {k: v for k, v in workload(args).items() if k not in ("infer_period", "forcing_aim")}
+        "config": {k: v for k, v in workload(args).items() if k not in ("infer_period", "forcing_aim", "launch_overlap")}
         | {"precision": "fp64", "predictor": "secant", "solver": "CPU restatement (oracle/nosh_solver.c)"},
         "cpu_baseline": {"value": val, "unit": "steps/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -345,6 +348,7 @@ def run_gb300(args):
     prec = ng.PREC_MIXED if args.precision == "mixed" else ng.PREC_FP64
     model = ng.nls(gm, A, -1.0, 1.0, 1.0, mu=args.mu0, precision=prec)
     model.set_forcing_aim(args.forcing_aim)
+    model.set_launch_overlap(bool(args.launch_overlap))
     stream = torch.cuda.ExternalStream(model.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
 
@@ -461,8 +465,9 @@ def run_gb300(args):
                        "and reads the new state back"}
 
     # roofline: extra steps of the same workload with CUDA events around every
-    # fine-level SpMV launch (events disable graph replay, so these steps are
-    # kept out of the timed regions above)
+    # fine-level SpMV launch (event-record nodes in the replayed MINRES
+    # graphs, one graph part per convergence poll; kept out of the timed
+    # regions above)
     prof = run("secant", max(3, args.steps // 2), 2, profile=True)
     peak, peak_kind = measured_peak()
     traffic = profiled_traffic()
@@ -482,8 +487,10 @@ def run_gb300(args):
                                "the step (--cache-control none): the working set stays in L2 between "
                                "launches, so DRAM moves far fewer bytes than the algorithmic count"
                                + ("" if args.m == 64 else "; scaled to this launch by its algorithmic bytes"),
-             "timing": "CUDA events around each launch on the library stream, during extra continuation "
-                       "steps of the same workload run after the timed ones"}
+             "timing": "CUDA events around each launch on the library stream (event-record nodes of the "
+                       "replayed MINRES graphs), during extra continuation steps of the same workload run "
+                       "after the timed ones; launches that did no work (after convergence inside a "
+                       "captured graph part) are not counted"}
         if name == dom:
             roof = d
         else:

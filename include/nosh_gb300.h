@@ -177,6 +177,14 @@ int nosh_nls_set_spmv_schedule(nosh_nls nls, int schedule);
  * 0.5; a larger aim takes fewer Krylov iterations per step and risks a
  * second Newton step). */
 int nosh_nls_set_forcing_aim(nosh_nls nls, double aim);
+/* Launch overlap (no counterpart in the reference): the kernels of a MINRES
+ * iteration and of the V-cycle are launched with programmatic stream
+ * serialisation, so each one is scheduled as its predecessor's CTAs exit,
+ * before that kernel's completion is signalled, and waits on the device for
+ * its predecessor's results before it reads them.  On by default; 0
+ * launches them one after the other (for timing comparisons).  Drops the
+ * preconditioner hierarchy and the captured MINRES graphs. */
+int nosh_nls_set_launch_overlap(nosh_nls nls, int enable);
 /* Diagnostics (no counterpart in the reference, whose Tpetra SpMV has no
  * bounded wait): the bound, in mbarrier polls, of the waits of the staged
  * SpMV schedule for the copies of its matrix rows into shared memory; the
@@ -474,8 +482,12 @@ int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const double *gram,
 #define NOSH_KERNEL_SMOOTHER 1 /* fine-level AMG smoothing/residual SpMVs  */
 #define NOSH_KERNEL_ALL 2      /* every kernel the handle launched (count
                                   only; always on)                         */
-/* While enabled, every launch of the selected fine-level SpMV kernels is
- * bracketed by CUDA events on the handle's stream. */
+/* While enabled, every launch of the fine-level SpMV kernels is bracketed
+ * by CUDA events on the handle's stream.  Inside a MINRES solve the launches
+ * run from its captured graphs (captured anew when timing is switched), the
+ * events are event-record nodes of those graphs, and only the launches that
+ * did work are counted (not those that return at once after convergence
+ * inside a captured part). */
 int nosh_nls_profile_enable(nosh_nls nls, int enable);
 /* Launch count, summed device time and summed algorithmic bytes (the bytes
  * the kernel must move at minimum: matrix, indices and vectors once each)

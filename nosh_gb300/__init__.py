@@ -125,6 +125,7 @@ _SIGS = {
     "nosh_diag_stream_read": (_I, [_P, _I64, _P, _P]),
     "nosh_nls_set_index_checks": (_I, [_P, _I]),
     "nosh_nls_set_forcing_aim": (_I, [_P, _D]),
+    "nosh_nls_set_launch_overlap": (_I, [_P, _I]),
     "nosh_graph_check": (_I, [_I64, _I64, _P, _P, _P]),
     "nosh_nls_amg_levels": (_I, [_P, C.POINTER(_I), _P, _I, C.POINTER(_I)]),
     "nosh_nls_set_systems": (_I, [_P, _I64, _P, _P]),
@@ -463,6 +464,12 @@ class nls:
         """Fraction of the Newton target a step's forcing term aims at
         (default 0.5; see nosh_nls_set_forcing_aim)."""
         _check(_lib.nosh_nls_set_forcing_aim(self._h, float(aim)))
+
+    def set_launch_overlap(self, enable=True):
+        """Overlapped launches of the MINRES iteration and V-cycle kernels
+        (programmatic dependent launch; on by default; see
+        nosh_nls_set_launch_overlap)."""
+        _check(_lib.nosh_nls_set_launch_overlap(self._h, 1 if enable else 0))
 
     def set_index_checks(self, enable=True):
         """Index-check mode: the KEO graph is validated on the device before

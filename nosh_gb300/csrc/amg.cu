@@ -366,6 +366,7 @@ template <typename T>
 __global__ void cheb_first(int64_t n, const T *__restrict__ dinv, const T *__restrict__ coef,
                            const C2<T> *__restrict__ b, C2<T> *__restrict__ d,
                            C2<T> *__restrict__ x) {
+  dep_sync();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   cheb_first_elem<T>(i, dinv, coef[0], b[i], d, x);
@@ -379,6 +380,7 @@ __global__ void lanczos_first(int64_t n, const MinresScalars *__restrict__ s,
                               const C2<T> *__restrict__ u, C2<T> *__restrict__ r_old,
                               const C2<T> *__restrict__ r_cur, const T *__restrict__ dinv,
                               const T *__restrict__ coef, C2<T> *__restrict__ d, C2<T> *__restrict__ x) {
+  dep_sync();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n || s->done >= 2) return;
   const T *la = lanczos_coef<T>(s);
@@ -451,6 +453,7 @@ template <typename T>
 __global__ void restrict_kernel(int64_t na, const int32_t *__restrict__ mptr,
                                 const int32_t *__restrict__ midx, const C2<T> *__restrict__ r,
                                 C2<T> *__restrict__ rc, const int *halt) {
+  dep_sync();
   const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (a >= na || (halt && *halt >= 2)) return;
   T sr = 0, si = 0;
@@ -469,6 +472,7 @@ __global__ void restrict_first(int64_t na, const int32_t *__restrict__ mptr,
                                C2<T> *__restrict__ rc, const T *__restrict__ dinv,
                                const T *__restrict__ coef, C2<T> *__restrict__ d,
                                C2<T> *__restrict__ x, const int *halt) {
+  dep_sync();
   const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (a >= na || (halt && *halt >= 2)) return;
   T sr = 0, si = 0;
@@ -485,6 +489,7 @@ __global__ void restrict_first(int64_t na, const int32_t *__restrict__ mptr,
 template <typename T>
 __global__ void prolong_kernel(int64_t n, const int32_t *__restrict__ agg,
                                const C2<T> *__restrict__ xc, C2<T> *__restrict__ x, const int *halt) {
+  dep_sync();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n || (halt && *halt >= 2)) return;
   const C2<T> c = xc[agg[i]];
@@ -618,6 +623,7 @@ __device__ __forceinline__ T dense_row(const DenseMap &D, const T *__restrict__ 
 template <typename T>
 __global__ void dense_matvec(int m, const T *__restrict__ Ainv, DenseMap D, const T *__restrict__ b,
                              T *__restrict__ x) {
+  dep_sync();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
     x[i] = dense_row(D, Ainv, i, b);
 }
@@ -753,6 +759,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restrict__ lv, int lt, int L,
                                                     int deg, const T *__restrict__ Ainv, DenseMap D,
                                                     const int *halt) {
+  dep_sync();
   if (halt && *halt >= 2) return;
   tail_body(lv, lt, L, deg, Ainv, D);
 }
@@ -761,6 +768,7 @@ __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restri
 template <typename T>
 __global__ void lanczos_only(int64_t n, const MinresScalars *__restrict__ s, const C2<T> *__restrict__ u,
                              C2<T> *__restrict__ r_old, const C2<T> *__restrict__ r_cur) {
+  dep_sync();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const T *la = lanczos_coef<T>(s);
@@ -772,6 +780,7 @@ __global__ void lanczos_only(int64_t n, const MinresScalars *__restrict__ s, con
 template <typename T>
 __global__ void dot_advance(int64_t n, const C2<T> *__restrict__ a, const C2<T> *__restrict__ b,
                             double *partials, unsigned *counter, MinresScalars *s) {
+  dep_sync();
   double v = 0.0;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) v = (double)a[i].x * b[i].x + (double)a[i].y * b[i].y;
@@ -845,6 +854,9 @@ struct Amg::Impl {
   // launches return at once once the solve has converged
   const int *halt = nullptr;
   template <typename T> void prime();
+  // V-cycle launches overlap their predecessors (launch_dep) unless the
+  // handle turned that off or times kernels with events between launches
+  bool ovl() const { return nls.overlap_launches && !nls.timers[0].on && !nls.timers[1].on; }
 };
 
 template <> AmgVals<float> &Amg::Impl::vals<float>() { return vf; }
@@ -1145,7 +1157,7 @@ void Amg::Impl::rows(int l, const C2<T> *x, const Op &op) {
   const int cap = sizeof(T) == 4 ? A.cap32 : A.cap64;
   const bool warp = l == 0 ? (sizeof(T) == 4 ? nls.warp32 : nls.warp64) : (sizeof(T) == 4 ? A.warp32 : A.warp64);
   launch_spmv<T, Op>(warp, (int)A.n, A.rp, A.ci, off<T>(l), x, cap, op, nls.red.partials.p, nls.red.counter.p,
-                     Op::kReduce ? &nls.red.out.p[32] : nullptr, nls.stream);
+                     Op::kReduce ? &nls.red.out.p[32] : nullptr, nls.stream, ovl());
   ++nls.launch_count;
 }
 
@@ -1183,19 +1195,21 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     // restriction + first step of level l+1, whose pre-smoothing must end in
     // its x buffer
     C2<T> *first = (deg % 2 == 1) ? V.x[l + 1].p : V.x2[l + 1].p;
-    restrict_first<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
-                                                      V.b[l + 1].p, V.dinv[l + 1].p, V.coef[l + 1].p,
-                                                      V.d[l + 1].p, first, halt);
+    launch_dep(ovl(), restrict_first<T>, dim3(div_up(Cl.n, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
+               A.mem_idx.p, V.res[l].p, V.b[l + 1].p, V.dinv[l + 1].p, V.coef[l + 1].p, V.d[l + 1].p, first,
+               halt);
     ++nls.launch_count;
     descend_ascend<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p, nullptr);
   } else {
-    restrict_kernel<T><<<div_up(Cl.n, B), B, 0, st>>>(Cl.n, A.mem_ptr.p, A.mem_idx.p, V.res[l].p,
-                                                       V.b[l + 1].p, halt);
+    launch_dep(ovl(), restrict_kernel<T>, dim3(div_up(Cl.n, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
+               A.mem_idx.p, V.res[l].p, V.b[l + 1].p, halt);
     ++nls.launch_count;
-    tail_vcycle<T><<<1, 1024, 0, st>>>(V.desc.p, lt, L, deg, dense_inv<T>(), dmap(), halt);
+    launch_dep(ovl(), tail_vcycle<T>, dim3(1), dim3(1024), 0, st, V.desc.p, lt, L, deg, dense_inv<T>(), dmap(),
+               halt);
     ++nls.launch_count;
   }
-  prolong_kernel<T><<<div_up(A.n, B), B, 0, st>>>(A.n, A.agg.p, V.x[l + 1].p, x, halt);
+  launch_dep(ovl(), prolong_kernel<T>, dim3(div_up(A.n, B)), dim3(B), 0, st, A.n, A.agg.p, V.x[l + 1].p, x,
+             halt);
   ++nls.launch_count;
   cur = x;
   oth = V.x2[l].p;
@@ -1226,15 +1240,16 @@ void Amg::apply(const T *r, T *z) {
   const AmgLevel &A = I.lev[0];
   if (L == 1) {
     const int m2 = (int)(2 * A.n);
-    dense_matvec<T><<<div_up(m2, 128), 128, 0, st>>>(m2, I.dense_inv<T>(), I.dmap(), r, z);
+    launch_dep(I.ovl(), dense_matvec<T>, dim3(div_up(m2, 128)), dim3(128), 0, st, m2, I.dense_inv<T>(), I.dmap(),
+               r, z);
     ++I.nls.launch_count;
     NOSH_CUDA(cudaGetLastError());
     return;
   }
   const int deg = std::max(I.opt.smooth_degree, 1);
   C2<T> *first = (deg % 2 == 1) ? (C2<T> *)z : V.x2[0].p;
-  cheb_first<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, V.dinv[0].p, V.coef[0].p, (const C2<T> *)r,
-                                                  V.d[0].p, first);
+  launch_dep(I.ovl(), cheb_first<T>, dim3(div_up(A.n, 256)), dim3(256), 0, st, A.n, V.dinv[0].p, V.coef[0].p,
+             (const C2<T> *)r, V.d[0].p, first);
   ++I.nls.launch_count;
   I.descend_ascend<T>(0, (const C2<T> *)r, (C2<T> *)z, nullptr);
   NOSH_CUDA(cudaGetLastError());
@@ -1252,8 +1267,8 @@ void Amg::presmooth(const T *b, T *x) {
   const int deg = std::max(I.opt.smooth_degree, 1);
   C2<T> *cur = (deg % 2 == 1) ? (C2<T> *)x : V.x2[0].p;
   C2<T> *oth = (deg % 2 == 1) ? V.x2[0].p : (C2<T> *)x;
-  cheb_first<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, V.dinv[0].p, V.coef[0].p, (const C2<T> *)b, V.d[0].p,
-                                                  cur);
+  launch_dep(I.ovl(), cheb_first<T>, dim3(div_up(A.n, 256)), dim3(256), 0, st, A.n, V.dinv[0].p, V.coef[0].p,
+             (const C2<T> *)b, V.d[0].p, cur);
   ++I.nls.launch_count;
   for (int k = 1; k < deg; k++) {
     ChebOp<T> op{I.dia<T>(0), V.dinv[0].p, V.coef[0].p, k, (const C2<T> *)b, cur, V.d[0].p, oth, nullptr};
@@ -1274,11 +1289,11 @@ void Amg::apply_minres(MinresScalars *ms, const T *u, T *r_old, const T *r_cur, 
   const int L = (int)I.lev.size();
   const AmgLevel &A = I.lev[0];
   if (L == 1) {
-    lanczos_only<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, ms, (const C2<T> *)u, (C2<T> *)r_old,
-                                                      (const C2<T> *)r_cur);
+    launch_dep(I.ovl(), lanczos_only<T>, dim3(div_up(A.n, 256)), dim3(256), 0, st, A.n, ms, (const C2<T> *)u,
+               (C2<T> *)r_old, (const C2<T> *)r_cur);
     apply<T>(r_old, z_out);
-    dot_advance<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, (const C2<T> *)r_old, (const C2<T> *)z_out,
-                                                     I.nls.red.partials.p, I.nls.red.counter.p, ms);
+    launch_dep(I.ovl(), dot_advance<T>, dim3(div_up(A.n, 256)), dim3(256), 0, st, A.n, (const C2<T> *)r_old,
+               (const C2<T> *)z_out, I.nls.red.partials.p, I.nls.red.counter.p, ms);
     I.nls.launch_count += 2;
     NOSH_CUDA(cudaGetLastError());
     return;
@@ -1286,9 +1301,8 @@ void Amg::apply_minres(MinresScalars *ms, const T *u, T *r_old, const T *r_cur, 
   const int deg = std::max(I.opt.smooth_degree, 1);
   // the fine level's right-hand side is r_new itself: point b[0] at r_old
   C2<T> *first = (deg % 2 == 1) ? (C2<T> *)z_out : V.x2[0].p;
-  lanczos_first<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, ms, (const C2<T> *)u, (C2<T> *)r_old,
-                                                     (const C2<T> *)r_cur, V.dinv[0].p, V.coef[0].p,
-                                                     V.d[0].p, first);
+  launch_dep(I.ovl(), lanczos_first<T>, dim3(div_up(A.n, 256)), dim3(256), 0, st, A.n, ms, (const C2<T> *)u,
+             (C2<T> *)r_old, (const C2<T> *)r_cur, V.dinv[0].p, V.coef[0].p, V.d[0].p, first);
   ++I.nls.launch_count;
   I.halt = &ms->done;
   I.descend_ascend<T>(0, (const C2<T> *)r_old, (C2<T> *)z_out, ms);

@@ -427,6 +427,15 @@ int nosh_nls_set_forcing_aim(nosh_nls nls, double aim) {
   });
 }
 
+int nosh_nls_set_launch_overlap(nosh_nls nls, int enable) {
+  return guarded([&] {
+    auto &s = N(nls);
+    require(enable == 0 || enable == 1, "enable must be 0 or 1");
+    s.overlap_launches = enable == 1;
+    nosh::reset_preconditioner(s);
+  });
+}
+
 int nosh_nls_set_stage_wait_limit(nosh_nls nls, int64_t polls) {
   return guarded([&] { N(nls).set_stage_wait_limit(polls); });
 }

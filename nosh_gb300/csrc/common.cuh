@@ -7,6 +7,7 @@
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "nosh_gb300.h"
@@ -130,6 +131,28 @@ __global__ void history_dots(int64_t n, const double *x0, const double *x1, cons
                              const double *x4, int count, double *partials, unsigned *counter, double *out);
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// Launch a kernel, with programmatic stream serialisation when `overlap` is
+// set: the kernel's CTAs may then be scheduled as soon as the previous
+// kernel's CTAs have exited, before that kernel's completion is signalled,
+// and run up to their dev::dep_sync(), which returns once it has completed
+// and its writes are visible.  Only kernels that call dep_sync() before
+// touching memory the previous kernel writes may be launched with overlap.
+template <typename... P, typename... Args>
+void launch_dep(bool overlap, void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = overlap ? 1 : 0;
+  NOSH_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
 }  // namespace nosh
 
 // ----------------------------------------------------- device-side helpers
@@ -139,6 +162,18 @@ namespace dev {
 template <typename T> struct C2;  // complex pair (interleaved storage)
 template <> struct alignas(8) C2<float> { float x, y; };
 template <> struct alignas(16) C2<double> { double x, y; };
+
+// Programmatic dependent launch (griddepcontrol, sm_90 and later).
+// dep_sync: block until the kernel this one was launched after (with
+// overlap, see launch_dep) has completed and flushed its writes; returns at
+// once for a plain launch.  The kernels never trigger their successors
+// explicitly (griddepcontrol.launch_dependents): a successor launches as the
+// last CTA exits.  Measured on GB300 over chains of 100 graph-captured
+// kernels (16 K to 8 M elements): the implicit trigger saved 0.16-0.25 us
+// per launch against plain edges, while a trigger at the start of every CTA
+// cost up to 3.8 us per launch (the successor's waiting CTAs hold the SMs)
+// and one after the work cost up to 1.4 us.
+__device__ __forceinline__ void dep_sync() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
 // read-only-path loads of complex pairs
 __device__ __forceinline__ C2<float> ldg(const C2<float> *p) {

@@ -29,19 +29,38 @@ struct Reducer {
 struct Amg;  // aggregation AMG hierarchy (amg.cu)
 
 // Event pairs around the launches of one kernel class (roofline timing).
+// Outside stream capture the events are recorded on the stream.  Inside a
+// capture they become event-record nodes of the graph (recorded again at
+// every replay); the graph's owner takes them with take() and adds the
+// replays it wants counted with harvest() once they have completed.
 struct KernelTimer {
   bool on = false;
   std::vector<cudaEvent_t> ev;  // start, stop, start, stop, ...
   size_t used = 0;
   int64_t launches = 0;
   double bytes = 0.0;
+  double graph_ms = 0.0;  // harvested graph pairs
+  struct Pair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    double bytes = 0.0;
+  };
+  std::vector<Pair> captured;  // pairs captured since the last take()
+  Pair cap;
+  bool cap_open = false;
   static bool capturing(cudaStream_t s) {
     cudaStreamCaptureStatus c = cudaStreamCaptureStatusNone;
     return cudaStreamIsCapturing(s, &c) == cudaSuccess && c != cudaStreamCaptureStatusNone;
   }
   bool open_pair = false;
   void begin(cudaStream_t s) {
-    if (!on || capturing(s)) return;
+    if (!on) return;
+    if (capturing(s)) {
+      NOSH_CUDA(cudaEventCreate(&cap.a));
+      NOSH_CUDA(cudaEventCreate(&cap.b));
+      NOSH_CUDA(cudaEventRecordWithFlags(cap.a, s, cudaEventRecordExternal));
+      cap_open = true;
+      return;
+    }
     open_pair = true;
     if (used + 2 > ev.size()) {
       for (int k = 0; k < 2; k++) {
@@ -53,15 +72,44 @@ struct KernelTimer {
     NOSH_CUDA(cudaEventRecord(ev[used], s));
   }
   void end(cudaStream_t s, double b) {
-    if (!on || !open_pair) return;
+    if (!on) return;
+    if (cap_open) {
+      cap_open = false;
+      NOSH_CUDA(cudaEventRecordWithFlags(cap.b, s, cudaEventRecordExternal));
+      cap.bytes = b;
+      captured.push_back(cap);
+      return;
+    }
+    if (!open_pair) return;
     open_pair = false;
     NOSH_CUDA(cudaEventRecord(ev[used + 1], s));
     used += 2;
     launches++;
     bytes += b;
   }
+  std::vector<Pair> take() {
+    std::vector<Pair> v;
+    v.swap(captured);
+    return v;
+  }
+  // one completed replay of a captured pair
+  void harvest(const Pair &p) {
+    float t = 0.f;
+    NOSH_CUDA(cudaEventElapsedTime(&t, p.a, p.b));
+    graph_ms += t;
+    launches++;
+    bytes += p.bytes;
+  }
+  static void release(std::vector<Pair> &v) {
+    for (Pair &p : v) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    v.clear();
+  }
   void read(int64_t &n, double &ms, double &b) {
-    ms = 0.0;
+    ms = graph_ms;
+    graph_ms = 0.0;
     for (size_t k = 0; k < used; k += 2) {
       NOSH_CUDA(cudaEventSynchronize(ev[k + 1]));
       float t = 0.f;
@@ -76,6 +124,7 @@ struct KernelTimer {
   }
   ~KernelTimer() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    release(captured);
   }
 };
 
@@ -140,6 +189,9 @@ struct NlsImpl {
   // the fraction of the Newton target a step's forcing term aims at when the
   // target bounds it (eta >= forcing_aim * target / ||F||)
   double forcing_aim = 0.5;
+  // launches of the MINRES iteration and the V-cycle overlap their
+  // predecessors (programmatic dependent launch); off for A/B timing
+  bool overlap_launches = true;
   double amg_theta = 0.0, amg_cheb_ratio = 15.0;
   KernelTimer timers[2];  // NOSH_KERNEL_JACOBIAN, NOSH_KERNEL_SMOOTHER
   mutable int64_t launch_count = 0;  // kernels launched by this handle

@@ -165,10 +165,23 @@ Minres<T>::Minres(NlsImpl &nls) : s(nls), n2(2 * nls.N) {
 }
 
 template <typename T>
-Minres<T>::~Minres() {
-  for (cudaGraphExec_t &e : part_exec)
+void Minres<T>::drop_graphs() {
+  for (cudaGraphExec_t &e : part_exec) {
     if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
+  }
   if (pro_exec) cudaGraphExecDestroy(pro_exec);
+  pro_exec = nullptr;
+  pro_b = nullptr;
+  for (auto &part : part_ev)
+    for (auto &it : part)
+      for (auto &v : it) KernelTimer::release(v);
+  for (auto &v : pro_ev) KernelTimer::release(v);
+}
+
+template <typename T>
+Minres<T>::~Minres() {
+  drop_graphs();
   if (h_params) cudaFreeHost(h_params);
   if (h_sc) cudaFreeHost(h_sc);
   if (h_err) cudaFreeHost(h_err);
@@ -191,8 +204,11 @@ void Minres<T>::iteration(int j) {
   const T *jd = sizeof(T) == 4 ? (const T *)s.d_jd32.p : (const T *)s.d_jd64.p;
   JacMinresOp<T> op{jd, (const C2<T> *)zc, (C2<T> *)u.p, d, zn, wa, wb, wc, x.p, &d->done};
   s.timers[NOSH_KERNEL_JACOBIAN].begin(st);
+  // overlaps the previous iteration's last V-cycle launch (the KEO values
+  // were assembled before the solve)
+  const bool overlap = s.overlap_launches && !s.timers[NOSH_KERNEL_JACOBIAN].on;
   launch_spmv<T>(sizeof(T) == 4 ? s.warp32 : s.warp64, (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val,
-                 (const C2<T> *)zc, cap, op, s.red.partials.p, s.red.counter.p, &d->zu, st);
+                 (const C2<T> *)zc, cap, op, s.red.partials.p, s.red.counter.p, &d->zu, st, overlap);
   ++s.launch_count;
   // bytes per vertex: z, diag block, u (+ the fused w/x update: z_prev, w2,
   // w, x read; w1, x written)
@@ -217,8 +233,14 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
   const int G = vec_grid(n2);
   const size_t bytes = n2 * sizeof(T);
   MinresScalars *d = sc.p;
-  // graphs are used unless kernel timing is on (event pairs per launch)
-  const bool graphs = !s.timers[NOSH_KERNEL_JACOBIAN].on;
+  // with kernel timing on, the graphs carry event-record nodes around the
+  // timed launches: captured anew when timing is switched
+  const bool timed = s.timers[NOSH_KERNEL_JACOBIAN].on || s.timers[NOSH_KERNEL_SMOOTHER].on;
+  if (timed != graphs_timed) {
+    NOSH_CUDA(cudaStreamSynchronize(st));
+    drop_graphs();
+    graphs_timed = timed;
+  }
   h_params[0] = rtol;
   h_params[1] = (double)maxit;
   NOSH_CUDA(cudaMemcpyAsync(params.p, h_params, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -234,14 +256,19 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     minres_init<<<1, 1, 0, st>>>(d, params.p);
     s.launch_count += 2;
   };
-  if (graphs) {
+  {
     if (!pro_exec || pro_b != b) {
-      if (pro_exec) NOSH_CUDA(cudaGraphExecDestroy(pro_exec));
+      if (pro_exec) {
+        NOSH_CUDA(cudaStreamSynchronize(st));
+        NOSH_CUDA(cudaGraphExecDestroy(pro_exec));
+      }
+      for (auto &v : pro_ev) KernelTimer::release(v);
       cudaGraph_t g;
       const int64_t before = s.launch_count;
       NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       prologue();
       NOSH_CUDA(cudaStreamEndCapture(st, &g));
+      for (int k = 0; k < 2; k++) pro_ev[k] = s.timers[k].take();
       pro_kernels = s.launch_count - before;
       s.launch_count = before;
       NOSH_CUDA(cudaGraphInstantiate(&pro_exec, g, 0));
@@ -250,16 +277,17 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     }
     NOSH_CUDA(cudaGraphLaunch(pro_exec, st));
     s.launch_count += pro_kernels;
-  } else {
-    prologue();
   }
   NOSH_CUDA(cudaGetLastError());
-  if (graphs && !part_exec[0]) {
+  if (!part_exec[0]) {
     for (int h = 0; h < kParts; h++) {
       cudaGraph_t g;
       const int64_t before = s.launch_count;
       NOSH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int j = h * kPart; j < (h + 1) * kPart; j++) iteration(j);
+      for (int j = h * kPart; j < (h + 1) * kPart; j++) {
+        iteration(j);
+        for (int k = 0; k < 2; k++) part_ev[h][j - h * kPart][k] = s.timers[k].take();
+      }
       NOSH_CUDA(cudaStreamEndCapture(st, &g));
       part_kernels[h] = s.launch_count - before;
       s.launch_count = before;
@@ -268,18 +296,17 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     }
   }
   auto launch_part = [&](int h) {
-    if (graphs) {
-      NOSH_CUDA(cudaGraphLaunch(part_exec[h], st));
-      s.launch_count += part_kernels[h];
-    } else {
-      for (int j = h * kPart; j < (h + 1) * kPart; j++) iteration(j);
-    }
+    NOSH_CUDA(cudaGraphLaunch(part_exec[h], st));
+    s.launch_count += part_kernels[h];
   };
   // first batch: as many parts as the previous solve used (one chunk at
-  // first)
-  int batch = last_its > 0 ? (last_its + kPart - 1) / kPart : kParts;
+  // first); one part per poll when timing, so that every replay's events
+  // are read before the part is replayed again
+  int batch = timed ? 1 : last_its > 0 ? (last_its + kPart - 1) / kPart : kParts;
   int it = 0, h = 0;
+  bool first = true;
   for (;;) {
+    const int it0 = it, h0 = h;
     for (int q = 0; q < batch; q++, h = (h + 1) % kParts, it += kPart) launch_part(h);
     batch = 1;
     NOSH_CUDA(cudaGetLastError());
@@ -288,6 +315,24 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
     NOSH_CUDA(cudaMemcpyAsync(h_err + 1, s.red.counter.p + kStageErrorSlot, sizeof(int), cudaMemcpyDeviceToHost,
                               st));
     NOSH_CUDA(cudaStreamSynchronize(st));
+    if (timed) {
+      // the launches that did work: iteration g's Jacobian apply runs unless
+      // the recurrence was frozen before it (it runs in the iteration after
+      // convergence, which applies the last w/x update), its V-cycle unless
+      // the solve converged before it (then itn <= g)
+      if (first)
+        for (int k = 0; k < 2; k++)
+          for (const auto &p : pro_ev[k]) s.timers[k].harvest(p);
+      const int jac_end = h_sc->itn + (h_sc->done ? 1 : 0);
+      for (int jj = 0; jj < kPart; jj++) {
+        const int g = it0 + jj;
+        if (g < jac_end)
+          for (const auto &p : part_ev[h0][jj][NOSH_KERNEL_JACOBIAN]) s.timers[NOSH_KERNEL_JACOBIAN].harvest(p);
+        if (g < h_sc->itn)
+          for (const auto &p : part_ev[h0][jj][NOSH_KERNEL_SMOOTHER]) s.timers[NOSH_KERNEL_SMOOTHER].harvest(p);
+      }
+    }
+    first = false;
     if (h_sc->done || h_err[1] != 0 || it >= maxit + kChunk) break;
   }
   // converged on the last issued iteration: its w/x update is still due

@@ -36,6 +36,13 @@ struct Minres {
   double *h_params = nullptr;
   int64_t part_kernels[kParts] = {};
   int last_its = 0;  // iterations of the previous solve
+  // Kernel timing (the handle's timers on): the graphs are captured with
+  // event-record nodes around the timed launches; the pairs of each
+  // iteration of each part (per timer) and of the prologue, harvested after
+  // a replay for the launches that did work
+  bool graphs_timed = false;
+  std::vector<KernelTimer::Pair> part_ev[kParts][kPart][2];
+  std::vector<KernelTimer::Pair> pro_ev[2];
   explicit Minres(NlsImpl &nls);
   ~Minres();
   // b: device vector of T (2N); returns iterations; x holds the solution
@@ -44,6 +51,7 @@ struct Minres {
  private:
   void iteration(int j);   // issue iteration j (0..kChunk-1) of a chunk
   void wx_final(int j);    // deferred w/x update of iteration j, the last issued
+  void drop_graphs();
 };
 
 // Batched independent solves: one Paige-Saunders recurrence per system

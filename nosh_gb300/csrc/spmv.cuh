@@ -116,6 +116,18 @@ __device__ __forceinline__ bool halted(const Op &op) {
     return false;
   }
 }
+// The same test before dep_sync(), read from L2: the flag only rises within
+// a solve and is reset several launches before the solve's first iteration,
+// so a true answer is final, while a false one may be stale (the kernel this
+// launch follows may have raised it without its write being visible yet).
+template <class Op>
+__device__ __forceinline__ bool halted_early(const Op &op) {
+  if constexpr (HasHalt<Op>::value) {
+    return op.halt != nullptr && __ldcg(op.halt) >= 2;
+  } else {
+    return false;
+  }
+}
 // ---- bulk-copy staging (TMA + mbarrier) ------------------------------
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -173,12 +185,11 @@ constexpr int kStageErrorSlot = 15;
 constexpr int kStageWaitSlot = 14;
 
 template <typename T, class Op>
-__global__ void __launch_bounds__(kRows)
+__global__ void __launch_bounds__(kRows, sizeof(T) == 4 ? 5 : 1)
     row_block_apply(int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                     const C2<T> *__restrict__ val, const C2<T> *__restrict__ x, int cap,
                     Op op, double *partials, unsigned *counter, double *red_out) {
   using A = typename Acc<T>::type;
-  if (halted(op)) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar[2];
   const size_t buf = stage_bytes<T>(cap);
@@ -209,6 +220,27 @@ __global__ void __launch_bounds__(kRows)
       bulk_g2s(base + (size_t)cap * sizeof(int32_t), val + ks, vb, &bar[stage]);
     }
   };
+  // The first row block's copy is issued before dep_sync(): the matrix (row
+  // pointers, column ids, values) is never written by the kernel that a
+  // launch with overlap follows, so the copy is in flight while the launch
+  // waits for that kernel's completion.
+  // row blocks blockIdx.x, + gridDim.x, ... (strided: consecutive row blocks,
+  // which share x gathers, run at the same time on different SMs; contiguous
+  // chunks per CTA measured 5 % slower at 64^3)
+  const int rb0 = blockIdx.x, rb_end = nblocks;
+  auto nxt = [&](int rb) { return rb + (int)gridDim.x; };
+  const bool skip = halted_early(op);
+  if (!skip && threadIdx.x == 0 && rb0 < rb_end) issue(rb0, 0);
+  dep_sync();
+  if (halted(op)) {
+    // let the copy issued above land before the CTA leaves
+    if (!skip && threadIdx.x == 0 && rb0 < rb_end) {
+      int ks, n;
+      range(rb0, ks, n);
+      if (n > 0 && n <= cap && !mbar_wait(&bar[0], 0u)) atomicOr(counter + kStageErrorSlot, 1u);
+    }
+    return;
+  }
   A part = 0;
   uint32_t parity[2] = {0u, 0u};
   bool ok = true;
@@ -219,12 +251,11 @@ __global__ void __launch_bounds__(kRows)
     const unsigned o = __ldcg(counter + kStageWaitSlot);
     if (o != 0u) limit = o - 1u;
   }
-  if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue(blockIdx.x, 0);
   int stage = 0;
-  for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, stage ^= 1) {
+  for (int rb = rb0; rb < rb_end; rb = nxt(rb), stage ^= 1) {
     // the other buffer was released by the barrier that ended the previous
     // iteration: start the next row block's copy into it
-    if (threadIdx.x == 0 && rb + (int)gridDim.x < nblocks) issue(rb + gridDim.x, stage ^ 1);
+    if (threadIdx.x == 0 && nxt(rb) < rb_end) issue(nxt(rb), stage ^ 1);
     int ks, n;
     range(rb, ks, n);
     const int row = rb * kRows + threadIdx.x;
@@ -233,9 +264,9 @@ __global__ void __launch_bounds__(kRows)
     const bool staged = n > 0 && n <= cap;
     cur_staged = staged;
     next_staged = false;
-    if (rb + (int)gridDim.x < nblocks) {
+    if (nxt(rb) < rb_end) {
       int ks2, n2;
-      range(rb + gridDim.x, ks2, n2);
+      range(nxt(rb), ks2, n2);
       next_staged = n2 > 0 && n2 <= cap;
     }
     const bool arrived = staged ? mbar_wait(&bar[stage], parity[stage], limit) : true;
@@ -252,22 +283,21 @@ __global__ void __launch_bounds__(kRows)
       if (staged) {
         // batches of kBatch nonzeros: all gathers of a batch are issued
         // before the first is used (rows of the mesh graph fit one batch)
+        // (the values are read from shared memory when used, so only the
+        // gathered x of a batch occupies registers)
         constexpr int kBatch = sizeof(T) == 4 ? 16 : 8;
         for (int k0 = b - ks; k0 < e - ks; k0 += kBatch) {
           const int cnt = e - ks - k0;
-          C2<T> v[kBatch], xv[kBatch];
+          C2<T> xv[kBatch];
+#pragma unroll
+          for (int u = 0; u < kBatch; u++)
+            if (u < cnt) xv[u] = ldg(x + s_col[k0 + u]);
 #pragma unroll
           for (int u = 0; u < kBatch; u++) {
             if (u < cnt) {
-              v[u] = s_val[k0 + u];
-              xv[u] = ldg(x + s_col[k0 + u]);
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < kBatch; u++) {
-            if (u < cnt) {
-              sr += v[u].x * xv[u].x - v[u].y * xv[u].y;
-              si += v[u].x * xv[u].y + v[u].y * xv[u].x;
+              const C2<T> v = s_val[k0 + u];
+              sr += v.x * xv[u].x - v.y * xv[u].y;
+              si += v.x * xv[u].y + v.y * xv[u].x;
             }
           }
         }
@@ -313,6 +343,7 @@ __global__ void __launch_bounds__(kWarpThreads)
                    const C2<T> *__restrict__ val, const C2<T> *__restrict__ x, Op op, double *partials,
                    unsigned *counter, double *red_out) {
   using A = typename Acc<T>::type;
+  dep_sync();
   if (halted(op)) return;
   const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4;
   const int nwb = (N + 31) / 32;
@@ -396,12 +427,18 @@ int row_grid(const void *kernel, size_t smem, int64_t n_rows);
 // Launch the SpMV + epilogue over an off-diagonal CSR with one of the two
 // schedules (warp: row_warp_apply, else the staged row_block_apply with
 // staging capacity cap).
+//
+// With `overlap` the launch may start while the previous kernel of the stream
+// finishes (launch_dep); the staged schedule then copies its first row block
+// before waiting for it, so the previous kernel must not write this matrix.
 template <typename T, class Op>
 void launch_spmv(bool warp, int N, const int32_t *rp, const int32_t *ci, const C2<T> *val, const C2<T> *x,
-                 int cap, const Op &op, double *partials, unsigned *counter, double *red_out, cudaStream_t st) {
+                 int cap, const Op &op, double *partials, unsigned *counter, double *red_out, cudaStream_t st,
+                 bool overlap = false) {
   if (warp) {
     const int grid = warp_grid((const void *)row_warp_apply<T, Op>, N);
-    row_warp_apply<T, Op><<<grid, kWarpThreads, 0, st>>>(N, rp, ci, val, x, op, partials, counter, red_out);
+    launch_dep(overlap, row_warp_apply<T, Op>, dim3(grid), dim3(kWarpThreads), 0, st, N, rp, ci, val, x, op,
+               partials, counter, red_out);
   } else {
     static bool attr_set = false;  // per instantiation; first call precedes any capture
     if (!attr_set) {
@@ -410,8 +447,8 @@ void launch_spmv(bool warp, int N, const int32_t *rp, const int32_t *ci, const C
       attr_set = true;
     }
     const size_t smem = 2 * stage_bytes<T>(cap);
-    row_block_apply<T, Op><<<row_grid((const void *)row_block_apply<T, Op>, smem, N), kRows, smem, st>>>(
-        N, rp, ci, val, x, cap, op, partials, counter, red_out);
+    launch_dep(overlap, row_block_apply<T, Op>, dim3(row_grid((const void *)row_block_apply<T, Op>, smem, N)),
+               dim3(kRows), smem, st, N, rp, ci, val, x, cap, op, partials, counter, red_out);
   }
   NOSH_CUDA(cudaGetLastError());
 }
