@@ -526,7 +526,7 @@ def run_gb300(args):
                                 "cold_gbs": nb / cold_us / 1e3, "warm_gbs": nb / warm_us / 1e3,
                                 "frac_of_peak_cold": nb / cold_us / 1e3 / peak,
                                 "kernel_over_cold_read": roof["achieved"] / (nb / cold_us / 1e3),
-                                "note": "nosh_diag_stream_read (16-byte streaming loads, 8 CTAs/SM) over the same "
+                                "note": "nosh_diag_stream_read (16-byte loads, 8 CTAs/SM, one atomic per CTA) over the same "
                                         "bytes, CUDA events around one launch: cold = after a 256 MB L2 flush, "
                                         "warm = L2-resident"}
         del buf

@@ -449,20 +449,40 @@ struct ResidOp {
   }
 };
 
+// Restriction: aggregate sums of the finer level's residual, a half-warp
+// per aggregate (lanes take every 16th member, then a shuffle tree), so the
+// coarse levels' few thousand aggregates spread over the whole GPU instead
+// of a few dozen CTAs each walking its members serially.
+constexpr int kAggLanes = 16;
+template <typename T>
+__device__ __forceinline__ C2<T> aggregate_sum(int64_t a, int64_t na, int li, const int32_t *__restrict__ mptr,
+                                               const int32_t *__restrict__ midx, const C2<T> *__restrict__ r) {
+  T sr = 0, si = 0;
+  if (a < na)
+    for (int32_t q = mptr[a] + li; q < mptr[a + 1]; q += kAggLanes) {
+      const C2<T> v = r[midx[q]];
+      sr += v.x;
+      si += v.y;
+    }
+#pragma unroll
+  for (int o = kAggLanes / 2; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  return C2<T>{sr, si};
+}
+
 template <typename T>
 __global__ void restrict_kernel(int64_t na, const int32_t *__restrict__ mptr,
                                 const int32_t *__restrict__ midx, const C2<T> *__restrict__ r,
                                 C2<T> *__restrict__ rc, const int *halt) {
   dep_sync();
-  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (a >= na || (halt && *halt >= 2)) return;
-  T sr = 0, si = 0;
-  for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
-    const C2<T> v = r[midx[q]];
-    sr += v.x;
-    si += v.y;
-  }
-  rc[a] = C2<T>{sr, si};
+  if (halt && *halt >= 2) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t a = t / kAggLanes;
+  const int li = (int)(t % kAggLanes);
+  const C2<T> b = aggregate_sum<T>(a, na, li, mptr, midx, r);
+  if (a < na && li == 0) rc[a] = b;
 }
 
 // restriction fused with the coarse level's first Chebyshev step
@@ -473,17 +493,15 @@ __global__ void restrict_first(int64_t na, const int32_t *__restrict__ mptr,
                                const T *__restrict__ coef, C2<T> *__restrict__ d,
                                C2<T> *__restrict__ x, const int *halt) {
   dep_sync();
-  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (a >= na || (halt && *halt >= 2)) return;
-  T sr = 0, si = 0;
-  for (int32_t q = mptr[a]; q < mptr[a + 1]; q++) {
-    const C2<T> v = r[midx[q]];
-    sr += v.x;
-    si += v.y;
+  if (halt && *halt >= 2) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t a = t / kAggLanes;
+  const int li = (int)(t % kAggLanes);
+  const C2<T> b = aggregate_sum<T>(a, na, li, mptr, midx, r);
+  if (a < na && li == 0) {
+    rc[a] = b;
+    cheb_first_elem<T>(a, dinv, coef[0], b, d, x);
   }
-  const C2<T> b{sr, si};
-  rc[a] = b;
-  cheb_first_elem<T>(a, dinv, coef[0], b, d, x);
 }
 
 template <typename T>
@@ -1195,13 +1213,13 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     // restriction + first step of level l+1, whose pre-smoothing must end in
     // its x buffer
     C2<T> *first = (deg % 2 == 1) ? V.x[l + 1].p : V.x2[l + 1].p;
-    launch_dep(ovl(), restrict_first<T>, dim3(div_up(Cl.n, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
+    launch_dep(ovl(), restrict_first<T>, dim3(div_up(Cl.n * kAggLanes, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
                A.mem_idx.p, V.res[l].p, V.b[l + 1].p, V.dinv[l + 1].p, V.coef[l + 1].p, V.d[l + 1].p, first,
                halt);
     ++nls.launch_count;
     descend_ascend<T>(l + 1, V.b[l + 1].p, V.x[l + 1].p, nullptr);
   } else {
-    launch_dep(ovl(), restrict_kernel<T>, dim3(div_up(Cl.n, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
+    launch_dep(ovl(), restrict_kernel<T>, dim3(div_up(Cl.n * kAggLanes, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
                A.mem_idx.p, V.res[l].p, V.b[l + 1].p, halt);
     ++nls.launch_count;
     launch_dep(ovl(), tail_vcycle<T>, dim3(1), dim3(1024), 0, st, V.desc.p, lt, L, deg, dense_inv<T>(), dmap(),

@@ -111,7 +111,7 @@ extern "C" int nosh_residual_norm_noalloc(int64_t num_vertices, const int32_t *r
     const int grid = div_up(num_vertices, dev::kRows);
     // cap = 0: nonzeros are read directly (no shared-memory staging), so the
     // launch needs no host-side knowledge of the row pointers
-    dev::row_block_apply<double, ResidualNormOp><<<grid, dev::kRows, 0, s>>>(
+    dev::row_block_apply<double, ResidualNormOp><<<grid, dev::block_threads<double>(), 0, s>>>(
         (int)num_vertices, row_ptr, cols, reinterpret_cast<const dev::C2<double> *>(keo_offdiag),
         reinterpret_cast<const dev::C2<double> *>(psi), 0, op, scratch + 1,
         reinterpret_cast<unsigned *>(scratch), norm);

@@ -365,7 +365,7 @@ int warp_grid(const void *kernel, int64_t n_rows) {
   return (int)std::max<int64_t>(1, std::min(blocks, cap));
 }
 
-int row_grid(const void *kernel, size_t smem, int64_t n_rows) {
+int row_grid(const void *kernel, int threads, size_t smem, int64_t n_rows) {
   static int sms = 0;
   if (sms == 0) {
     int d = 0;
@@ -373,7 +373,7 @@ int row_grid(const void *kernel, size_t smem, int64_t n_rows) {
     NOSH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d));
   }
   int per_sm = 0;
-  NOSH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRows, smem));
+  NOSH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
   const int64_t blocks = (n_rows + kRows - 1) / kRows;
   const int64_t cap = (int64_t)std::max(per_sm, 1) * sms;
   return (int)std::max<int64_t>(1, std::min(blocks, cap));
@@ -475,27 +475,29 @@ void report_graph_error(unsigned long long w) {
                                 "entry " + std::to_string(pos));
 }
 
-// Achievable-bandwidth probe: a streaming read of n16 16-byte words with a
-// cheap integer reduction (XOR), four independent loads in flight per
-// thread, eight CTAs per SM.
+// Achievable-bandwidth probe: a streaming read of n16 16-byte words
+// (L2-allocating loads, one in flight per thread per iteration, eight
+// 256-thread CTAs per SM) XOR-folded per CTA, one atomic per CTA: per-warp
+// atomics on the single result word serialised at the L2 and cost ~10 us
+// per launch.
 __global__ void __launch_bounds__(256) stream_read_kernel(int64_t n16, const uint4 *__restrict__ a,
                                                           unsigned *out) {
+  __shared__ unsigned s_acc[8];
   unsigned acc = 0u;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < n16; i += 4 * stride) {
-    const uint4 v0 = __ldcs(a + i), v1 = __ldcs(a + i + stride), v2 = __ldcs(a + i + 2 * stride),
-                v3 = __ldcs(a + i + 3 * stride);
-    acc ^= v0.x ^ v0.y ^ v0.z ^ v0.w ^ v1.x ^ v1.y ^ v1.z ^ v1.w ^ v2.x ^ v2.y ^ v2.z ^ v2.w ^ v3.x ^ v3.y ^ v3.z ^
-           v3.w;
-  }
-  for (; i < n16; i += stride) {
-    const uint4 v = __ldcs(a + i);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += stride) {
+    const uint4 v = __ldcg(a + i);
     acc ^= v.x ^ v.y ^ v.z ^ v.w;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) atomicXor(out, acc);
+  if ((threadIdx.x & 31) == 0) s_acc[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = 0u;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t ^= s_acc[w];
+    atomicXor(out, t);
+  }
 }
 
 void stream_read(const void *buf, int64_t bytes, unsigned *out, cudaStream_t st) {

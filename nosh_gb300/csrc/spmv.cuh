@@ -1,14 +1,15 @@
 // Row-block SpMV over the off-diagonal KEO graph with a fused per-vertex
 // epilogue (diagonal 2x2 block, residual nonlinearity, reductions).
 //
-// One CTA = kRows consecutive rows = kRows threads, persistent over row
-// blocks.  A row block's nonzeros [rp[r0], rp[r1]) are contiguous: one
-// thread stages them into shared memory with two bulk asynchronous copies
-// (TMA, cp.async.bulk: column ids and complex values) completing on an
-// mbarrier, double-buffered so that the copy of the CTA's next row block
-// overlaps the current one's arithmetic.  Every thread then reduces its own
-// row out of shared memory and gathers x through the read-only path.  A
-// row block whose nonzeros exceed the staging capacity reads them directly.
+// One CTA = kRows consecutive rows (row_threads<T>() threads per row),
+// persistent over row blocks.  A row block's nonzeros [rp[r0], rp[r1]) are
+// contiguous: one thread stages them into shared memory with two bulk
+// asynchronous copies (TMA, cp.async.bulk: column ids and complex values)
+// completing on an mbarrier, double-buffered so that the copy of the CTA's
+// next row block overlaps the current one's arithmetic.  The threads of a
+// row then reduce its nonzeros out of shared memory and gather x through
+// the read-only path.  A row block whose nonzeros exceed the staging
+// capacity reads them directly.
 #pragma once
 
 #include <utility>
@@ -21,6 +22,18 @@ namespace nosh {
 namespace dev {
 
 constexpr int kRows = 128;
+// Threads per row of the staged schedule (adjacent lanes, each taking every
+// row_threads-th nonzero).  One: two lanes per FP32 row (twice the warps
+// per SM for the gathers' latency, four CTAs per SM instead of five)
+// measured 4 % slower on the 64^3 smoother launch and 9 % on the 160^3 one.
+template <typename T>
+__host__ __device__ constexpr int row_threads() {
+  return 1;
+}
+template <typename T>
+__host__ __device__ constexpr int block_threads() {
+  return kRows * row_threads<T>();
+}
 
 template <typename T>
 struct Acc;  // accumulator type per value type
@@ -185,7 +198,7 @@ constexpr int kStageErrorSlot = 15;
 constexpr int kStageWaitSlot = 14;
 
 template <typename T, class Op>
-__global__ void __launch_bounds__(kRows, sizeof(T) == 4 ? 5 : 1)
+__global__ void __launch_bounds__(block_threads<T>(), sizeof(T) == 4 ? 5 : 1)
     row_block_apply(int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                     const C2<T> *__restrict__ val, const C2<T> *__restrict__ x, int cap,
                     Op op, double *partials, unsigned *counter, double *red_out) {
@@ -258,9 +271,10 @@ __global__ void __launch_bounds__(kRows, sizeof(T) == 4 ? 5 : 1)
     if (threadIdx.x == 0 && nxt(rb) < rb_end) issue(nxt(rb), stage ^ 1);
     int ks, n;
     range(rb, ks, n);
-    const int row = rb * kRows + threadIdx.x;
+    constexpr int R = row_threads<T>();
+    const int row = rb * kRows + (int)threadIdx.x / R, lane_r = (int)threadIdx.x % R;
     typename Op::Pre pre{};
-    if (row < N) pre = op.load(row);
+    if (row < N && lane_r == 0) pre = op.load(row);
     const bool staged = n > 0 && n <= cap;
     cur_staged = staged;
     next_staged = false;
@@ -277,40 +291,47 @@ __global__ void __launch_bounds__(kRows, sizeof(T) == 4 ? 5 : 1)
     if (staged) parity[stage] ^= 1u;
     const int32_t *s_col = reinterpret_cast<const int32_t *>(smem_raw + stage * buf);
     const C2<T> *s_val = reinterpret_cast<const C2<T> *>(smem_raw + stage * buf + (size_t)cap * sizeof(int32_t));
+    A sr = 0, si = 0;
     if (row < N) {
-      A sr = 0, si = 0;
       const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
       if (staged) {
-        // batches of kBatch nonzeros: all gathers of a batch are issued
-        // before the first is used (rows of the mesh graph fit one batch)
-        // (the values are read from shared memory when used, so only the
-        // gathered x of a batch occupies registers)
-        constexpr int kBatch = sizeof(T) == 4 ? 16 : 8;
-        for (int k0 = b - ks; k0 < e - ks; k0 += kBatch) {
-          const int cnt = e - ks - k0;
+        // batches of kBatch nonzeros per lane (the row's lanes take every
+        // R-th one): all gathers of a batch are issued before the first is
+        // used (rows of the mesh graph fit one batch); the values are read
+        // from shared memory when used, so only the gathered x of a batch
+        // occupies registers
+        constexpr int kBatch = (sizeof(T) == 4 ? 16 : 8) / R;
+        for (int k0 = b - ks + lane_r; k0 < e - ks; k0 += kBatch * R) {
+          const int cnt = (e - ks - k0 + R - 1) / R;
           C2<T> xv[kBatch];
 #pragma unroll
           for (int u = 0; u < kBatch; u++)
-            if (u < cnt) xv[u] = ldg(x + s_col[k0 + u]);
+            if (u < cnt) xv[u] = ldg(x + s_col[k0 + u * R]);
 #pragma unroll
           for (int u = 0; u < kBatch; u++) {
             if (u < cnt) {
-              const C2<T> v = s_val[k0 + u];
+              const C2<T> v = s_val[k0 + u * R];
               sr += v.x * xv[u].x - v.y * xv[u].y;
               si += v.x * xv[u].y + v.y * xv[u].x;
             }
           }
         }
       } else {
-        for (int k = b; k < e; k++) {
+        for (int k = b + lane_r; k < e; k += R) {
           const C2<T> v = ldg(val + k);
           const C2<T> xv = ldg(x + __ldg(ci + k));
           sr += v.x * xv.x - v.y * xv.y;
           si += v.x * xv.y + v.y * xv.x;
         }
       }
-      part += (A)op.finish(row, sr, si, pre);
     }
+    // the row's lanes are adjacent: fold their partial sums into lane 0
+#pragma unroll
+    for (int o = R / 2; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (row < N && lane_r == 0) part += (A)op.finish(row, sr, si, pre);
     __syncthreads();  // this buffer is refilled two row blocks later
   }
   if (!ok) {
@@ -420,9 +441,10 @@ __global__ void __launch_bounds__(kWarpThreads)
 // Resident CTAs of row_warp_apply on the device, capped by the work.
 int warp_grid(const void *kernel, int64_t n_rows);
 
-// Grid for a persistent row kernel: the resident capacity of the device for
-// this kernel and shared-memory size, capped by the number of row blocks.
-int row_grid(const void *kernel, size_t smem, int64_t n_rows);
+// Grid for a persistent row kernel of `threads` threads per CTA: the
+// resident capacity of the device for this kernel and shared-memory size,
+// capped by the number of row blocks.
+int row_grid(const void *kernel, int threads, size_t smem, int64_t n_rows);
 
 // Launch the SpMV + epilogue over an off-diagonal CSR with one of the two
 // schedules (warp: row_warp_apply, else the staged row_block_apply with
@@ -447,8 +469,9 @@ void launch_spmv(bool warp, int N, const int32_t *rp, const int32_t *ci, const C
       attr_set = true;
     }
     const size_t smem = 2 * stage_bytes<T>(cap);
-    launch_dep(overlap, row_block_apply<T, Op>, dim3(row_grid((const void *)row_block_apply<T, Op>, smem, N)),
-               dim3(kRows), smem, st, N, rp, ci, val, x, cap, op, partials, counter, red_out);
+    launch_dep(overlap, row_block_apply<T, Op>,
+               dim3(row_grid((const void *)row_block_apply<T, Op>, block_threads<T>(), smem, N)),
+               dim3(block_threads<T>()), smem, st, N, rp, ci, val, x, cap, op, partials, counter, red_out);
   }
   NOSH_CUDA(cudaGetLastError());
 }

@@ -46,3 +46,19 @@ def test_timed_solve_counts_working_launches(prec):
     for launches, ms, nbytes in (jac, smo):
         assert ms > 0.0 and nbytes > 0.0
         assert 0.5e-3 < ms / launches < 1.0  # ms per launch
+
+
+def test_stream_read_probe_folds_every_word():
+    import torch
+
+    import nosh_gb300 as ng
+
+    rng = np.random.default_rng(7)
+    words = rng.integers(0, 2**32, size=(3 << 20) // 4 + 12, dtype=np.uint64).astype(np.uint32)
+    buf = torch.from_numpy(words.view(np.int32)).cuda()
+    out = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nb = (words.size * 4) // 16 * 16
+    ng.stream_read(buf, nb, out, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    expect = np.bitwise_xor.reduce(words[: nb // 4])
+    assert int(out.cpu().numpy().view(np.uint32)[0]) == int(expect)
