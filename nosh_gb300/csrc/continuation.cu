@@ -70,7 +70,7 @@ __global__ void dot_set_kernel(int64_t n, DotSet d, double *partials, unsigned *
       }
     }
   }
-  for (int j = 0; j < d.k; j++) dev::grid_reduce(v[j], partials + j * gridDim.x, counter + j, out + j);
+  dev::grid_reduce_n<6>(v, d.k, partials, counter, out);
 }
 
 // y = c0 x0 + c1 x1 + c2 (rot2 ? i x2 : x2); y may alias x0 or x1

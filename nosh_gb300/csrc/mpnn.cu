@@ -950,9 +950,8 @@ __global__ void features_a(int64_t n, const double *__restrict__ dots, const dou
     aq += o[2] * o[2] + o[3] * o[3];
     ac += o[4] * o[4] + o[5] * o[5];
   }
-  grid_reduce(as, partials, counter, red);
-  grid_reduce(aq, partials + gridDim.x, counter + 1, red + 1);
-  grid_reduce(ac, partials + 2 * gridDim.x, counter + 2, red + 2);
+  const double v[3] = {as, aq, ac};
+  grid_reduce_n<3>(v, 3, partials, counter, red);
 }
 
 // X = [x0, s~, q~, c~, mu_new, 1]
@@ -1015,7 +1014,7 @@ __global__ void gram3_kernel(int64_t n2, const double *__restrict__ u, const dou
     acc[1] += a * b;
     acc[2] += b * b;
   }
-  for (int k = 0; k < 3; k++) grid_reduce(acc[k], partials + k * gridDim.x, counter + k, g + k);
+  grid_reduce_n<3>(acc, 3, partials, counter, g);
 }
 
 // out = sec + q + w c (sec: the secant prediction)

@@ -65,26 +65,26 @@ __global__ void vertex_fields_kernel(int64_t N, const int32_t *__restrict__ rp,
 // sin and cos of an FP64 angle.  Magnetic phases on a mesh edge are small
 // (|mu A . e| <= 0.1 covers every mesh finer than about 10 cells per unit
 // field length): there the Maclaurin series of sin to x^11 and cos to x^12
-// (Horner form; truncation below 1e-21 relative at |x| = 0.1) costs a dozen
-// FP64 FMAs, well below a general sincos with argument reduction, which the
+// (Horner form in x^2; truncation below 1e-21 relative at |x| = 0.1) costs a
+// dozen FP64 FMAs, well below a general sincos with argument reduction, which the
 // larger angles still use.  Most phases are far smaller (|x| <= 0.02 on the
 // 64^3 cube at mu = 1): there sin to x^7 and cos to x^8 suffice (truncation
 // below 1e-18 relative), and the assembly is bound by FP64 arithmetic on
 // GB300.
 __device__ __forceinline__ void edge_sincos(double x, double &s, double &c) {
+  // Maclaurin coefficients (-1)^k / (2k+1)! and (-1)^k / (2k)!, folded at
+  // compile time; Horner in x^2 with one FMA per term
+  constexpr double s1 = -1.0 / 6, s2 = 1.0 / 120, s3 = -1.0 / 5040, s4 = 1.0 / 362880, s5 = -1.0 / 39916800;
+  constexpr double c1 = -1.0 / 2, c2 = 1.0 / 24, c3 = -1.0 / 720, c4 = 1.0 / 40320, c5 = -1.0 / 3628800,
+                   c6 = 1.0 / 479001600;
   if (fabs(x) <= 0.02) {
     const double x2 = x * x;
-    constexpr double r6 = 1.0 / 6, r20 = 1.0 / 20, r42 = 1.0 / 42;
-    constexpr double r2 = 1.0 / 2, r12 = 1.0 / 12, r30 = 1.0 / 30, r56 = 1.0 / 56;
-    s = x * (1.0 - x2 * r6 * (1.0 - x2 * r20 * (1.0 - x2 * r42)));
-    c = 1.0 - x2 * r2 * (1.0 - x2 * r12 * (1.0 - x2 * r30 * (1.0 - x2 * r56)));
+    s = fma(x * x2, fma(x2, fma(x2, s3, s2), s1), x);
+    c = fma(x2, fma(x2, fma(x2, fma(x2, c4, c3), c2), c1), 1.0);
   } else if (fabs(x) <= 0.1) {
     const double x2 = x * x;
-    // reciprocals folded at compile time: multiplications, no FP64 division
-    constexpr double r6 = 1.0 / 6, r20 = 1.0 / 20, r42 = 1.0 / 42, r72 = 1.0 / 72, r110 = 1.0 / 110;
-    constexpr double r2 = 1.0 / 2, r12 = 1.0 / 12, r30 = 1.0 / 30, r56 = 1.0 / 56, r90 = 1.0 / 90, r132 = 1.0 / 132;
-    s = x * (1.0 - x2 * r6 * (1.0 - x2 * r20 * (1.0 - x2 * r42 * (1.0 - x2 * r72 * (1.0 - x2 * r110)))));
-    c = 1.0 - x2 * r2 * (1.0 - x2 * r12 * (1.0 - x2 * r30 * (1.0 - x2 * r56 * (1.0 - x2 * r90 * (1.0 - x2 * r132)))));
+    s = fma(x * x2, fma(x2, fma(x2, fma(x2, fma(x2, s5, s4), s3), s2), s1), x);
+    c = fma(x2, fma(x2, fma(x2, fma(x2, fma(x2, fma(x2, c6, c5), c4), c3), c2), c1), 1.0);
   } else {
     sincos(x, &s, &c);
   }
@@ -302,10 +302,8 @@ __global__ void history_dots(int64_t n, const double *x0, const double *x1, cons
       }
     }
   }
-  for (int k = 0; k < count; k++) {
-    dev::grid_reduce(re[k], partials + (2 * k) * gridDim.x, counter + 2 * k, out + 2 * k);
-    dev::grid_reduce(im[k], partials + (2 * k + 1) * gridDim.x, counter + 2 * k + 1, out + 2 * k + 1);
-  }
+  const double v[8] = {re[0], im[0], re[1], im[1], re[2], im[2], re[3], im[3]};
+  dev::grid_reduce_n<8>(v, 2 * count, partials, counter, out);
 }
 
 namespace dev {
@@ -425,8 +423,8 @@ __global__ void __launch_bounds__(128) residual_pair_kernel(
     na = far * far + fai * fai;
     nb = fbr * fbr + fbi * fbi;
   }
-  grid_reduce(na, partials, counter, out);
-  grid_reduce(nb, partials + gridDim.x, counter + 1, out + 1);
+  const double v[2] = {na, nb};
+  grid_reduce_n<2>(v, 2, partials, counter, out);
 }
 
 // Device-side validation of an off-diagonal CSR graph (index-check mode):

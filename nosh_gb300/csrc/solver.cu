@@ -368,8 +368,8 @@ __global__ void cdot_kernel(int64_t n, const C2<double> *__restrict__ a,
     re += x.x * y.x + x.y * y.y;
     im += x.x * y.y - x.y * y.x;
   }
-  grid_reduce(re, partials, counter, out);
-  grid_reduce(im, partials + gridDim.x, counter + 1, out + 1);
+  const double v[2] = {re, im};
+  grid_reduce_n<2>(v, 2, partials, counter, out);
 }
 
 // secant prediction x_new = x + r (x - e^{i phi} x_prev), e^{i phi} = c (the
@@ -408,8 +408,8 @@ __global__ void gauge_dots(int64_t n, const T *__restrict__ x, const double *__r
     a += pr * (double)x[2 * i + 1] - pi * (double)x[2 * i];
     b += pr * pr + pi * pi;
   }
-  grid_reduce(a, partials, counter, out);
-  grid_reduce(b, partials + gridDim.x, counter + 1, out + 1);
+  const double v[2] = {a, b};
+  grid_reduce_n<2>(v, 2, partials, counter, out);
 }
 
 // x -= (<i psi, x> / |psi|^2) i psi, the coefficients from gauge_dots

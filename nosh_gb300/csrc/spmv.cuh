@@ -82,6 +82,91 @@ __device__ __forceinline__ bool grid_reduce(double v, double *partials, unsigned
   return finisher;
 }
 
+// The same for m <= K values at once (v[0..m-1], partials in columns
+// partials + k gridDim.x, one arrival counter): one pass of block sums and
+// one arrival instead of m successive grid_reduce calls, each with its own
+// barriers, fence and atomic.  The sums are bitwise those of m grid_reduce
+// calls (the same block and final summation orders).  Writes out[0..m-1]
+// in the last CTA; returns true in exactly one thread.
+template <int K>
+__device__ __forceinline__ bool grid_reduce_n(const double (&v)[K], int m, double *partials, unsigned *counter,
+                                              double *out) {
+  __shared__ double sw[32 * K];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double r[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) r[k] = k < m ? warp_sum(v[k]) : 0.0;
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (k < m) sw[w * K + k] = r[k];
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (k < m) {
+        double t = lane < nw ? sw[lane * K + k] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) partials[(size_t)k * gridDim.x + blockIdx.x] = t;
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  bool finisher = false;
+  if (last) {
+    __threadfence();
+    const unsigned G = gridDim.x, st = blockDim.x;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      acc[k] = 0.0;
+      if (k < m) {
+        const double *pk = partials + (size_t)k * G;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        unsigned j = threadIdx.x;
+        for (; j + 3 * st < G; j += 4 * st) {
+          a0 += __ldcg(pk + j);
+          a1 += __ldcg(pk + j + st);
+          a2 += __ldcg(pk + j + 2 * st);
+          a3 += __ldcg(pk + j + 3 * st);
+        }
+        for (; j < G; j += st) a0 += __ldcg(pk + j);
+        acc[k] = warp_sum((a0 + a1) + (a2 + a3));
+      }
+    }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k < m) sw[w * K + k] = acc[k];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        if (k < m) {
+          double t = lane < nw ? sw[lane * K + k] : 0.0;
+          t = warp_sum(t);
+          if (lane == 0) out[k] = t;
+        }
+      }
+    }
+    if (threadIdx.x == 0) {
+      *counter = 0u;
+      finisher = true;
+    }
+  }
+  return finisher;
+}
+
 // Op must provide:
 //   static constexpr bool kReduce;
 //   struct Pre;                                  -- the row's epilogue operands
