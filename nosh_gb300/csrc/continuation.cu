@@ -384,11 +384,16 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
       // first overlapped step)
       const bool have_w = w_pending || w_valid;
       drain_side();
-      // the node features only when an inference reads them
-      net->prepare(x, m, mu_new, ns.psi.p, !have_w || infer_count + 1 >= infer_period);
-      if (!have_w) net->infer(s.stream);
+      // the node features only when an inference reads them; otherwise the
+      // prediction straight from the states
+      if (!have_w || infer_count + 1 >= infer_period) {
+        net->prepare(x, m, mu_new, ns.psi.p, true);
+        if (!have_w) net->infer(s.stream);
+        net->combine(ns.psi.p, ns.tmp.p, w_host);
+      } else {
+        net->predict_fields(x, m, mu_new, ns.psi.p, ns.tmp.p, w_host);
+      }
       w_valid = true;
-      net->combine(ns.psi.p, ns.tmp.p, w_host);
       // the next coefficient from these features, under this Newton
       if (++infer_count >= infer_period) {
         infer_count = 0;

@@ -1017,6 +1017,41 @@ __global__ void gram3_kernel(int64_t n2, const double *__restrict__ u, const dou
   grid_reduce_n<3>(acc, 3, partials, counter, g);
 }
 
+// features_a's prediction fields and combine_kernel's sum in one pass, with
+// the same operations in the same order (bitwise the two-kernel result):
+// the secant into sec_out, out = sec + (q + w c)
+__global__ void predict_fields_kernel(int64_t n, const double *__restrict__ dots, const double *__restrict__ Ls,
+                                      const double *__restrict__ w, const C2<double> *__restrict__ x0,
+                                      const C2<double> *__restrict__ x1, const C2<double> *__restrict__ x2,
+                                      const C2<double> *__restrict__ x3, C2<double> *__restrict__ sec_out,
+                                      C2<double> *__restrict__ out) {
+  double er[3], ei[3];
+  for (int k = 0; k < 3; k++) phases(dots, k, er[k], ei[k]);
+  const double wc = w[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double xr[4], xi[4];
+    xr[0] = x0[i].x;
+    xi[0] = x0[i].y;
+    const C2<double> *xs[3] = {x1, x2, x3};
+    for (int k = 0; k < 3; k++) {
+      const C2<double> p = xs[k][i];
+      xr[k + 1] = er[k] * p.x - ei[k] * p.y;
+      xi[k + 1] = er[k] * p.y + ei[k] * p.x;
+    }
+    const double secr = Ls[0] * xr[0] + Ls[1] * xr[1], seci = Ls[0] * xi[0] + Ls[1] * xi[1];
+    const double qdr = Ls[2] * xr[0] + Ls[3] * xr[1] + Ls[4] * xr[2];
+    const double qdi = Ls[2] * xi[0] + Ls[3] * xi[1] + Ls[4] * xi[2];
+    const double cbr = Ls[5] * xr[0] + Ls[6] * xr[1] + Ls[7] * xr[2] + Ls[8] * xr[3];
+    const double cbi = Ls[5] * xi[0] + Ls[6] * xi[1] + Ls[7] * xi[2] + Ls[8] * xi[3];
+    sec_out[i] = C2<double>{secr, seci};
+    const double f2 = qdr - secr, f3 = qdi - seci, f4 = cbr - qdr, f5 = cbi - qdi;
+    C2<double> o{secr, seci};
+    o.x += f2 + wc * f4;
+    o.y += f3 + wc * f5;
+    out[i] = o;
+  }
+}
+
 // out = sec + q + w c (sec: the secant prediction)
 __global__ void combine_kernel(int64_t n, const double *__restrict__ w, const double *__restrict__ sq,
                                const C2<double> *__restrict__ sec, C2<double> *__restrict__ out) {
@@ -1173,6 +1208,9 @@ struct Mpnn::Impl {
   double backward_and_step(float lr);     // needs gram
   void features(const double *const x[4], const double mu[4], double mu_t, const double *target,
                 double *secant = nullptr, bool node_features = true);
+  // Lagrange weights (into Ls) and phase factors of x[1..3] (and target)
+  // against x[0] (into dots)
+  void align(const double *const x[4], const double mu[4], double t, const double *target);
   void gemm(int epi, const float *in0, int K0, const float *in1, int K1, int64_t wt_off, float *out);
   void wgrad(const float *in0, int K0, const float *in1, int K1, const float *dout, int ncol, int64_t dst,
              int64_t bias_dst);
@@ -1420,10 +1458,8 @@ double Mpnn::Impl::backward_and_step(float lr) {
 
 // node features at mu_t from the newest states x[0..3] (mu[0..3]) and, with
 // a target (the converged state at mu_t), the sample's Gram scalars
-void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target,
-                          double *secant, bool node_features) {
+void Mpnn::Impl::align(const double *const x[4], const double mu[4], double t, const double *target) {
   cudaStream_t st = stream;
-  const int G = vgrid(N);
   double Lh[9];
   Lh[0] = (t - mu[1]) / (mu[0] - mu[1]);
   Lh[1] = (t - mu[0]) / (mu[1] - mu[0]);
@@ -1446,6 +1482,13 @@ void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t
   ++s.launch_count;
   normalize_phases<<<1, 32, 0, st>>>(target ? 4 : 3, dots.p);
   ++s.launch_count;
+}
+
+void Mpnn::Impl::features(const double *const x[4], const double mu[4], double t, const double *target,
+                          double *secant, bool node_features) {
+  cudaStream_t st = stream;
+  const int G = vgrid(N);
+  align(x, mu, t, target);
   features_a<<<reduce_grid(N), 256, 0, st>>>(N, dots.p, Ls.p, (const C2<double> *)x[0], (const C2<double> *)x[1],
                                 (const C2<double> *)x[2], (const C2<double> *)x[3], sq.p, (C2<double> *)secant,
                                 rd.partials.p,
@@ -1512,6 +1555,18 @@ void Mpnn::combine(const double *secant, double *out, double *w_host) {
   Impl &I = *impl;
   combine_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(I.N, I.w.p, I.sq.p, (const C2<double> *)secant,
                                                      (C2<double> *)out);
+  ++I.s.launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  if (w_host) NOSH_CUDA(cudaMemcpyAsync(w_host, I.w.p, sizeof(double), cudaMemcpyDeviceToHost, I.s.stream));
+}
+
+void Mpnn::predict_fields(const double *const x[4], const double mu[4], double mu_new, double *secant, double *out,
+                          double *w_host) {
+  Impl &I = *impl;
+  I.align(x, mu, mu_new, nullptr);
+  predict_fields_kernel<<<vgrid(I.N), 256, 0, I.s.stream>>>(
+      I.N, I.dots.p, I.Ls.p, I.w.p, (const C2<double> *)x[0], (const C2<double> *)x[1], (const C2<double> *)x[2],
+      (const C2<double> *)x[3], (C2<double> *)secant, (C2<double> *)out);
   ++I.s.launch_count;
   NOSH_CUDA(cudaGetLastError());
   if (w_host) NOSH_CUDA(cudaMemcpyAsync(w_host, I.w.p, sizeof(double), cudaMemcpyDeviceToHost, I.s.stream));

@@ -25,6 +25,11 @@ struct Mpnn {
                bool node_features = true);
   void infer(cudaStream_t st);
   void combine(const double *secant, double *out, double *w_host);
+  // prepare(node_features = false) + combine in one pass over the states,
+  // for a step whose features feed no inference: the secant into `secant`,
+  // out = secant + q + w c with the current w (w copied to w_host)
+  void predict_fields(const double *const x[4], const double mu[4], double mu_new, double *secant, double *out,
+                      double *w_host);
   // optimiser iterations on the transition x[0..3] -> target at mu_t;
   // returns the last relative loss
   double train(const double *const x[4], const double mu[4], const double *target, double mu_t, int iters,

@@ -218,6 +218,54 @@ def test_learned_predictor_gains_over_secant():
     assert np.median(gains) > 10.0, gains
 
 
+def test_learned_prediction_between_inferences_matches_oracle():
+    """With the coefficient re-inferred on every fourth learned step only,
+    the steps in between form the prediction straight from the states (one
+    pass, no node features).  On every step past the training window the
+    learned prediction's starting residual is the oracle's residual of
+    quadratic + w (cubic - quadratic) from the same four phase-aligned
+    states, w being the coefficient the step reports."""
+    import nosh_gb300 as ng
+
+    m, P, psi0 = _square(33, 5)
+    mu0 = 0.0
+    model = ng.nls(ng.mesh(m.x, m.cells), P.A, -1.0, 1.0, 1.0, mu=mu0)
+    x0 = psi0.copy()
+    model.newton(x0, {"mu": mu0}, refine=1e-12)
+    cont = ng.continuation(model, x0, mu0)
+    cont.learning(train_steps=8, iters_per_step=10, learning_rate=2e-3)
+    cont.inference_period(4)
+    hist = [(x0.copy(), mu0)]
+    mu, checked = mu0, 0
+    for k in range(24):
+        mu += 0.01
+        st = cont.advance(mu, predictor=ng.PREDICT_LEARNED, refine=1e-12)
+        assert st["status"] == 0 and st["f_norm"] <= 1e-10
+        lp = cont.last_prediction()
+        if k >= 14:  # past the 8 training steps and the 4 history steps
+            assert lp["used"] == ng.PREDICT_LEARNED
+            xs = [h[0] for h in hist[-4:]][::-1]
+            ms = [h[1] for h in hist[-4:]][::-1]
+            al = [xs[0]] + [O.align_phase(v, xs[0]) for v in xs[1:]]
+
+            def lag(n):
+                out = np.zeros_like(xs[0])
+                for i in range(n):
+                    w = 1.0
+                    for j in range(n):
+                        if j != i:
+                            w *= (mu - ms[j]) / (ms[i] - ms[j])
+                    out += w * al[i]
+                return out
+
+            q, c = lag(3), lag(4)
+            f = np.linalg.norm(P.compute_f(q + lp["coef"] * (c - q), 1.0, mu))
+            assert abs(lp["f_learned"] - f) <= 1e-4 * f, (k, lp["f_learned"], f)
+            checked += 1
+        hist.append(cont.state())
+    assert checked == 10
+
+
 @pytest.mark.parametrize("name", ["cube64", "square65"])
 def test_learned_adapts_to_the_better_extrapolation(name):
     """On held-out steps after the training window, the trained network's
