@@ -646,7 +646,8 @@ __global__ void dense_matvec(int m, const T *__restrict__ Ainv, DenseMap D, cons
     x[i] = dense_row(D, Ainv, i, b);
 }
 
-// ---- single-CTA tail: every level from `lt` down, in one launch
+// ---- coarse-level tail: every level from `lt` down, in one launch (one CTA,
+// or one thread-block cluster)
 template <typename T>
 struct LevelDesc {
   int64_t n;
@@ -658,21 +659,49 @@ struct LevelDesc {
 };
 
 
+// The threads that run the tail: one CTA (barrier: __syncthreads), or the
+// CTAs of one thread-block cluster (barrier: the hardware cluster barrier,
+// whose arrive/wait pair has release/acquire semantics at cluster scope, so
+// the vectors one CTA writes to global memory are visible to the others
+// after it).  A cluster spreads the coarse levels' SpMVs over several SMs,
+// whose L2 bandwidth one SM alone does not have.
+struct CtaTeam {
+  __device__ int rank() const { return threadIdx.x; }
+  __device__ int size() const { return blockDim.x; }
+  __device__ void sync() const { __syncthreads(); }
+};
+struct ClusterTeam {
+  int r, n;  // CTA rank in the cluster, CTAs in the cluster
+  __device__ static ClusterTeam here() {
+    unsigned r, n;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+    return ClusterTeam{(int)r, (int)n};
+  }
+  __device__ int rank() const { return r * (int)blockDim.x + (int)threadIdx.x; }
+  __device__ int size() const { return n * (int)blockDim.x; }
+  __device__ void sync() const {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+  }
+};
+
 // Threads per row for a tail level of n rows: the largest power of two
 // <= 32 that still leaves a thread group per row, so the short serial chains
 // of the coarse rows (and aggregates) are split across lanes.
-__device__ __forceinline__ int tail_tpr(int64_t n) {
+template <class Team>
+__device__ __forceinline__ int tail_tpr(const Team &tm, int64_t n) {
   int t = 1;
-  while (t < 32 && (int64_t)(blockDim.x / (2 * t)) >= n) t *= 2;
+  while (t < 32 && (int64_t)(tm.size() / (2 * t)) >= n) t *= 2;
   return t;
 }
 
 // For every row i < n: the row's off-diagonal sum over x, reduced across its
 // tpr lanes, then epi(i, sr, si) on the group's first lane.
-template <typename T, class F>
-__device__ __forceinline__ void tail_rows(const LevelDesc<T> &A, const C2<T> *x, F &&epi) {
-  const int tpr = tail_tpr(A.n);
-  const int groups = blockDim.x / tpr, g = threadIdx.x / tpr, li = threadIdx.x % tpr;
+template <typename T, class Team, class F>
+__device__ __forceinline__ void tail_rows(const Team &tm, const LevelDesc<T> &A, const C2<T> *x, F &&epi) {
+  const int tpr = tail_tpr(tm, A.n);
+  const int groups = tm.size() / tpr, g = tm.rank() / tpr, li = tm.rank() % tpr;
   for (int64_t base = 0; base < A.n; base += groups) {
     const int64_t i = base + g;
     T sr = 0, si = 0;
@@ -690,34 +719,34 @@ __device__ __forceinline__ void tail_rows(const LevelDesc<T> &A, const C2<T> *x,
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L, int deg, const T *__restrict__ Ainv,
-                                          const DenseMap &D) {
-  const int tid = threadIdx.x, bs = blockDim.x;
+template <typename T, class Team>
+__device__ __forceinline__ void tail_body(const Team &tm, const LevelDesc<T> *lv, int lt, int L, int deg,
+                                          const T *__restrict__ Ainv, const DenseMap &D) {
+  const int tid = tm.rank(), bs = tm.size();
   for (int l = lt; l < L - 1; l++) {
     const LevelDesc<T> A = lv[l];
     C2<T> *cur = (deg % 2) ? A.x : A.x2, *oth = (deg % 2) ? A.x2 : A.x;
     for (int64_t i = tid; i < A.n; i += bs) cheb_first_elem<T>(i, A.dinv, A.coef[0], A.b[i], A.d, cur);
-    __syncthreads();
+    tm.sync();
     for (int k = 1; k < deg; k++) {
-      tail_rows<T>(A, cur, [&](int64_t i, T sr, T si) {
+      tail_rows<T>(tm, A, cur, [&](int64_t i, T sr, T si) {
         cheb_elem<T>(i, k, sr, si, A.dia, A.dinv, A.coef, A.b, cur, A.d, oth);
       });
-      __syncthreads();
+      tm.sync();
       C2<T> *t = cur;
       cur = oth;
       oth = t;
     }
-    tail_rows<T>(A, A.x, [&](int64_t i, T sr, T si) {
+    tail_rows<T>(tm, A, A.x, [&](int64_t i, T sr, T si) {
       const C2<T> xi = A.x[i], bi = A.b[i];
       const T d0r = A.dia[3 * i], d0i = A.dia[3 * i + 1], d1b = A.dia[3 * i + 2];
       A.res[i] = C2<T>{bi.x - (sr + d0r * xi.x + d1b * xi.y), bi.y - (si + d1b * xi.x + d0i * xi.y)};
     });
-    __syncthreads();
+    tm.sync();
     // restriction: aggregate sums, split across lanes like the rows
     const LevelDesc<T> Cl = lv[l + 1];
     {
-      const int tpr = tail_tpr(Cl.n);
+      const int tpr = tail_tpr(tm, Cl.n);
       const int groups = bs / tpr, g = tid / tpr, li = tid % tpr;
       for (int64_t base = 0; base < Cl.n; base += groups) {
         const int64_t a = base + g;
@@ -735,7 +764,7 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
         if (a < Cl.n && li == 0) Cl.b[a] = C2<T>{sr, si};
       }
     }
-    __syncthreads();
+    tm.sync();
   }
   {
     const LevelDesc<T> C = lv[L - 1];
@@ -743,7 +772,7 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
     const T *b = reinterpret_cast<const T *>(C.b);
     T *x = reinterpret_cast<T *>(C.x);
     for (int i = tid; i < m; i += bs) x[i] = dense_row(D, Ainv, i, b);
-    __syncthreads();
+    tm.sync();
   }
   for (int l = L - 2; l >= lt; l--) {
     const LevelDesc<T> A = lv[l];
@@ -755,20 +784,20 @@ __device__ __forceinline__ void tail_body(const LevelDesc<T> *lv, int lt, int L,
       v.y += c.y;
       A.x[i] = v;
     }
-    __syncthreads();
+    tm.sync();
     C2<T> *cur = A.x, *oth = A.x2;
     for (int k = 0; k < deg; k++) {
-      tail_rows<T>(A, cur, [&](int64_t i, T sr, T si) {
+      tail_rows<T>(tm, A, cur, [&](int64_t i, T sr, T si) {
         cheb_elem<T>(i, k, sr, si, A.dia, A.dinv, A.coef, A.b, cur, A.d, oth);
       });
-      __syncthreads();
+      tm.sync();
       C2<T> *t = cur;
       cur = oth;
       oth = t;
     }
     if (cur != A.x) {
       for (int64_t i = tid; i < A.n; i += bs) A.x[i] = cur[i];
-      __syncthreads();
+      tm.sync();
     }
   }
 }
@@ -779,7 +808,19 @@ __global__ void __launch_bounds__(1024) tail_vcycle(const LevelDesc<T> *__restri
                                                     const int *halt) {
   dep_sync();
   if (halt && *halt >= 2) return;
-  tail_body(lv, lt, L, deg, Ainv, D);
+  tail_body(CtaTeam{}, lv, lt, L, deg, Ainv, D);
+}
+
+// The same over a thread-block cluster (launched with a cluster dimension
+// equal to the grid): the halt flag is read by every CTA alike, so the
+// cluster leaves or stays together.
+template <typename T>
+__global__ void __launch_bounds__(1024) tail_vcycle_cluster(const LevelDesc<T> *__restrict__ lv, int lt, int L,
+                                                            int deg, const T *__restrict__ Ainv, DenseMap D,
+                                                            const int *halt) {
+  dep_sync();
+  if (halt && *halt >= 2) return;
+  tail_body(ClusterTeam::here(), lv, lt, L, deg, Ainv, D);
 }
 
 // plain MINRES pieces for the single-level case
@@ -839,14 +880,14 @@ struct AmgVals {
   std::vector<DevBuf<T>> dia;      // level >= 1
   std::vector<DevBuf<T>> dinv, coef;
   std::vector<DevBuf<C2<T>>> b, x, x2, d, res;
-  DevBuf<LevelDesc<T>> desc;       // for the single-CTA tail
+  DevBuf<LevelDesc<T>> desc;       // for the coarse-level tail
 };
 
 struct Amg::Impl {
   NlsImpl &nls;
   AmgOptions opt;
   std::vector<AmgLevel> lev;
-  int lt = 1;  // first level handled by the single-CTA tail
+  int lt = 1;  // first level handled by the coarse-level tail
   AmgVals<float> vf;
   AmgVals<double> vd;
   DevBuf<unsigned long long> lmax_bits;  // one per level
@@ -872,6 +913,13 @@ struct Amg::Impl {
   // launches return at once once the solve has converged
   const int *halt = nullptr;
   template <typename T> void prime();
+  // CTAs of the coarse-level tail, FP32 and FP64 (a thread-block cluster
+  // when > 1).  The FP64 tail runs on a cluster of 8: the coarse SpMVs'
+  // FP64 arithmetic then spreads over 8 SMs (plain FP64 continuation at
+  // 64^3: 68.2 -> 71.2 steps/s).  The FP32 tail stays on one CTA, whose
+  // vectors stay in its L1 between phases: clusters of 8 and 16 took the
+  // learned line from 671 to 649 and 647 steps/s (in-place A/B).
+  int tail_ctas[2] = {1, 1};
   // V-cycle launches overlap their predecessors (launch_dep) unless the
   // handle turned that off or times kernels with events between launches
   bool ovl() const { return nls.overlap_launches && !nls.timers[0].on && !nls.timers[1].on; }
@@ -1167,6 +1215,24 @@ void Amg::Impl::prime() {
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
   NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, ResidOp<T>>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  tail_ctas[sizeof(T) == 8] = 1;
+  if (sizeof(T) == 8) {
+    constexpr int c = 8;  // portable cluster size
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(1024);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, tail_vcycle_cluster<T>, &cfg) == cudaSuccess && nc > 0)
+      tail_ctas[1] = c;
+    cudaGetLastError();  // a device without clusters of 8 keeps the one-CTA tail
+  }
 }
 
 template <typename T, class Op>
@@ -1222,7 +1288,12 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     launch_dep(ovl(), restrict_kernel<T>, dim3(div_up(Cl.n * kAggLanes, B)), dim3(B), 0, st, Cl.n, A.mem_ptr.p,
                A.mem_idx.p, V.res[l].p, V.b[l + 1].p, halt);
     ++nls.launch_count;
-    launch_dep(ovl(), tail_vcycle<T>, dim3(1), dim3(1024), 0, st, V.desc.p, lt, L, deg, dense_inv<T>(), dmap(),
+    const int tc = tail_ctas[sizeof(T) == 8];
+    if (tc > 1)
+      launch_cluster_dep(ovl(), tc, tail_vcycle_cluster<T>, dim3(1024), 0, st, V.desc.p, lt, L, deg,
+                         dense_inv<T>(), dmap(), halt);
+    else
+      launch_dep(ovl(), tail_vcycle<T>, dim3(1), dim3(1024), 0, st, V.desc.p, lt, L, deg, dense_inv<T>(), dmap(),
                halt);
     ++nls.launch_count;
   }

@@ -153,6 +153,27 @@ void launch_dep(bool overlap, void (*kernel)(P...), dim3 grid, dim3 block, size_
   NOSH_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 }
 
+// The same for a grid of one thread-block cluster of `ctas` CTAs.
+template <typename... P, typename... Args>
+void launch_cluster_dep(bool overlap, int ctas, void (*kernel)(P...), dim3 block, size_t smem, cudaStream_t st,
+                        Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = overlap ? 2 : 1;
+  NOSH_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
 }  // namespace nosh
 
 // ----------------------------------------------------- device-side helpers
