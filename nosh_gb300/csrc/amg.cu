@@ -914,11 +914,12 @@ struct Amg::Impl {
   const int *halt = nullptr;
   template <typename T> void prime();
   // CTAs of the coarse-level tail, FP32 and FP64 (a thread-block cluster
-  // when > 1).  The FP64 tail runs on a cluster of 8: the coarse SpMVs'
-  // FP64 arithmetic then spreads over 8 SMs (plain FP64 continuation at
-  // 64^3: 68.2 -> 71.2 steps/s).  The FP32 tail stays on one CTA, whose
-  // vectors stay in its L1 between phases: clusters of 8 and 16 took the
-  // learned line from 671 to 649 and 647 steps/s (in-place A/B).
+  // when > 1).  The FP64 tail of a tetrahedral mesh runs on a cluster of 8:
+  // the coarse SpMVs' FP64 arithmetic then spreads over 8 SMs (plain FP64
+  // continuation at 64^3: 68.2 -> 71.2 steps/s).  The
+  // FP32 tail stays on one CTA, whose vectors stay in its L1 between phases:
+  // clusters of 8 and 16 took the learned line from 671 to 649 and 647
+  // steps/s (in-place A/B).
   int tail_ctas[2] = {1, 1};
   // V-cycle launches overlap their predecessors (launch_dep) unless the
   // handle turned that off or times kernels with events between launches
@@ -1216,7 +1217,8 @@ void Amg::Impl::prime() {
   NOSH_CUDA(cudaFuncSetAttribute(row_block_apply<T, ResidOp<T>>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
   tail_ctas[sizeof(T) == 8] = 1;
-  if (sizeof(T) == 8) {
+  const int L = (int)lev.size();
+  if (sizeof(T) == 8 && L >= 2 && lt < L) {
     constexpr int c = 8;  // portable cluster size
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(c);
@@ -1229,9 +1231,13 @@ void Amg::Impl::prime() {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int nc = 0;
-    if (cudaOccupancyMaxActiveClusters(&nc, tail_vcycle_cluster<T>, &cfg) == cudaSuccess && nc > 0)
-      tail_ctas[1] = c;
+    const bool ok = cudaOccupancyMaxActiveClusters(&nc, tail_vcycle_cluster<T>, &cfg) == cudaSuccess && nc > 0;
     cudaGetLastError();  // a device without clusters of 8 keeps the one-CTA tail
+    // tetrahedral hierarchies only: their coarse rows hold about twice the
+    // nonzeros of triangular ones, and the FP64 tail of a 2-D 65 x 65 mesh
+    // lost more to the cluster barriers than it gained (FP64 Newton solve
+    // 111.8 -> 104.4 solves/s), while the 64^3 one gained
+    if (ok && nls.mesh->nvc == 4) tail_ctas[1] = c;
   }
 }
 
