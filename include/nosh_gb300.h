@@ -345,6 +345,15 @@ typedef struct {
   double f_norm;          /* final ||F||_2                                */
   double f_norm0;         /* initial ||F||_2                              */
   int status;             /* NOSH_OK / NOSH_ERR_NOT_CONVERGED / ...       */
+  int residual_updates;   /* mixed path: Newton residuals evaluated from
+                             the previous one's FP64 off-diagonal sums and
+                             an FP32 product of the (small) update instead
+                             of afresh; each deviates from the FP64
+                             evaluation by at most the bound below, and is
+                             only kept when it decides convergence with that
+                             margin                                       */
+  double f_norm_bound;    /* bound on |f_norm - FP64 ||F||_2| (0 when the
+                             final residual was evaluated afresh)         */
 } nosh_newton_stats;
 
 /* Fills the defaults above. */

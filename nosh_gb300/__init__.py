@@ -98,6 +98,8 @@ class NewtonStats(C.Structure):
         ("f_norm", C.c_double),
         ("f_norm0", C.c_double),
         ("status", C.c_int),
+        ("residual_updates", C.c_int),
+        ("f_norm_bound", C.c_double),
     ]
 
 
@@ -547,6 +549,8 @@ class nls:
             "f_norm": st.f_norm,
             "f_norm0": st.f_norm0,
             "status": st.status,
+            "residual_updates": st.residual_updates,
+            "f_norm_bound": st.f_norm_bound,
         }
 
     def continuation_step(self, x, x_prev, mu_new, mu_cur, mu_prev=float("nan"), predictor=PREDICT_SECANT,

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -74,6 +75,10 @@ struct DevBuf {
   void download(T *h, size_t count, cudaStream_t s) const {
     if (count)
       NOSH_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+  void download_at(T *h, size_t count, size_t offset, cudaStream_t s) const {
+    if (count)
+      NOSH_CUDA(cudaMemcpyAsync(h, p + offset, count * sizeof(T), cudaMemcpyDeviceToHost, s));
   }
   void zero(cudaStream_t s) {
     if (n) NOSH_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));

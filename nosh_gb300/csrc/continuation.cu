@@ -413,21 +413,25 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
     // starts Newton: the plain secant is the fallback whenever the
     // network's starting residual is worse
     double nrm[2];
-    s.residual_pair(ns.tmp.p, ns.psi.p, g, mu_new, ns.f.p, ns.xc.p, nrm);
+    ns.ensure_soff(2 * s.N);
+    s.residual_pair(ns.tmp.p, ns.psi.p, g, mu_new, ns.f.p, ns.xc.p, nrm, ns.soff_alt.p, ns.soff.p);
     if (overlap) coef = *w_host;
     f_learned = nrm[0];
     f_secant = nrm[1];
     compare = !(f_learned <= opt.tol);
     if (!compare || f_learned < f_secant) {
       std::swap(ns.psi, ns.tmp);
+      std::swap(ns.soff, ns.soff_alt);
       last_used = NOSH_PREDICT_LEARNED;
       f0 = f_learned;  // ns.f holds F of the learned prediction
     } else {
       std::swap(ns.f, ns.xc);
       f0 = f_secant;
     }
+    ns.soff_valid = ns.soff_fresh = true;  // ns.soff: K's off-diagonal sums at the chosen prediction
+    ns.soff_mu = mu_new;
   }
-  newton_core(s, ns, g, mu_new, opt, st, f0);
+  newton_core(s, ns, g, mu_new, opt, st, f0, learned);
   if (st.status != NOSH_OK) return;
   // push the converged state
   head = (head + 1) % kHist;

@@ -211,13 +211,25 @@ struct NlsImpl {
   void dkeo_refill(double mu);
   void keo_apply64(const double *x, double *y);
   void dkeo_apply64(const double *x, double *y);
-  // y = F(x); optional ||F||^2 into red.out[slot]
-  void compute_f64(const double *x, double g, double mu, double *f, int norm_slot);
+  // y = F(x); optional ||F||^2 into red.out[slot]; with soff, also the
+  // off-diagonal sums of K x (2N doubles), the base of residual_update
+  void compute_f64(const double *x, double g, double mu, double *f, int norm_slot, double *soff = nullptr);
+  // F and ||F||^2 (into red.out[0]; not waited for) of x = x_old + dx, dx
+  // an FP32 update already added to x, from soff = the off-diagonal sums of
+  // K x_old (updated in place to those of K x): an FP32 SpMV of dx with an
+  // FP64 epilogue (ResidualUpdateOp)
+  void residual_update(const double *x, const float *dx, double g, double mu, double *f, double *soff);
+  // bounds for residual_update's rounding (computed once): the largest row
+  // sum of |K| (mu-independent: |K_ij| = |alpha_ij|) and the longest row
+  double keo_abs_rowmax();
+  int max_row_nnz();
+  double abs_rowmax_ = -1.0;
+  int max_row_nnz_ = -1;
   void dfdp64(const double *x, double g, double mu, int param, double *out);
   // F(xa) into fa and F(xb) into fb in one pass, norms[0..1] = their norms
-  // (synchronises)
+  // (synchronises); with sa / sb, also the off-diagonal sums of K xa / K xb
   void residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
-                     double norms[2]);
+                     double norms[2], double *sa = nullptr, double *sb = nullptr);
   void jac_rebuild(const double *x, double g, double mu);
   void reg_rebuild(const double *x, double g, double mu);
   template <typename T>

@@ -381,12 +381,14 @@ int row_grid(const void *kernel, int threads, size_t smem, int64_t n_rows) {
 // F(a) and F(b) (FP64, compute_f_) in one pass over the KEO graph, their
 // squared norms into out[0], out[1]: thread per row, the nonzeros read once
 // for both states, gathers in batches of four.  Per row the same summation
-// order as the row-block kernel's ResidualOp.
+// order as the row-block kernel's ResidualOp.  sa / sb (optional): the
+// off-diagonal sums of K a and K b.
 __global__ void __launch_bounds__(128) residual_pair_kernel(
     int N, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci, const C2<double> *__restrict__ val,
     const double *__restrict__ kdiag, const double *__restrict__ cvt, const double *__restrict__ V, double g,
     const C2<double> *__restrict__ xa, const C2<double> *__restrict__ xb, C2<double> *__restrict__ fa,
-    C2<double> *__restrict__ fb, double *partials, unsigned *counter, double *out) {
+    C2<double> *__restrict__ fb, C2<double> *__restrict__ sa, C2<double> *__restrict__ sb, double *partials,
+    unsigned *counter, double *out) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   double na = 0.0, nb = 0.0;
   if (row < N) {
@@ -413,6 +415,8 @@ __global__ void __launch_bounds__(128) residual_pair_kernel(
         }
       }
     }
+    if (sa) sa[row] = C2<double>{ar, ai};
+    if (sb) sb[row] = C2<double>{br, bi};
     const double kd = kdiag[row], ct = cvt[row], vv = V[row];
     const C2<double> pa = xa[row], pb = xb[row];
     const double ca = kd + ct * (vv + g * (pa.x * pa.x + pa.y * pa.y));
@@ -737,24 +741,72 @@ void NlsImpl::dkeo_apply64(const double *x, double *y) {
                       nullptr);
 }
 
-void NlsImpl::compute_f64(const double *x, double g, double mu, double *f, int norm_slot) {
+void NlsImpl::compute_f64(const double *x, double g, double mu, double *f, int norm_slot, double *soff) {
   if (!(keo_mu == mu)) keo_refill(mu);
   const int cap = cap64;
   if (norm_slot >= 0) {
-    ResidualOp<true> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f};
+    ResidualOp<true> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f, (C2<double> *)soff};
     launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, red.out.p + norm_slot);
   } else {
-    ResidualOp<false> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f};
+    ResidualOp<false> op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f,
+                         (C2<double> *)soff};
     launch_rows<double>(*this, d_keo64.p, (const C2<double> *)x, op, cap, nullptr);
   }
 }
 
+void NlsImpl::residual_update(const double *x, const float *dx, double g, double mu, double *f, double *soff) {
+  if (!(keo_mu == mu)) keo_refill(mu);
+  ResidualUpdateOp op{d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)x, (C2<double> *)f, (C2<double> *)soff};
+  launch_rows<float>(*this, d_keo32.p, (const C2<float> *)dx, op, cap32, red.out.p);
+}
+
+namespace {
+// max over rows of sum_k |v_k| (FP64 sums of the FP32 values' moduli),
+// as the bits of a non-negative double (ordered like the values)
+__global__ void abs_rowmax_kernel(int64_t n, const int32_t *__restrict__ rp, const C2<float> *__restrict__ val,
+                                  unsigned long long *out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) s += sqrt((double)val[k].x * val[k].x + (double)val[k].y * val[k].y);
+  atomicMax(out, (unsigned long long)__double_as_longlong(s));
+}
+}  // namespace
+
+double NlsImpl::keo_abs_rowmax() {
+  if (abs_rowmax_ >= 0.0) return abs_rowmax_;
+  if (!(keo_mu == keo_mu)) keo_refill(mu0);
+  DevBuf<unsigned long long> w(1);
+  w.zero(stream);
+  abs_rowmax_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, mesh->d_rp.p, d_keo32.p, w.p);
+  ++launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  unsigned long long h = 0;
+  w.download(&h, 1, stream);
+  sync();
+  // the FP32 values' moduli: |alpha| to 2^-24
+  double v = 0.0;
+  std::memcpy(&v, &h, sizeof(v));
+  abs_rowmax_ = v * (1.0 + std::ldexp(1.0, -22));
+  return abs_rowmax_;
+}
+
+int NlsImpl::max_row_nnz() {
+  if (max_row_nnz_ < 0) {
+    int m = 0;
+    for (int64_t i = 0; i < N; i++) m = std::max(m, (int)(mesh->rp[i + 1] - mesh->rp[i]));
+    max_row_nnz_ = m;
+  }
+  return max_row_nnz_;
+}
+
 void NlsImpl::residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
-                            double norms[2]) {
+                            double norms[2], double *sa, double *sb) {
   if (!(keo_mu == mu)) keo_refill(mu);
   residual_pair_kernel<<<div_up(N, 128), 128, 0, stream>>>(
       (int)N, mesh->d_rp.p, mesh->d_ci.p, d_keo64.p, d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)xa,
-      (const C2<double> *)xb, (C2<double> *)fa, (C2<double> *)fb, red.partials.p, red.counter.p, red.out.p);
+      (const C2<double> *)xb, (C2<double> *)fa, (C2<double> *)fb, (C2<double> *)sa, (C2<double> *)sb,
+      red.partials.p, red.counter.p, red.out.p);
   ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   red.out.download(norms, 2, stream);

@@ -462,6 +462,74 @@ double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double 
   return std::sqrt(n2);
 }
 
+// The same for ns.psi, keeping the off-diagonal sums of K psi in ns.soff
+static double residual_norm_kept(NlsImpl &s, NewtonState &ns, double g, double mu) {
+  ns.ensure_soff(2 * s.N);
+  s.compute_f64(ns.psi.p, g, mu, ns.f.p, 0, ns.soff.p);
+  double n2 = 0.0;
+  s.red.out.download(&n2, 1, s.stream);
+  s.sync();
+  ns.soff_valid = true;
+  ns.soff_fresh = true;
+  ns.soff_mu = mu;
+  return std::sqrt(n2);
+}
+
+// psi += dx (FP64 += FP32 or FP64), and ||dx||_2^2 into *out (FP64 sums)
+template <typename T>
+__global__ void axpy_cast_norm(int64_t n, const T *__restrict__ dx, double *__restrict__ x, double *partials,
+                               unsigned *counter, double *out) {
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = (double)dx[i];
+    x[i] += d;
+    v += d * d;
+  }
+  grid_reduce(v, partials, counter, out);
+}
+
+// ns.psi += dx, then F and ||F|| of the updated state.
+//
+// On the mixed path, when ns.soff holds the off-diagonal sums of K psi from
+// a fresh FP64 evaluation at this mu and the state is close to converged
+// (||F|| <= 100 tol before the step), the update is evaluated from them:
+// soff += K dx by an FP32 SpMV of the FP32 update, F = soff + the per-vertex
+// FP64 terms (ResidualUpdateOp).  Its deviation from the FP64 evaluation is
+// bounded by e = 2 (n_max + 2) 2^-24 R ||dx||_2 (an FP32 dot product of at
+// most n_max terms, the FP32 rounding of K; R bounds the row sums of |K|).
+// The estimate is kept when it decides convergence either way with margin
+// e (||F|| <= tol - e, or ||F|| > tol + e with e <= ||F|| / 100, so that
+// it serves as the next step's right-hand side); otherwise F is evaluated
+// afresh in FP64.  Only one update follows each fresh evaluation.
+template <typename T>
+static double residual_after_update(NlsImpl &s, NewtonState &ns, const T *dx, double g, double mu, double fn_prev,
+                                    double tol, double &bound) {
+  bound = 0.0;
+  const int64_t n2 = 2 * s.N;
+  const bool try_update = sizeof(T) == 4 && ns.soff_valid && ns.soff_fresh && ns.soff_mu == mu &&
+                          fn_prev <= 100.0 * tol;
+  if (!try_update) {
+    axpy_cast<T><<<vec_grid(n2), 256, 0, s.stream>>>(n2, dx, ns.psi.p);
+    ++s.launch_count;
+    return residual_norm_kept(s, ns, g, mu);
+  }
+  axpy_cast_norm<T><<<reduce_grid(n2), 256, 0, s.stream>>>(n2, dx, ns.psi.p, s.red.partials.p, s.red.counter.p,
+                                                           s.red.out.p + 1);
+  ++s.launch_count;
+  s.residual_update(ns.psi.p, (const float *)dx, g, mu, ns.f.p, ns.soff.p);
+  double sq[2] = {0.0, 0.0};  // ||F||^2, ||dx||^2
+  s.red.out.download(sq, 2, s.stream);
+  s.sync();
+  const double fn = std::sqrt(sq[0]);
+  const double e = 2.0 * (s.max_row_nnz() + 2) * std::ldexp(1.0, -24) * s.keo_abs_rowmax() * std::sqrt(sq[1]);
+  if (fn <= tol - e || (fn > tol + e && e <= 0.01 * fn)) {
+    ns.soff_fresh = false;
+    bound = e;
+    return fn;
+  }
+  return residual_norm_kept(s, ns, g, mu);
+}
+
 Amg &ensure_preconditioner(NlsImpl &s) {
   if (!s.amg) {
     AmgOptions o;
@@ -580,6 +648,7 @@ static void newton_loop_systems(NlsImpl &s, NewtonState &ns, double g, double mu
     axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, ns.psi.p);
     ++s.launch_count;
     residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+    ns.soff_valid = false;
     fn_prev = fn;
     fn = s.system_norms(ns.f.p);
     fcur = s.h_sys_norm;
@@ -637,11 +706,19 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
       gauge_remove<T><<<Gc, 256, 0, s.stream>>>(s.N, mr.x.p, ns.psi.p, ns.red2.p);
       s.launch_count += 2;
     }
-    axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, ns.psi.p);
-    ++s.launch_count;
     fn_prev = fn;
-    fn = residual_norm(s, ns.psi.p, g, mu, ns.f.p);
-    if (!s.sys_off.empty()) fn = s.system_norms(ns.f.p);
+    if (s.sys_off.empty()) {
+      double bound = 0.0;
+      fn = residual_after_update<T>(s, ns, mr.x.p, g, mu, fn_prev, opt.tol, bound);
+      st.f_norm_bound = bound;
+      if (bound > 0.0) ++st.residual_updates;
+    } else {
+      axpy_cast<T><<<G, 256, 0, s.stream>>>(n2, mr.x.p, ns.psi.p);
+      ++s.launch_count;
+      residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+      ns.soff_valid = false;
+      fn = s.system_norms(ns.f.p);
+    }
     st.newton_iters = it + 1;
     st.f_norm = fn;
     if (opt.verbose)
@@ -655,9 +732,14 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
 }
 
 void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
-                 nosh_newton_stats &st, double f0) {
+                 nosh_newton_stats &st, double f0, bool soff_ready) {
   st = nosh_newton_stats{};
-  st.f_norm0 = f0 >= 0.0 ? f0 : residual_norm(s, ns.psi.p, g, mu, ns.f.p);
+  if (f0 >= 0.0) {
+    if (!soff_ready) ns.soff_valid = false;
+    st.f_norm0 = f0;
+  } else {
+    st.f_norm0 = residual_norm_kept(s, ns, g, mu);
+  }
   // batched systems: the largest per-system norm decides convergence
   if (!s.sys_off.empty()) st.f_norm0 = s.system_norms(ns.f.p);
   st.f_norm = st.f_norm0;

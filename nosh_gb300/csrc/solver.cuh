@@ -102,6 +102,16 @@ struct NewtonState {
   // batched solves: per-system Newton steps and MINRES iterations of the
   // last Newton solve
   std::vector<int> sys_newton, sys_krylov;
+  // off-diagonal sums of K psi (FP64, 2N) for the current psi at soff_mu,
+  // kept by the mixed-precision Newton steps (residual_update); soff_alt
+  // holds a second candidate's (the learned step's two predictions)
+  DevBuf<double> soff, soff_alt;
+  bool soff_valid = false, soff_fresh = false;  // fresh: from an FP64 evaluation, no update since
+  double soff_mu = 0.0;
+  void ensure_soff(int64_t n2) {
+    if (soff.n < (size_t)n2) soff.alloc(n2);
+    if (soff_alt.n < (size_t)n2) soff_alt.alloc(n2);
+  }
 };
 NewtonState &state_of(NlsImpl &s);
 // drop the AMG hierarchy (and the MINRES graphs that reference it); the next
@@ -112,9 +122,10 @@ Amg &ensure_preconditioner(NlsImpl &s);
 // ||F(psi)||_2 (writes F into f; synchronises)
 double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double *f);
 // Newton on state_of(s).psi in place.  With f0 >= 0, ns.f already holds
-// F(psi) and f0 is its norm (no re-evaluation).
+// F(psi) and f0 is its norm (no re-evaluation), and soff_ready says whether
+// ns.soff holds the off-diagonal sums of K psi as well.
 void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
-                 nosh_newton_stats &st, double f0 = -1.0);
+                 nosh_newton_stats &st, double f0 = -1.0, bool soff_ready = false);
 
 // Relative MINRES tolerance of Newton step `it` (fixed forcing, else
 // safeguarded Eisenstat-Walker), floored at what the Krylov precision resolves.

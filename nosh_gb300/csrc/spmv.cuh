@@ -167,6 +167,17 @@ __device__ __forceinline__ bool grid_reduce_n(const double (&v)[K], int m, doubl
   return finisher;
 }
 
+// The type a launch accumulates the epilogues' partials in: the SpMV's
+// accumulator type unless the Op asks for FP64 (`using Part = double`).
+template <class Op, class A, class = void>
+struct PartOf {
+  using type = A;
+};
+template <class Op, class A>
+struct PartOf<Op, A, decltype((void)sizeof(typename Op::Part), void())> {
+  using type = typename Op::Part;
+};
+
 // Op must provide:
 //   static constexpr bool kReduce;
 //   struct Pre;                                  -- the row's epilogue operands
@@ -339,7 +350,7 @@ __global__ void __launch_bounds__(block_threads<T>(), sizeof(T) == 4 ? 5 : 1)
     }
     return;
   }
-  A part = 0;
+  typename PartOf<Op, A>::type part = 0;
   uint32_t parity[2] = {0u, 0u};
   bool ok = true;
   // copies issued and not yet waited for: the current and the next row block
@@ -416,7 +427,7 @@ __global__ void __launch_bounds__(block_threads<T>(), sizeof(T) == 4 ? 5 : 1)
       sr += __shfl_xor_sync(0xffffffffu, sr, o);
       si += __shfl_xor_sync(0xffffffffu, si, o);
     }
-    if (row < N && lane_r == 0) part += (A)op.finish(row, sr, si, pre);
+    if (row < N && lane_r == 0) part += (typename PartOf<Op, A>::type)op.finish(row, sr, si, pre);
     __syncthreads();  // this buffer is refilled two row blocks later
   }
   if (!ok) {
@@ -454,7 +465,7 @@ __global__ void __launch_bounds__(kWarpThreads)
   const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4;
   const int nwb = (N + 31) / 32;
   const int wpb = kWarpThreads / 32;
-  A part = 0;
+  typename PartOf<Op, A>::type part = 0;
   for (int wb = blockIdx.x * wpb + (threadIdx.x >> 5); wb < nwb; wb += gridDim.x * wpb) {
     const int r0 = wb * 32;
     const int row = r0 + lane;
@@ -515,7 +526,7 @@ __global__ void __launch_bounds__(kWarpThreads)
         }
       }
     }
-    if (row < N) part += (A)op.finish(row, msr, msi, pre);
+    if (row < N) part += (typename PartOf<Op, A>::type)op.finish(row, msr, msi, pre);
   }
   if (Op::kReduce) {
     double total = 0.0;
@@ -621,7 +632,9 @@ struct BlockDiagOp {
   }
 };
 
-// F = K psi + cv t (V + g|psi|^2) psi (FP64), optionally ||F||^2
+// F = K psi + cv t (V + g|psi|^2) psi (FP64), optionally ||F||^2; with soff,
+// also the off-diagonal sums (K psi)_i - K_ii psi_i (the base of a later
+// ResidualUpdateOp)
 template <bool kNorm>
 struct ResidualOp {
   static constexpr bool kReduce = kNorm;
@@ -629,16 +642,47 @@ struct ResidualOp {
   double g;
   const C2<double> *x;
   C2<double> *y;
+  C2<double> *soff = nullptr;
   struct Pre {
     C2<double> p;
     double kd, ct, v;
   };
   __device__ Pre load(int i) const { return Pre{x[i], kdiag[i], cvt[i], V[i]}; }
   __device__ double finish(int i, double sr, double si, const Pre &q) const {
+    if (soff) soff[i] = C2<double>{sr, si};
     const double a = q.kd + q.ct * (q.v + g * (q.p.x * q.p.x + q.p.y * q.p.y));
     const double fr = sr + a * q.p.x, fi = si + a * q.p.y;
     y[i] = C2<double>{fr, fi};
     return kNorm ? fr * fr + fi * fi : 0.0;
+  }
+};
+
+// F of psi + dx from the off-diagonal sums of K psi (soff, FP64) and the
+// FP32 SpMV of the update: soff += K dx (in place), F = soff + cv t (V +
+// g|psi+dx|^2)(psi+dx) with the updated state `x` (FP64), ||F||^2 summed in
+// FP64.  K is linear and the nonlinearity is per vertex, so this is F itself;
+// the FP32 part is the product of the small update only, whose rounding
+// (~1e-7 of |K dx|) lies far below the FP64 rounding of the O(1) sums.
+struct ResidualUpdateOp {
+  static constexpr bool kReduce = true;
+  using Part = double;
+  const double *kdiag, *cvt, *V;
+  double g;
+  const C2<double> *x;
+  C2<double> *y;
+  C2<double> *soff;
+  struct Pre {
+    C2<double> p, s;
+    double kd, ct, v;
+  };
+  __device__ Pre load(int i) const { return Pre{x[i], soff[i], kdiag[i], cvt[i], V[i]}; }
+  __device__ double finish(int i, float sr, float si, const Pre &q) const {
+    const double s_r = q.s.x + (double)sr, s_i = q.s.y + (double)si;
+    soff[i] = C2<double>{s_r, s_i};
+    const double a = q.kd + q.ct * (q.v + g * (q.p.x * q.p.x + q.p.y * q.p.y));
+    const double fr = s_r + a * q.p.x, fi = s_i + a * q.p.y;
+    y[i] = C2<double>{fr, fi};
+    return fr * fr + fi * fi;
   }
 };
 
