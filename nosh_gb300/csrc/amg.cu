@@ -244,10 +244,26 @@ __global__ void rap_diag(int64_t na, const int32_t *__restrict__ mptr,
 
 // inverse diagonal blocks and the Gershgorin bound of lambda_max(D^-1 A):
 // 1 + ||D_i^-1||_2 sum_j |a_ij|, reduced by max over rows (arithmetic in T)
+// sum_j |a_ij| per row (the loop dinv_gershgorin runs without rowabs)
+template <typename T>
+__global__ void row_abs_sums(int64_t n, const int32_t *__restrict__ rp, const C2<T> *__restrict__ off,
+                             T *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T s = 0;
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
+    const C2<T> v = off[k];
+    s += sqrt(v.x * v.x + v.y * v.y);
+  }
+  out[i] = s;
+}
+
+// (rowabs: the rows' sums of |a_ij| when known, else summed here)
 template <typename T>
 __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
                                 const C2<T> *__restrict__ off, const T *__restrict__ dia,
-                                T *__restrict__ dinv, unsigned long long *lmax_bits, int *err) {
+                                T *__restrict__ dinv, unsigned long long *lmax_bits, int *err,
+                                const T *__restrict__ rowabs = nullptr) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double bound = 0.0;
   if (i < n) {
@@ -258,9 +274,13 @@ __global__ void dinv_gershgorin(int64_t n, const int32_t *__restrict__ rp,
     dinv[3 * i + 2] = -b / det;
     const T lmin = (T)0.5 * (a + d) - sqrt((T)0.25 * (a - d) * (a - d) + b * b);
     T s = 0;
-    for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
-      const C2<T> v = off[k];
-      s += sqrt(v.x * v.x + v.y * v.y);
+    if (rowabs) {
+      s = rowabs[i];
+    } else {
+      for (int32_t k = rp[i]; k < rp[i + 1]; k++) {
+        const C2<T> v = off[k];
+        s += sqrt(v.x * v.x + v.y * v.y);
+      }
     }
     bound = (lmin > 0 && det > 0) ? 1.0 + (double)(s / lmin) : 1e300;
     // a diagonal block that is not positive definite: the operator is not
@@ -881,6 +901,11 @@ struct AmgVals {
   std::vector<DevBuf<T>> dinv, coef;
   std::vector<DevBuf<C2<T>>> b, x, x2, d, res;
   DevBuf<LevelDesc<T>> desc;       // for the coarse-level tail
+  // row sums of |K_ij| on the fine level for its Gershgorin bound, computed
+  // once: |K_ij| = |alpha_ij| does not depend on mu (the phase factor has
+  // modulus one), so only the diagonal blocks change between refreshes
+  DevBuf<T> rowabs0;
+  bool rowabs_ready = false;
 };
 
 struct Amg::Impl {
@@ -1143,6 +1168,12 @@ void Amg::refresh() {
   const int L = (int)I.lev.size();
   const bool partial = I.opt.reuse_period > 1 && L > 1 && V.refreshes % I.opt.reuse_period != 0;
   ++V.refreshes;
+  if (!V.rowabs_ready) {
+    V.rowabs0.alloc(I.lev[0].n);
+    row_abs_sums<T><<<div_up(I.lev[0].n, 256), 256, 0, st>>>(I.lev[0].n, I.lev[0].rp, I.off<T>(0), V.rowabs0.p);
+    ++I.nls.launch_count;
+    V.rowabs_ready = true;
+  }
   if (partial) {
     // hierarchy reuse (MueLu "reuse: type full", src/keo_regularized.cpp:
     // 298-330): the fine level reads the current operator directly; only its
@@ -1151,7 +1182,8 @@ void Amg::refresh() {
     // an SPD preconditioner)
     NOSH_CUDA(cudaMemsetAsync(I.lmax_bits.p, 0, sizeof(unsigned long long), st));
     dinv_gershgorin<T><<<div_up(I.lev[0].n, 256), 256, 0, st>>>(I.lev[0].n, I.lev[0].rp, I.off<T>(0), I.dia<T>(0),
-                                                                V.dinv[0].p, I.lmax_bits.p, I.err.p);
+                                                                V.dinv[0].p, I.lmax_bits.p, I.err.p,
+                                                                V.rowabs0.p);
     cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p, std::max(I.opt.smooth_degree, 1), I.opt.cheb_ratio, V.coef[0].p,
                                     I.lmax.p);
     I.nls.launch_count += 2;
@@ -1173,7 +1205,8 @@ void Amg::refresh() {
     }
     if (l < L - 1) {  // the coarsest level is solved directly
       dinv_gershgorin<T><<<div_up(A.n, 256), 256, 0, st>>>(A.n, A.rp, I.off<T>(l), I.dia<T>(l),
-                                                            V.dinv[l].p, I.lmax_bits.p + l, I.err.p);
+                                                            V.dinv[l].p, I.lmax_bits.p + l, I.err.p,
+                                                            l == 0 ? (const T *)V.rowabs0.p : nullptr);
       ++I.nls.launch_count;
       cheb_coeffs<T><<<1, 1, 0, st>>>(I.lmax_bits.p + l, std::max(I.opt.smooth_degree, 1), I.opt.cheb_ratio,
                                       V.coef[l].p, I.lmax.p + l);
