@@ -231,6 +231,9 @@ struct NlsImpl {
   void residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
                      double norms[2], double *sa = nullptr, double *sb = nullptr);
   void jac_rebuild(const double *x, double g, double mu);
+  // the FP32 diagonal blocks of J and of the regularised KEO only, for a
+  // mixed-precision solve
+  void operators32_rebuild(const double *x, double g, double mu);
   void reg_rebuild(const double *x, double g, double mu);
   template <typename T>
   void jac_apply(const T *x, T *y, double *dot_out = nullptr);

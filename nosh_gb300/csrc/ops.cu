@@ -189,6 +189,40 @@ __global__ void reg_diag_kernel(int64_t N, const double *__restrict__ kdiag,
   d32[3 * k + 2] = (float)c;
 }
 
+// Both FP32 diagonal blocks (Jacobian and regularised KEO) in one pass, for
+// the mixed-precision Newton step's operators: the arithmetic of the two
+// kernels above (so the FP32 blocks are bitwise theirs), the FP64 blocks not
+// written.  (The same formulas in FP32 arithmetic saved a few more
+// microseconds but moved the Krylov counts of the 64^3 continuation.)
+__global__ void jac_reg_diag32_kernel(int64_t N, const double *__restrict__ kdiag, const double *__restrict__ cvt,
+                                      const double *__restrict__ V, double g, const C2<double> *__restrict__ x,
+                                      float *jd32, float *rd32) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const C2<double> p = x[k];
+  const double w = cvt[k], kd = kdiag[k];
+  {
+    const double al = w * (V[k] + g * 2.0 * (p.x * p.x + p.y * p.y));
+    const double rx2 = g * w * (p.x * p.x - p.y * p.y);
+    jd32[3 * k] = (float)(kd + al + rx2);
+    jd32[3 * k + 1] = (float)(kd + al - rx2);
+    jd32[3 * k + 2] = (float)(g * w * (2.0 * p.x * p.y));
+  }
+  double a = kd, b = kd, c = 0.0;
+  if (g > 0.0) {
+    const double wg = g * w;
+    const double al = wg * 2.0 * (p.x * p.x + p.y * p.y);
+    const double be = wg * (2.0 * p.x * p.y);
+    const double ga = wg * (p.x * p.x - p.y * p.y);
+    a += al + ga;
+    b += al - ga;
+    c = be;
+  }
+  rd32[3 * k] = (float)a;
+  rd32[3 * k + 1] = (float)b;
+  rd32[3 * k + 2] = (float)c;
+}
+
 // dF/dp diagonal terms (src/model_evaluator_nls.cpp:665-691): out +=
 // cv t |x|^2 x for "g", cv t dV/dp x otherwise (dV/dp = 0 for the explicit
 // potential used here).
@@ -832,6 +866,17 @@ void NlsImpl::jac_rebuild(const double *x, double g, double mu) {
   ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   jac_ready = true;
+}
+
+void NlsImpl::operators32_rebuild(const double *x, double g, double mu) {
+  if (!(keo_mu == mu)) keo_refill(mu);
+  jac_reg_diag32_kernel<<<div_up(N, 256), 256, 0, stream>>>(N, d_kdiag.p, d_cvt.p, d_V.p, g,
+                                                             (const C2<double> *)x, d_jd32.p, d_rd32.p);
+  ++launch_count;
+  NOSH_CUDA(cudaGetLastError());
+  // the FP64 blocks no longer belong to the same state: the operator entry
+  // points want their own rebuild
+  jac_ready = reg_ready = false;
 }
 
 void NlsImpl::reg_rebuild(const double *x, double g, double mu) {

@@ -547,8 +547,12 @@ Amg &ensure_preconditioner(NlsImpl &s) {
 // Refresh the Jacobian and the preconditioner at (psi, g, mu) in precision T.
 template <typename T>
 static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu) {
-  s.jac_rebuild(psi, g, mu);
-  s.reg_rebuild(psi, g, mu);
+  if constexpr (sizeof(T) == 4) {
+    s.operators32_rebuild(psi, g, mu);
+  } else {
+    s.jac_rebuild(psi, g, mu);
+    s.reg_rebuild(psi, g, mu);
+  }
   ensure_preconditioner(s).refresh<T>();
 }
 
