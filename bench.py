@@ -76,9 +76,10 @@ def parse():
                     help="optimiser iterations per training step (default 10; 2 for cont48, whose timed "
                          "amortized line includes the training: 500 against 191 steps/s at 10)")
     ap.add_argument("--lr", type=float, default=2e-3, help="learning rate of the online training")
-    ap.add_argument("--infer-period", type=int, default=8,
+    ap.add_argument("--infer-period", type=int, default=16,
                     help="after training, re-infer the learned coefficient every this many steps (a sweep at "
-                         "64^3: 1, 2, 4, 8 gave 509, 559, 588, 603 steps/s at the same 6.4 MINRES iterations)")
+                         "64^3: 1, 2, 4, 8 gave 509, 559, 588, 603 steps/s at the same 6.4 MINRES iterations; "
+                         "later, 8 and 16 gave 690.5 and 703.4)")
     ap.add_argument("--forcing-aim", type=float, default=0.5,
                     help="fraction of the tolerance a Newton step's forcing term aims at")
     ap.add_argument("--launch-overlap", type=int, default=1, choices=[0, 1],

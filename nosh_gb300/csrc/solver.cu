@@ -475,17 +475,18 @@ static double residual_norm_kept(NlsImpl &s, NewtonState &ns, double g, double m
   return std::sqrt(n2);
 }
 
-// psi += dx (FP64 += FP32 or FP64), and ||dx||_2^2 into *out (FP64 sums)
+// psi += dx (FP64 += FP32), and ||dx||_2^2 into *out: the per-thread sums
+// in FP32 (the norm only scales a rounding bound), the grid sum in FP64
 template <typename T>
 __global__ void axpy_cast_norm(int64_t n, const T *__restrict__ dx, double *__restrict__ x, double *partials,
                                unsigned *counter, double *out) {
-  double v = 0.0;
+  float v = 0.0f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double d = (double)dx[i];
-    x[i] += d;
-    v += d * d;
+    const T d = dx[i];
+    x[i] += (double)d;
+    v += (float)d * (float)d;
   }
-  grid_reduce(v, partials, counter, out);
+  grid_reduce((double)v, partials, counter, out);
 }
 
 // ns.psi += dx, then F and ||F|| of the updated state.
@@ -513,8 +514,8 @@ static double residual_after_update(NlsImpl &s, NewtonState &ns, const T *dx, do
     ++s.launch_count;
     return residual_norm_kept(s, ns, g, mu);
   }
-  axpy_cast_norm<T><<<reduce_grid(n2), 256, 0, s.stream>>>(n2, dx, ns.psi.p, s.red.partials.p, s.red.counter.p,
-                                                           s.red.out.p + 1);
+  axpy_cast_norm<T><<<vec_grid(n2), 256, 0, s.stream>>>(n2, dx, ns.psi.p, s.red.partials.p, s.red.counter.p,
+                                                        s.red.out.p + 1);
   ++s.launch_count;
   s.residual_update(ns.psi.p, (const float *)dx, g, mu, ns.f.p, ns.soff.p);
   double sq[2] = {0.0, 0.0};  // ||F||^2, ||dx||^2
