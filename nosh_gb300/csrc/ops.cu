@@ -325,7 +325,29 @@ __global__ void history_dots(int64_t n, const double *x0, const double *x1, cons
                              (const C2<double> *)x4};
   const C2<double> *a0 = (const C2<double> *)x0;
   double re[4] = {0, 0, 0, 0}, im[4] = {0, 0, 0, 0};
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // two elements per pass, all their loads issued before the first product
+  for (; i + stride < n; i += 2 * stride) {
+    const C2<double> y0 = a0[i], y1 = a0[i + stride];
+    C2<double> u[4], v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (k < count) {
+        u[k] = xs[k][i];
+        v[k] = xs[k][i + stride];
+      }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (k < count) {
+        re[k] += u[k].x * y0.x + u[k].y * y0.y;
+        im[k] += u[k].x * y0.y - u[k].y * y0.x;
+        re[k] += v[k].x * y1.x + v[k].y * y1.y;
+        im[k] += v[k].x * y1.y - v[k].y * y1.x;
+      }
+    }
+  }
+  for (; i < n; i += stride) {
     const C2<double> y = a0[i];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
