@@ -414,7 +414,12 @@ void ContinuationImpl::advance(double mu_new, int predictor, const nosh_newton_o
     // network's starting residual is worse
     double nrm[2];
     ns.ensure_soff(2 * s.N);
-    s.residual_pair(ns.tmp.p, ns.psi.p, g, mu_new, ns.f.p, ns.xc.p, nrm, ns.soff_alt.p, ns.soff.p);
+    s.residual_pair(ns.tmp.p, ns.psi.p, g, mu_new, ns.f.p, ns.xc.p, nrm, ns.soff_alt.p, ns.soff.p, false);
+    // while the host waits for the two norms, the GPU builds the mixed
+    // Newton step's operators at the learned prediction (the usual winner;
+    // a secant that wins is rebuilt for in the Newton loop)
+    if (opt.precision != NOSH_PREC_FP64) prebuild_operators32(s, ns, ns.tmp.p, g, mu_new);
+    s.residual_pair_norms(nrm);
     if (overlap) coef = *w_host;
     f_learned = nrm[0];
     f_secant = nrm[1];

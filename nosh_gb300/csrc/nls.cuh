@@ -229,7 +229,9 @@ struct NlsImpl {
   // F(xa) into fa and F(xb) into fb in one pass, norms[0..1] = their norms
   // (synchronises); with sa / sb, also the off-diagonal sums of K xa / K xb
   void residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
-                     double norms[2], double *sa = nullptr, double *sb = nullptr);
+                     double norms[2], double *sa = nullptr, double *sb = nullptr, bool wait = true);
+  // the norms of a residual_pair(..., wait = false): waits, then norms[0..1]
+  void residual_pair_norms(double norms[2]);
   void jac_rebuild(const double *x, double g, double mu);
   // the FP32 diagonal blocks of J and of the regularised KEO only, for a
   // mixed-precision solve

@@ -857,7 +857,7 @@ int NlsImpl::max_row_nnz() {
 }
 
 void NlsImpl::residual_pair(const double *xa, const double *xb, double g, double mu, double *fa, double *fb,
-                            double norms[2], double *sa, double *sb) {
+                            double norms[2], double *sa, double *sb, bool wait) {
   if (!(keo_mu == mu)) keo_refill(mu);
   residual_pair_kernel<<<div_up(N, 128), 128, 0, stream>>>(
       (int)N, mesh->d_rp.p, mesh->d_ci.p, d_keo64.p, d_kdiag.p, d_cvt.p, d_V.p, g, (const C2<double> *)xa,
@@ -865,6 +865,10 @@ void NlsImpl::residual_pair(const double *xa, const double *xb, double g, double
       red.partials.p, red.counter.p, red.out.p);
   ++launch_count;
   NOSH_CUDA(cudaGetLastError());
+  if (wait) residual_pair_norms(norms);
+}
+
+void NlsImpl::residual_pair_norms(double norms[2]) {
   red.out.download(norms, 2, stream);
   sync();
   norms[0] = std::sqrt(norms[0]);

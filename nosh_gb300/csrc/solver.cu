@@ -557,6 +557,13 @@ static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu
   ensure_preconditioner(s).refresh<T>();
 }
 
+void prebuild_operators32(NlsImpl &s, NewtonState &ns, const double *psi, double g, double mu) {
+  rebuild_operators<float>(s, psi, g, mu);
+  ns.ops_state = psi;
+  ns.ops_g = g;
+  ns.ops_mu = mu;
+}
+
 template <typename T>
 static Minres<T> &minres_of(NlsImpl &s, NewtonState &ns);
 template <>
@@ -626,6 +633,7 @@ static void newton_loop_systems(NlsImpl &s, NewtonState &ns, double g, double mu
   std::vector<double> fcur = s.h_sys_norm, rtol(S, sizeof(T) == 4 ? 1e-6 : 1e-12);
   std::vector<int> its;
   double fn = st.f_norm0, fn_prev = fn;
+  ns.ops_state = nullptr;
   for (int it = 0; it < opt.max_newton && fn > opt.tol; it++) {
     rebuild_operators<T>(s, ns.psi.p, g, mu);
     s.mask_converged(ns.f.p, opt.tol);
@@ -684,8 +692,10 @@ static void newton_loop(NlsImpl &s, NewtonState &ns, double g, double mu,
   double fn = st.f_norm0, fn_prev = fn;
   // with a refine target, a state above 4 refine gets at least one step
   const bool polish = opt.refine > 0.0 && fn > 4.0 * opt.refine;
+  const bool prebuilt = sizeof(T) == 4 && ns.ops_state == ns.psi.p && ns.ops_g == g && ns.ops_mu == mu;
+  ns.ops_state = nullptr;
   for (int it = 0; it < opt.max_newton && (fn > opt.tol || (it == 0 && polish)); it++) {
-    rebuild_operators<T>(s, ns.psi.p, g, mu);
+    if (!(it == 0 && prebuilt)) rebuild_operators<T>(s, ns.psi.p, g, mu);
     // batched systems: converged ones get a zero right-hand side (their
     // Newton update is zero: the Jacobian is block diagonal)
     if (!s.sys_off.empty()) s.mask_converged(ns.f.p, opt.tol);

@@ -105,6 +105,11 @@ struct NewtonState {
   // off-diagonal sums of K psi (FP64, 2N) for the current psi at soff_mu,
   // kept by the mixed-precision Newton steps (residual_update); soff_alt
   // holds a second candidate's (the learned step's two predictions)
+  // the FP32 operators (diagonal blocks, preconditioner) already built for
+  // this state buffer at (ops_g, ops_mu) by prebuild_operators32; the next
+  // mixed-precision Newton step from it skips its first rebuild
+  const double *ops_state = nullptr;
+  double ops_g = 0.0, ops_mu = 0.0;
   DevBuf<double> soff, soff_alt;
   bool soff_valid = false, soff_fresh = false;  // fresh: from an FP64 evaluation, no update since
   double soff_mu = 0.0;
@@ -126,6 +131,11 @@ double residual_norm(NlsImpl &s, const double *psi, double g, double mu, double 
 // ns.soff holds the off-diagonal sums of K psi as well.
 void newton_core(NlsImpl &s, NewtonState &ns, double g, double mu, const nosh_newton_options &opt,
                  nosh_newton_stats &st, double f0 = -1.0, bool soff_ready = false);
+
+// The mixed-precision Newton step's operators at (psi, g, mu), enqueued
+// ahead (e.g. while the host waits for a residual): psi must be the buffer
+// that is ns.psi when newton_core runs.
+void prebuild_operators32(NlsImpl &s, NewtonState &ns, const double *psi, double g, double mu);
 
 // Relative MINRES tolerance of Newton step `it` (fixed forcing, else
 // safeguarded Eisenstat-Walker), floored at what the Krylov precision resolves.

@@ -85,3 +85,29 @@ def test_continuation_identical_with_and_without_overlap():
     assert states[True][1] == states[False][1]
     assert np.array_equal(states[True][0], states[False][0])
     assert np.linalg.norm(P.compute_f(states[True][0], 1.0, mu + 0.05)) <= 2e-10
+
+
+def test_learned_continuation_identical_with_and_without_overlap():
+    # the learned path adds the inference on a second stream (every second
+    # step here) and the operators built while the host waits for the
+    # predictor residuals
+    import nosh_gb300 as ng
+
+    states = {}
+    for overlap in (True, False):
+        model, P, psi0, mu = _model("square65", 1, 0)
+        model.set_launch_overlap(overlap)
+        psi = psi0.copy()
+        assert model.newton(psi, {"g": 1.0, "mu": mu}, tol=1e-10)["status"] == 0
+        run = ng.continuation(model, psi, mu)
+        run.learning(4, 5, 2e-3)
+        run.inference_period(2)
+        its = []
+        for k in range(1, 15):
+            st = run.advance(mu + 0.005 * k, ng.PREDICT_LEARNED)
+            assert st["status"] == 0, st
+            its.append((st["krylov_iters"], run.last_prediction()["used"]))
+        states[overlap] = (run.state()[0], its)
+    assert states[True][1] == states[False][1]
+    assert np.array_equal(states[True][0], states[False][0])
+    assert np.linalg.norm(P.compute_f(states[True][0], 1.0, mu + 0.07)) <= 2e-10
