@@ -29,9 +29,16 @@ template <typename T>
 __global__ void dot_kernel(int64_t n, const T *__restrict__ a, const T *__restrict__ b,
                            double *partials, unsigned *counter, double *out) {
   double v = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    v += (double)a[i] * (double)b[i];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // two elements per pass, their loads issued first (the per-thread order
+  // stays i, i + stride, ...)
+  for (; i + stride < n; i += 2 * stride) {
+    const T a0 = a[i], b0 = b[i], a1 = a[i + stride], b1 = b[i + stride];
+    v += (double)a0 * (double)b0;
+    v += (double)a1 * (double)b1;
+  }
+  for (; i < n; i += stride) v += (double)a[i] * (double)b[i];
   grid_reduce(v, partials, counter, out);
 }
 
