@@ -46,69 +46,78 @@ __device__ __forceinline__ const double *wx_coef<double>(const MinresScalars *s)
 // Lanczos coefficients once <z, J z> (zu) is known.  Single thread.  After
 // convergence (done == 1) the launch has applied the last deferred w/x
 // update, and the recurrence is frozen (done = 2): the remaining launches of
-// the chunk return at once.
-__device__ __forceinline__ void minres_lanczos_coefs(MinresScalars *s, double zu) {
-  if (s->done) {
-    s->done = 2;
-    s->wx_pending = 0;
+// the chunk return at once.  The state is read into registers in one go and
+// written back once: field by field, its dependent global loads and stores
+// were the longest chain of the launch's tail.
+__device__ __forceinline__ void minres_lanczos_coefs(MinresScalars *sp, double zu) {
+  MinresScalars s = *sp;
+  if (s.done) {
+    sp->done = 2;
+    sp->wx_pending = 0;
     return;
   }
-  s->zu = zu;
-  const double beta = s->beta, alfa = zu / (beta * beta);
-  const double c[3] = {1.0 / beta, s->itn > 0 ? beta / s->oldb : 0.0, alfa / beta};
+  s.zu = zu;
+  const double beta = s.beta, alfa = zu / (beta * beta);
+  const double c[3] = {1.0 / beta, s.itn > 0 ? beta / s.oldb : 0.0, alfa / beta};
   for (int k = 0; k < 3; k++) {
-    s->la64[k] = c[k];
-    s->la32[k] = (float)c[k];
+    s.la64[k] = c[k];
+    s.la32[k] = (float)c[k];
   }
+  *sp = s;
 }
 
 // One step of the Paige-Saunders Givens recurrence after <r_new, M r_new>
-// (rz) is known; scipy / Paige-Saunders variable names.  Single thread.
-__device__ __forceinline__ void minres_advance(MinresScalars *s, double rz) {
-  s->rz = rz;
-  if (s->done) {
-    s->done = 2;
-    s->wx_pending = 0;
+// (rz) is known; scipy / Paige-Saunders variable names.  Single thread; the
+// state in registers as above.
+__device__ __forceinline__ void minres_advance(MinresScalars *sp, double rz) {
+  MinresScalars s = *sp;
+  s.rz = rz;
+  if (s.done) {
+    s.done = 2;
+    s.wx_pending = 0;
+    *sp = s;
     return;
   }
-  const double beta = s->beta;
-  const double alfa = s->zu / (beta * beta);
-  s->alfa = alfa;
-  s->oldb = beta;
+  const double beta = s.beta;
+  const double alfa = s.zu / (beta * beta);
+  s.alfa = alfa;
+  s.oldb = beta;
   if (!(rz >= 0.0) || isinf(rz) || isnan(alfa)) {
-    s->flag = (isnan(rz) || isinf(rz) || isnan(alfa)) ? NOSH_ERR_NAN : NOSH_ERR_BREAKDOWN;
-    s->done = 2;
-    s->wx_pending = 0;
+    s.flag = (isnan(rz) || isinf(rz) || isnan(alfa)) ? NOSH_ERR_NAN : NOSH_ERR_BREAKDOWN;
+    s.done = 2;
+    s.wx_pending = 0;
+    *sp = s;
     return;
   }
   const double nb = sqrt(rz);
-  s->beta = nb;
-  s->oldeps = s->epsln;
-  const double delta = s->cs * s->dbar + s->sn * alfa;
-  const double gbar = s->sn * s->dbar - s->cs * alfa;
-  s->epsln = s->sn * nb;
-  s->dbar = -s->cs * nb;
+  s.beta = nb;
+  s.oldeps = s.epsln;
+  const double delta = s.cs * s.dbar + s.sn * alfa;
+  const double gbar = s.sn * s.dbar - s.cs * alfa;
+  s.epsln = s.sn * nb;
+  s.dbar = -s.cs * nb;
   double gamma = hypot(gbar, nb);
   if (gamma == 0.0) gamma = 2.2e-16;
-  s->cs = gbar / gamma;
-  s->sn = nb / gamma;
-  s->phi = s->cs * s->phibar;
-  s->phibar = s->sn * s->phibar;
-  s->gamma = gamma;
-  s->delta = delta;
-  s->itn += 1;
-  s->wx_pending = 1;
-  const double w[5] = {1.0 / s->oldb, s->oldeps, delta, 1.0 / gamma, s->phi};
+  s.cs = gbar / gamma;
+  s.sn = nb / gamma;
+  s.phi = s.cs * s.phibar;
+  s.phibar = s.sn * s.phibar;
+  s.gamma = gamma;
+  s.delta = delta;
+  s.itn += 1;
+  s.wx_pending = 1;
+  const double w[5] = {1.0 / s.oldb, s.oldeps, delta, 1.0 / gamma, s.phi};
   for (int k = 0; k < 5; k++) {
-    s->wx64[k] = w[k];
-    s->wx32[k] = (float)w[k];
+    s.wx64[k] = w[k];
+    s.wx32[k] = (float)w[k];
   }
-  if (s->phibar <= s->rtol * s->beta1 || nb == 0.0) {
-    s->done = 1;
-  } else if (s->itn >= s->maxit) {
-    s->done = 1;
-    s->flag = NOSH_ERR_NOT_CONVERGED;
+  if (s.phibar <= s.rtol * s.beta1 || nb == 0.0) {
+    s.done = 1;
+  } else if (s.itn >= s.maxit) {
+    s.done = 1;
+    s.flag = NOSH_ERR_NOT_CONVERGED;
   }
+  *sp = s;
 }
 
 // The deferred w/x update of one Lanczos step for element i:
