@@ -192,14 +192,20 @@ template <> struct alignas(16) C2<double> { double x, y; };
 // Programmatic dependent launch (griddepcontrol, sm_90 and later).
 // dep_sync: block until the kernel this one was launched after (with
 // overlap, see launch_dep) has completed and flushed its writes; returns at
-// once for a plain launch.  The kernels never trigger their successors
-// explicitly (griddepcontrol.launch_dependents): a successor launches as the
-// last CTA exits.  Measured on GB300 over chains of 100 graph-captured
+// once for a plain launch.  Kernels do not trigger their successors
+// explicitly (griddepcontrol.launch_dependents), so a successor launches as
+// the last CTA exits, except for the one CTA that finishes a grid reduction
+// (dep_trigger).  Measured on GB300 over chains of 100 graph-captured
 // kernels (16 K to 8 M elements): the implicit trigger saved 0.16-0.25 us
 // per launch against plain edges, while a trigger at the start of every CTA
 // cost up to 3.8 us per launch (the successor's waiting CTAs hold the SMs)
-// and one after the work cost up to 1.4 us.
+// and one after the work in every CTA up to 1.4 us.
 __device__ __forceinline__ void dep_sync() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+// Let the next kernel of the stream start launching now (used by the CTA
+// that finishes a grid reduction: every other CTA has left by then, and its
+// own tail of serial work overlaps the successor's launch; the successor
+// still waits in dep_sync for this kernel's completion).
+__device__ __forceinline__ void dep_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
 // read-only-path loads of complex pairs
 __device__ __forceinline__ C2<float> ldg(const C2<float> *p) {

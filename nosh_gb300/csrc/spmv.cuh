@@ -58,6 +58,7 @@ __device__ __forceinline__ bool grid_reduce(double v, double *partials, unsigned
   __syncthreads();
   bool finisher = false;
   if (last) {
+    dep_trigger();
     __threadfence();
     // four independent accumulators so the partial loads overlap (fixed
     // order per thread: deterministic)
