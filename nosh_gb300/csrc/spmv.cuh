@@ -21,6 +21,18 @@
 namespace nosh {
 namespace dev {
 
+// Arrival at a grid reduction: counter += 1 with acquire-release semantics
+// at GPU scope, returning the old value.  The release publishes the CTA's
+// partial written before it; the acquire, in the CTA that arrives last,
+// orders the partials read after it (behind the CTA barrier that follows)
+// after every other CTA's write.  It takes the place of a full fence on
+// either side of a relaxed atomic.
+__device__ __forceinline__ unsigned arrive_acq_rel(unsigned *counter) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(counter) : "memory");
+  return old;
+}
+
 constexpr int kRows = 128;
 // Threads per row of the staged schedule (adjacent lanes, each taking every
 // row_threads-th nonzero).  One: two lanes per FP32 row (twice the warps
@@ -51,15 +63,13 @@ __device__ __forceinline__ bool grid_reduce(double v, double *partials, unsigned
   const double b = block_sum(v, s32);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = b;
-    __threadfence();
-    const unsigned t = atomicAdd(counter, 1u);
+    const unsigned t = arrive_acq_rel(counter);
     last = (t == gridDim.x - 1);
   }
   __syncthreads();
   bool finisher = false;
   if (last) {
     dep_trigger();
-    __threadfence();
     // four independent accumulators so the partial loads overlap (fixed
     // order per thread: deterministic)
     const unsigned G = gridDim.x, st = blockDim.x;
@@ -116,14 +126,13 @@ __device__ __forceinline__ bool grid_reduce_n(const double (&v)[K], int m, doubl
     }
   }
   if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned t = atomicAdd(counter, 1u);
+    const unsigned t = arrive_acq_rel(counter);
     last = (t == gridDim.x - 1);
   }
   __syncthreads();
   bool finisher = false;
   if (last) {
-    __threadfence();
+    dep_trigger();
     const unsigned G = gridDim.x, st = blockDim.x;
     double acc[K];
 #pragma unroll
