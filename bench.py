@@ -488,10 +488,12 @@ def run_gb300(args):
                                "the step (--cache-control none): the working set stays in L2 between "
                                "launches, so DRAM moves far fewer bytes than the algorithmic count"
                                + ("" if args.m == 64 else "; scaled to this launch by its algorithmic bytes"),
-             "timing": "CUDA events around each launch on the library stream (event-record nodes of the "
-                       "replayed MINRES graphs), during extra continuation steps of the same workload run "
-                       "after the timed ones; launches that did no work (after convergence inside a "
-                       "captured graph part) are not counted"}
+             "timing": "CUDA events on the library stream (event-record nodes of the replayed MINRES "
+                       "graphs) around each Jacobian launch and around each run of consecutive fine-level "
+                       "smoother launches (the pre-smoothing step with the residual, the two post-smoothing "
+                       "steps), during extra continuation steps of the same workload run after the timed "
+                       "ones; launches that did no work (after convergence inside a captured graph part) "
+                       "are not counted"}
         if name == dom:
             roof = d
         else:

@@ -1302,17 +1302,17 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
   const int vb = (int)sizeof(T);
   const double cheb_bytes = nls.spmv_bytes(2 * vb, 16 * vb);
   const double res_bytes = nls.spmv_bytes(2 * vb, 9 * vb);
+  // timed as one event pair around the consecutive fine-level launches of
+  // the pre-smoothing and the residual (and of the post-smoothing below)
+  if (tm) tm->begin(st);
   for (int k = 1; k < deg; k++) {
     ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, halt};
-    if (tm) tm->begin(st);
     rows<T>(l, cur, op);
-    if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
   ResidOp<T> rop{dv, b, x, V.res[l].p, halt};
-  if (tm) tm->begin(st);
   rows<T>(l, x, rop);
-  if (tm) tm->end(st, res_bytes);
+  if (tm) tm->end(st, (deg - 1) * cheb_bytes + res_bytes, deg);
   const AmgLevel &Cl = lev[l + 1];
   if (l + 1 < lt) {
     // restriction + first step of level l+1, whose pre-smoothing must end in
@@ -1341,8 +1341,8 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
   ++nls.launch_count;
   cur = x;
   oth = V.x2[l].p;
+  if (tm) tm->begin(st);
   for (int k = 0; k < deg; k++) {
-    if (tm) tm->begin(st);
     if (ms && k == deg - 1) {
       ChebMinresOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, ms, halt};
       rows<T>(l, cur, op);
@@ -1350,9 +1350,9 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
       ChebOp<T> op{dv, V.dinv[l].p, V.coef[l].p, k, b, cur, V.d[l].p, oth, halt};
       rows<T>(l, cur, op);
     }
-    if (tm) tm->end(st, cheb_bytes);
     std::swap(cur, oth);
   }
+  if (tm) tm->end(st, deg * cheb_bytes, deg);
   if (cur != x) {
     NOSH_CUDA(cudaMemcpyAsync(x, cur, A.n * sizeof(C2<T>), cudaMemcpyDeviceToDevice, st));
   }

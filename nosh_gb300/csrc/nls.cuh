@@ -43,6 +43,7 @@ struct KernelTimer {
   struct Pair {
     cudaEvent_t a = nullptr, b = nullptr;
     double bytes = 0.0;
+    int n = 1;  // launches between the two events
   };
   std::vector<Pair> captured;  // pairs captured since the last take()
   Pair cap;
@@ -71,12 +72,15 @@ struct KernelTimer {
     }
     NOSH_CUDA(cudaEventRecord(ev[used], s));
   }
-  void end(cudaStream_t s, double b) {
+  // n: the launches of the class issued since begin (consecutive, with no
+  // other kernel between them); b: their algorithmic bytes
+  void end(cudaStream_t s, double b, int n = 1) {
     if (!on) return;
     if (cap_open) {
       cap_open = false;
       NOSH_CUDA(cudaEventRecordWithFlags(cap.b, s, cudaEventRecordExternal));
       cap.bytes = b;
+      cap.n = n;
       captured.push_back(cap);
       return;
     }
@@ -84,7 +88,7 @@ struct KernelTimer {
     open_pair = false;
     NOSH_CUDA(cudaEventRecord(ev[used + 1], s));
     used += 2;
-    launches++;
+    launches += n;
     bytes += b;
   }
   std::vector<Pair> take() {
@@ -97,7 +101,7 @@ struct KernelTimer {
     float t = 0.f;
     NOSH_CUDA(cudaEventElapsedTime(&t, p.a, p.b));
     graph_ms += t;
-    launches++;
+    launches += p.n;
     bytes += p.bytes;
   }
   static void release(std::vector<Pair> &v) {
