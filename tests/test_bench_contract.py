@@ -1,0 +1,31 @@
+"""The benchmark's reference arm on a small cube, on the CPU: one JSON line
+with the fields the driver reads, the arm's own cpu_baseline and e2e, and no
+CUDA library mapped into the process (the arm runs the FP64 CPU
+restatement only)."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = subprocess.run(
+        [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--m", "12", "--steps", "2",
+         "--warmup", "1", "--cpu-seconds", "2"],
+        capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["unit"] == "steps/s" and d["value"] > 0
+    assert d["steps"] == 2 and d["higher_is_better"] is True
+    assert d["config"]["predictor"] == "secant" and d["config"]["precision"] == "fp64"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert d["e2e"]["d2h_bytes_per_step"] == 0
