@@ -1,7 +1,7 @@
-"""The benchmark's reference arm on a small cube, on the CPU: one JSON line
-with the fields the driver reads, the arm's own cpu_baseline and e2e, and no
-CUDA library mapped into the process (the arm runs the FP64 CPU
-restatement only)."""
+"""The benchmark's reference arm on a small cube, on the CPU (it runs the
+FP64 CPU restatement only): one JSON line with the fields the driver reads,
+the arm's own cpu_baseline and e2e, and the predictor and precision it
+actually runs in its config."""
 import json
 import os
 import subprocess
