@@ -144,7 +144,7 @@ struct NlsImpl {
   DevBuf<double> d_A, d_V, d_t, d_cvt;  // 3N, N, N, N (cv * thickness)
   std::vector<double> h_V, h_t;
   DevBuf<double> d_p, d_alpha, d_kdiag;  // E, E, N
-  DevBuf<float> d_pf, d_alphaf, d_kdiagf;
+  DevBuf<float> d_kdiagf;
   double cv_sum = 0.0;
 
   // off-diagonal KEO values in adjacency-CSR order (2E + kPad)

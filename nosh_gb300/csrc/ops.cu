@@ -23,8 +23,7 @@ namespace {
 __global__ void edge_fields_kernel(int64_t E, const int32_t *__restrict__ edges,
                                    const double *__restrict__ x, const double *__restrict__ A,
                                    const double *__restrict__ len, const double *__restrict__ covol,
-                                   const double *__restrict__ t, double *p, double *alpha,
-                                   float *pf, float *alphaf) {
+                                   const double *__restrict__ t, double *p, double *alpha) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= E) return;
   const int64_t a = edges[2 * e], b = edges[2 * e + 1];
@@ -34,8 +33,6 @@ __global__ void edge_fields_kernel(int64_t E, const int32_t *__restrict__ edges,
   const double al = covol[e] / len[e] * 0.5 * (t[a] + t[b]);
   p[e] = s;
   alpha[e] = al;
-  pf[e] = (float)s;
-  alphaf[e] = (float)al;
 }
 
 // K_ii = sum of alpha over the edges of row i (mu-independent), in column
@@ -92,33 +89,28 @@ __device__ __forceinline__ void edge_sincos(double x, double &s, double &c) {
 
 // KEO assembly, edge-parallel through the scatter map (no atomics): c_e =
 // -alpha_e e^{-i mu p_e} at (v0, v1), conj(c_e) at (v1, v0).  mu_sys / esys
-// (optional): the edge's system supplies its own mu.
-__global__ void keo_assemble64(int64_t E, const double *__restrict__ alpha, const double *__restrict__ p, double mu,
-                               const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
-                               C2<double> *__restrict__ val, const double *__restrict__ mu_sys,
-                               const int32_t *__restrict__ esys) {
+// (optional): the edge's system supplies its own mu.  The FP32 operator of
+// the mixed path is written in the same pass, each component the FP64
+// value rounded to nearest (|K32 - K| <= 2^-24 |K| per component, the
+// premise of the residual update's bound): the pass is bound by FP64
+// arithmetic, so the extra 16 bytes per edge cost no time, and a separate
+// FP32 assembly pass (16 us at 64^3) is saved.
+__global__ void keo_assemble(int64_t E, const double *__restrict__ alpha, const double *__restrict__ p, double mu,
+                             const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
+                             C2<double> *__restrict__ val, C2<float> *__restrict__ val32,
+                             const double *__restrict__ mu_sys, const int32_t *__restrict__ esys) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= E) return;
   const double m = mu_sys ? mu_sys[esys[e]] : mu;
   double s, c;
   edge_sincos(m * p[e], s, c);
   const double al = alpha[e];
-  val[pf[e]] = C2<double>{-al * c, al * s};
-  val[pb[e]] = C2<double>{-al * c, -al * s};
-}
-
-__global__ void keo_assemble32(int64_t E, const float *__restrict__ alpha, const float *__restrict__ p, float mu,
-                               const int32_t *__restrict__ pf, const int32_t *__restrict__ pb,
-                               C2<float> *__restrict__ val, const double *__restrict__ mu_sys,
-                               const int32_t *__restrict__ esys) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  const float m = mu_sys ? (float)mu_sys[esys[e]] : mu;
-  float s, c;
-  sincosf(m * p[e], &s, &c);
-  const float al = alpha[e];
-  val[pf[e]] = C2<float>{-al * c, al * s};
-  val[pb[e]] = C2<float>{-al * c, -al * s};
+  const double re = -al * c, im = al * s;
+  const int32_t f = pf[e], b = pb[e];
+  val[f] = C2<double>{re, im};
+  val[b] = C2<double>{re, -im};
+  val32[f] = C2<float>{(float)re, (float)im};
+  val32[b] = C2<float>{(float)re, -(float)im};
 }
 
 // DkeoDP::refill_ (src/parameter_matrix_dkeo_dp.cpp:96-151): block entries
@@ -599,14 +591,11 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
   d_t.upload(h_t, s);
   d_p.alloc(E);
   d_alpha.alloc(E);
-  d_pf.alloc(E);
-  d_alphaf.alloc(E);
   d_kdiag.alloc(N);
   d_kdiagf.alloc(N);
   d_cvt.alloc(N);
   edge_fields_kernel<<<div_up(E, 256), 256, 0, s>>>(E, m->d_edges.p, m->d_x.p, d_A.p, m->d_len.p,
-                                                     m->d_covol.p, d_t.p, d_p.p, d_alpha.p, d_pf.p,
-                                                     d_alphaf.p);
+                                                     m->d_covol.p, d_t.p, d_p.p, d_alpha.p);
   ++launch_count;
   vertex_fields_kernel<<<div_up(N, 256), 256, 0, s>>>(N, m->d_rp.p, m->d_nz_edge.p, d_alpha.p,
                                                        m->d_cv.p, d_t.p, d_kdiag.p, d_kdiagf.p,
@@ -624,6 +613,10 @@ NlsImpl::NlsImpl(MeshImpl *m, const double *mvp, double mu, const double *V, dou
   d_rd64.alloc(3 * N);
   d_jd32.alloc(3 * N);
   d_rd32.alloc(3 * N);
+  d_jd64.zero(s);
+  d_rd64.zero(s);
+  d_jd32.zero(s);
+  d_rd32.zero(s);
   d_in.alloc(2 * N);
   d_out.alloc(2 * N);
   d_tmp.alloc(2 * N);
@@ -768,11 +761,9 @@ void NlsImpl::set_stage_wait_limit(int64_t polls) {
 
 void NlsImpl::keo_refill(double mu) {
   const double *ms = sys_off.empty() ? nullptr : d_mu_sys.p;
-  keo_assemble64<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, mesh->d_pos_fwd.p,
-                                                      mesh->d_pos_bwd.p, d_keo64.p, ms, d_esys.p);
-  keo_assemble32<<<div_up(E, 256), 256, 0, stream>>>(E, d_alphaf.p, d_pf.p, (float)mu, mesh->d_pos_fwd.p,
-                                                      mesh->d_pos_bwd.p, d_keo32.p, ms, d_esys.p);
-  launch_count += 2;
+  keo_assemble<<<div_up(E, 256), 256, 0, stream>>>(E, d_alpha.p, d_p.p, mu, mesh->d_pos_fwd.p, mesh->d_pos_bwd.p,
+                                                    d_keo64.p, d_keo32.p, ms, d_esys.p);
+  ++launch_count;
   NOSH_CUDA(cudaGetLastError());
   keo_mu = mu;
 }

@@ -556,6 +556,10 @@ Amg &ensure_preconditioner(NlsImpl &s) {
 template <typename T>
 static void rebuild_operators(NlsImpl &s, const double *psi, double g, double mu) {
   if constexpr (sizeof(T) == 4) {
+    // the preconditioner's one-time setup (the host aggregation's strength
+    // test) reads the FP64 regularised diagonal, which the mixed rebuild
+    // does not write: fill it at this state first
+    if (!s.amg) s.reg_rebuild(psi, g, mu);
     s.operators32_rebuild(psi, g, mu);
   } else {
     s.jac_rebuild(psi, g, mu);
