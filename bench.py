@@ -297,6 +297,21 @@ def cpu_run(args, steps, time_budget=None, x=None, cells=None, psi0=None):
     return times, its, S.threads()
 
 
+def cpu_single_thread(args, budget, x=None, cells=None, psi0=None):
+    """The same CPU sample on one OpenMP thread (bounded by `budget` seconds
+    of timed steps); the thread count is restored afterwards."""
+    from oracle import oracle as O
+
+    prev = O.CpuSolver.set_threads(1)
+    try:
+        times, its, threads = cpu_run(args, 1000, time_budget=budget, x=x, cells=cells, psi0=psi0)
+    finally:
+        O.CpuSolver.set_threads(prev)
+    return {"value": 1.0 / float(np.mean(times)), "unit": "steps/s", "cores": threads,
+            "sample": f"{len(times)} secant continuation steps, FP64 CPU restatement on one thread",
+            "newton_krylov_per_step": [float(np.mean([a for a, b in its])), float(np.mean([b for a, b in its]))]}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -594,6 +609,7 @@ def run_gb300(args):
         out["cpu_baseline"] = {"value": cv, "unit": "steps/s", "cores": threads, "kind": "port",
                                "sample": f"{len(times)} secant continuation steps of the same workload "
                                          f"(FP64 CPU restatement, {threads} OpenMP threads)"}
+        out["cpu_baseline"]["single_thread"] = cpu_single_thread(args, args.cpu_seconds / 2, x, cells, psi0)
         out["same_precision"] = {"plain_fp64_gpu": out["plain_fp64"]["value"], "cpu_fp64": cv,
                                  "ratio": out["plain_fp64"]["value"] / cv,
                                  "note": "the FP64 GPU path with the plain predictor against the FP64 CPU "

@@ -113,6 +113,9 @@ nor_solver *nor_solver_create(int64_t N, int64_t E, const int32_t *edges,
                               const double *V, double g);
 void nor_solver_destroy(nor_solver *s);
 int nor_num_threads(void);
+/* OpenMP threads of the solver calls that follow on the calling host thread
+   (n >= 1; n < 1 leaves it unchanged); returns the previous maximum. */
+int nor_set_num_threads(int n);
 int nor_newton(nor_solver *s, double *psi, double mu, double tol,
                int max_newton, int *newton_its, int *krylov_its,
                double *fnorm0, double *fnorm);

@@ -138,6 +138,18 @@ int nor_num_threads(void)
 #endif
 }
 
+int nor_set_num_threads(int n)
+{
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (n >= 1) omp_set_num_threads(n);
+  return prev;
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
 /* ------------------------------------------------------------ operators */
 static void keo_refill(nor_solver *s, double mu)
 {

@@ -68,6 +68,7 @@ def lib():
             "nor_solver_create": (C.c_void_p, [I64, I64, i32p, f64p, f64p, f64p, f64p, f64p, F64]),
             "nor_solver_destroy": (None, [C.c_void_p]),
             "nor_num_threads": (I, []),
+            "nor_set_num_threads": (I, [I]),
             "nor_newton": (I, [C.c_void_p, f64p, F64, F64, I, C.POINTER(I), C.POINTER(I),
                                C.POINTER(F64), C.POINTER(F64)]),
             "nor_continuation_step": (I, [C.c_void_p, f64p, C.c_void_p, F64, F64, F64, F64, C.POINTER(I),
@@ -565,6 +566,12 @@ class CpuSolver:
     @staticmethod
     def threads():
         return lib().nor_num_threads()
+
+    @staticmethod
+    def set_threads(n):
+        """OpenMP threads of the solver calls that follow on this thread;
+        returns the previous count."""
+        return lib().nor_set_num_threads(int(n))
 
     def newton(self, psi, mu, tol=1e-10, max_newton=20):
         ni, ki = C.c_int(), C.c_int()

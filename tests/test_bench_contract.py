@@ -29,3 +29,21 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_single_thread_cpu_sample_restores_the_thread_count():
+    """The headline's CPU baseline also reports the restatement on one
+    OpenMP thread; the sample runs on one thread and leaves the count as it
+    found it."""
+    import argparse
+
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import oracle as O
+
+    before = O.CpuSolver.threads()
+    args = argparse.Namespace(m=8, seed=2, field="constant_curl", mu0=0.5, dmu=0.005)
+    out = bench.cpu_single_thread(args, 0.5)
+    assert out["cores"] == 1 and out["value"] > 0 and out["unit"] == "steps/s"
+    assert out["newton_krylov_per_step"][0] >= 1
+    assert O.CpuSolver.threads() == before
