@@ -132,8 +132,9 @@ int nosh_nls_get_precision(nosh_nls nls, int *precision);
  * 1.1 lmax]).  Defaults 10, 64, 2, 8 and, from sweeps, 0 and 15 on
  * tetrahedral meshes, 0.05 and 30 on triangular ones (a batched union of
  * many squares solved 12 % faster at threshold 0).  A connection (i, j) is
- * strong when |K_ij| >= threshold sqrt(d_i d_j), d the regularised
- * operator's diagonal at the state of the first rebuild.  Drops the
+ * strong when |K_ij| >= threshold sqrt(d_i d_j), d_i the mean of the two
+ * diagonal entries of the regularised operator's block at vertex i, at the
+ * state of the first rebuild.  Drops the
  * current hierarchy; the next rebuild builds a new one. */
 int nosh_nls_set_amg_options(nosh_nls nls, int max_levels, int coarse_size,
                              int smooth_degree, int reuse_period,
