@@ -502,9 +502,16 @@ __global__ void axpy_cast_norm(int64_t n, const T *__restrict__ dx, double *__re
 // a fresh FP64 evaluation at this mu and the state is close to converged
 // (||F|| <= 100 tol before the step), the update is evaluated from them:
 // soff += K dx by an FP32 SpMV of the FP32 update, F = soff + the per-vertex
-// FP64 terms (ResidualUpdateOp).  Its deviation from the FP64 evaluation is
-// bounded by e = 2 (n_max + 2) 2^-24 R ||dx||_2 (an FP32 dot product of at
-// most n_max terms, the FP32 rounding of K; R bounds the row sums of |K|).
+// FP64 terms (ResidualUpdateOp).  Beyond FP64 rounding, it deviates from
+// the FP64 evaluation by the FP32 product's error alone: per real component
+// of row i, at most gamma_{2n} (one rounding per real multiply-add of the
+// row's 2n, n <= n_max off-diagonal nonzeros) plus 2^-24 (K32 is K rounded
+// per component) times sum_j |K_ij| |dx_j|, since |a x| + |b y| <= |K_ij|
+// |dx_j| for K_ij = a + ib, dx_j = x + iy.  Over the 2N components, with
+// || |K| ||_2 <= R (the largest row sum of |K|, |K| symmetric), that is
+// sqrt(2) (2 n_max + 1) 2^-24 R ||dx||_2, taken as e = 3 (n_max + 1) 2^-24 R
+// ||dx||_2 (the margin covers gamma's denominator and the FP32 sums of
+// ||dx||^2).
 // The estimate is kept when it decides convergence either way with margin
 // e (||F|| <= tol - e, or ||F|| > tol + e with e <= ||F|| / 100, so that
 // it serves as the next step's right-hand side); otherwise F is evaluated
@@ -529,7 +536,7 @@ static double residual_after_update(NlsImpl &s, NewtonState &ns, const T *dx, do
   s.red.out.download(sq, 2, s.stream);
   s.sync();
   const double fn = std::sqrt(sq[0]);
-  const double e = 2.0 * (s.max_row_nnz() + 2) * std::ldexp(1.0, -24) * s.keo_abs_rowmax() * std::sqrt(sq[1]);
+  const double e = 3.0 * (s.max_row_nnz() + 1) * std::ldexp(1.0, -24) * s.keo_abs_rowmax() * std::sqrt(sq[1]);
   if (fn <= tol - e || (fn > tol + e && e <= 0.01 * fn)) {
     ns.soff_fresh = false;
     bound = e;

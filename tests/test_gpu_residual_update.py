@@ -3,7 +3,7 @@
 Close to convergence a Newton step's residual is evaluated as F(psi + dx) =
 [off-diagonal sums of K psi, FP64] + K dx (FP32 product of the small update)
 + the per-vertex FP64 terms at psi + dx, with the bound
-e = 2 (n_max + 2) 2^-24 R ||dx|| on its deviation from the FP64 evaluation.
+e = 3 (n_max + 1) 2^-24 R ||dx|| on its deviation from the FP64 evaluation.
 Checked here against the oracle's FP64 residual of the returned states:
 every reported ||F|| lies within its stated bound (plus the FP64 rounding of
 a fresh evaluation) of the oracle's, the states converge, and the steps that
