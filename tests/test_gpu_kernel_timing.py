@@ -28,6 +28,9 @@ def test_timed_solve_counts_working_launches(prec):
     out = {}
     for timed in (False, True):
         model = ng.nls(ng.mesh(m.x, m.cells), A, -1.0, 1.0, 1.0, mu=0.5, precision=prec)
+        # an explicit schedule: the autotuner decides by timing, and the two
+        # handles are compared bitwise
+        model.set_spmv_schedule(1)
         model.profile(timed)
         psi = psi0.copy()
         st = model.newton(psi, {"g": 1.0, "mu": 0.5}, tol=1e-10)
