@@ -31,6 +31,22 @@ def test_reference_arm_prints_one_contract_line():
     assert d["e2e"]["d2h_bytes_per_step"] == 0
 
 
+def test_solve65_reference_arm_prints_one_contract_line():
+    """The configuration-1 workload's reference arm: one Newton solve of the
+    65 x 65 square on the CPU restatement, in the same JSON contract."""
+    r = subprocess.run(
+        [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", "solve65", "--impl", "reference",
+         "--cpu-seconds", "1"],
+        capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "solves/s" and d["value"] > 0
+    assert d["config"]["precision"] == "fp64" and d["config"]["mu"] == 0.1
+    assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["value"] == d["value"]
+
+
 def test_single_thread_cpu_sample_restores_the_thread_count():
     """The headline's CPU baseline also reports the restatement on one
     OpenMP thread; the sample runs on one thread and leaves the count as it
