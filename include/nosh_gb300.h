@@ -166,7 +166,8 @@ int nosh_nls_system_norms(nosh_nls nls, double *norms);
 int nosh_nls_amg_levels(nosh_nls nls, int *num_levels, int64_t *sizes,
                         int max_sizes, int *tail_level);
 /* SpMV schedule of the handle's operators: NOSH_SPMV_AUTO (default: each
- * matrix times both schedules once and keeps the faster), NOSH_SPMV_STAGED
+ * matrix times both schedules once and keeps the staged one unless the warp
+ * schedule is at least 10 % faster), NOSH_SPMV_STAGED
  * (128-row blocks staged into shared memory by bulk copies) or
  * NOSH_SPMV_WARP (warp-cooperative, a half-warp per row).  Drops the
  * preconditioner hierarchy. */

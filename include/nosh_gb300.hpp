@@ -275,6 +275,19 @@ class nls {
   void set_index_checks(bool on) { check(nosh_nls_set_index_checks(h_, on ? 1 : 0)); }
   // the fraction of the tolerance a Newton step's forcing term aims at
   void set_forcing_aim(double aim) { check(nosh_nls_set_forcing_aim(h_, aim)); }
+  // programmatic dependent launch of the MINRES / V-cycle kernels (on by
+  // default; results are bitwise the same either way)
+  void set_launch_overlap(bool on) { check(nosh_nls_set_launch_overlap(h_, on ? 1 : 0)); }
+  // SpMV schedule of every level: NOSH_SPMV_AUTO (timed once per matrix),
+  // _STAGED or _WARP
+  void set_spmv_schedule(int schedule) { check(nosh_nls_set_spmv_schedule(h_, schedule)); }
+  // the preconditioner's options (MueLu parameter list of
+  // src/keo_regularized.cpp:296-315); the next rebuild builds a new hierarchy
+  void set_amg_options(int max_levels, int coarse_size, int smooth_degree, int reuse_period,
+                       double strength_threshold, double cheb_ratio) {
+    check(nosh_nls_set_amg_options(h_, max_levels, coarse_size, smooth_degree, reuse_period, strength_threshold,
+                                   cheb_ratio));
+  }
   int precision() const {
     int p = 0;
     check(nosh_nls_get_precision(h_, &p));
