@@ -1299,8 +1299,13 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
   C2<T> *cur = (deg % 2 == 1) ? x : V.x2[l].p;
   C2<T> *oth = (deg % 2 == 1) ? V.x2[l].p : x;
   KernelTimer *tm = l == 0 ? &nls.timers[NOSH_KERNEL_SMOOTHER] : nullptr;
+  // values per vertex: a Chebyshev step reads x, b, the diagonal block and
+  // its inverse and the previous direction d, and writes d and x (16; the
+  // first step of a sweep reads no d: 14); the residual reads x, b and the
+  // diagonal block and writes the residual (9)
   const int vb = (int)sizeof(T);
   const double cheb_bytes = nls.spmv_bytes(2 * vb, 16 * vb);
+  const double cheb0_bytes = nls.spmv_bytes(2 * vb, 14 * vb);
   const double res_bytes = nls.spmv_bytes(2 * vb, 9 * vb);
   // timed as one event pair around the consecutive fine-level launches of
   // the pre-smoothing and the residual (and of the post-smoothing below)
@@ -1352,7 +1357,7 @@ void Amg::Impl::descend_ascend(int l, const C2<T> *b, C2<T> *x, MinresScalars *m
     }
     std::swap(cur, oth);
   }
-  if (tm) tm->end(st, deg * cheb_bytes, deg);
+  if (tm) tm->end(st, cheb0_bytes + (deg - 1) * cheb_bytes, deg);
   if (cur != x) {
     NOSH_CUDA(cudaMemcpyAsync(x, cur, A.n * sizeof(C2<T>), cudaMemcpyDeviceToDevice, st));
   }

@@ -96,13 +96,14 @@ struct KernelTimer {
     v.swap(captured);
     return v;
   }
-  // one completed replay of a captured pair
-  void harvest(const Pair &p) {
+  // one completed replay of a captured pair (bytes >= 0: this replay's
+  // algorithmic bytes, when they differ from the captured launch's)
+  void harvest(const Pair &p, double b = -1.0) {
     float t = 0.f;
     NOSH_CUDA(cudaEventElapsedTime(&t, p.a, p.b));
     graph_ms += t;
     launches += p.n;
-    bytes += p.bytes;
+    bytes += b >= 0.0 ? b : p.bytes;
   }
   static void release(std::vector<Pair> &v) {
     for (Pair &p : v) {

@@ -217,9 +217,10 @@ void Minres<T>::iteration(int j) {
   launch_spmv<T>(sizeof(T) == 4 ? s.warp32 : s.warp64, (int)s.N, s.mesh->d_rp.p, s.mesh->d_ci.p, val,
                  (const C2<T> *)zc, cap, op, s.red.partials.p, s.red.counter.p, &d->zu, st, overlap);
   ++s.launch_count;
-  // bytes per vertex: z, diag block, u (+ the fused w/x update: z_prev, w2,
-  // w, x read; w1, x written)
-  s.timers[NOSH_KERNEL_JACOBIAN].end(st, s.spmv_bytes(2 * sizeof(T), 13 * sizeof(T)));
+  // values per vertex: z (2) and the diagonal block (3) read, u (2) written;
+  // the fused w/x update reads z_prev, w2, w, x and writes w1, x (12).  The
+  // first launch of a solve has no update pending (7: see the harvest)
+  s.timers[NOSH_KERNEL_JACOBIAN].end(st, s.spmv_bytes(2 * sizeof(T), 19 * sizeof(T)));
   s.amg->apply_minres<T>(d, u.p, r_old, r_cur, zn);
 }
 
@@ -331,10 +332,13 @@ int Minres<T>::solve(const T *b, double rtol, int maxit, int &status, double &re
         for (int k = 0; k < 2; k++)
           for (const auto &p : pro_ev[k]) s.timers[k].harvest(p);
       const int jac_end = h_sc->itn + (h_sc->done ? 1 : 0);
+      // the solve's first Jacobian apply has no deferred w/x update to apply
+      const double jac_first = s.spmv_bytes(2 * sizeof(T), 7 * sizeof(T));
       for (int jj = 0; jj < kPart; jj++) {
         const int g = it0 + jj;
         if (g < jac_end)
-          for (const auto &p : part_ev[h0][jj][NOSH_KERNEL_JACOBIAN]) s.timers[NOSH_KERNEL_JACOBIAN].harvest(p);
+          for (const auto &p : part_ev[h0][jj][NOSH_KERNEL_JACOBIAN])
+            s.timers[NOSH_KERNEL_JACOBIAN].harvest(p, g == 0 ? jac_first : -1.0);
         if (g < h_sc->itn)
           for (const auto &p : part_ev[h0][jj][NOSH_KERNEL_SMOOTHER]) s.timers[NOSH_KERNEL_SMOOTHER].harvest(p);
       }
