@@ -504,8 +504,9 @@ int nosh_mpnn_loss_grad(nosh_mpnn net, const float *X, const double *gram,
  * inside a captured part). */
 int nosh_nls_profile_enable(nosh_nls nls, int enable);
 /* Launch count, summed device time and summed algorithmic bytes (the bytes
- * the kernel must move at minimum: matrix, indices and vectors once each)
- * of one kernel class since the last read; resets the counters.  For
+ * the kernel must move at minimum: matrix, indices and the vectors it reads
+ * and writes, once each) of one kernel class since the last read; resets
+ * the counters.  For
  * NOSH_KERNEL_ALL only the launch count is returned. */
 int nosh_nls_profile_read(nosh_nls nls, int kernel, int64_t *launches,
                           double *total_ms, double *bytes);
